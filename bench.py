@@ -1,0 +1,458 @@
+"""Benchmark: PQIVF search on a 10M x 96 unit-norm index, one GB300.
+
+Workload (the 10M x 96 search configuration): 10,000,000 float32 vectors,
+d = 96, drawn from a Gaussian mixture of 10,000 centers and L2-normalised;
+coarse k = 16,384; 24 subquantizers x 256 codewords (4 dims each), uint8
+codes; 10,000 queries from the same mixture; top-10; Euclidean. Data are
+synthetic and seeded. The index is trained on the GPU before timing.
+
+A step is one batched Search of all 10,000 queries (coarse probe, list scan,
+exact rerank) with the queries already resident in HBM. `e2e` repeats the
+metric through the host C-ABI call (queries copied host->device and results
+device->host inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+Under torchrun each rank builds and searches its own replica (the path has no
+exchange step), rank 0 prints one JSON line with the whole-job throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "PQIVF queries/sec at recall@10>=0.9 (10M x 96)"
+PEAKS_PATH = os.path.join(HERE, "MEASURED_PEAKS.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--n", type=int, default=10_000_000)
+    ap.add_argument("--dim", type=int, default=96)
+    ap.add_argument("--centers", type=int, default=10_000)
+    ap.add_argument("--sigma", type=float, default=0.5)
+    ap.add_argument("--nlist", type=int, default=16384)
+    ap.add_argument("--m", type=int, default=24)
+    ap.add_argument("--pqk", type=int, default=256)
+    ap.add_argument("--iters", type=int, default=10)
+    ap.add_argument("--nq", type=int, default=10_000)
+    ap.add_argument("--k", type=int, default=10)
+    ap.add_argument("--nprobe", type=str, default="32,128")
+    ap.add_argument("--recall-queries", type=int, default=1000)
+    ap.add_argument("--target-recall", type=float, default=0.9)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--json-extra", action="store_true", help="print extra diagnostics to stderr")
+    return ap.parse_args()
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# data
+
+
+def make_data(args, torch, dev):
+    """Gaussian mixture of `centers` centers (N(0,1)), per-point noise sigma,
+    rows L2-normalised. Queries come from the same mixture."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed)
+    centers = torch.randn(args.centers, args.dim, generator=g, device=dev)
+    x = torch.empty(args.n, args.dim, device=dev)
+    chunk = 1 << 20
+    for s in range(0, args.n, chunk):
+        e = min(args.n, s + chunk)
+        lab = torch.randint(0, args.centers, (e - s,), generator=g, device=dev)
+        v = centers[lab] + args.sigma * torch.randn(e - s, args.dim, generator=g, device=dev)
+        x[s:e] = v / v.norm(dim=1, keepdim=True)
+    lab = torch.randint(0, args.centers, (args.nq,), generator=g, device=dev)
+    q = centers[lab] + args.sigma * torch.randn(args.nq, args.dim, generator=g, device=dev)
+    q = q / q.norm(dim=1, keepdim=True)
+    return x.contiguous(), q.contiguous()
+
+
+def ground_truth(torch, x, q, k):
+    """Exact top-k by Euclidean distance: FP32 GEMM candidates (top 64),
+    re-ranked in FP64."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    xn = (x * x).sum(1)
+    out = []
+    cand_k = max(64, 4 * k)
+    for s in range(0, q.shape[0], 256):
+        qb = q[s:s + 256]
+        best_d = None
+        best_i = None
+        for xs in range(0, x.shape[0], 1 << 21):
+            xe = min(x.shape[0], xs + (1 << 21))
+            d = xn[xs:xe][None, :] - 2.0 * qb @ x[xs:xe].T
+            v, i = torch.topk(d, cand_k, dim=1, largest=False)
+            i = i + xs
+            if best_d is None:
+                best_d, best_i = v, i
+            else:
+                cd = torch.cat([best_d, v], 1)
+                ci = torch.cat([best_i, i], 1)
+                vv, jj = torch.topk(cd, cand_k, dim=1, largest=False)
+                best_d, best_i = vv, torch.gather(ci, 1, jj)
+        cx = x[best_i].double()
+        d64 = ((cx - qb.double()[:, None, :]) ** 2).sum(-1)
+        o = torch.argsort(d64, dim=1)[:, :k]
+        out.append(torch.gather(best_i, 1, o).cpu().numpy())
+    return np.concatenate(out, 0)
+
+
+def recall_at(ids, gt):
+    k = gt.shape[1]
+    return float(np.mean([len(set(ids[i, :k].tolist()) & set(gt[i].tolist())) / k for i in range(gt.shape[0])]))
+
+
+# ---------------------------------------------------------------------------
+# clocks
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [s.strip() for s in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+
+
+def dist_setup(args):
+    import torch
+
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v, torch, dev):
+    if ws == 1:
+        return v
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_index(args, x, torch):
+    import hann_gb300 as hg
+
+    t0 = time.perf_counter()
+    xh = x.cpu().numpy()
+    idx = hg.New(args.dim, hg.WithCoarseK(args.nlist), hg.WithNumSubquantizers(args.m), hg.WithPQK(args.pqk),
+                 hg.WithKMeansIters(args.iters), hg.WithSeed(args.seed), hg.WithDevice(torch.cuda.current_device()))
+    idx.BulkAddArrays(np.arange(args.n, dtype=np.int64), xh)
+    t1 = time.perf_counter()
+    idx.Train()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    log(f"bulk_add {t1 - t0:.1f}s train {t2 - t1:.1f}s")
+    return idx, xh, t2 - t1
+
+
+def cpu_baseline(args, idx, q_host, nprobe, mode_rows):
+    """The oracle (C restatement of the reference's Search) timed on the host
+    cores on a bounded sample of the same queries."""
+    import oracle
+
+    oracle.build()
+    st = idx.export_state()
+    lay = st["layout"]
+    ix = oracle.OracleIndex.from_csr(lay["dimension"], lay["num_subquantizers"], lay["pq_k_eff"], st["coarse"],
+                                     st["codebooks"], st["list_len"], st["ids"], st["vectors"], st["codes"])
+    del st
+    cores = os.cpu_count() or 1
+    probe_n = min(64, q_host.shape[0])
+    t0 = time.perf_counter()
+    ix.search(q_host[:probe_n], args.k, nprobe, nthreads=cores)
+    dt = time.perf_counter() - t0
+    per_q = dt / probe_n
+    n = int(min(q_host.shape[0], max(probe_n, args.cpu_seconds / max(per_q, 1e-9))))
+    t0 = time.perf_counter()
+    ix.search(q_host[:n], args.k, nprobe, nthreads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "queries/s", "cores": cores, "kind": "port",
+            "sample": f"{n} of {q_host.shape[0]} queries, nprobe {nprobe}, k {args.k}, parity (reconstructed-"
+                      f"vector) distances, {cores} threads, {dt:.1f} s"}
+
+
+def main():
+    args = parse()
+    import torch
+
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference" and rank != 0:
+        return 0
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import __graft_entry__ as ge
+
+    ge.build()
+    import hann_gb300 as hg
+
+    x, q = make_data(args, torch, dev)
+    idx, xh, train_s = build_index(args, x, torch)
+    q_host = q.cpu().numpy()
+    nr = min(args.recall_queries, args.nq)
+    gt = ground_truth(torch, x, q[:nr], args.k)
+    del x
+    torch.cuda.empty_cache()
+
+    # recall at each nprobe, exact-rerank mode and parity mode
+    probes = [int(p) for p in args.nprobe.split(",")]
+    rec = {}
+    for npb in probes:
+        for mode in (1, 0):
+            ids, _, _ = idx.SearchBatch(q_host[:nr], args.k, nprobe=npb, mode=mode)
+            rec[(npb, mode)] = recall_at(ids, gt)
+    log("recall", {f"nprobe{a}_mode{b}": round(v, 4) for (a, b), v in rec.items()})
+    choice = None
+    for npb in probes:
+        if rec[(npb, 1)] >= args.target_recall:
+            choice = npb
+            break
+    if choice is None:
+        choice = probes[-1]
+    mode = 1
+
+    if args.impl == "reference":
+        cb = cpu_baseline(args, idx, q_host, choice, None)
+        # steps: repeat bounded samples
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "queries/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * 1.0 / cb["value"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": workload_config(args, choice, mode, rec),
+                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    # ------------------------------------------------------------------ timed
+    nq = args.nq
+    ids_d = torch.empty(nq, args.k, dtype=torch.int64, device=dev)
+    dist_d = torch.empty(nq, args.k, dtype=torch.float64, device=dev)
+    nout_d = torch.empty(nq, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        idx.SearchBatchDevice(q.data_ptr(), nq, args.k, choice, mode, ids_d.data_ptr(), dist_d.data_ptr(),
+                              nout_d.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    idx.StageTimes()  # clear
+    idx.SetProfiling(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    clocks = sampler.stop()
+    idx.SetProfiling(False)
+    stage_ms, launches, rows_scanned = idx.StageTimes()
+    ms_max = max_over_ranks(ws, ms, torch, dev)
+    value = ws * nq * args.steps / (ms_max / 1000.0)
+
+    # sanity: the timed results equal the host-API results
+    ids_t = ids_d.cpu().numpy()
+    ids_h, _, _ = idx.SearchBatch(q_host[:256], args.k, nprobe=choice, mode=mode)
+    if not np.array_equal(ids_t[:256], ids_h):
+        log("WARNING: device-path ids differ from host-path ids")
+
+    # e2e through the host C-ABI (pinned host buffers, copies inside the timed region)
+    L = hg.load_library()
+    qp = torch.from_numpy(q_host).pin_memory()
+    kk = torch.full((nq,), args.k, dtype=torch.int32).pin_memory()
+    npv = torch.full((nq,), choice, dtype=torch.int32).pin_memory()
+    oi = torch.empty(nq, args.k, dtype=torch.int64).pin_memory()
+    od = torch.empty(nq, args.k, dtype=torch.float64).pin_memory()
+    on = torch.empty(nq, dtype=torch.int32).pin_memory()
+
+    def e2e_step():
+        rc = L.hann_pqivf_search_batch(idx.handle, ctypes.c_void_p(qp.data_ptr()), nq,
+                                       ctypes.c_void_p(kk.data_ptr()), ctypes.c_void_p(npv.data_ptr()), args.k, mode,
+                                       ctypes.c_void_p(oi.data_ptr()), ctypes.c_void_p(od.data_ptr()),
+                                       ctypes.c_void_p(on.data_ptr()))
+        assert rc == 0, L.hann_pqivf_last_error(idx.handle)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(ws, time.perf_counter() - t0, torch, dev)
+    e2e_value = ws * nq * e2e_steps / e2e_s
+    h2d = nq * args.dim * 4 + nq * 4 * 2
+    d2h = nq * args.k * (8 + 8) + nq * 4
+
+    # one-query-per-call path (plain, one launch sequence per query)
+    nplain = 200
+    t0 = time.perf_counter()
+    for i in range(nplain):
+        idx.SearchBatch(q_host[i:i + 1], args.k, nprobe=choice, mode=mode)
+    plain_qps = nplain / (time.perf_counter() - t0)
+
+    # roofline of the scan kernel: algorithmic bytes = rows scanned (counted
+    # by the kernel) x (M code bytes + the 4-byte per-row term)
+    code_bytes = args.m + 4
+    scan_launches = max(launches // 4, 1)
+    scan_ms = stage_ms[2] / scan_launches
+    per_launch_bytes = rows_scanned / scan_launches * code_bytes
+    achieved = per_launch_bytes / (scan_ms / 1000.0) / 1e9
+    peak = 6782.4
+    peak_src = "fallback"
+    if os.path.exists(PEAKS_PATH):
+        try:
+            peak = float(json.load(open(PEAKS_PATH))["hbm_gbs"])
+            peak_src = "measured"
+        except Exception:
+            pass
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            cb = cpu_baseline(args, idx, q_host, choice, None)
+        except Exception as e:  # pragma: no cover
+            log("cpu baseline failed:", e)
+            cb = {"value": None, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port", "sample": str(e)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(args, choice, mode, rec),
+            "recall_at_10": rec[(choice, mode)],
+            "stage_ms_per_step": [round(v / args.steps, 4) for v in stage_ms],
+            "train_s": round(train_s, 2),
+            "plain_one_query_per_call_qps": plain_qps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "scan_kernel",
+                         "bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
+            "cpu_baseline": cb,
+            "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    idx.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def workload_config(args, nprobe, mode, rec):
+    return {
+        "workload": f"pqivf-search {args.n // 1_000_000}M x {args.dim} unit-norm Gaussian mixture "
+                    f"({args.centers} centers, sigma {args.sigma}); coarse {args.nlist}; "
+                    f"{args.m} x {args.pqk} PQ; {args.nq} queries; k {args.k}; nprobe {nprobe}; "
+                    f"{'exact FP32 rerank of raw vectors' if mode == 1 else 'reference PQ distances'}",
+        "n": args.n, "dim": args.dim, "nlist": args.nlist, "M": args.m, "pq_k": args.pqk, "nq": args.nq,
+        "k": args.k, "nprobe": nprobe, "mode": "exact_rerank" if mode == 1 else "parity",
+        "recall_by_nprobe": {f"{a}/{'exact' if b == 1 else 'pq'}": round(v, 4) for (a, b), v in rec.items()},
+        "l2": "inputs larger than L2 (240 MB codes + 3.84 GB raw vectors), no flush",
+    }
+
+
+if __name__ == "__main__":
+    sys.exit(main())

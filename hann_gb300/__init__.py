@@ -1,0 +1,548 @@
+"""hann_gb300 -- GB300-native PQIVF index with the interface of hann's pqivf.
+
+The index lives on one GPU; this module is a thin ctypes binding over the C
+ABI in ``include/hann_gb300.h`` (``libhann_gb300.so``, built by
+``hann_gb300.build``). It mirrors the reference's Go API
+(pqivf/index.go, core/index.go): ``New(dim, With...(...))`` and the methods
+Add, BulkAdd, Delete, BulkDelete, Update, BulkUpdate, Train, Search, Stats,
+Save and Load, with the same argument meaning, error conditions and error
+messages. Errors raise :class:`HannError`.
+
+There is no CPU fallback: if the CUDA library is missing or cannot load,
+importing the binding's entry points raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import io
+import os
+import threading
+from typing import Dict, Iterable, List, NamedTuple, Sequence
+
+import numpy as np
+
+from . import gob
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhann_gb300.so")
+
+HANN_OK = 0
+HANN_E_INVALID = -1
+HANN_E_NOT_FOUND = -2
+HANN_E_EXISTS = -3
+HANN_E_STATE = -4
+HANN_E_CUDA = -5
+HANN_E_NOMEM = -6
+HANN_E_UNSUPPORTED = -7
+
+MODE_PARITY = 0
+MODE_EXACT_RERANK = 1
+
+METRIC_SQEUCLID, METRIC_EUCLID, METRIC_MANHATTAN, METRIC_COSINE = 0, 1, 2, 3
+
+
+class HannError(Exception):
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+class Neighbor(NamedTuple):
+    """core.Neighbor (core/index.go:125-128)."""
+    ID: int
+    Distance: float
+
+
+class IndexStats(NamedTuple):
+    """core.IndexStats (core/index.go:131-140)."""
+    Count: int
+    Dimension: int
+    Distance: str
+    FallbackSearches: int
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("dimension", ctypes.c_int32), ("coarse_k", ctypes.c_int32),
+                ("num_subquantizers", ctypes.c_int32), ("pq_k", ctypes.c_int32),
+                ("kmeans_iters", ctypes.c_int32), ("candidate_clusters", ctypes.c_int32),
+                ("fallback", ctypes.c_int32), ("seed", ctypes.c_uint64), ("device", ctypes.c_int32),
+                ("rerank", ctypes.c_int32)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int64), ("dimension", ctypes.c_int32),
+                ("fallback_searches", ctypes.c_int64), ("trained", ctypes.c_int32), ("nlist", ctypes.c_int32),
+                ("rows_capacity", ctypes.c_int64)]
+
+
+class _Layout(ctypes.Structure):
+    _fields_ = [("dimension", ctypes.c_int32), ("coarse_k", ctypes.c_int32),
+                ("num_subquantizers", ctypes.c_int32), ("pq_k", ctypes.c_int32),
+                ("kmeans_iters", ctypes.c_int32), ("candidate_clusters", ctypes.c_int32),
+                ("fallback", ctypes.c_int32), ("trained", ctypes.c_int32), ("nlist", ctypes.c_int32),
+                ("pq_k_eff", ctypes.c_int32), ("n_rows", ctypes.c_int64), ("n_pending", ctypes.c_int64)]
+
+
+_P = ctypes.c_void_p
+_lib = None
+_lib_lock = threading.Lock()
+
+# Every entry point include/hann_gb300.h declares.
+EXPORTED = (
+    "hann_pqivf_options_init", "hann_pqivf_new", "hann_pqivf_free", "hann_pqivf_last_error", "hann_pqivf_add",
+    "hann_pqivf_bulk_add", "hann_pqivf_delete", "hann_pqivf_bulk_delete", "hann_pqivf_update",
+    "hann_pqivf_bulk_update", "hann_pqivf_train", "hann_pqivf_train_seeded", "hann_pqivf_search",
+    "hann_pqivf_search_batch", "hann_pqivf_search_batch_device", "hann_pqivf_stats", "hann_pqivf_export_layout",
+    "hann_pqivf_export", "hann_pqivf_import", "hann_gpu_distance_batch", "hann_pqivf_set_profiling",
+    "hann_pqivf_stage_times", "hann_pqivf_list_lengths",
+)
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load libhann_gb300.so. Raises when it is missing: there is no fallback."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(
+                "libhann_gb300.so is not built (run hann_gb300.build.build()); the GPU index has no CPU fallback")
+        L = ctypes.CDLL(p)
+        L.hann_pqivf_options_init.argtypes = [ctypes.POINTER(_Options), ctypes.c_int32]
+        L.hann_pqivf_options_init.restype = None
+        L.hann_pqivf_new.argtypes = [ctypes.POINTER(_Options), ctypes.POINTER(_P)]
+        L.hann_pqivf_free.argtypes = [_P]
+        L.hann_pqivf_free.restype = None
+        L.hann_pqivf_last_error.argtypes = [_P]
+        L.hann_pqivf_last_error.restype = ctypes.c_char_p
+        L.hann_pqivf_add.argtypes = [_P, ctypes.c_int64, _P]
+        L.hann_pqivf_bulk_add.argtypes = [_P, _P, _P, ctypes.c_int64]
+        L.hann_pqivf_delete.argtypes = [_P, ctypes.c_int64]
+        L.hann_pqivf_bulk_delete.argtypes = [_P, _P, ctypes.c_int64]
+        L.hann_pqivf_update.argtypes = [_P, ctypes.c_int64, _P]
+        L.hann_pqivf_bulk_update.argtypes = [_P, _P, _P, ctypes.c_int64]
+        L.hann_pqivf_train.argtypes = [_P]
+        L.hann_pqivf_train_seeded.argtypes = [_P, _P, _P, _P, ctypes.c_int64]
+        L.hann_pqivf_search.argtypes = [_P, _P, ctypes.c_int32, _P, _P, _P]
+        L.hann_pqivf_search_batch.argtypes = [_P, _P, ctypes.c_int64, _P, _P, ctypes.c_int32, ctypes.c_int32, _P,
+                                              _P, _P]
+        L.hann_pqivf_search_batch_device.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                                     ctypes.c_int32, _P, _P, _P, _P]
+        L.hann_pqivf_stats.argtypes = [_P, ctypes.POINTER(_Stats)]
+        L.hann_pqivf_export_layout.argtypes = [_P, ctypes.POINTER(_Layout)]
+        L.hann_pqivf_export.argtypes = [_P] + [_P] * 10
+        L.hann_pqivf_import.argtypes = [_P, ctypes.POINTER(_Layout)] + [_P] * 11
+        L.hann_gpu_distance_batch.argtypes = [ctypes.c_int32, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]
+        L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
+        L.hann_pqivf_list_lengths.argtypes = [_P, _P]
+        if path is None:
+            _lib = L
+        return L
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else ctypes.c_void_p(0)
+
+
+# ---------------------------------------------------------------------------
+# Options, as the reference's functional options (pqivf/index.go:56-94).
+
+def WithCoarseK(k: int):
+    return lambda o: setattr(o, "coarse_k", int(k))
+
+
+def WithNumSubquantizers(m: int):
+    return lambda o: setattr(o, "num_subquantizers", int(m))
+
+
+def WithPQK(k: int):
+    return lambda o: setattr(o, "pq_k", int(k))
+
+
+def WithKMeansIters(n: int):
+    return lambda o: setattr(o, "kmeans_iters", int(n))
+
+
+def WithCandidateClusters(n: int):
+    return lambda o: setattr(o, "candidate_clusters", int(n))
+
+
+def WithBruteForceFallback(allow: bool):
+    return lambda o: setattr(o, "fallback", 1 if allow else 0)
+
+
+def WithSeed(seed: int):
+    """The index's k-means seeding source (the reference reads HANN_SEED)."""
+    return lambda o: setattr(o, "seed", int(seed) & 0xFFFFFFFFFFFFFFFF)
+
+
+def WithDevice(device: int):
+    return lambda o: setattr(o, "device", int(device))
+
+
+def WithRerank(r: int):
+    """Candidates rescored exactly per query (0 = automatic)."""
+    return lambda o: setattr(o, "rerank", int(r))
+
+
+def New(dimension: int, *opts) -> "Index":
+    """pqivf.New (pqivf/index.go:106-146)."""
+    return Index(dimension, *opts)
+
+
+class Index:
+    """GPU PQIVF index with the method set of the reference's pqivf.Index."""
+
+    def __init__(self, dimension: int, *opts):
+        L = load_library()
+        o = _Options()
+        L.hann_pqivf_options_init(ctypes.byref(o), int(dimension))
+        if "HANN_SEED" in os.environ:
+            try:
+                o.seed = int(os.environ["HANN_SEED"]) & 0xFFFFFFFFFFFFFFFF
+            except ValueError:
+                pass
+        for fn in opts:
+            fn(o)
+        h = _P()
+        rc = L.hann_pqivf_new(ctypes.byref(o), ctypes.byref(h))
+        if rc != HANN_OK:
+            raise HannError(rc, L.hann_pqivf_last_error(None).decode())
+        self._L = L
+        self._h = h
+        self._opts = o
+        self._dim = int(dimension)
+
+    # -- plumbing ----------------------------------------------------------
+    def _check(self, rc: int) -> None:
+        if rc != HANN_OK:
+            raise HannError(rc, self._L.hann_pqivf_last_error(self._h).decode())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.hann_pqivf_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def dimension(self) -> int:
+        return self._dim
+
+    def _vec(self, v) -> np.ndarray:
+        return np.ascontiguousarray(v, dtype=np.float32).reshape(-1)
+
+    def _dim_error(self, got: int) -> HannError:
+        return HannError(HANN_E_INVALID, "vector dimension %d does not match index dimension %d" % (got, self._dim))
+
+    # -- core.Index ----------------------------------------------------------
+    def Add(self, id: int, vector) -> None:
+        v = self._vec(vector)
+        if v.size != self._dim:
+            raise self._dim_error(v.size)
+        self._check(self._L.hann_pqivf_add(self._h, int(id), _ptr(v)))
+
+    def BulkAdd(self, vectors: Dict[int, Sequence[float]]) -> None:
+        keys = sorted(int(k) for k in vectors)
+        good: List[int] = []
+        bad = None
+        for k in keys:
+            v = self._vec(vectors[k])
+            if v.size != self._dim:
+                bad = (k, v.size)
+                break
+            good.append(k)
+        if good:
+            ids = np.asarray(good, dtype=np.int64)
+            mat = np.stack([self._vec(vectors[k]) for k in good]).astype(np.float32)
+            self._check(self._L.hann_pqivf_bulk_add(self._h, _ptr(ids), _ptr(mat), ids.size))
+        if bad is not None:
+            raise HannError(HANN_E_INVALID, "vector dimension %d does not match index dimension %d for id %d"
+                            % (bad[1], self._dim, bad[0]))
+
+    def BulkAddArrays(self, ids, matrix) -> None:
+        """BulkAdd from an id array and a row-major [n, dim] float32 matrix."""
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        mat = np.ascontiguousarray(matrix, dtype=np.float32)
+        if mat.ndim != 2 or mat.shape[1] != self._dim or mat.shape[0] != ids.size:
+            raise HannError(HANN_E_INVALID, "matrix shape does not match ids and index dimension")
+        self._check(self._L.hann_pqivf_bulk_add(self._h, _ptr(ids), _ptr(mat), ids.size))
+
+    def Delete(self, id: int) -> None:
+        self._check(self._L.hann_pqivf_delete(self._h, int(id)))
+
+    def BulkDelete(self, ids: Iterable[int]) -> None:
+        a = np.asarray(list(ids), dtype=np.int64)
+        self._check(self._L.hann_pqivf_bulk_delete(self._h, _ptr(a), a.size))
+
+    def Update(self, id: int, vector) -> None:
+        v = self._vec(vector)
+        if v.size != self._dim:
+            raise self._dim_error(v.size)
+        self._check(self._L.hann_pqivf_update(self._h, int(id), _ptr(v)))
+
+    def BulkUpdate(self, updates: Dict[int, Sequence[float]]) -> None:
+        keys = sorted(int(k) for k in updates)
+        for k in keys:
+            v = self._vec(updates[k])
+            if v.size != self._dim:
+                raise HannError(HANN_E_INVALID, "invalid vector for id %d: vector dimension %d does not match "
+                                "index dimension %d" % (k, v.size, self._dim))
+        if not keys:
+            return
+        ids = np.asarray(keys, dtype=np.int64)
+        mat = np.stack([self._vec(updates[k]) for k in keys]).astype(np.float32)
+        self._check(self._L.hann_pqivf_bulk_update(self._h, _ptr(ids), _ptr(mat), ids.size))
+
+    def Train(self) -> None:
+        self._check(self._L.hann_pqivf_train(self._h))
+
+    def TrainSeeded(self, coarse_init=None, pq_init=None, reseed=None) -> None:
+        """Train with explicit k-means init rows and reseed stream."""
+        ci = None if coarse_init is None else np.ascontiguousarray(coarse_init, dtype=np.int64)
+        pi = None if pq_init is None else np.ascontiguousarray(pq_init, dtype=np.int64)
+        rs = None if reseed is None else np.ascontiguousarray(reseed, dtype=np.int64)
+        nrs = 0 if rs is None else rs.size
+        if rs is not None and rs.size == 0:
+            rs = np.zeros(1, dtype=np.int64)
+        self._check(self._L.hann_pqivf_train_seeded(
+            self._h, _ptr(ci) if ci is not None else None, _ptr(pi) if pi is not None else None,
+            _ptr(rs) if rs is not None else None, nrs))
+
+    def _stats_raw(self) -> _Stats:
+        s = _Stats()
+        self._check(self._L.hann_pqivf_stats(self._h, ctypes.byref(s)))
+        return s
+
+    def Search(self, query, k: int) -> List[Neighbor]:
+        if int(k) <= 0:
+            raise HannError(HANN_E_INVALID, "k must be positive")
+        if not self._stats_raw().trained:
+            raise HannError(HANN_E_STATE,
+                            "PQIVF index is not trained. Call Train() after adding data before searching")
+        q = self._vec(query)
+        if q.size != self._dim:
+            raise HannError(HANN_E_INVALID, "query dimension %d does not match index dimension %d"
+                            % (q.size, self._dim))
+        k = int(k)
+        ids = np.zeros(k, dtype=np.int64)
+        dist = np.zeros(k, dtype=np.float64)
+        n = ctypes.c_int32(0)
+        self._check(self._L.hann_pqivf_search(self._h, _ptr(q), k, _ptr(ids), _ptr(dist), ctypes.byref(n)))
+        return [Neighbor(int(ids[i]), float(dist[i])) for i in range(n.value)]
+
+    def SearchBatch(self, queries, k, nprobe=None, mode: int = MODE_PARITY):
+        """Batched Search. Returns (ids [nq, kmax], distances [nq, kmax], counts [nq])."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim == 1:
+            q = q.reshape(1, -1)
+        if q.shape[1] != self._dim:
+            raise HannError(HANN_E_INVALID, "query dimension %d does not match index dimension %d"
+                            % (q.shape[1], self._dim))
+        nq = q.shape[0]
+        kk = np.broadcast_to(np.asarray(k, dtype=np.int32), (nq,)).copy()
+        kmax = int(kk.max()) if nq else 1
+        npb = None if nprobe is None else np.broadcast_to(np.asarray(nprobe, dtype=np.int32), (nq,)).copy()
+        ids = np.full((nq, kmax), -1, dtype=np.int64)
+        dist = np.zeros((nq, kmax), dtype=np.float64)
+        nout = np.zeros(nq, dtype=np.int32)
+        self._check(self._L.hann_pqivf_search_batch(
+            self._h, _ptr(q), nq, _ptr(kk), _ptr(npb) if npb is not None else None, kmax, int(mode), _ptr(ids),
+            _ptr(dist), _ptr(nout)))
+        return ids, dist, nout
+
+    def SearchBatchDevice(self, d_queries: int, nq: int, k: int, nprobe: int, mode: int, d_ids: int, d_dist: int,
+                          d_nout: int, stream: int = 0) -> None:
+        """Device-pointer batch search (integers are device addresses)."""
+        self._check(self._L.hann_pqivf_search_batch_device(
+            self._h, ctypes.c_void_p(d_queries), int(nq), int(k), int(nprobe), int(mode), ctypes.c_void_p(d_ids),
+            ctypes.c_void_p(d_dist), ctypes.c_void_p(d_nout), ctypes.c_void_p(stream)))
+
+    def SetProfiling(self, on: bool) -> None:
+        self._check(self._L.hann_pqivf_set_profiling(self._h, 1 if on else 0))
+
+    def StageTimes(self):
+        """Device ms of [coarse distances, probe select, scan, rerank], the
+        launch count and the rows scanned since the last call (profiling on)."""
+        ms = np.zeros(4, dtype=np.float64)
+        n = ctypes.c_int64(0)
+        rows = ctypes.c_int64(0)
+        self._check(self._L.hann_pqivf_stage_times(self._h, _ptr(ms), ctypes.byref(n), ctypes.byref(rows)))
+        return ms, int(n.value), int(rows.value)
+
+    def ListLengths(self) -> np.ndarray:
+        out = np.zeros(max(self.DeviceStats()["nlist"], 1), dtype=np.int64)
+        self._check(self._L.hann_pqivf_list_lengths(self._h, _ptr(out)))
+        return out[:self.DeviceStats()["nlist"]]
+
+    def Stats(self) -> IndexStats:
+        s = self._stats_raw()
+        return IndexStats(int(s.count), int(s.dimension), "euclidean", int(s.fallback_searches))
+
+    def DeviceStats(self) -> dict:
+        s = self._stats_raw()
+        return {"trained": bool(s.trained), "nlist": int(s.nlist), "rows_capacity": int(s.rows_capacity)}
+
+    # -- persistence ---------------------------------------------------------
+    def export_state(self) -> dict:
+        """The index state as arrays (the GobEncode payload, pqivf/index.go:992-1017)."""
+        lay = _Layout()
+        self._check(self._L.hann_pqivf_export_layout(self._h, ctypes.byref(lay)))
+        dim, M = lay.dimension, lay.num_subquantizers
+        nl, kq, nr, npd = lay.nlist, lay.pq_k_eff, lay.n_rows, lay.n_pending
+        coarse = np.zeros((nl, dim), np.float32)
+        cbs = np.zeros((M, kq, dim // M), np.float32)
+        llen = np.zeros(nl, np.int64)
+        lkey = np.zeros(nl, np.uint8)
+        counts = np.zeros(nl, np.int64)
+        ids = np.zeros(nr, np.int64)
+        vecs = np.zeros((nr, dim), np.float32)
+        codes = np.zeros((nr, M), np.int32)
+        pids = np.zeros(npd, np.int64)
+        pvecs = np.zeros((npd, dim), np.float32)
+        self._check(self._L.hann_pqivf_export(self._h, _ptr(coarse), _ptr(cbs), _ptr(llen), _ptr(lkey),
+                                              _ptr(counts), _ptr(ids), _ptr(vecs), _ptr(codes), _ptr(pids),
+                                              _ptr(pvecs)))
+        return {"layout": {f: getattr(lay, f) for f, _ in _Layout._fields_}, "coarse": coarse, "codebooks": cbs,
+                "list_len": llen, "list_key": lkey, "cluster_counts": counts, "ids": ids, "vectors": vecs,
+                "codes": codes, "pending_ids": pids, "pending_vectors": pvecs}
+
+    def import_state(self, st: dict) -> None:
+        lay = _Layout(**{f: int(st["layout"][f]) for f, _ in _Layout._fields_})
+        has = st.get("has_codes")
+        arrs = [np.ascontiguousarray(st["coarse"], np.float32), np.ascontiguousarray(st["codebooks"], np.float32),
+                np.ascontiguousarray(st["list_len"], np.int64), np.ascontiguousarray(st["list_key"], np.uint8),
+                np.ascontiguousarray(st["cluster_counts"], np.int64), np.ascontiguousarray(st["ids"], np.int64),
+                np.ascontiguousarray(st["vectors"], np.float32), np.ascontiguousarray(st["codes"], np.int32),
+                None if has is None else np.ascontiguousarray(has, np.uint8),
+                np.ascontiguousarray(st["pending_ids"], np.int64),
+                np.ascontiguousarray(st["pending_vectors"], np.float32)]
+        ptrs = [(_ptr(a) if a is not None else None) for a in arrs]
+        self._check(self._L.hann_pqivf_import(self._h, ctypes.byref(lay), *ptrs))
+        self._dim = lay.dimension
+
+    def Save(self, w) -> None:
+        """Write the reference's gob format (pqivf/index.go:1086-1093)."""
+        w.write(gob.encode_pqivf(state_to_gob(self.export_state())))
+
+    def Load(self, r) -> None:
+        """Read the reference's gob format (pqivf/index.go:1095-1101)."""
+        data = r.read() if hasattr(r, "read") else bytes(r)
+        ser = gob.decode_pqivf(data)
+        self.import_state(gob_to_state(ser, self._opts))
+
+
+# ---------------------------------------------------------------------------
+# gob <-> array state
+
+
+def state_to_gob(st: dict) -> dict:
+    lay = st["layout"]
+    dim = lay["dimension"]
+    lists, counts = {}, {}
+    off = 0
+    for c in range(lay["nlist"]):
+        n = int(st["list_len"][c])
+        if st["list_key"][c]:
+            counts[c] = int(st["cluster_counts"][c])
+            lists[c] = [{"ID": int(st["ids"][off + j]), "Vector": st["vectors"][off + j],
+                         "Codes": [int(x) for x in st["codes"][off + j]], "Cluster": c} for j in range(n)]
+        off += n
+    return {
+        "Dimension": dim, "CoarseK": lay["coarse_k"], "CoarseCentroids": list(st["coarse"]),
+        "ClusterCounts": counts, "InvertedLists": lists, "NumSubquantizers": lay["num_subquantizers"],
+        "Codebooks": [list(cb) for cb in st["codebooks"]] if lay["nlist"] else None, "PqK": lay["pq_k"],
+        "KMeansIters": lay["kmeans_iters"], "AllowBruteForceFallback": bool(lay["fallback"]),
+        "Trained": bool(lay["trained"]),
+        "PendingVectors": {int(i): st["pending_vectors"][j] for j, i in enumerate(st["pending_ids"])},
+        "NumCandidateClusters": lay["candidate_clusters"],
+    }
+
+
+def gob_to_state(ser: dict, opts: _Options | None = None) -> dict:
+    """GobDecode (pqivf/index.go:1020-1084): validation and defaults."""
+    fv = int(ser.get("FormatVersion", 0))
+    if fv > gob.FORMAT_VERSION:
+        raise HannError(HANN_E_INVALID, "index file has format version %d, but this build supports up to %d"
+                        % (fv, gob.FORMAT_VERSION))
+    dim = int(ser.get("Dimension", 0))
+    M = int(ser.get("NumSubquantizers", 0))
+    ck, pk, it = int(ser.get("CoarseK", 0)), int(ser.get("PqK", 0)), int(ser.get("KMeansIters", 0))
+    if dim <= 0:
+        raise HannError(HANN_E_INVALID, "serialized index has invalid dimension %d" % dim)
+    if M <= 0 or dim % M != 0:
+        raise HannError(HANN_E_INVALID, "serialized index has invalid subquantizer count %d for dimension %d"
+                        % (M, dim))
+    if ck <= 0 or pk <= 0 or it <= 0:
+        raise HannError(HANN_E_INVALID, "serialized index has invalid training parameters: coarseK %d, pqK %d, "
+                        "kMeansIters %d" % (ck, pk, it))
+    ncc = int(ser.get("NumCandidateClusters", 0))
+    if ncc <= 0:
+        ncc = opts.candidate_clusters if opts is not None and opts.candidate_clusters > 0 else 3
+    coarse = np.asarray(ser.get("CoarseCentroids") or [], dtype=np.float32).reshape(-1, dim)
+    nl = coarse.shape[0]
+    cbl = ser.get("Codebooks") or []
+    kq = len(cbl[0]) if cbl else 0
+    cbs = np.asarray(cbl, dtype=np.float32).reshape(M, kq, dim // M) if kq else np.zeros((M, 0, dim // M),
+                                                                                            np.float32)
+    lists = ser.get("InvertedLists") or {}
+    counts_map = ser.get("ClusterCounts") or {}
+    for c in list(lists) + list(counts_map):
+        if c < 0 or c >= max(nl, 1) and lists.get(c):
+            raise HannError(HANN_E_UNSUPPORTED, "inverted list %d has no coarse centroid" % c)
+    llen = np.zeros(nl, np.int64)
+    lkey = np.zeros(nl, np.uint8)
+    counts = np.zeros(nl, np.int64)
+    ids, vecs, codes, has = [], [], [], []
+    for c in range(nl):
+        if c in lists or c in counts_map:
+            lkey[c] = 1
+        counts[c] = int(counts_map.get(c, 0))
+        ents = lists.get(c) or []
+        llen[c] = len(ents)
+        for e in ents:
+            ids.append(int(e.get("ID", 0)))
+            v = np.asarray(e.get("Vector") or [], dtype=np.float32)
+            if v.size != dim:
+                raise HannError(HANN_E_INVALID, "entry %d has a vector of dimension %d" % (ids[-1], v.size))
+            vecs.append(v)
+            cd = e.get("Codes") or []
+            ok = len(cd) == M and all(0 <= int(x) < kq for x in cd)
+            codes.append(np.asarray(cd if ok else [0] * M, dtype=np.int32))
+            has.append(1 if ok else 0)
+    pend = ser.get("PendingVectors") or {}
+    pids = np.asarray(sorted(pend), dtype=np.int64)
+    pvecs = np.asarray([pend[i] for i in sorted(pend)], dtype=np.float32).reshape(-1, dim)
+    layout = {"dimension": dim, "coarse_k": ck, "num_subquantizers": M, "pq_k": pk, "kmeans_iters": it,
+              "candidate_clusters": ncc, "fallback": 1 if ser.get("AllowBruteForceFallback") else 0,
+              "trained": 1 if ser.get("Trained") else 0, "nlist": nl, "pq_k_eff": kq, "n_rows": len(ids),
+              "n_pending": int(pids.size)}
+    return {"layout": layout, "coarse": coarse, "codebooks": cbs, "list_len": llen, "list_key": lkey,
+            "cluster_counts": counts, "ids": np.asarray(ids, np.int64),
+            "vectors": np.asarray(vecs, np.float32).reshape(-1, dim),
+            "codes": np.asarray(codes, np.int32).reshape(-1, M), "has_codes": np.asarray(has, np.uint8),
+            "pending_ids": pids, "pending_vectors": pvecs}
+
+
+def distance_batch(metric: int, query, flat) -> np.ndarray:
+    """simd_<metric>_batch on the GPU (core/simd_kernels.inc.h:235-264)."""
+    L = load_library()
+    q = np.ascontiguousarray(query, dtype=np.float32).reshape(-1)
+    x = np.ascontiguousarray(flat, dtype=np.float32).reshape(-1)
+    dim = q.size
+    n = x.size // dim if dim else 0
+    out = np.zeros(n, dtype=np.float64)
+    rc = L.hann_gpu_distance_batch(int(metric), _ptr(q), _ptr(x), dim, n, _ptr(out))
+    if rc != HANN_OK:
+        raise HannError(rc, "distance batch failed")
+    return out

@@ -1,0 +1,146 @@
+// common.cuh -- shared device helpers for the hann_gb300 PQIVF kernels.
+//
+// Exact FP32 distances on the device reproduce the summation order of the
+// reference's NEON tier (core/simd_kernels.inc.h:64-102 instantiated by
+// core/simd_kernels_neon.inc.h): element i of the unrolled part accumulates
+// into chain (u, l) = ((i % 16) / 4, i % 4) with a fused multiply-add; the
+// one-vector cleanup loop continues chain (0, l); the chains combine as
+// (c0 + c1) + (c2 + c3) per lane, the four lanes as (l0 + l1) + (l2 + l3),
+// and the scalar tail adds (a - b)^2 as a separate multiply and add. The
+// Grace host that sits beside the GB300 runs exactly this tier, so a device
+// distance is bit-identical to the reference's CPU distance on that host.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hann {
+
+// ---------------------------------------------------------------------------
+// Reference-order squared Euclidean distance, generic length.
+// a and b may live in any address space; the loop order is fixed.
+template <typename PA, typename PB>
+__device__ __forceinline__ float sqeuclid_ref(PA a, PB b, int n) {
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[u][l] = 0.0f;
+    int i = 0;
+    const int lim4 = n - (n % 16);
+    for (; i < lim4; i += 16) {
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                float d = a[i + 4 * u + l] - b[i + 4 * u + l];
+                acc[u][l] = __fmaf_rn(d, d, acc[u][l]);
+            }
+    }
+    const int lim = n - (n % 4);
+    for (; i < lim; i += 4) {
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+            float d = a[i + l] - b[i + l];
+            acc[0][l] = __fmaf_rn(d, d, acc[0][l]);
+        }
+    }
+    float v[4];
+#pragma unroll
+    for (int l = 0; l < 4; l++)
+        v[l] = __fadd_rn(__fadd_rn(acc[0][l], acc[1][l]), __fadd_rn(acc[2][l], acc[3][l]));
+    float sum = __fadd_rn(__fadd_rn(v[0], v[1]), __fadd_rn(v[2], v[3]));
+    for (; i < n; i++) {
+        float d = a[i] - b[i];
+        sum = __fadd_rn(sum, __fmul_rn(d, d));
+    }
+    return sum;
+}
+
+// Reference-order Manhattan distance (core/simd_kernels.inc.h:115-149, NEON).
+template <typename PA, typename PB>
+__device__ __forceinline__ float manhattan_ref(PA a, PB b, int n) {
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[u][l] = 0.0f;
+    int i = 0;
+    const int lim4 = n - (n % 16);
+    for (; i < lim4; i += 16) {
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int l = 0; l < 4; l++)
+                acc[u][l] = __fadd_rn(acc[u][l], fabsf(a[i + 4 * u + l] - b[i + 4 * u + l]));
+    }
+    const int lim = n - (n % 4);
+    for (; i < lim; i += 4) {
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[0][l] = __fadd_rn(acc[0][l], fabsf(a[i + l] - b[i + l]));
+    }
+    float v[4];
+#pragma unroll
+    for (int l = 0; l < 4; l++)
+        v[l] = __fadd_rn(__fadd_rn(acc[0][l], acc[1][l]), __fadd_rn(acc[2][l], acc[3][l]));
+    float sum = __fadd_rn(__fadd_rn(v[0], v[1]), __fadd_rn(v[2], v[3]));
+    for (; i < n; i++) sum = __fadd_rn(sum, fabsf(a[i] - b[i]));
+    return sum;
+}
+
+// Reference-order dot product of the cosine kernel's accumulations
+// (core/simd_kernels.inc.h:153-219, NEON); the scalar tail is fused there.
+template <typename PA, typename PB>
+__device__ __forceinline__ float dot_ref(PA a, PB b, int n) {
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[u][l] = 0.0f;
+    int i = 0;
+    const int lim4 = n - (n % 16);
+    for (; i < lim4; i += 16) {
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int l = 0; l < 4; l++) acc[u][l] = __fmaf_rn(a[i + 4 * u + l], b[i + 4 * u + l], acc[u][l]);
+    }
+    const int lim = n - (n % 4);
+    for (; i < lim; i += 4) {
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[0][l] = __fmaf_rn(a[i + l], b[i + l], acc[0][l]);
+    }
+    float v[4];
+#pragma unroll
+    for (int l = 0; l < 4; l++)
+        v[l] = __fadd_rn(__fadd_rn(acc[0][l], acc[1][l]), __fadd_rn(acc[2][l], acc[3][l]));
+    float sum = __fadd_rn(__fadd_rn(v[0], v[1]), __fadd_rn(v[2], v[3]));
+    for (; i < n; i++) sum = __fmaf_rn(a[i], b[i], sum);
+    return sum;
+}
+
+// Cosine distance from the three reference-order accumulations: zero norm
+// gives 1, the similarity is clamped to [-1, 1] (core/simd_kernels.inc.h:220-228).
+__device__ __forceinline__ float cosine_from_parts(float dot, float na, float nb) {
+    float A = __fsqrt_rn(na), B = __fsqrt_rn(nb);
+    if (A == 0.0f || B == 0.0f) return 1.0f;
+    float s = __fdiv_rn(dot, __fmul_rn(A, B));
+    s = fminf(fmaxf(s, -1.0f), 1.0f);
+    return __fsub_rn(1.0f, s);
+}
+
+// ---------------------------------------------------------------------------
+// Order-preserving map of a float to an unsigned key (smaller float, smaller
+// key), so thresholds can be kept with integer atomics.
+__device__ __forceinline__ uint32_t float_key(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k) {
+    uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+
+__host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace hann

@@ -1,0 +1,569 @@
+// kernels_train.cu -- k-means assignment, FP64 centroid update, product
+// quantizer assignment and encoding.
+//
+// Every argmin here uses the reference-order FP32 squared Euclidean distance
+// (common.cuh) and lets the lowest index win a tie, as assignPoints and
+// encodeWithCodebooks do (pqivf/index.go:641-666, 738-789). Centroid sums are
+// FP64 on the device (the reference sums in FP32 in point order,
+// pqivf/index.go:816-843); the mean is rounded once to FP32.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace hann {
+
+// ---------------------------------------------------------------------------
+// Tiled exact distances. A block owns TP points and walks every centroid in
+// tiles of TC. Each thread owns 4 points x 4 centroids and accumulates the 16
+// pairs chain by chain in the reference's order, so all 16 pairs share each
+// shared-memory load (one float4 of points, one float4 of centroids per
+// element).
+constexpr int TD_THREADS = 256;
+constexpr int TD_TP = 128;
+constexpr int TD_TC = 32;
+constexpr int TD_DMAX = 128;
+
+struct Acc16 {
+    float v[4][4];
+};
+
+__device__ __forceinline__ void chain16(const float* __restrict__ Xs, const float* __restrict__ Cs, int tp, int tc,
+                                        int u, int l, int t16, int lim4, int s4, Acc16& acc) {
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc.v[a][b] = 0.0f;
+    for (int t = 0; t < t16; t++) {
+        const int i = 16 * t + 4 * u + l;
+        const float4 xp = *reinterpret_cast<const float4*>(Xs + i * TD_TP + 4 * tp);
+        const float4 cc = *reinterpret_cast<const float4*>(Cs + i * TD_TC + 4 * tc);
+        const float xa[4] = {xp.x, xp.y, xp.z, xp.w};
+        const float cb[4] = {cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                float d = xa[a] - cb[b];
+                acc.v[a][b] = __fmaf_rn(d, d, acc.v[a][b]);
+            }
+    }
+    if (u == 0) {
+        for (int s = 0; s < s4; s++) {
+            const int i = lim4 + 4 * s + l;
+            const float4 xp = *reinterpret_cast<const float4*>(Xs + i * TD_TP + 4 * tp);
+            const float4 cc = *reinterpret_cast<const float4*>(Cs + i * TD_TC + 4 * tc);
+            const float xa[4] = {xp.x, xp.y, xp.z, xp.w};
+            const float cb[4] = {cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    float d = xa[a] - cb[b];
+                    acc.v[a][b] = __fmaf_rn(d, d, acc.v[a][b]);
+                }
+        }
+    }
+}
+
+// Reference-order distances of the thread's 16 pairs for the current tiles.
+__device__ __forceinline__ void tile_pairs(const float* __restrict__ Xs, const float* __restrict__ Cs, int tp,
+                                           int tc, int dim, float out[4][4]) {
+    const int lim4 = dim - (dim % 16);
+    const int lim = dim - (dim % 4);
+    const int t16 = lim4 / 16;
+    const int s4 = (lim - lim4) / 4;
+    Acc16 acc, c01, c2;
+    float v01[4][4], v2[4][4];
+#pragma unroll 1
+    for (int l = 0; l < 4; l++) {
+        chain16(Xs, Cs, tp, tc, 0, l, t16, lim4, s4, acc);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) c01.v[a][b] = acc.v[a][b];
+        chain16(Xs, Cs, tp, tc, 1, l, t16, lim4, s4, acc);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) c01.v[a][b] = __fadd_rn(c01.v[a][b], acc.v[a][b]);
+        chain16(Xs, Cs, tp, tc, 2, l, t16, lim4, s4, acc);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) c2.v[a][b] = acc.v[a][b];
+        chain16(Xs, Cs, tp, tc, 3, l, t16, lim4, s4, acc);
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                float vl = __fadd_rn(c01.v[a][b], __fadd_rn(c2.v[a][b], acc.v[a][b]));
+                if (l == 0) v01[a][b] = vl;
+                else if (l == 1) v01[a][b] = __fadd_rn(v01[a][b], vl);
+                else if (l == 2) v2[a][b] = vl;
+                else out[a][b] = __fadd_rn(v01[a][b], __fadd_rn(v2[a][b], vl));
+            }
+    }
+    for (int i = lim; i < dim; i++) {
+        const float4 xp = *reinterpret_cast<const float4*>(Xs + i * TD_TP + 4 * tp);
+        const float4 cc = *reinterpret_cast<const float4*>(Cs + i * TD_TC + 4 * tc);
+        const float xa[4] = {xp.x, xp.y, xp.z, xp.w};
+        const float cb[4] = {cc.x, cc.y, cc.z, cc.w};
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                float d = xa[a] - cb[b];
+                out[a][b] = __fadd_rn(out[a][b], __fmul_rn(d, d));
+            }
+    }
+}
+
+// MODE 0: argmin per point. MODE 1: full distance matrix.
+template <int MODE>
+__global__ void __launch_bounds__(TD_THREADS) tile_dist_kernel(const float* __restrict__ x, int64_t n, int dim,
+                                                               const float* __restrict__ cent, int k,
+                                                               int32_t* __restrict__ out_idx,
+                                                               float* __restrict__ out_dist,
+                                                               float* __restrict__ out_mat) {
+    extern __shared__ __align__(16) float sm[];
+    float* Xs = sm;
+    float* Cs = sm + dim * TD_TP;
+    __shared__ float red_d[8][TD_TP];
+    __shared__ int red_i[8][TD_TP];
+    const int tid = threadIdx.x;
+    const int tp = tid & 31, tc = tid >> 5;
+    const int64_t p0 = (int64_t)blockIdx.x * TD_TP;
+    for (int e = tid; e < TD_TP * dim; e += TD_THREADS) {
+        const int p = e / dim, i = e - p * dim;
+        const int64_t gp = p0 + p;
+        Xs[i * TD_TP + p] = gp < n ? x[gp * dim + i] : 0.0f;
+    }
+    float best_d[4];
+    int best_i[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        best_d[a] = __int_as_float(0x7f800000);
+        best_i[a] = 0x7fffffff;
+    }
+    for (int c0 = 0; c0 < k; c0 += TD_TC) {
+        __syncthreads();
+        for (int e = tid; e < TD_TC * dim; e += TD_THREADS) {
+            const int c = e / dim, i = e - c * dim;
+            Cs[i * TD_TC + c] = (c0 + c < k) ? cent[(int64_t)(c0 + c) * dim + i] : 0.0f;
+        }
+        __syncthreads();
+        float dd[4][4];
+        tile_pairs(Xs, Cs, tp, tc, dim, dd);
+        if (MODE == 0) {
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const int c = c0 + 4 * tc + b;
+                    if (c < k && dd[a][b] < best_d[a]) {
+                        best_d[a] = dd[a][b];
+                        best_i[a] = c;
+                    }
+                }
+        } else {
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int64_t gp = p0 + 4 * tp + a;
+                if (gp >= n) continue;
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const int c = c0 + 4 * tc + b;
+                    if (c < k) out_mat[gp * k + c] = dd[a][b];
+                }
+            }
+        }
+    }
+    if (MODE == 0) {
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            red_d[tc][4 * tp + a] = best_d[a];
+            red_i[tc][4 * tp + a] = best_i[a];
+        }
+        __syncthreads();
+        if (tid < TD_TP) {
+            float bd = red_d[0][tid];
+            int bi = red_i[0][tid];
+            for (int w = 1; w < 8; w++) {
+                const float d = red_d[w][tid];
+                const int i = red_i[w][tid];
+                if (d < bd || (d == bd && i < bi)) {
+                    bd = d;
+                    bi = i;
+                }
+            }
+            const int64_t gp = p0 + tid;
+            if (gp < n) {
+                // No finite distance at all (NaN input): the reference keeps
+                // index 0 (pqivf/index.go:772-778).
+                out_idx[gp] = bi == 0x7fffffff ? 0 : bi;
+                if (out_dist) out_dist[gp] = bd;
+            }
+        }
+    }
+}
+
+// Generic path for dimensions above the tile limit: one thread per point.
+template <int MODE>
+__global__ void rowwise_dist_kernel(const float* __restrict__ x, int64_t n, int dim, const float* __restrict__ cent,
+                                    int k, int32_t* __restrict__ out_idx, float* __restrict__ out_dist,
+                                    float* __restrict__ out_mat) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float* xp = x + p * dim;
+    float bd = __int_as_float(0x7f800000);
+    int bi = 0;
+    for (int c = 0; c < k; c++) {
+        const float d = sqeuclid_ref(xp, cent + (int64_t)c * dim, dim);
+        if (MODE == 0) {
+            if (c == 0 || d < bd) {
+                bd = d;
+                bi = c;
+            }
+        } else {
+            out_mat[p * k + c] = d;
+        }
+    }
+    if (MODE == 0) {
+        out_idx[p] = bi;
+        if (out_dist) out_dist[p] = bd;
+    }
+}
+
+template <int MODE>
+static cudaError_t launch_tile(const float* x, int64_t n, int dim, const float* cent, int k, int32_t* out_idx,
+                               float* out_dist, float* out_mat, cudaStream_t s) {
+    if (n <= 0 || k <= 0) return cudaSuccess;
+    if (dim <= TD_DMAX) {
+        const size_t smem = (size_t)dim * (TD_TP + TD_TC) * sizeof(float);
+        static bool attr_set = false;
+        if (!attr_set) {
+            cudaError_t e = cudaFuncSetAttribute(tile_dist_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)((size_t)TD_DMAX * (TD_TP + TD_TC) * sizeof(float)));
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
+        const int64_t blocks = ceil_div(n, TD_TP);
+        tile_dist_kernel<MODE><<<(unsigned)blocks, TD_THREADS, smem, s>>>(x, n, dim, cent, k, out_idx, out_dist,
+                                                                         out_mat);
+    } else {
+        rowwise_dist_kernel<MODE><<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(x, n, dim, cent, k, out_idx, out_dist,
+                                                                            out_mat);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assign_exact(const float* x, int64_t n, int dim, const float* cent, int k, int32_t* out_idx,
+                                float* out_dist, cudaStream_t s) {
+    return launch_tile<0>(x, n, dim, cent, k, out_idx, out_dist, nullptr, s);
+}
+
+cudaError_t launch_dist_matrix(const float* q, int64_t nq, int dim, const float* cent, int k, float* out,
+                               cudaStream_t s) {
+    return launch_tile<1>(q, nq, dim, cent, k, nullptr, nullptr, out, s);
+}
+
+// ---------------------------------------------------------------------------
+// k-means update: FP64 sums by global atomics, then mean rounded to FP32.
+__global__ void kmeans_accumulate_kernel(const float* __restrict__ x, int64_t n, int dim,
+                                         const int32_t* __restrict__ assign, double* __restrict__ sums,
+                                         int64_t* __restrict__ counts) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * dim) return;
+    const int64_t p = e / dim;
+    const int i = (int)(e - p * dim);
+    const int c = assign[p];
+    atomicAdd(&sums[(int64_t)c * dim + i], (double)x[e]);
+    if (i == 0) atomicAdd(reinterpret_cast<unsigned long long*>(&counts[c]), 1ull);
+}
+
+cudaError_t launch_kmeans_accumulate(const float* x, int64_t n, int dim, const int32_t* assign, double* sums,
+                                     int64_t* counts, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    kmeans_accumulate_kernel<<<(unsigned)ceil_div(n * dim, 256), 256, 0, s>>>(x, n, dim, assign, sums, counts);
+    return cudaGetLastError();
+}
+
+__global__ void kmeans_finalize_kernel(const double* __restrict__ sums, const int64_t* __restrict__ counts, int k,
+                                       int dim, float* __restrict__ cent) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)k * dim) return;
+    const int64_t c = e / dim;
+    const int64_t cnt = counts[c];
+    if (cnt > 0) cent[e] = (float)(sums[e] / (double)cnt);
+}
+
+cudaError_t launch_kmeans_finalize(const double* sums, const int64_t* counts, int k, int dim, float* cent,
+                                   cudaStream_t s) {
+    if (k <= 0) return cudaSuccess;
+    kmeans_finalize_kernel<<<(unsigned)ceil_div((int64_t)k * dim, 256), 256, 0, s>>>(sums, counts, k, dim, cent);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Product quantizer assignment: block = 256 points of one subquantizer, the
+// codebook in shared memory, the sub-vector in registers.
+template <int DSUB>
+__global__ void __launch_bounds__(256) pq_assign_kernel(const float* __restrict__ res, int64_t n, int M,
+                                                        const float* __restrict__ cb, int pqK, int m_begin,
+                                                        int32_t* __restrict__ out) {
+    extern __shared__ __align__(16) float scb[];
+    const int m = m_begin + blockIdx.y;
+    const int dim = M * DSUB;
+    for (int e = threadIdx.x; e < pqK * DSUB; e += blockDim.x) scb[e] = cb[(int64_t)m * pqK * DSUB + e];
+    __syncthreads();
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float sub[DSUB];
+#pragma unroll
+    for (int e = 0; e < DSUB; e++) sub[e] = res[p * dim + m * DSUB + e];
+    float bd = sqeuclid_ref(sub, scb, DSUB);
+    int bi = 0;
+    for (int j = 1; j < pqK; j++) {
+        const float d = sqeuclid_ref(sub, scb + j * DSUB, DSUB);
+        if (d < bd) {
+            bd = d;
+            bi = j;
+        }
+    }
+    out[p * M + m] = bi;
+}
+
+// Generic sub-dimension: sub-vector read from global memory.
+__global__ void __launch_bounds__(256) pq_assign_generic_kernel(const float* __restrict__ res, int64_t n, int M,
+                                                                int dsub, const float* __restrict__ cb, int pqK,
+                                                                int m_begin, int32_t* __restrict__ out) {
+    extern __shared__ __align__(16) float scb[];
+    const int m = m_begin + blockIdx.y;
+    const int dim = M * dsub;
+    for (int e = threadIdx.x; e < pqK * dsub; e += blockDim.x) scb[e] = cb[(int64_t)m * pqK * dsub + e];
+    __syncthreads();
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const float* sub = res + p * dim + m * dsub;
+    float bd = sqeuclid_ref(sub, scb, dsub);
+    int bi = 0;
+    for (int j = 1; j < pqK; j++) {
+        const float d = sqeuclid_ref(sub, scb + j * dsub, dsub);
+        if (d < bd) {
+            bd = d;
+            bi = j;
+        }
+    }
+    out[p * M + m] = bi;
+}
+
+cudaError_t launch_pq_assign(const float* res, int64_t n, int M, int dsub, const float* codebooks, int pqK,
+                             int m_begin, int m_end, int32_t* out, cudaStream_t s) {
+    if (n <= 0 || m_end <= m_begin) return cudaSuccess;
+    const size_t smem = (size_t)pqK * dsub * sizeof(float);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(pq_assign_generic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    dim3 grid((unsigned)ceil_div(n, 256), (unsigned)(m_end - m_begin));
+    switch (smem > 48 * 1024 ? 0 : dsub) {
+    case 1: pq_assign_kernel<1><<<grid, 256, smem, s>>>(res, n, M, codebooks, pqK, m_begin, out); break;
+    case 2: pq_assign_kernel<2><<<grid, 256, smem, s>>>(res, n, M, codebooks, pqK, m_begin, out); break;
+    case 4: pq_assign_kernel<4><<<grid, 256, smem, s>>>(res, n, M, codebooks, pqK, m_begin, out); break;
+    case 8: pq_assign_kernel<8><<<grid, 256, smem, s>>>(res, n, M, codebooks, pqK, m_begin, out); break;
+    case 16: pq_assign_kernel<16><<<grid, 256, smem, s>>>(res, n, M, codebooks, pqK, m_begin, out); break;
+    default:
+        pq_assign_generic_kernel<<<grid, 256, smem, s>>>(res, n, M, dsub, codebooks, pqK, m_begin, out);
+        break;
+    }
+    return cudaGetLastError();
+}
+
+__global__ void pq_accumulate_kernel(const float* __restrict__ res, int64_t n, int M, int dsub,
+                                     const int32_t* __restrict__ codes, int pqK, int m_begin, int m_cnt,
+                                     double* __restrict__ sums, int64_t* __restrict__ counts) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t per_point = (int64_t)m_cnt * dsub;
+    if (e >= n * per_point) return;
+    const int64_t p = e / per_point;
+    const int r = (int)(e - p * per_point);
+    const int m = m_begin + r / dsub;
+    const int i = r % dsub;
+    const int dim = M * dsub;
+    const int c = codes[p * M + m];
+    atomicAdd(&sums[((int64_t)m * pqK + c) * dsub + i], (double)res[p * dim + m * dsub + i]);
+    if (i == 0) atomicAdd(reinterpret_cast<unsigned long long*>(&counts[(int64_t)m * pqK + c]), 1ull);
+}
+
+cudaError_t launch_pq_accumulate(const float* res, int64_t n, int M, int dsub, const int32_t* codes, int pqK,
+                                 int m_begin, int m_end, double* sums, int64_t* counts, cudaStream_t s) {
+    if (n <= 0 || m_end <= m_begin) return cudaSuccess;
+    const int64_t total = n * (int64_t)(m_end - m_begin) * dsub;
+    pq_accumulate_kernel<<<(unsigned)ceil_div(total, 256), 256, 0, s>>>(res, n, M, dsub, codes, pqK, m_begin,
+                                                                       m_end - m_begin, sums, counts);
+    return cudaGetLastError();
+}
+
+__global__ void residuals_kernel(const float* __restrict__ x, const int64_t* __restrict__ src,
+                                 const int32_t* __restrict__ cluster, int64_t n, int dim,
+                                 const float* __restrict__ coarse, float* __restrict__ out) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * dim) return;
+    const int64_t r = e / dim;
+    const int i = (int)(e - r * dim);
+    const int64_t sr = src ? src[r] : r;
+    out[e] = x[sr * dim + i] - coarse[(int64_t)cluster[r] * dim + i];
+}
+
+cudaError_t launch_residuals(const float* x, const int64_t* src, const int32_t* cluster, int64_t n, int dim,
+                             const float* coarse, float* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    residuals_kernel<<<(unsigned)ceil_div(n * dim, 256), 256, 0, s>>>(x, src, cluster, n, dim, coarse, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Encoding: one thread per row, one subquantizer codebook at a time in
+// shared memory. The residual is x - c in FP32 (vectorSub,
+// pqivf/index.go:692-702); each code is the reference-order argmin.
+__global__ void __launch_bounds__(256) encode_kernel(const float* __restrict__ x, const int64_t* __restrict__ rows,
+                                                     const int32_t* __restrict__ cluster, int64_t n, int dim,
+                                                     const float* __restrict__ coarse,
+                                                     const float* __restrict__ cb, int M, int pqK,
+                                                     uint8_t* __restrict__ codes, int code_stride,
+                                                     float* __restrict__ term) {
+    extern __shared__ __align__(16) float scb[];
+    const int dsub = dim / M;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    const int64_t p = live ? (rows ? rows[i] : i) : 0;
+    const int cl = live ? cluster[p] : 0;
+    const float* xp = x + p * dim;
+    const float* cp = coarse + (int64_t)cl * dim;
+    float tsum = 0.0f;
+    struct Res {
+        const float* a;
+        const float* b;
+        __device__ float operator[](int t) const { return a[t] - b[t]; }
+    };
+    for (int m = 0; m < M; m++) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < pqK * dsub; e += blockDim.x) scb[e] = cb[(int64_t)m * pqK * dsub + e];
+        __syncthreads();
+        if (!live) continue;
+        const Res rs{xp + m * dsub, cp + m * dsub};
+        float bd = sqeuclid_ref(rs, scb, dsub);
+        int bi = 0;
+        for (int j = 1; j < pqK; j++) {
+            const float d = sqeuclid_ref(rs, scb + j * dsub, dsub);
+            if (d < bd) {
+                bd = d;
+                bi = j;
+            }
+        }
+        codes[p * code_stride + m] = (uint8_t)bi;
+        const float* w = scb + bi * dsub;
+        for (int e = 0; e < dsub; e++) tsum += w[e] * (w[e] + 2.0f * cp[m * dsub + e]);
+    }
+    if (live) {
+        for (int m = M; m < code_stride; m++) codes[p * code_stride + m] = 0;
+        term[p] = tsum;
+    }
+}
+
+cudaError_t launch_encode(const float* x, const int64_t* rows, const int32_t* cluster, int64_t n, int dim,
+                          const float* coarse, const float* codebooks, int M, int pqK, uint8_t* codes,
+                          int code_stride, float* term, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const size_t smem = (size_t)pqK * (dim / M) * sizeof(float);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(encode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    encode_kernel<<<(unsigned)ceil_div(n, 256), 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK,
+                                                                codes, code_stride, term);
+    return cudaGetLastError();
+}
+
+__global__ void term_kernel(const uint8_t* __restrict__ codes, const int64_t* __restrict__ rows,
+                            const int32_t* __restrict__ cluster, int64_t n, int dim, const float* __restrict__ coarse,
+                            const float* __restrict__ cb, int M, int pqK, int code_stride, float* __restrict__ term) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t p = rows ? rows[i] : i;
+    const int dsub = dim / M;
+    const float* cp = coarse + (int64_t)cluster[p] * dim;
+    float tsum = 0.0f;
+    for (int m = 0; m < M; m++) {
+        const float* w = cb + ((int64_t)m * pqK + codes[p * code_stride + m]) * dsub;
+        for (int e = 0; e < dsub; e++) tsum += w[e] * (w[e] + 2.0f * cp[m * dsub + e]);
+    }
+    term[p] = tsum;
+}
+
+cudaError_t launch_term(const uint8_t* codes, const int64_t* rows, const int32_t* cluster, int64_t n, int dim,
+                        const float* coarse, const float* codebooks, int M, int pqK, int code_stride, float* term,
+                        cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    term_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(codes, rows, cluster, n, dim, coarse, codebooks, M, pqK,
+                                                           code_stride, term);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Row movement.
+__global__ void copy_words_kernel(const uint32_t* __restrict__ in, const int64_t* __restrict__ src,
+                                  uint32_t* __restrict__ out, const int64_t* __restrict__ dst, int64_t n, int width) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * width) return;
+    const int64_t r = e / width;
+    const int j = (int)(e - r * width);
+    const int64_t sr = src ? src[r] : r;
+    const int64_t dr = dst ? dst[r] : r;
+    out[dr * width + j] = in[sr * width + j];
+}
+
+cudaError_t launch_copy_words(const void* in, const int64_t* src, void* out, const int64_t* dst, int64_t n, int width,
+                              cudaStream_t s) {
+    if (n <= 0 || width <= 0) return cudaSuccess;
+    copy_words_kernel<<<(unsigned)ceil_div(n * width, 256), 256, 0, s>>>(
+        static_cast<const uint32_t*>(in), src, static_cast<uint32_t*>(out), dst, n, width);
+    return cudaGetLastError();
+}
+
+__global__ void gather2_kernel(const float* __restrict__ a, const float* __restrict__ b,
+                               const int64_t* __restrict__ src, int64_t n, int dim, float* __restrict__ out) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * dim) return;
+    const int64_t r = e / dim;
+    const int j = (int)(e - r * dim);
+    const int64_t s = src[r];
+    out[e] = s >= 0 ? a[s * dim + j] : b[(-s - 1) * dim + j];
+}
+
+cudaError_t launch_gather2(const float* a, const float* b, const int64_t* src, int64_t n, int dim, float* out,
+                           cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    gather2_kernel<<<(unsigned)ceil_div(n * dim, 256), 256, 0, s>>>(a, b, src, n, dim, out);
+    return cudaGetLastError();
+}
+
+__global__ void gather_cols_kernel(const float* __restrict__ in, int64_t ld, int off, const int64_t* __restrict__ src,
+                                   const int32_t* __restrict__ dst, int64_t n, int w, float* __restrict__ out,
+                                   int64_t ldo) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * w) return;
+    const int64_t r = e / w;
+    const int j = (int)(e - r * w);
+    const int64_t dr = dst ? dst[r] : r;
+    out[dr * ldo + j] = in[src[r] * ld + off + j];
+}
+
+cudaError_t launch_gather_cols(const float* in, int64_t ld, int off, const int64_t* src, const int32_t* dst, int64_t n,
+                               int w, float* out, int64_t ldo, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    gather_cols_kernel<<<(unsigned)ceil_div(n * w, 256), 256, 0, s>>>(in, ld, off, src, dst, n, w, out, ldo);
+    return cudaGetLastError();
+}
+
+}  // namespace hann

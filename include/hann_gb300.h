@@ -1,0 +1,184 @@
+/*
+ * hann_gb300.h -- C ABI of the GB300 PQIVF index and the GPU distance layer.
+ *
+ * This is the boundary a host binding (the cgo package of a Go drop-in
+ * beside hann's pqivf, or the ctypes mirror in hann_gb300/__init__.py)
+ * calls. Plain pointers and sizes only. Every function returns 0 on success
+ * or a negative HANN_E* status; hann_pqivf_last_error() then describes the
+ * failure. Every host input is copied before the call returns, so a caller
+ * may free or reuse its buffers at once (the cgo rule against retained Go
+ * pointers). A handle is safe for concurrent use: mutations are exclusive and
+ * searches are serialised on the handle's stream.
+ *
+ * Each entry point names the reference interface it replaces (file:line in
+ * habedi/hann).
+ */
+#ifndef HANN_GB300_H
+#define HANN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define HANN_OK 0
+#define HANN_E_INVALID -1     /* invalid argument (dimension, k, parameter) */
+#define HANN_E_NOT_FOUND -2   /* id not present */
+#define HANN_E_EXISTS -3      /* id already present */
+#define HANN_E_STATE -4       /* not trained / empty index / not enough vectors */
+#define HANN_E_CUDA -5        /* CUDA runtime failure */
+#define HANN_E_NOMEM -6       /* device or host allocation failed */
+#define HANN_E_UNSUPPORTED -7 /* valid for the reference, outside this build's limits */
+
+typedef struct hann_pqivf hann_pqivf;
+
+/* Options of pqivf.New (pqivf/index.go:57-146). hann_pqivf_options_init
+ * fills the reference's defaults: coarse_k 16, pq_k 16, kmeans_iters 10,
+ * candidate_clusters 3, fallback on, num_subquantizers = the largest of
+ * 8/4/2/1 dividing the dimension (pqivf/index.go:106-157); the With*
+ * options then overwrite single fields. */
+typedef struct {
+    int32_t dimension;
+    int32_t coarse_k;           /* WithCoarseK */
+    int32_t num_subquantizers;  /* WithNumSubquantizers */
+    int32_t pq_k;               /* WithPQK; this build stores uint8 codes, so pq_k <= 256 */
+    int32_t kmeans_iters;       /* WithKMeansIters */
+    int32_t candidate_clusters; /* WithCandidateClusters (nprobe) */
+    int32_t fallback;           /* WithBruteForceFallback: 1 on, 0 off */
+    uint64_t seed;              /* plays HANN_SEED's role (core/utils.go:12-20) */
+    int32_t device;             /* CUDA device ordinal */
+    int32_t rerank;             /* candidates rescored exactly per query; 0 = automatic */
+} hann_pqivf_options;
+
+/* Defaults of pqivf.New for the given dimension (pqivf/index.go:106-157). */
+void hann_pqivf_options_init(hann_pqivf_options* opts, int32_t dimension);
+
+/* core.IndexStats (core/index.go:131-140). */
+typedef struct {
+    int64_t count;
+    int32_t dimension;
+    int64_t fallback_searches;
+    int32_t trained;
+    int32_t nlist;
+    int64_t rows_capacity;
+} hann_pqivf_index_stats;
+
+/* pqivf.New (pqivf/index.go:106-146). Validation errors as the reference. */
+int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out);
+void hann_pqivf_free(hann_pqivf* h);
+/* Message of the last failure on this handle (or of the last failed
+ * hann_pqivf_new on this thread when h is NULL). */
+const char* hann_pqivf_last_error(const hann_pqivf* h);
+
+/* Index.Add (core/index.go:25; pqivf/index.go:212-237). */
+int hann_pqivf_add(hann_pqivf* h, int64_t id, const float* vector);
+/* BulkIndex.BulkAdd (core/index.go:57; pqivf/index.go:266-297): applied in
+ * ascending id order; stops at the first failing id, keeping earlier ones. */
+int hann_pqivf_bulk_add(hann_pqivf* h, const int64_t* ids, const float* vectors, int64_t n);
+/* Index.Delete (core/index.go:29; pqivf/index.go:300-345). */
+int hann_pqivf_delete(hann_pqivf* h, int64_t id);
+/* BulkIndex.BulkDelete (core/index.go:60; pqivf/index.go:350-384): unknown
+ * ids are skipped. */
+int hann_pqivf_bulk_delete(hann_pqivf* h, const int64_t* ids, int64_t n);
+/* Index.Update (core/index.go:34; pqivf/index.go:402-413). */
+int hann_pqivf_update(hann_pqivf* h, int64_t id, const float* vector);
+/* BulkIndex.BulkUpdate (core/index.go:63; pqivf/index.go:419-444). */
+int hann_pqivf_bulk_update(hann_pqivf* h, const int64_t* ids, const float* vectors, int64_t n);
+
+/* Trainer.Train (core/index.go:68; pqivf/index.go:451-605). */
+int hann_pqivf_train(hann_pqivf* h);
+/* Train with explicit k-means seeding, replacing the reference's draws from
+ * its package RNG (pqivf/index.go:804-810, 830-837): coarse_init holds
+ * coarse_k row indices into the id-sorted data (its Perm(n)[:k]); pq_init
+ * holds num_subquantizers x pq_k row indices into each subquantizer's
+ * residual data; reseed is the stream of row indices used in order for
+ * every empty cluster (coarse run first, then subquantizer 0, 1, ...).
+ * Any pointer may be NULL to draw from the handle's seeded generator. */
+int hann_pqivf_train_seeded(hann_pqivf* h, const int64_t* coarse_init, const int64_t* pq_init,
+                            const int64_t* reseed, int64_t n_reseed);
+
+/* Index.Search (core/index.go:38; pqivf/index.go:850-949) for one query:
+ * ids/distances (true Euclidean distance as float64) of up to k neighbours
+ * in non-decreasing order; *n_out receives the count. */
+int hann_pqivf_search(hann_pqivf* h, const float* query, int32_t k, int64_t* ids, double* distances,
+                      int32_t* n_out);
+
+/* Batched Search: nq independent Search calls in one device pass. k and
+ * nprobe are per query (nprobe NULL = the index's candidate clusters).
+ * Row i of ids/distances starts at i * kmax. mode 0 returns the reference's
+ * reconstructed-vector PQ distances (parity); mode 1 reranks the candidates
+ * against the stored raw vectors (exact distances, higher recall). */
+int hann_pqivf_search_batch(hann_pqivf* h, const float* queries, int64_t nq, const int32_t* k,
+                            const int32_t* nprobe, int32_t kmax, int32_t mode, int64_t* ids, double* distances,
+                            int32_t* n_out);
+
+/* Same as hann_pqivf_search_batch with every buffer in device memory and
+ * the work enqueued on `stream` (a cudaStream_t, NULL = the handle's own);
+ * k and nprobe are uniform. Returns once enqueued. */
+int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k, int32_t nprobe,
+                                   int32_t mode, int64_t* d_ids, double* d_distances, int32_t* d_n_out,
+                                   void* stream);
+
+/* Diagnostics (no reference counterpart). With profiling on, every search
+ * stage is bracketed by CUDA events on the stream it runs on and the list
+ * scan counts the rows it reads; hann_pqivf_stage_times waits for the events
+ * and returns the accumulated device milliseconds of the stages [coarse
+ * distances, probe select, list scan, rerank], the kernel launch count and
+ * the rows scanned, then clears them. */
+int hann_pqivf_set_profiling(hann_pqivf* h, int32_t on);
+int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_t* rows_scanned);
+/* Current length of every inverted list (nlist entries). */
+int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out);
+
+/* Index.Stats (core/index.go:41; pqivf/index.go:953-966). */
+int hann_pqivf_stats(hann_pqivf* h, hann_pqivf_index_stats* out);
+
+/* ---- persisted state (Save/Load, pqivf/index.go:969-1101) ----------------
+ * The binding encodes/decodes the reference's gob stream itself and moves
+ * the arrays through these calls. */
+typedef struct {
+    int32_t dimension, coarse_k, num_subquantizers, pq_k, kmeans_iters, candidate_clusters, fallback, trained;
+    int32_t nlist;          /* rows of coarse centroids */
+    int32_t pq_k_eff;       /* codewords per subquantizer actually trained */
+    int64_t n_rows;         /* entries held in inverted lists */
+    int64_t n_pending;      /* vectors waiting for Train */
+} hann_pqivf_layout;
+
+int hann_pqivf_export_layout(hann_pqivf* h, hann_pqivf_layout* out);
+/* Arrays sized from the layout: coarse [nlist*dim], codebooks
+ * [M*pq_k_eff*(dim/M)], list_len [nlist], list_key [nlist] (1 when the
+ * reference's list map holds the cluster), cluster_counts [nlist], ids
+ * [n_rows] (list by list, in storage order), vectors [n_rows*dim], codes
+ * [n_rows*M] (int32), pending_ids [n_pending], pending_vectors
+ * [n_pending*dim]. */
+int hann_pqivf_export(hann_pqivf* h, float* coarse, float* codebooks, int64_t* list_len, uint8_t* list_key,
+                      int64_t* cluster_counts, int64_t* ids, float* vectors, int32_t* codes, int64_t* pending_ids,
+                      float* pending_vectors);
+/* Replaces the handle's state (GobDecode, pqivf/index.go:1020-1084). Codes
+ * of an entry with has_codes[i] == 0 are recomputed on the device. */
+int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* layout, const float* coarse, const float* codebooks,
+                      const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
+                      const int64_t* ids, const float* vectors, const int32_t* codes, const uint8_t* has_codes,
+                      const int64_t* pending_ids, const float* pending_vectors);
+
+/* ---- distance layer (core/simd_distance.h:30-33, core/metric.go:64-99) ----
+ * metric: 0 squared Euclidean, 1 Euclidean, 2 Manhattan, 3 cosine. */
+#define HANN_METRIC_SQEUCLID 0
+#define HANN_METRIC_EUCLID 1
+#define HANN_METRIC_MANHATTAN 2
+#define HANN_METRIC_COSINE 3
+
+/* simd_<metric>_batch (core/simd_kernels.inc.h:235-264): distance from one
+ * query to n rows of flat, FP32 in the reference's NEON summation order,
+ * widened to double. Host buffers. */
+int hann_gpu_distance_batch(int32_t metric, const float* query, const float* flat, size_t dim, size_t n,
+                            double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HANN_GB300_H */
