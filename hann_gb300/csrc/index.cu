@@ -290,7 +290,9 @@ static int assign_batch(hann_pqivf* h, const int64_t* ids, const float* vecs, in
     CK(asg.reserve((size_t)n));
     CK(term.reserve((size_t)n));
     CK(codes.reserve((size_t)n * h->code_stride));
-    CK(launch_assign_exact(x.p, n, dim, h->d_coarse.p, h->nlist, asg.p, nullptr, h->stream));
+    DBuf<unsigned long long> keys;
+    CK(keys.reserve((size_t)n));
+    CK(launch_assign_exact(x.p, n, dim, h->d_coarse.p, h->nlist, asg.p, nullptr, keys.p, h->stream));
     CK(launch_encode(x.p, nullptr, asg.p, n, dim, h->d_coarse.p, h->d_codebooks.p, M, h->pqk_eff, codes.p,
                      h->code_stride, term.p, h->stream));
     std::vector<int32_t> hasg((size_t)n);
@@ -428,7 +430,7 @@ static int kmeans_device(hann_pqivf* h, const float* x, int64_t ld, int off, int
     std::vector<int64_t> hcounts(k);
     for (int it = 0; it < iters; it++) {
         if (!sub_mode) {
-            CK(launch_assign_exact(x, n, dim, cent, k, asg_buf, nullptr, h->stream));
+            CK(launch_assign_exact(x, n, dim, cent, k, asg_buf, nullptr, nullptr, h->stream));
             CK(cudaMemsetAsync(sums.p, 0, (size_t)k * dim * sizeof(double), h->stream));
             CK(cudaMemsetAsync(counts.p, 0, (size_t)k * sizeof(int64_t), h->stream));
             CK(launch_kmeans_accumulate(x, n, dim, asg_buf, sums.p, counts.p, h->stream));
@@ -525,7 +527,7 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
                            0);
     if (rc) return rc;
     // Final assignment and inverted lists in ascending (cluster, id) order.
-    CK(launch_assign_exact(X.p, n, dim, C.p, k, asg.p, nullptr, h->stream));
+    CK(launch_assign_exact(X.p, n, dim, C.p, k, asg.p, nullptr, nullptr, h->stream));
     std::vector<int32_t> hasg(n);
     CK(cudaMemcpyAsync(hasg.data(), asg.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));

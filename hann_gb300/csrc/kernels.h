@@ -11,9 +11,12 @@ namespace hann {
 
 // For every point, the index of the nearest centroid under the reference-order
 // FP32 squared Euclidean distance, the lowest index winning a tie
-// (assignPoints, pqivf/index.go:738-789). out_dist may be null.
+// (assignPoints, pqivf/index.go:738-789). out_dist may be null. key_scratch
+// (n entries, may be null) lets small batches split the centroids over more
+// blocks.
 cudaError_t launch_assign_exact(const float* x, int64_t n, int dim, const float* cent, int k,
-                                int32_t* out_idx, float* out_dist, cudaStream_t s);
+                                int32_t* out_idx, float* out_dist, unsigned long long* key_scratch,
+                                cudaStream_t s);
 
 // Full matrix D[q][c] of reference-order squared Euclidean distances.
 cudaError_t launch_dist_matrix(const float* q, int64_t nq, int dim, const float* cent, int k,

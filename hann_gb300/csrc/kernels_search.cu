@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(ScanParams p, const fl
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int64_t q = blockIdx.x;
     const float* qv = Q + q * p.dim;
-    if (tid == 0) s_tau = 0xffffffffu;
+    if (tid == 0) s_tau = float_key(F_INF);
     for (int e = tid; e < p.M * 256; e += SC_THREADS) {
         const int m = e >> 8, j = e & 255;
         float s = 0.0f;

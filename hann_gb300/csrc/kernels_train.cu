@@ -9,6 +9,8 @@
 #include "common.cuh"
 #include "kernels.h"
 
+#include <algorithm>
+
 namespace hann {
 
 // ---------------------------------------------------------------------------
@@ -118,12 +120,18 @@ __device__ __forceinline__ void tile_pairs(const float* __restrict__ Xs, const f
 }
 
 // MODE 0: argmin per point. MODE 1: full distance matrix.
+// The centroid range is split over gridDim.y blocks (tiles_per_split tiles
+// each); with more than one split an argmin is combined across blocks by a
+// 64-bit atomicMin on (distance key, index), which keeps the lowest index on
+// a tie.
 template <int MODE>
 __global__ void __launch_bounds__(TD_THREADS) tile_dist_kernel(const float* __restrict__ x, int64_t n, int dim,
                                                                const float* __restrict__ cent, int k,
+                                                               int tiles_per_split,
                                                                int32_t* __restrict__ out_idx,
                                                                float* __restrict__ out_dist,
-                                                               float* __restrict__ out_mat) {
+                                                               float* __restrict__ out_mat,
+                                                               unsigned long long* __restrict__ out_key) {
     extern __shared__ __align__(16) float sm[];
     float* Xs = sm;
     float* Cs = sm + dim * TD_TP;
@@ -144,7 +152,9 @@ __global__ void __launch_bounds__(TD_THREADS) tile_dist_kernel(const float* __re
         best_d[a] = __int_as_float(0x7f800000);
         best_i[a] = 0x7fffffff;
     }
-    for (int c0 = 0; c0 < k; c0 += TD_TC) {
+    const int c_begin = blockIdx.y * tiles_per_split * TD_TC;
+    const int c_end = min(k, c_begin + tiles_per_split * TD_TC);
+    for (int c0 = c_begin; c0 < c_end; c0 += TD_TC) {
         __syncthreads();
         for (int e = tid; e < TD_TC * dim; e += TD_THREADS) {
             const int c = e / dim, i = e - c * dim;
@@ -197,10 +207,15 @@ __global__ void __launch_bounds__(TD_THREADS) tile_dist_kernel(const float* __re
             }
             const int64_t gp = p0 + tid;
             if (gp < n) {
-                // No finite distance at all (NaN input): the reference keeps
-                // index 0 (pqivf/index.go:772-778).
-                out_idx[gp] = bi == 0x7fffffff ? 0 : bi;
-                if (out_dist) out_dist[gp] = bd;
+                if (gridDim.y > 1) {
+                    if (bi != 0x7fffffff)
+                        atomicMin(&out_key[gp], ((unsigned long long)float_key(bd) << 32) | (uint32_t)bi);
+                } else {
+                    // No finite distance at all (NaN input): the reference
+                    // keeps index 0 (pqivf/index.go:772-778).
+                    out_idx[gp] = bi == 0x7fffffff ? 0 : bi;
+                    if (out_dist) out_dist[gp] = bd;
+                }
             }
         }
     }
@@ -233,9 +248,19 @@ __global__ void rowwise_dist_kernel(const float* __restrict__ x, int64_t n, int 
     }
 }
 
+__global__ void unpack_argmin_kernel(const unsigned long long* __restrict__ key, int64_t n, int32_t* __restrict__ idx,
+                                     float* __restrict__ dist) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const unsigned long long v = key[p];
+    const bool none = v == ~0ull;
+    idx[p] = none ? 0 : (int32_t)(uint32_t)(v & 0xffffffffull);
+    if (dist) dist[p] = none ? __int_as_float(0x7fc00000) : key_float((uint32_t)(v >> 32));
+}
+
 template <int MODE>
 static cudaError_t launch_tile(const float* x, int64_t n, int dim, const float* cent, int k, int32_t* out_idx,
-                               float* out_dist, float* out_mat, cudaStream_t s) {
+                               float* out_dist, float* out_mat, unsigned long long* key_scratch, cudaStream_t s) {
     if (n <= 0 || k <= 0) return cudaSuccess;
     if (dim <= TD_DMAX) {
         const size_t smem = (size_t)dim * (TD_TP + TD_TC) * sizeof(float);
@@ -247,8 +272,20 @@ static cudaError_t launch_tile(const float* x, int64_t n, int dim, const float* 
             attr_set = true;
         }
         const int64_t blocks = ceil_div(n, TD_TP);
-        tile_dist_kernel<MODE><<<(unsigned)blocks, TD_THREADS, smem, s>>>(x, n, dim, cent, k, out_idx, out_dist,
-                                                                         out_mat);
+        const int tiles = (int)ceil_div(k, TD_TC);
+        // Enough blocks for two waves of one block per SM.
+        int splits = (int)std::min<int64_t>(tiles, std::max<int64_t>(1, ceil_div(2 * 152, blocks)));
+        if (MODE == 0 && key_scratch == nullptr) splits = 1;
+        const int per = (int)ceil_div(tiles, splits);
+        splits = (int)ceil_div(tiles, per);
+        if (MODE == 0 && splits > 1) {
+            cudaError_t e = cudaMemsetAsync(key_scratch, 0xff, (size_t)n * sizeof(unsigned long long), s);
+            if (e != cudaSuccess) return e;
+        }
+        tile_dist_kernel<MODE><<<dim3((unsigned)blocks, (unsigned)splits), TD_THREADS, smem, s>>>(
+            x, n, dim, cent, k, per, out_idx, out_dist, out_mat, key_scratch);
+        if (MODE == 0 && splits > 1)
+            unpack_argmin_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(key_scratch, n, out_idx, out_dist);
     } else {
         rowwise_dist_kernel<MODE><<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(x, n, dim, cent, k, out_idx, out_dist,
                                                                             out_mat);
@@ -257,13 +294,13 @@ static cudaError_t launch_tile(const float* x, int64_t n, int dim, const float* 
 }
 
 cudaError_t launch_assign_exact(const float* x, int64_t n, int dim, const float* cent, int k, int32_t* out_idx,
-                                float* out_dist, cudaStream_t s) {
-    return launch_tile<0>(x, n, dim, cent, k, out_idx, out_dist, nullptr, s);
+                                float* out_dist, unsigned long long* key_scratch, cudaStream_t s) {
+    return launch_tile<0>(x, n, dim, cent, k, out_idx, out_dist, nullptr, key_scratch, s);
 }
 
 cudaError_t launch_dist_matrix(const float* q, int64_t nq, int dim, const float* cent, int k, float* out,
                                cudaStream_t s) {
-    return launch_tile<1>(q, nq, dim, cent, k, nullptr, nullptr, out, s);
+    return launch_tile<1>(q, nq, dim, cent, k, nullptr, nullptr, out, nullptr, s);
 }
 
 // ---------------------------------------------------------------------------
