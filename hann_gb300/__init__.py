@@ -94,7 +94,7 @@ EXPORTED = (
     "hann_pqivf_bulk_update", "hann_pqivf_train", "hann_pqivf_train_seeded", "hann_pqivf_search",
     "hann_pqivf_search_batch", "hann_pqivf_search_batch_device", "hann_pqivf_stats", "hann_pqivf_export_layout",
     "hann_pqivf_export", "hann_pqivf_import", "hann_gpu_distance_batch", "hann_pqivf_set_profiling",
-    "hann_pqivf_stage_times", "hann_pqivf_list_lengths",
+    "hann_pqivf_stage_times", "hann_pqivf_list_lengths", "hann_pqivf_search_batch_device_noalloc",
 )
 
 

@@ -1297,3 +1297,117 @@ int hann_gpu_distance_batch(int32_t metric, const float* query, const float* fla
 }
 
 }  // extern "C"
+// ---------------------------------------------------------------------------
+// Allocation-free batch search.
+//
+// Some callers cannot allocate device memory at the moment they search: a
+// latency-bound serving thread must not stall on the device-wide
+// synchronisation that cudaMalloc/cudaFree may imply; code that records its
+// launches into a CUDA graph may not call the allocator while the stream is
+// being captured; and a process that fixes its device-memory budget at start
+// must not grow it per request. hann_pqivf_search_batch_device_noalloc serves
+// them. It runs the same kernels as hann_pqivf_search_batch_device, but every
+// scratch buffer of the search (coarse distance matrix, probe lists,
+// fallback flags, candidates, per-query k and nprobe, the fallback counter)
+// is carved out of one fixed device array of NOALLOC_ARENA_BYTES that every
+// GPU which loads this library holds until the process exits. The index's
+// own arrays were allocated when it was built; the call allocates nothing.
+
+namespace {
+
+constexpr size_t NOALLOC_ARENA_BYTES = (size_t)16 << 20;  // 16 MiB per device
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+// Host code must not take this symbol's address directly: on the host it is
+// only a stand-in. The device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_arena[NOALLOC_ARENA_BYTES];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the arena on the current device `dev`, looked up once.
+cudaError_t noalloc_arena(int dev, unsigned char** out) {
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_arena);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+    return cudaSuccess;
+}
+
+__global__ void noalloc_fill_kernel(int32_t* a, int32_t va, int32_t* b, int32_t vb, int64_t n,
+                                    unsigned long long* counter) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *counter = 0ull;
+    if (i < n) {
+        a[i] = va;
+        b[i] = vb;
+    }
+}
+
+size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+}  // namespace
+
+extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k,
+                                                      int32_t nprobe, int32_t mode, int64_t* d_ids,
+                                                      double* d_distances, int32_t* d_n_out, void* stream) {
+    if (!h) return HANN_E_INVALID;
+    std::shared_lock<std::shared_mutex> lk(h->mu);
+    std::lock_guard<std::mutex> rl(h->run_mu);
+    cudaSetDevice(h->o.device);
+    if (k <= 0) return h->fail(HANN_E_INVALID, "k must be positive");
+    if (nprobe <= 0) nprobe = h->o.candidate_clusters;
+    if (mode != 0 && mode != 1) return h->fail(HANN_E_INVALID, "mode must be 0 or 1");
+    int rc = check_searchable(h);
+    if (rc) return rc;
+    if (nq <= 0) return HANN_OK;
+    const int np = std::min<int>(nprobe, h->nlist);
+    const int R = rerank_depth(h, k, mode);
+    if (R > 480) return h->fail(HANN_E_UNSUPPORTED, "k (%d) above this build's limit of 448", k);
+    if (np > 4096) return h->fail(HANN_E_UNSUPPORTED, "more than 4096 probed lists per query");
+    // Scratch layout inside the arena, every region 256-byte aligned.
+    const size_t b_D = align256((size_t)nq * h->nlist * sizeof(float));
+    const size_t b_pid = align256((size_t)nq * np * sizeof(int32_t));
+    const size_t b_pd = align256((size_t)nq * np * sizeof(float));
+    const size_t b_q32 = align256((size_t)nq * sizeof(int32_t));
+    const size_t b_cr = align256((size_t)nq * R * sizeof(int32_t));
+    const size_t b_cd = align256((size_t)nq * R * sizeof(float));
+    const size_t b_cs = align256((size_t)nq * R * sizeof(uint32_t));
+    const size_t need = b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd + b_cs + 256;
+    if (need > NOALLOC_ARENA_BYTES)
+        return h->fail(HANN_E_UNSUPPORTED,
+                       "allocation-free search of %lld queries needs %zu bytes of scratch, above its fixed %zu-byte "
+                       "arena; split the batch (at most about %lld queries at nlist %d, nprobe %d, k %d)",
+                       (long long)nq, need, NOALLOC_ARENA_BYTES,
+                       (long long)(NOALLOC_ARENA_BYTES / (need / nq + 1)), h->nlist, np, k);
+    unsigned char* base = nullptr;
+    CK(noalloc_arena(h->o.device, &base));
+    float* D = reinterpret_cast<float*>(base);
+    int32_t* pid = reinterpret_cast<int32_t*>(base + b_D);
+    float* pd = reinterpret_cast<float*>(base + b_D + b_pid);
+    int32_t* fb = reinterpret_cast<int32_t*>(base + b_D + b_pid + b_pd);
+    int32_t* dk = reinterpret_cast<int32_t*>(base + b_D + b_pid + b_pd + b_q32);
+    int32_t* dnp = reinterpret_cast<int32_t*>(base + b_D + b_pid + b_pd + 2 * b_q32);
+    int32_t* crow = reinterpret_cast<int32_t*>(base + b_D + b_pid + b_pd + 3 * b_q32);
+    float* cd = reinterpret_cast<float*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr);
+    uint32_t* cs = reinterpret_cast<uint32_t*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd);
+    unsigned long long* fbc =
+        reinterpret_cast<unsigned long long*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd + b_cs);
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    // The arena keeps the previous call's contents: the per-query k and
+    // nprobe and the fallback counter are written first; every other region
+    // is fully written by the kernel that produces it before it is read.
+    noalloc_fill_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(dk, k, dnp, np, nq, fbc);
+    CK(cudaGetLastError());
+    const ScanParams p = h->scan_params();
+    CK(launch_dist_matrix(d_queries, nq, h->o.dimension, h->d_coarse.p, h->nlist, D, s));
+    CK(launch_probe_select(D, nq, h->nlist, dnp, np, dk, h->d_len.p, h->o.fallback ? 1 : 0, pid, pd, fb, fbc, s));
+    CK(launch_scan(p, d_queries, nq, pid, D, dnp, np, fb, R, crow, cd, cs, nullptr, s));
+    CK(launch_rerank(p, d_queries, nq, crow, cs, R, dk, k, mode, d_ids, d_distances, d_n_out, s));
+    return HANN_OK;
+}

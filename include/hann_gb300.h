@@ -133,6 +133,25 @@ int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_
 /* Current length of every inverted list (nlist entries). */
 int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out);
 
+/* Allocation-free variant of hann_pqivf_search_batch_device. It has no
+ * counterpart in the reference. It is for callers that cannot allocate
+ * device memory while they search: a serving thread that must not stall on
+ * the device-wide synchronisation cudaMalloc/cudaFree may cause, code that
+ * records the search into a CUDA graph (no allocator calls while a stream is
+ * captured), or a process whose device-memory budget is fixed at start-up.
+ * All scratch comes from one fixed 16 MiB device array that every GPU which
+ * loads this library holds until the process exits; a batch whose scratch
+ * (about nq * (4 * nlist + 8 * nprobe + 12 * rerank depth + 12) bytes) does
+ * not fit is rejected with HANN_E_UNSUPPORTED and a message that says so.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the array, so calls whose work overlaps on the GPU
+ * (different streams, threads or handles) race; serialise them. Like the
+ * call it mirrors, it does not update FallbackSearches. */
+int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k,
+                                           int32_t nprobe, int32_t mode, int64_t* d_ids, double* d_distances,
+                                           int32_t* d_n_out, void* stream);
+
 /* Index.Stats (core/index.go:41; pqivf/index.go:953-966). */
 int hann_pqivf_stats(hann_pqivf* h, hann_pqivf_index_stats* out);
 
