@@ -59,7 +59,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--json-extra", action="store_true", help="print extra diagnostics to stderr")
+    ap.add_argument("--profile-region", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
+    ap.add_argument("--serve-seconds", type=float, default=8.0, help="served-stream phase length (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=5000.0, help="Poisson request arrivals per second")
     return ap.parse_args()
 
 
@@ -334,10 +337,15 @@ def main():
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    if args.profile_region:
+        torch.cuda.profiler.start()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
+    if args.profile_region:
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     torch.cuda.synchronize()
     barrier(ws)
     ms = e0.elapsed_time(e1)
@@ -406,6 +414,14 @@ def main():
         except Exception:
             pass
 
+    served = None
+    if args.serve_seconds > 0:
+        try:
+            served = serve_stream(args, idx, q_host, gt, nr)
+        except Exception as e:  # pragma: no cover
+            log("served stream failed:", e)
+            served = {"error": str(e)}
+
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -431,7 +447,11 @@ def main():
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "clocks": clocks,
+            "served_stream": served,
         }
+        if served and "p50_ms" in served:
+            line["p50_ms"] = served["p50_ms"]
+            line["p99_ms"] = served["p99_ms"]
         print(json.dumps(line), flush=True)
     idx.close()
     if ws > 1:
@@ -439,6 +459,93 @@ def main():
 
         dist.destroy_process_group()
     return 0
+
+
+def serve_stream(args, idx, q_host, gt, nr):
+    """The served stream: Poisson arrivals at --serve-rate requests/s, each a
+    block of 1-512 queries (log-uniform), k uniform in [1, 100], nprobe
+    log-uniform in [8, 256]; BulkAdd of 1,000-vector chunks and Deletes of
+    random ids, each at 1% of the request rate, applied between batches.
+    Queries are drawn from the first `nr` queries (which have ground truth).
+    Reports p50/p99 latency (submit to result), queries/s and recall@10 of
+    requests with k >= 10."""
+    import threading
+    import queue as qmod
+
+    import hann_gb300 as hg
+
+    rng = np.random.default_rng(args.seed + 7)
+    srv = hg.Server(idx, slots=4, max_batch_queries=8192, max_k=100, max_nprobe=256, mode=1,
+                    memory_budget=120 << 30)
+    pending = qmod.Queue()
+    results = []
+    stop = threading.Event()
+
+    def waiter():
+        while True:
+            item = pending.get()
+            if item is None:
+                return
+            kind, t, meta = item
+            r = srv.wait(t, timeout_ms=120000)
+            if kind == 0:
+                results.append((meta, r))
+
+    ws = [threading.Thread(target=waiter, daemon=True) for _ in range(4)]
+    for w in ws:
+        w.start()
+    next_id = 50_000_000
+    t0 = time.perf_counter()
+    t_next = t0
+    sent = 0
+    while True:
+        now = time.perf_counter()
+        if now - t0 > args.serve_seconds:
+            break
+        if now < t_next:
+            time.sleep(min(t_next - now, 0.001))
+            continue
+        t_next += rng.exponential(1.0 / args.serve_rate)
+        u = rng.random()
+        if u < 0.01:
+            # random unit vectors: far from every query, so they do not
+            # disturb the recall measured against the original ground truth
+            chunk = rng.standard_normal((1000, q_host.shape[1])).astype(np.float32)
+            chunk /= np.linalg.norm(chunk, axis=1, keepdims=True)
+            ids = np.arange(next_id, next_id + 1000)
+            next_id += 1000
+            pending.put((1, srv.submit_add(ids, chunk), None))
+            continue
+        if u < 0.02:
+            pending.put((2, srv.submit_delete(rng.integers(0, args.n, 100)), None))
+            continue
+        nq = int(np.exp(rng.uniform(0, np.log(512))))
+        k = int(rng.integers(1, 101))
+        npb = int(np.exp(rng.uniform(np.log(8), np.log(256))))
+        rows = rng.integers(0, nr, nq)
+        pending.put((0, srv.submit(q_host[rows], k, npb), (rows, k)))
+        sent += 1
+    for _ in ws:
+        pending.put(None)
+    for w in ws:
+        w.join()
+    st = srv.stats()
+    srv.stop()
+    hits = tot = 0
+    for (rows, k), (ids, dist, n, lat) in results:
+        if k < 10:
+            continue
+        for j, r in enumerate(rows):
+            hits += len(set(ids[j, :10].tolist()) & set(gt[r].tolist()))
+            tot += 10
+    return {"requests": int(st["requests"]), "queries": int(st["queries"]), "batches": int(st["batches"]),
+            "mutations": int(st["mutations"]), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+            "queries_per_s": st["queries_per_s"], "offered_requests_per_s": args.serve_rate,
+            "recall_at_10_k_ge_10": hits / tot if tot else None,
+            "peak_admitted_bytes": int(st["peak_admitted_bytes"]), "relayouts": int(st["relayouts"]),
+            "mutation_ms_total": round(st["mutation_ms"], 1),
+            "stream": "Poisson arrivals; 1-512 queries/request log-uniform; k U[1,100]; nprobe log-U[8,256]; "
+                      "BulkAdd 1000-vector chunks and Deletes at 1% of the request rate; exact rerank"}
 
 
 def workload_config(args, nprobe, mode, rec):

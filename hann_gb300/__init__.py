@@ -546,3 +546,117 @@ def distance_batch(metric: int, query, flat) -> np.ndarray:
     if rc != HANN_OK:
         raise HannError(rc, "distance batch failed")
     return out
+
+
+# ---------------------------------------------------------------------------
+# continuous-batching server
+
+
+class _ServeOptions(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int32), ("max_batch_queries", ctypes.c_int32), ("max_k", ctypes.c_int32),
+                ("max_nprobe", ctypes.c_int32), ("mode", ctypes.c_int32), ("memory_budget", ctypes.c_int64)]
+
+
+class _ServeStats(ctypes.Structure):
+    _fields_ = [("requests", ctypes.c_int64), ("queries", ctypes.c_int64), ("batches", ctypes.c_int64),
+                ("mutations", ctypes.c_int64), ("peak_admitted_bytes", ctypes.c_int64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("queries_per_s", ctypes.c_double), ("relayouts", ctypes.c_int64),
+                ("mutation_ms", ctypes.c_double)]
+
+
+def _serve_lib():
+    L = load_library()
+    if getattr(L, "_serve_ready", False):
+        return L
+    L.hann_serve_options_init.argtypes = [ctypes.POINTER(_ServeOptions)]
+    L.hann_serve_options_init.restype = None
+    L.hann_serve_start.argtypes = [_P, ctypes.POINTER(_ServeOptions), ctypes.POINTER(_P)]
+    L.hann_serve_submit.argtypes = [_P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.POINTER(ctypes.c_uint64)]
+    L.hann_serve_submit_add.argtypes = [_P, _P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
+    L.hann_serve_submit_delete.argtypes = [_P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
+    L.hann_serve_wait.argtypes = [_P, ctypes.c_uint64, _P, _P, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+    L.hann_serve_stats.argtypes = [_P, ctypes.POINTER(_ServeStats)]
+    L.hann_serve_last_error.argtypes = [_P]
+    L.hann_serve_last_error.restype = ctypes.c_char_p
+    L.hann_serve_stop.argtypes = [_P]
+    L._serve_ready = True
+    return L
+
+
+class Server:
+    """Continuous-batching server over an Index (hann_serve_* in the C ABI).
+
+    submit() may be called from many threads; wait() returns the request's
+    (ids [nq, k], distances [nq, k], counts [nq], latency_ms)."""
+
+    def __init__(self, index: Index, slots=4, max_batch_queries=4096, max_k=100, max_nprobe=256,
+                 mode=MODE_EXACT_RERANK, memory_budget=120 << 30):
+        L = _serve_lib()
+        o = _ServeOptions()
+        L.hann_serve_options_init(ctypes.byref(o))
+        o.slots, o.max_batch_queries, o.max_k, o.max_nprobe = slots, max_batch_queries, max_k, max_nprobe
+        o.mode, o.memory_budget = mode, memory_budget
+        h = _P()
+        rc = L.hann_serve_start(index.handle, ctypes.byref(o), ctypes.byref(h))
+        if rc != HANN_OK:
+            raise HannError(rc, L.hann_pqivf_last_error(index.handle).decode())
+        self._L, self._h, self._index, self._dim = L, h, index, index.dimension
+        self._meta = {}
+        self._meta_lock = threading.Lock()
+
+    def _check(self, rc):
+        if rc != HANN_OK:
+            raise HannError(rc, self._L.hann_serve_last_error(self._h).decode())
+
+    def submit(self, queries, k: int, nprobe: int = 0) -> int:
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self._dim)
+        t = ctypes.c_uint64(0)
+        self._check(self._L.hann_serve_submit(self._h, _ptr(q), q.shape[0], int(k), int(nprobe), ctypes.byref(t)))
+        with self._meta_lock:
+            self._meta[t.value] = (q.shape[0], int(k))
+        return t.value
+
+    def submit_add(self, ids, matrix) -> int:
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        m = np.ascontiguousarray(matrix, dtype=np.float32).reshape(-1, self._dim)
+        t = ctypes.c_uint64(0)
+        self._check(self._L.hann_serve_submit_add(self._h, _ptr(ids), _ptr(m), ids.size, ctypes.byref(t)))
+        with self._meta_lock:
+            self._meta[t.value] = (0, 0)
+        return t.value
+
+    def submit_delete(self, ids) -> int:
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        t = ctypes.c_uint64(0)
+        self._check(self._L.hann_serve_submit_delete(self._h, _ptr(ids), ids.size, ctypes.byref(t)))
+        with self._meta_lock:
+            self._meta[t.value] = (0, 0)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000):
+        with self._meta_lock:
+            nq, k = self._meta.pop(ticket)
+        ids = np.zeros((nq, max(k, 1)), np.int64)
+        dist = np.zeros((nq, max(k, 1)), np.float64)
+        n = np.zeros(max(nq, 1), np.int32)
+        lat = ctypes.c_double(0)
+        self._check(self._L.hann_serve_wait(self._h, ticket, _ptr(ids), _ptr(dist), _ptr(n), int(timeout_ms),
+                                            ctypes.byref(lat)))
+        return ids, dist, n[:nq], lat.value
+
+    def stats(self) -> dict:
+        s = _ServeStats()
+        self._check(self._L.hann_serve_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in _ServeStats._fields_}
+
+    def stop(self):
+        if self._h:
+            self._L.hann_serve_stop(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.stop()

@@ -15,8 +15,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhann_gb300.so")
-SOURCES = ["kernels_train.cu", "kernels_search.cu", "kernels_exact.cu", "index.cu"]
-HEADERS = ["common.cuh", "kernels.h"]
+SOURCES = ["kernels_train.cu", "kernels_search.cu", "kernels_scan.cu", "kernels_exact.cu", "kernels_gemm.cu", "kernels_rescore.cu", "index.cu", "serve.cu"]
+HEADERS = ["common.cuh", "kernels.h", "index_internal.h", "select.cuh", "tile_dist.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -32,7 +32,8 @@ def _stale(out: str, deps) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "hann_gb300.h")]
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "hann_gb300.h"),
+                                                      os.path.join(ROOT, "include", "hann_gb300_diag.h")]
     objs, procs = [], []
     for src in SOURCES:
         sp = os.path.join(CSRC, src)

@@ -143,4 +143,28 @@ __device__ __forceinline__ float key_float(uint32_t k) {
 
 __host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Candidates rescored exactly per query: k + 32 for the reference's PQ
+// distances (mode 0), max(4k, 64) for the raw-vector rerank (mode 1), a
+// multiple of 32; `fixed` > 0 overrides. A query's depth depends only on its
+// own k, so its result does not depend on the batch it runs in.
+__host__ __device__ __forceinline__ int rerank_depth_for(int k, int mode, int fixed) {
+    if (fixed > 0) return fixed > k ? fixed : k;
+    const int r = mode == 0 ? k + 32 : (4 * k > 64 ? 4 * k : 64);
+    return (r + 31) / 32 * 32;
+}
+
+// Bound on |s~ - s| for the BF16 ranking score s = ||b||^2 - 2<a, b>
+// (an = |a|, ar = |a - a~|, bmax = max|b|, brmax = max|b - b~|, a~ and b~
+// the BF16 roundings, kp the padded length):
+//   operand rounding      2 (ar bmax + |a~| brmax)       (Cauchy-Schwarz)
+//   FP32 accumulation     2 kp 2^-22 |a~| |b~|
+//   FP32 ||b||^2          kp 2^-23 bmax^2
+//   score rounding        2^-22 (bmax^2 + 2 |a~| bmax)
+__host__ __device__ __forceinline__ float bf16_score_eps(float an, float ar, float bmax, float brmax, int kp) {
+    const float at = an + ar, bt = bmax + brmax;
+    const float u22 = 2.384185791015625e-7f, u23 = 1.1920928955078125e-7f;
+    return 2.0f * (ar * bmax + at * brmax) + 2.0f * (float)kp * u22 * at * bt + (float)kp * u23 * bmax * bmax +
+           u22 * (bmax * bmax + 2.0f * at * bmax);
+}
+
 }  // namespace hann

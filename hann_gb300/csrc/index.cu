@@ -10,206 +10,10 @@
 //   row_id [rows] i64, row_cluster [rows] i32
 // Rows of one inverted list are contiguous; every list starts on a multiple
 // of 32 rows and keeps spare capacity so Adds append in place.
-#include <algorithm>
-#include <atomic>
-#include <cmath>
-#include <cstdarg>
-#include <cstdio>
-#include <cstring>
-#include <mutex>
-#include <new>
-#include <numeric>
-#include <shared_mutex>
-#include <string>
-#include <unordered_map>
-#include <unordered_set>
-#include <vector>
-
-#include "hann_gb300.h"
-#include "kernels.h"
-
-namespace hann {
-
-template <typename T>
-struct DBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    DBuf() = default;
-    DBuf(const DBuf&) = delete;
-    DBuf& operator=(const DBuf&) = delete;
-    ~DBuf() { reset(); }
-    void reset() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    // Grows to at least cnt elements; contents are not kept.
-    cudaError_t reserve(size_t cnt) {
-        if (cnt <= n && p) return cudaSuccess;
-        reset();
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(cnt, 1) * sizeof(T));
-        if (e == cudaSuccess) n = std::max<size_t>(cnt, 1);
-        else p = nullptr;
-        return e;
-    }
-    void swap(DBuf& o) {
-        std::swap(p, o.p);
-        std::swap(n, o.n);
-    }
-};
-
-// xoshiro256** seeded through splitmix64: the index's own seeded source for
-// k-means seeding and empty-cluster reseeds (the reference's seededRand,
-// pqivf/index.go:20-23).
-struct Rng {
-    uint64_t s[4];
-    void seed(uint64_t x) {
-        for (int i = 0; i < 4; i++) {
-            x += 0x9e3779b97f4a7c15ull;
-            uint64_t z = x;
-            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-            z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-            s[i] = z ^ (z >> 31);
-        }
-    }
-    static uint64_t rotl(uint64_t v, int k) { return (v << k) | (v >> (64 - k)); }
-    uint64_t next() {
-        const uint64_t r = rotl(s[1] * 5, 7) * 9;
-        const uint64_t t = s[1] << 17;
-        s[2] ^= s[0];
-        s[3] ^= s[1];
-        s[1] ^= s[2];
-        s[0] ^= s[3];
-        s[2] ^= t;
-        s[3] = rotl(s[3], 45);
-        return r;
-    }
-    int64_t intn(int64_t n) {
-        const uint64_t un = (uint64_t)n;
-        const uint64_t lim = UINT64_MAX - UINT64_MAX % un;
-        uint64_t v;
-        do v = next();
-        while (v >= lim);
-        return (int64_t)(v % un);
-    }
-    // First k entries of a uniform random permutation of [0, n).
-    std::vector<int64_t> perm_prefix(int64_t n, int64_t k) {
-        std::unordered_map<int64_t, int64_t> sw;
-        std::vector<int64_t> out((size_t)k);
-        for (int64_t i = 0; i < k; i++) {
-            const int64_t j = i + intn(n - i);
-            auto get = [&](int64_t a) {
-                auto it = sw.find(a);
-                return it == sw.end() ? a : it->second;
-            };
-            const int64_t vi = get(i), vj = get(j);
-            out[(size_t)i] = vj;
-            sw[j] = vi;
-        }
-        return out;
-    }
-};
-
-}  // namespace hann
-
-using namespace hann;
-
-struct hann_pqivf {
-    hann_pqivf_options o{};
-    int dsub = 0, code_stride = 0;
-    std::shared_mutex mu;
-    std::mutex run_mu;
-    std::string err;
-    cudaStream_t stream = nullptr;
-    Rng rng;
-    bool trained = false;
-    std::atomic<int64_t> fallback_searches{0};
-
-    std::unordered_map<int64_t, std::vector<float>> pending;
-
-    int nlist = 0, pqk_eff = 0;
-    std::vector<float> h_coarse, h_codebooks;
-    std::vector<std::vector<int64_t>> list_ids;
-    std::vector<uint8_t> list_key;
-    std::vector<int64_t> cluster_counts;
-    std::unordered_map<int64_t, int32_t> id_cluster;
-    std::vector<int64_t> h_start, h_cap;
-    int64_t rows_cap = 0;
-
-    DBuf<float> d_coarse, d_codebooks, d_vectors, d_term;
-    DBuf<int64_t> d_start, d_row_id;
-    DBuf<int32_t> d_len, d_row_cluster;
-    DBuf<uint8_t> d_codes;
-
-    // search scratch
-    DBuf<float> s_q, s_D, s_probe_d, s_cand_d;
-    DBuf<int32_t> s_probe_ids, s_fb, s_cand_row, s_k, s_np, s_nout;
-    DBuf<uint32_t> s_cand_seq;
-    DBuf<int64_t> s_ids;
-    DBuf<double> s_dist;
-    DBuf<unsigned long long> s_fbcount, s_rows;
-
-    // stage profiling: pairs of events per stage
-    bool profile = false;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[4];
-    int64_t launches = 0;
-
-    int fail(int code, const char* fmt, ...) {
-        char buf[512];
-        va_list ap;
-        va_start(ap, fmt);
-        vsnprintf(buf, sizeof(buf), fmt, ap);
-        va_end(ap);
-        err = buf;
-        return code;
-    }
-    int cuda_fail(cudaError_t e, const char* what) {
-        return fail(e == cudaErrorMemoryAllocation ? HANN_E_NOMEM : HANN_E_CUDA, "%s: %s", what,
-                    cudaGetErrorString(e));
-    }
-    int64_t total_rows() const {
-        int64_t t = 0;
-        for (const auto& l : list_ids) t += (int64_t)l.size();
-        return t;
-    }
-    ScanParams scan_params() const {
-        ScanParams p;
-        p.dim = o.dimension;
-        p.M = o.num_subquantizers;
-        p.dsub = dsub;
-        p.pqK = pqk_eff;
-        p.nlist = nlist;
-        p.code_stride = code_stride;
-        p.coarse = d_coarse.p;
-        p.codebooks = d_codebooks.p;
-        p.list_start = d_start.p;
-        p.list_len = d_len.p;
-        p.codes = d_codes.p;
-        p.term = d_term.p;
-        p.row_cluster = d_row_cluster.p;
-        p.vectors = d_vectors.p;
-        p.row_id = d_row_id.p;
-        return p;
-    }
-};
+#include "index_internal.h"
 
 static thread_local std::string g_new_error;
 
-#define CK(expr)                                          \
-    do {                                                  \
-        cudaError_t _e = (expr);                          \
-        if (_e != cudaSuccess) return h->cuda_fail(_e, #expr); \
-    } while (0)
-
-template <typename T>
-static cudaError_t upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s) {
-    cudaError_t e = b.reserve(n);
-    if (e != cudaSuccess) return e;
-    if (n == 0) return cudaSuccess;
-    return cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s);
-}
-
-static int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
 // Capacity for a list that must hold `len` rows.
 static int64_t list_capacity(int64_t len) { return round_up(len + len / 8 + 32, 32); }
@@ -218,7 +22,10 @@ static int64_t list_capacity(int64_t len) { return round_up(len + len / 8 + 32, 
 // Device layout management.
 
 // Lays the lists out afresh with capacities caps[], moving the live rows.
-static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps) {
+// With move_rows false it only allocates (the caller fills the rows).
+// Deleted (tombstoned) slots are dropped while the live rows move, so a
+// relayout also compacts the lists.
+static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_rows = true) {
     const int dim = h->o.dimension;
     std::vector<int64_t> start(h->nlist);
     int64_t total = 0;
@@ -236,15 +43,22 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps) {
     CK(rid.reserve((size_t)total));
     CK(rcl.reserve((size_t)total));
     CK(codes.reserve((size_t)total * h->code_stride));
-    if (h->rows_cap > 0) {
+    if (move_rows && h->rows_cap > 0) {
         std::vector<int64_t> src, dst;
         for (int l = 0; l < h->nlist; l++) {
             const int64_t len = (int64_t)h->list_ids[l].size();
+            int64_t w = 0;
             for (int64_t j = 0; j < len; j++) {
+                if (!h->list_alive[l][j]) continue;
                 src.push_back(h->h_start[l] + j);
-                dst.push_back(start[l] + j);
+                dst.push_back(start[l] + w);
+                h->list_ids[l][w] = h->list_ids[l][j];
+                w++;
             }
+            h->list_ids[l].resize(w);
+            h->list_alive[l].assign(w, 1);
         }
+        h->dead_rows = 0;
         DBuf<int64_t> dsrc, ddst;
         CK(upload(dsrc, src.data(), src.size(), h->stream));
         CK(upload(ddst, dst.data(), dst.size(), h->stream));
@@ -271,120 +85,215 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps) {
 }
 
 static int upload_lens(hann_pqivf* h) {
-    std::vector<int32_t> len(h->nlist);
-    for (int l = 0; l < h->nlist; l++) len[l] = (int32_t)h->list_ids[l].size();
+    std::vector<int32_t> len(h->nlist), live(h->nlist);
+    for (int l = 0; l < h->nlist; l++) {
+        len[l] = (int32_t)h->list_ids[l].size();
+        live[l] = (int32_t)h->live_count[l];
+    }
     CK(upload(h->d_len, len.data(), len.size(), h->stream));
+    CK(upload(h->d_live, live.data(), live.size(), h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return HANN_OK;
 }
 
-// Places n vectors (ids ascending, host memory) into a trained index:
-// nearest coarse list, codes, append (assignLocked, pqivf/index.go:245-260).
-static int assign_batch(hann_pqivf* h, const int64_t* ids, const float* vecs, int64_t n) {
+// BF16 centroids, their FP32 squared norms and the largest norm, for the
+// tensor-core preselection (dimensions up to 128).
+static int prepare_coarse(hann_pqivf* h) {
+    h->tc = h->o.dimension <= 128 && h->nlist > 0;
+    if (!h->tc) return HANN_OK;
+    h->kp = gemm_kpad(h->o.dimension);
+    CK(h->d_coarse_bf16.reserve((size_t)h->nlist * h->kp));
+    CK(h->d_coarse_norm.reserve((size_t)h->nlist));
+    CK(h->d_cmax.reserve(2));
+    DBuf<float> cres;
+    CK(cres.reserve((size_t)h->nlist));
+    CK(h->d_err.reserve(1));
+    CK(cudaMemsetAsync(h->d_err.p, 0, sizeof(int), h->stream));
+    CK(launch_to_bf16(h->d_coarse.p, h->nlist, h->o.dimension, h->kp, h->d_coarse_bf16.p, h->d_coarse_norm.p,
+                      cres.p, h->stream));
+    CK(launch_norm_maxes(h->d_coarse_norm.p, cres.p, h->nlist, h->d_cmax.p, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HANN_OK;
+}
+
+
+// Exact nearest centroid (reference-order FP32, lowest index on a tie) of
+// every row of x: BF16 tensor-core preselection of 8 candidates per row, an
+// exact rescore of the candidates, and the exact tiled kernel for the rows
+// whose candidate band overflows (kernels_rescore.cu).
+static int assign_rows(hann_pqivf* h, AssignScratch& sc, const float* x, int64_t n, int dim, const float* cent,
+                       int k, int32_t* out_idx) {
+    cudaStream_t s = h->stream;
+    if (n <= 0) return HANN_OK;
+    if (dim > 128) {
+        DBuf<unsigned long long> keys;
+        CK(keys.reserve((size_t)n));
+        CK(launch_assign_exact(x, n, dim, cent, k, out_idx, nullptr, keys.p, s));
+        return HANN_OK;
+    }
+    const int kp = gemm_kpad(dim);
+    if (!sc.x_ready) {
+        CK(sc.xbf.reserve((size_t)n * kp));
+        CK(sc.xn2.reserve((size_t)n));
+        CK(sc.xres.reserve((size_t)n));
+        CK(launch_to_bf16(x, n, dim, kp, sc.xbf.p, sc.xn2.p, sc.xres.p, s));
+        CK(sc.cand_idx.reserve((size_t)n * gemm_topc()));
+        CK(sc.cand_val.reserve((size_t)n * gemm_topc()));
+        CK(sc.ovf_rows.reserve((size_t)n));
+        CK(sc.counters.reserve(2));
+        CK(sc.cmax.reserve(2));
+        sc.x_ready = true;
+    }
+    CK(sc.cbf.reserve((size_t)k * kp));
+    CK(sc.cn2.reserve((size_t)k));
+    CK(sc.cres.reserve((size_t)k));
+    CK(launch_to_bf16(cent, k, dim, kp, sc.cbf.p, sc.cn2.p, sc.cres.p, s));
+    CK(launch_norm_maxes(sc.cn2.p, sc.cres.p, k, sc.cmax.p, s));
+    CK(cudaMemsetAsync(sc.counters.p, 0, 2 * sizeof(int), s));
+    CK(launch_gemm_top8(sc.xbf.p, n, sc.cbf.p, k, kp, sc.cn2.p, sc.cand_idx.p, sc.cand_val.p, sc.counters.p + 1, s));
+    CK(launch_rescore_top8(x, sc.xn2.p, sc.xres.p, n, dim, kp, cent, k, sc.cmax.p, sc.cand_idx.p, sc.cand_val.p,
+                           out_idx,
+                           sc.ovf_rows.p, sc.counters.p, s));
+    int hc[2] = {0, 0};
+    CK(cudaMemcpyAsync(hc, sc.counters.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (hc[1]) return h->fail(HANN_E_CUDA, "tensor-core distance kernel timed out waiting on its pipeline");
+    const int64_t novf = hc[0];
+    if (novf > 0) {
+        CK(sc.ovf_x.reserve((size_t)novf * dim));
+        CK(sc.ovf_idx.reserve((size_t)novf));
+        DBuf<unsigned long long> keys;
+        CK(keys.reserve((size_t)novf));
+        CK(launch_copy_words(x, sc.ovf_rows.p, sc.ovf_x.p, nullptr, novf, dim, s));
+        CK(launch_assign_exact(sc.ovf_x.p, novf, dim, cent, k, sc.ovf_idx.p, nullptr, keys.p, s));
+        CK(launch_copy_words(sc.ovf_idx.p, nullptr, out_idx, sc.ovf_rows.p, novf, 1, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return HANN_OK;
+}
+
+// Adding n vectors (ids ascending, host memory) to a trained index
+// (assignLocked, pqivf/index.go:245-260) runs in two phases. add_prepare
+// computes every vector's nearest list, codes and term into the handle's
+// mutation scratch and changes nothing; it reports whether some list would
+// overflow its capacity (a relayout). add_commit then appends the rows in
+// place -- a concurrent search sees each list either before or after the
+// append -- or relayouts first when needed.
+int add_prepare(hann_pqivf* h, const int64_t* ids, const float* vecs, int64_t n) {
+    MutationScratch& m = h->mut;
+    m.n = n;
+    m.grow = false;
     if (n <= 0) return HANN_OK;
     const int dim = h->o.dimension, M = h->o.num_subquantizers;
-    DBuf<float> x, term;
-    DBuf<int32_t> asg;
-    DBuf<uint8_t> codes;
-    CK(upload(x, vecs, (size_t)n * dim, h->stream));
-    CK(asg.reserve((size_t)n));
-    CK(term.reserve((size_t)n));
-    CK(codes.reserve((size_t)n * h->code_stride));
-    DBuf<unsigned long long> keys;
-    CK(keys.reserve((size_t)n));
-    CK(launch_assign_exact(x.p, n, dim, h->d_coarse.p, h->nlist, asg.p, nullptr, keys.p, h->stream));
-    CK(launch_encode(x.p, nullptr, asg.p, n, dim, h->d_coarse.p, h->d_codebooks.p, M, h->pqk_eff, codes.p,
-                     h->code_stride, term.p, h->stream));
-    std::vector<int32_t> hasg((size_t)n);
-    CK(cudaMemcpyAsync(hasg.data(), asg.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(upload(m.x, vecs, (size_t)n * dim, h->stream));
+    CK(m.asg.reserve((size_t)n));
+    CK(m.term.reserve((size_t)n));
+    CK(m.codes.reserve((size_t)n * h->code_stride));
+    m.asc.x_ready = false;
+    int rc = assign_rows(h, m.asc, m.x.p, n, dim, h->d_coarse.p, h->nlist, m.asg.p);
+    if (rc) return rc;
+    CK(launch_encode(m.x.p, nullptr, m.asg.p, n, dim, h->d_coarse.p, h->d_codebooks.p, M, h->pqk_eff, m.codes.p,
+                     h->code_stride, m.term.p, h->stream));
+    m.hasg.resize((size_t)n);
+    CK(cudaMemcpyAsync(m.hasg.data(), m.asg.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    std::vector<int64_t> need(h->nlist);
-    bool grow = false;
-    for (int l = 0; l < h->nlist; l++) need[l] = (int64_t)h->list_ids[l].size();
-    for (int64_t i = 0; i < n; i++) need[hasg[i]]++;
-    std::vector<int64_t> caps(h->nlist);
-    for (int l = 0; l < h->nlist; l++) {
-        caps[l] = h->h_cap[l];
-        if (need[l] > h->h_cap[l]) {
-            caps[l] = list_capacity(need[l] + need[l] / 2);
-            grow = true;
+    m.add.assign(h->nlist, 0);
+    for (int64_t i = 0; i < n; i++) m.add[m.hasg[i]]++;
+    for (int l = 0; l < h->nlist; l++)
+        if ((int64_t)h->list_ids[l].size() + m.add[l] > h->h_cap[l]) m.grow = true;
+    return HANN_OK;
+}
+
+int add_commit(hann_pqivf* h, const int64_t* ids) {
+    MutationScratch& m = h->mut;
+    const int64_t n = m.n;
+    if (n <= 0) return HANN_OK;
+    const int dim = h->o.dimension;
+    if (m.grow) {
+        // one relayout that also drops every tombstone
+        std::vector<int64_t> caps(h->nlist);
+        for (int l = 0; l < h->nlist; l++) {
+            const int64_t live = h->live_count[l] + m.add[l];
+            caps[l] = std::max(h->h_cap[l], live > h->h_cap[l] ? list_capacity(live + live / 2) : (int64_t)0);
         }
-    }
-    if (grow) {
         int rc = relayout(h, caps);
         if (rc) return rc;
+        m.grow = false;
     }
     std::vector<int64_t> dst((size_t)n);
     for (int64_t i = 0; i < n; i++) {
-        const int c = hasg[i];
+        const int c = m.hasg[i];
         dst[i] = h->h_start[c] + (int64_t)h->list_ids[c].size();
         h->list_ids[c].push_back(ids[i]);
+        h->list_alive[c].push_back(1);
+        h->live_count[c]++;
         h->id_cluster[ids[i]] = c;
         h->cluster_counts[c]++;
         h->list_key[c] = 1;
     }
-    DBuf<int64_t> ddst, did;
-    CK(upload(ddst, dst.data(), dst.size(), h->stream));
-    CK(upload(did, ids, (size_t)n, h->stream));
-    CK(launch_copy_words(x.p, nullptr, h->d_vectors.p, ddst.p, n, dim, h->stream));
-    CK(launch_copy_words(term.p, nullptr, h->d_term.p, ddst.p, n, 1, h->stream));
-    CK(launch_copy_words(did.p, nullptr, h->d_row_id.p, ddst.p, n, 2, h->stream));
-    CK(launch_copy_words(asg.p, nullptr, h->d_row_cluster.p, ddst.p, n, 1, h->stream));
-    CK(launch_copy_words(codes.p, nullptr, h->d_codes.p, ddst.p, n, h->code_stride / 4, h->stream));
+    CK(upload(m.dst, dst.data(), dst.size(), h->stream));
+    CK(upload(m.ids, ids, (size_t)n, h->stream));
+    CK(launch_copy_words(m.x.p, nullptr, h->d_vectors.p, m.dst.p, n, dim, h->stream));
+    CK(launch_copy_words(m.codes.p, nullptr, h->d_codes.p, m.dst.p, n, h->code_stride / 4, h->stream));
+    CK(launch_copy_words(m.ids.p, nullptr, h->d_row_id.p, m.dst.p, n, 2, h->stream));
+    CK(launch_copy_words(m.asg.p, nullptr, h->d_row_cluster.p, m.dst.p, n, 1, h->stream));
+    // the term last: a row becomes selectable only once it is complete
+    CK(launch_copy_words(m.term.p, nullptr, h->d_term.p, m.dst.p, n, 1, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return upload_lens(h);
 }
 
-// Removes the given (already validated, trained-side) ids from their lists,
-// keeping every list's order (deleteLocked, pqivf/index.go:313-345).
+static int assign_batch(hann_pqivf* h, const int64_t* ids, const float* vecs, int64_t n) {
+    int rc = add_prepare(h, ids, vecs, n);
+    if (rc) return rc;
+    return add_commit(h, ids);
+}
+
+// Removes the given (already validated, trained-side) ids (deleteLocked,
+// pqivf/index.go:313-345). A removed row becomes a tombstone: its term is set
+// to +inf, so no scan can select it, and its id to -1; the live rows keep
+// their places, so the lists keep their order and concurrent readers never
+// see a row move. A relayout compacts the tombstones away once they exceed a
+// quarter of the slots.
 static int remove_rows(hann_pqivf* h, const std::vector<int64_t>& ids) {
     if (ids.empty()) return HANN_OK;
-    std::unordered_map<int, std::unordered_set<int64_t>> by_list;
+    std::vector<int64_t> rows;
     for (int64_t id : ids) {
         auto it = h->id_cluster.find(id);
         if (it == h->id_cluster.end()) continue;
-        by_list[it->second].insert(id);
-    }
-    std::vector<int64_t> src, dst;
-    for (auto& kv : by_list) {
-        const int l = kv.first;
+        const int l = it->second;
         auto& lst = h->list_ids[l];
-        std::vector<int64_t> kept;
-        kept.reserve(lst.size());
-        int64_t w = 0;
         for (size_t j = 0; j < lst.size(); j++) {
-            if (kv.second.count(lst[j])) {
-                h->cluster_counts[l]--;
-                h->id_cluster.erase(lst[j]);
-                continue;
+            if (h->list_alive[l][j] && lst[j] == id) {
+                h->list_alive[l][j] = 0;
+                rows.push_back(h->h_start[l] + (int64_t)j);
+                break;
             }
-            if ((int64_t)j != w) {
-                src.push_back(h->h_start[l] + (int64_t)j);
-                dst.push_back(h->h_start[l] + w);
-            }
-            kept.push_back(lst[j]);
-            w++;
         }
-        lst.swap(kept);
+        h->live_count[l]--;
+        h->cluster_counts[l]--;
+        h->dead_rows++;
+        h->id_cluster.erase(it);
     }
-    if (!src.empty()) {
-        // Stage through a temporary so overlapping moves stay correct.
-        const int dim = h->o.dimension;
-        const int64_t n = (int64_t)src.size();
-        DBuf<int64_t> dsrc, ddst;
-        CK(upload(dsrc, src.data(), src.size(), h->stream));
-        CK(upload(ddst, dst.data(), dst.size(), h->stream));
-        DBuf<uint32_t> tmp;
-        const int widths[5] = {dim, 1, 2, 1, h->code_stride / 4};
-        void* arrs[5] = {h->d_vectors.p, h->d_term.p, h->d_row_id.p, h->d_row_cluster.p, h->d_codes.p};
-        CK(tmp.reserve((size_t)n * std::max(dim, h->code_stride / 4 + 2)));
-        for (int a = 0; a < 5; a++) {
-            CK(launch_copy_words(arrs[a], dsrc.p, tmp.p, nullptr, n, widths[a], h->stream));
-            CK(launch_copy_words(tmp.p, nullptr, arrs[a], ddst.p, n, widths[a], h->stream));
-        }
+    if (!rows.empty()) {
+        CK(upload(h->mut.rows, rows.data(), rows.size(), h->stream));
+        CK(launch_tombstone(h->mut.rows.p, (int64_t)rows.size(), h->d_term.p, h->d_row_id.p, h->stream));
         CK(cudaStreamSynchronize(h->stream));
     }
+    if (compaction_due(h, 0)) {
+        const std::vector<int64_t> caps = h->h_cap;
+        int rc = relayout(h, caps);
+        if (rc) return rc;
+    }
     return upload_lens(h);
+}
+
+// Whether deleting `extra` more live rows would trigger the compacting
+// relayout (tombstones above a quarter of the slots).
+bool compaction_due(const hann_pqivf* h, int64_t extra) {
+    int64_t slots = 0;
+    for (int l = 0; l < h->nlist; l++) slots += (int64_t)h->list_ids[l].size();
+    return (h->dead_rows + extra) * 4 > slots;
 }
 
 // ---------------------------------------------------------------------------
@@ -417,7 +326,7 @@ static int64_t draw_reseed(hann_pqivf* h, SeedSource& src, int64_t n, bool& ok) 
 // clusters reseeded from `reseed` in cluster order.
 static int kmeans_device(hann_pqivf* h, const float* x, int64_t ld, int off, int64_t n, int dim, int k, int iters,
                          const std::vector<int64_t>& init, SeedSource& seeds, float* cent, int32_t* asg_buf,
-                         bool sub_mode, const float* sub_full, int M, int m) {
+                         bool sub_mode, const float* sub_full, int M, int m, AssignScratch* sc) {
     // sub_mode: x is the full residual matrix [n][M*dim]; k-means runs on
     // columns [m*dim, (m+1)*dim) and cent is codebook m ([k][dim]).
     DBuf<int64_t> dsrc;
@@ -430,7 +339,8 @@ static int kmeans_device(hann_pqivf* h, const float* x, int64_t ld, int off, int
     std::vector<int64_t> hcounts(k);
     for (int it = 0; it < iters; it++) {
         if (!sub_mode) {
-            CK(launch_assign_exact(x, n, dim, cent, k, asg_buf, nullptr, nullptr, h->stream));
+            int rc = assign_rows(h, *sc, x, n, dim, cent, k, asg_buf);
+            if (rc) return rc;
             CK(cudaMemsetAsync(sums.p, 0, (size_t)k * dim * sizeof(double), h->stream));
             CK(cudaMemsetAsync(counts.p, 0, (size_t)k * sizeof(int64_t), h->stream));
             CK(launch_kmeans_accumulate(x, n, dim, asg_buf, sums.p, counts.p, h->stream));
@@ -480,7 +390,7 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     all.reserve(h->id_cluster.size() + h->pending.size());
     for (int l = 0; l < h->nlist; l++)
         for (size_t j = 0; j < h->list_ids[l].size(); j++)
-            all.emplace_back(h->list_ids[l][j], h->h_start[l] + (int64_t)j);
+            if (h->list_alive[l][j]) all.emplace_back(h->list_ids[l][j], h->h_start[l] + (int64_t)j);
     std::vector<const std::vector<float>*> pend;
     for (auto& kv : h->pending) {
         all.emplace_back(kv.first, -(int64_t)pend.size() - 1);
@@ -523,11 +433,13 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     DBuf<int32_t> asg;
     CK(C.reserve((size_t)k * dim));
     CK(asg.reserve((size_t)n));
+    AssignScratch asc;
     int rc = kmeans_device(h, X.p, dim, 0, n, dim, k, h->o.kmeans_iters, init, seeds, C.p, asg.p, false, nullptr, 0,
-                           0);
+                           0, &asc);
     if (rc) return rc;
     // Final assignment and inverted lists in ascending (cluster, id) order.
-    CK(launch_assign_exact(X.p, n, dim, C.p, k, asg.p, nullptr, nullptr, h->stream));
+    rc = assign_rows(h, asc, X.p, n, dim, C.p, k, asg.p);
+    if (rc) return rc;
     std::vector<int32_t> hasg(n);
     CK(cudaMemcpyAsync(hasg.data(), asg.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -567,7 +479,7 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
             pinit = h->rng.perm_prefix(n, kpq);
         }
         rc = kmeans_device(h, Rm.p, dim, m * ds, n, ds, kpq, h->o.kmeans_iters, pinit, seeds,
-                           CB.p + (size_t)m * kpq * ds, pqa.p, true, Rm.p, M, m);
+                           CB.p + (size_t)m * kpq * ds, pqa.p, true, Rm.p, M, m, nullptr);
         if (rc) return rc;
     }
     Rm.reset();
@@ -584,6 +496,13 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
         h->list_ids[c].push_back(ids[order[j]]);
         h->id_cluster[ids[order[j]]] = c;
     }
+    h->list_alive.assign(k, {});
+    h->live_count.assign(k, 0);
+    for (int c = 0; c < k; c++) {
+        h->list_alive[c].assign(h->list_ids[c].size(), 1);
+        h->live_count[c] = (int64_t)h->list_ids[c].size();
+    }
+    h->dead_rows = 0;
     for (int c = 0; c < k; c++) {
         h->cluster_counts[c] = cnt[c];
         h->list_key[c] = cnt[c] > 0;
@@ -598,12 +517,7 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     h->rows_cap = 0;
     std::vector<int64_t> caps(k);
     for (int c = 0; c < k; c++) caps[c] = list_capacity(cnt[c]);
-    // relayout() with rows_cap == 0 only allocates.
-    std::vector<std::vector<int64_t>> saved;
-    saved.swap(h->list_ids);
-    h->list_ids.assign(k, {});
-    rc = relayout(h, caps);
-    h->list_ids.swap(saved);
+    rc = relayout(h, caps, false);
     if (rc) return rc;
     std::vector<int64_t> dst(n), rid(n);
     std::vector<int32_t> rcl(n);
@@ -634,36 +548,41 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
                   cudaMemcpyDeviceToHost));
     h->pending.clear();
     h->trained = true;
+    rc = prepare_coarse(h);
+    if (rc) return rc;
     return upload_lens(h);
 }
 
 // ---------------------------------------------------------------------------
 // Search.
 
-static int rerank_depth(const hann_pqivf* h, int kmax, int mode) {
-    if (h->o.rerank > 0) return std::max(h->o.rerank, kmax);
-    const int r = mode == 0 ? kmax + 32 : std::max(4 * kmax, 64);
-    return (int)round_up(r, 32);
-}
+int rerank_depth(const hann_pqivf* h, int kmax, int mode) { return rerank_depth_for(kmax, mode, h->o.rerank); }
 
 // Runs the device search for nq queries already in d_q; k/nprobe per query
 // in device arrays d_k/d_np. Outputs to device buffers.
-static int run_search(hann_pqivf* h, const float* d_q, int64_t nq, const int32_t* d_k, const int32_t* d_np,
-                      int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist, int32_t* d_nout,
-                      cudaStream_t s) {
+int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k,
+                      const int32_t* d_np, int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist,
+                      int32_t* d_nout, cudaStream_t s) {
     const int R = rerank_depth(h, kmax, mode);
     if (R > 480) return h->fail(HANN_E_UNSUPPORTED, "k (%d) above this build's limit of 448", kmax);
     np_max = std::min(np_max, h->nlist);
     if (np_max > 4096) return h->fail(HANN_E_UNSUPPORTED, "more than 4096 probed lists per query");
-    const ScanParams p = h->scan_params();
+    ScanParams p = h->scan_params();
+    p.mode = mode;
+    p.rerank_fixed = h->o.rerank;
     const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)1 << 28) / std::max(1, h->nlist)));
-    CK(h->s_D.reserve((size_t)chunk * h->nlist));
-    CK(h->s_probe_ids.reserve((size_t)chunk * np_max));
-    CK(h->s_probe_d.reserve((size_t)chunk * np_max));
-    CK(h->s_fb.reserve((size_t)chunk));
-    CK(h->s_cand_row.reserve((size_t)chunk * R));
-    CK(h->s_cand_d.reserve((size_t)chunk * R));
-    CK(h->s_cand_seq.reserve((size_t)chunk * R));
+    CK(sc.D.reserve((size_t)chunk * h->nlist));
+    if (h->tc) {
+        CK(sc.qbf.reserve((size_t)chunk * h->kp));
+        CK(sc.qn2.reserve((size_t)chunk));
+        CK(sc.qres.reserve((size_t)chunk));
+    }
+    CK(sc.probe_ids.reserve((size_t)chunk * np_max));
+    CK(sc.probe_d.reserve((size_t)chunk * np_max));
+    CK(sc.fb.reserve((size_t)chunk));
+    CK(sc.cand_row.reserve((size_t)chunk * R));
+    CK(sc.cand_d.reserve((size_t)chunk * R));
+    CK(sc.cand_seq.reserve((size_t)chunk * R));
     auto mark = [&](int stage, bool begin) -> cudaError_t {
         if (!h->profile) return cudaSuccess;
         cudaEvent_t e;
@@ -677,27 +596,41 @@ static int run_search(hann_pqivf* h, const float* d_q, int64_t nq, const int32_t
         const int64_t nc = std::min(chunk, nq - q0);
         const float* qp = d_q + q0 * h->o.dimension;
         CK(mark(0, true));
-        CK(launch_dist_matrix(qp, nc, h->o.dimension, h->d_coarse.p, h->nlist, h->s_D.p, s));
+        if (h->tc) {
+            CK(launch_to_bf16(qp, nc, h->o.dimension, h->kp, sc.qbf.p, sc.qn2.p, sc.qres.p, s));
+            CK(launch_gemm_scores(sc.qbf.p, nc, h->d_coarse_bf16.p, h->nlist, h->kp, h->d_coarse_norm.p, sc.D.p,
+                                  h->d_err.p, s));
+        } else {
+            CK(launch_dist_matrix(qp, nc, h->o.dimension, h->d_coarse.p, h->nlist, sc.D.p, s));
+        }
         CK(mark(0, false));
         CK(mark(1, true));
-        CK(launch_probe_select(h->s_D.p, nc, h->nlist, d_np + q0, np_max, d_k + q0, h->d_len.p,
-                               h->o.fallback ? 1 : 0, h->s_probe_ids.p, h->s_probe_d.p, h->s_fb.p,
-                               h->s_fbcount.p, s));
+        if (h->tc) {
+            CK(launch_probe_select_band(sc.D.p, qp, sc.qn2.p, sc.qres.p, nc, h->o.dimension, h->kp, h->d_coarse.p,
+                                        h->d_cmax.p,
+                                        h->nlist, d_np + q0, np_max, d_k + q0, h->d_live.p, h->o.fallback ? 1 : 0,
+                                        sc.probe_ids.p, sc.probe_d.p, sc.fb.p, sc.fbcount.p, s));
+        } else {
+            CK(launch_probe_select(sc.D.p, nc, h->nlist, d_np + q0, np_max, d_k + q0, h->d_live.p,
+                                   h->o.fallback ? 1 : 0, sc.probe_ids.p, sc.probe_d.p, sc.fb.p,
+                                   sc.fbcount.p, s));
+        }
         CK(mark(1, false));
         CK(mark(2, true));
-        CK(launch_scan(p, qp, nc, h->s_probe_ids.p, h->s_D.p, d_np + q0, np_max, h->s_fb.p, R, h->s_cand_row.p,
-                       h->s_cand_d.p, h->s_cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
+        p.kq = d_k + q0;
+        CK(launch_scan(p, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R,
+                       sc.cand_row.p, sc.cand_d.p, sc.cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
         CK(mark(2, false));
         CK(mark(3, true));
-        CK(launch_rerank(p, qp, nc, h->s_cand_row.p, h->s_cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+        CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
                          d_dist + q0 * kmax, d_nout + q0, s));
         CK(mark(3, false));
-        h->launches += 4;
+        h->launches += h->tc ? 5 : 4;
     }
     return HANN_OK;
 }
 
-static int check_searchable(hann_pqivf* h) {
+int check_searchable(hann_pqivf* h) {
     if (!h->trained)
         return h->fail(HANN_E_STATE, "PQIVF index is not trained. Call Train() after adding data before searching");
     bool any = false;
@@ -706,9 +639,9 @@ static int check_searchable(hann_pqivf* h) {
     return HANN_OK;
 }
 
-static int read_fallbacks(hann_pqivf* h, cudaStream_t s) {
+static int read_fallbacks(hann_pqivf* h, SearchScratch& sc, cudaStream_t s) {
     unsigned long long v = 0;
-    CK(cudaMemcpyAsync(&v, h->s_fbcount.p, sizeof(v), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&v, sc.fbcount.p, sizeof(v), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     h->fallback_searches += (int64_t)v;
     return HANN_OK;
@@ -790,7 +723,7 @@ int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out) {
     h->rng.seed(o.seed);
     cudaError_t e = cudaSetDevice(o.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = h->s_fbcount.reserve(1);
+    if (e == cudaSuccess) e = h->main.fbcount.reserve(1);
     if (e == cudaSuccess) e = h->s_rows.reserve(1);
     if (e == cudaSuccess) e = cudaMemset(h->s_rows.p, 0, sizeof(unsigned long long));
     if (e != cudaSuccess) {
@@ -817,8 +750,17 @@ const char* hann_pqivf_last_error(const hann_pqivf* h) { return h ? h->err.c_str
 int hann_pqivf_bulk_add(hann_pqivf* h, const int64_t* ids, const float* vectors, int64_t n) {
     if (!h) return HANN_E_INVALID;
     if (n < 0 || (n > 0 && (!ids || !vectors))) return h->fail(HANN_E_INVALID, "invalid arguments");
+    std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
+    return bulk_add_locked(h, ids, vectors, n);
+}
+
+}  // extern "C"
+
+int bulk_add_locked(hann_pqivf* h, const int64_t* ids, const float* vectors, int64_t n, bool allow_relayout,
+                    bool* needs_relayout) {
+    if (needs_relayout) *needs_relayout = false;
     const int dim = h->o.dimension;
     std::vector<int64_t> order(n);
     std::iota(order.begin(), order.end(), 0);
@@ -856,12 +798,20 @@ int hann_pqivf_bulk_add(hann_pqivf* h, const int64_t* ids, const float* vectors,
             sid[i] = ids[order[i]];
             std::memcpy(&sv[(size_t)i * dim], vectors + order[i] * dim, sizeof(float) * dim);
         }
-        int rc = assign_batch(h, sid.data(), sv.data(), f);
+        int rc = add_prepare(h, sid.data(), sv.data(), f);
+        if (rc) return rc;
+        if (h->mut.grow && !allow_relayout) {
+            if (needs_relayout) *needs_relayout = true;
+            return HANN_OK;
+        }
+        rc = add_commit(h, sid.data());
         if (rc) return rc;
     }
     if (code) return h->fail(code, "%s", msg.c_str());
     return HANN_OK;
 }
+
+extern "C" {
 
 int hann_pqivf_add(hann_pqivf* h, int64_t id, const float* vector) { return hann_pqivf_bulk_add(h, &id, vector, 1); }
 
@@ -891,6 +841,7 @@ static int delete_ids(hann_pqivf* h, std::vector<int64_t> ids, bool strict) {
 
 int hann_pqivf_delete(hann_pqivf* h, int64_t id) {
     if (!h) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
     return delete_ids(h, {id}, true);
@@ -899,16 +850,36 @@ int hann_pqivf_delete(hann_pqivf* h, int64_t id) {
 int hann_pqivf_bulk_delete(hann_pqivf* h, const int64_t* ids, int64_t n) {
     if (!h) return HANN_E_INVALID;
     if (n < 0 || (n > 0 && !ids)) return h->fail(HANN_E_INVALID, "invalid arguments");
+    std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
+    return bulk_delete_locked(h, ids, n);
+}
+
+}  // extern "C"
+
+int bulk_delete_locked(hann_pqivf* h, const int64_t* ids, int64_t n, bool allow_relayout, bool* needs_relayout) {
+    if (needs_relayout) *needs_relayout = false;
     std::vector<int64_t> v(ids, ids + n);
     std::sort(v.begin(), v.end());
+    if (!allow_relayout) {
+        std::unordered_set<int64_t> live;
+        for (int64_t id : v)
+            if (h->id_cluster.count(id)) live.insert(id);
+        if (compaction_due(h, (int64_t)live.size())) {
+            if (needs_relayout) *needs_relayout = true;
+            return HANN_OK;
+        }
+    }
     return delete_ids(h, v, false);
 }
+
+extern "C" {
 
 int hann_pqivf_bulk_update(hann_pqivf* h, const int64_t* ids, const float* vectors, int64_t n) {
     if (!h) return HANN_E_INVALID;
     if (n < 0 || (n > 0 && (!ids || !vectors))) return h->fail(HANN_E_INVALID, "invalid arguments");
+    std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
     const int dim = h->o.dimension;
@@ -958,6 +929,7 @@ int hann_pqivf_update(hann_pqivf* h, int64_t id, const float* vector) {
 int hann_pqivf_train_seeded(hann_pqivf* h, const int64_t* coarse_init, const int64_t* pq_init, const int64_t* reseed,
                             int64_t n_reseed) {
     if (!h) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
@@ -996,20 +968,21 @@ int hann_pqivf_search_batch(hann_pqivf* h, const float* queries, int64_t nq, con
         np_max = std::max(np_max, np[i]);
     }
     cudaStream_t s = h->stream;
-    CK(upload(h->s_q, queries, (size_t)nq * h->o.dimension, s));
-    CK(upload(h->s_k, k, (size_t)nq, s));
-    CK(upload(h->s_np, np.data(), (size_t)nq, s));
-    CK(h->s_ids.reserve((size_t)nq * kmax));
-    CK(h->s_dist.reserve((size_t)nq * kmax));
-    CK(h->s_nout.reserve((size_t)nq));
-    CK(cudaMemsetAsync(h->s_fbcount.p, 0, sizeof(unsigned long long), s));
-    rc = run_search(h, h->s_q.p, nq, h->s_k.p, h->s_np.p, np_max, kmax, mode, h->s_ids.p, h->s_dist.p, h->s_nout.p,
-                    s);
+    SearchScratch& sc = h->main;
+    CK(upload(sc.q, queries, (size_t)nq * h->o.dimension, s));
+    CK(upload(sc.k, k, (size_t)nq, s));
+    CK(upload(sc.np, np.data(), (size_t)nq, s));
+    CK(sc.ids.reserve((size_t)nq * kmax));
+    CK(sc.dist.reserve((size_t)nq * kmax));
+    CK(sc.nout.reserve((size_t)nq));
+    CK(sc.fbcount.reserve(1));
+    CK(cudaMemsetAsync(sc.fbcount.p, 0, sizeof(unsigned long long), s));
+    rc = run_search(h, sc, sc.q.p, nq, sc.k.p, sc.np.p, np_max, kmax, mode, sc.ids.p, sc.dist.p, sc.nout.p, s);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(ids, h->s_ids.p, (size_t)nq * kmax * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(distances, h->s_dist.p, (size_t)nq * kmax * sizeof(double), cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(n_out, h->s_nout.p, (size_t)nq * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    return read_fallbacks(h, s);
+    CK(cudaMemcpyAsync(ids, sc.ids.p, (size_t)nq * kmax * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(distances, sc.dist.p, (size_t)nq * kmax * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(n_out, sc.nout.p, (size_t)nq * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    return read_fallbacks(h, sc, s);
 }
 
 int hann_pqivf_search(hann_pqivf* h, const float* query, int32_t k, int64_t* ids, double* distances,
@@ -1034,18 +1007,13 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
     if (nq <= 0) return HANN_OK;
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     const int np = std::min<int>(nprobe, h->nlist);
-    if ((int64_t)h->s_k.n < nq || h->s_k.p == nullptr) {
-        std::vector<int32_t> kv(nq, k), nv(nq, np);
-        CK(upload(h->s_k, kv.data(), kv.size(), s));
-        CK(upload(h->s_np, nv.data(), nv.size(), s));
-        CK(cudaStreamSynchronize(s));
-    } else {
-        std::vector<int32_t> kv(nq, k), nv(nq, np);
-        CK(cudaMemcpyAsync(h->s_k.p, kv.data(), nq * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(h->s_np.p, nv.data(), nq * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-        CK(cudaStreamSynchronize(s));
-    }
-    return run_search(h, d_queries, nq, h->s_k.p, h->s_np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
+    SearchScratch& sc = h->main;
+    std::vector<int32_t> kv(nq, k), nv(nq, np);
+    CK(upload(sc.k, kv.data(), kv.size(), s));
+    CK(upload(sc.np, nv.data(), nv.size(), s));
+    CK(sc.fbcount.reserve(1));
+    CK(cudaStreamSynchronize(s));
+    return run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
 }
 
 int hann_pqivf_set_profiling(hann_pqivf* h, int32_t on) {
@@ -1086,7 +1054,7 @@ int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_
 int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out) {
     if (!h || !out) return HANN_E_INVALID;
     std::shared_lock<std::shared_mutex> lk(h->mu);
-    for (int l = 0; l < h->nlist; l++) out[l] = (int64_t)h->list_ids[l].size();
+    for (int l = 0; l < h->nlist; l++) out[l] = h->live_count[l];
     return HANN_OK;
 }
 
@@ -1124,6 +1092,7 @@ int hann_pqivf_export(hann_pqivf* h, float* coarse, float* codebooks, int64_t* l
                       int64_t* cluster_counts, int64_t* ids, float* vectors, int32_t* codes, int64_t* pending_ids,
                       float* pending_vectors) {
     if (!h) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
@@ -1134,21 +1103,26 @@ int hann_pqivf_export(hann_pqivf* h, float* coarse, float* codebooks, int64_t* l
     }
     int64_t r = 0;
     std::vector<uint8_t> cbuf;
+    std::vector<float> vbuf;
     for (int l = 0; l < h->nlist; l++) {
         const int64_t len = (int64_t)h->list_ids[l].size();
-        list_len[l] = len;
+        list_len[l] = h->live_count[l];
         list_key[l] = h->list_key[l];
         cluster_counts[l] = h->cluster_counts[l];
         if (len == 0) continue;
-        std::memcpy(ids + r, h->list_ids[l].data(), len * sizeof(int64_t));
-        CK(cudaMemcpy(vectors + r * dim, h->d_vectors.p + h->h_start[l] * dim, (size_t)len * dim * sizeof(float),
+        vbuf.resize((size_t)len * dim);
+        CK(cudaMemcpy(vbuf.data(), h->d_vectors.p + h->h_start[l] * dim, (size_t)len * dim * sizeof(float),
                       cudaMemcpyDeviceToHost));
         cbuf.resize((size_t)len * h->code_stride);
         CK(cudaMemcpy(cbuf.data(), h->d_codes.p + h->h_start[l] * h->code_stride, cbuf.size(),
                       cudaMemcpyDeviceToHost));
-        for (int64_t j = 0; j < len; j++)
-            for (int m = 0; m < M; m++) codes[(r + j) * M + m] = cbuf[(size_t)j * h->code_stride + m];
-        r += len;
+        for (int64_t j = 0; j < len; j++) {
+            if (!h->list_alive[l][j]) continue;
+            ids[r] = h->list_ids[l][j];
+            std::memcpy(vectors + r * dim, &vbuf[(size_t)j * dim], sizeof(float) * dim);
+            for (int m = 0; m < M; m++) codes[r * M + m] = cbuf[(size_t)j * h->code_stride + m];
+            r++;
+        }
     }
     // Pending vectors in ascending id order.
     std::vector<int64_t> pid;
@@ -1166,6 +1140,7 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
                       const int64_t* ids, const float* vectors, const int32_t* codes, const uint8_t* has_codes,
                       const int64_t* pending_ids, const float* pending_vectors) {
     if (!h || !L) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
@@ -1201,6 +1176,9 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
     h->h_coarse.assign(coarse, coarse + (size_t)L->nlist * dim);
     h->h_codebooks.assign(codebooks, codebooks + (size_t)M * L->pq_k_eff * h->dsub);
     h->list_ids.assign(h->nlist, {});
+    h->list_alive.assign(h->nlist, {});
+    h->live_count.assign(h->nlist, 0);
+    h->dead_rows = 0;
     h->list_key.assign(h->nlist, 0);
     h->cluster_counts.assign(h->nlist, 0);
     h->id_cluster.clear();
@@ -1212,6 +1190,8 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
             h->list_ids[l].push_back(ids[r]);
             h->id_cluster[ids[r]] = l;
         }
+        h->list_alive[l].assign(h->list_ids[l].size(), 1);
+        h->live_count[l] = (int64_t)h->list_ids[l].size();
     }
     h->d_vectors.reset();
     h->d_term.reset();
@@ -1226,13 +1206,13 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
     if (h->nlist == 0) return HANN_OK;
     CK(upload(h->d_coarse, h->h_coarse.data(), h->h_coarse.size(), h->stream));
     CK(upload(h->d_codebooks, h->h_codebooks.data(), h->h_codebooks.size(), h->stream));
+    {
+        int prc = prepare_coarse(h);
+        if (prc) return prc;
+    }
     std::vector<int64_t> caps(h->nlist);
     for (int l = 0; l < h->nlist; l++) caps[l] = list_capacity(list_len[l]);
-    std::vector<std::vector<int64_t>> saved;
-    saved.swap(h->list_ids);
-    h->list_ids.assign(h->nlist, {});
-    int rc = relayout(h, caps);
-    h->list_ids.swap(saved);
+    int rc = relayout(h, caps, false);
     if (rc) return rc;
     const int64_t n = L->n_rows;
     if (n == 0) return upload_lens(h);
@@ -1297,6 +1277,7 @@ int hann_gpu_distance_batch(int32_t metric, const float* query, const float* fla
 }
 
 }  // extern "C"
+
 // ---------------------------------------------------------------------------
 // Allocation-free batch search.
 //
@@ -1404,10 +1385,13 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     // is fully written by the kernel that produces it before it is read.
     noalloc_fill_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(dk, k, dnp, np, nq, fbc);
     CK(cudaGetLastError());
-    const ScanParams p = h->scan_params();
+    ScanParams p = h->scan_params();
+    p.kq = dk;
+    p.mode = mode;
+    p.rerank_fixed = h->o.rerank;
     CK(launch_dist_matrix(d_queries, nq, h->o.dimension, h->d_coarse.p, h->nlist, D, s));
-    CK(launch_probe_select(D, nq, h->nlist, dnp, np, dk, h->d_len.p, h->o.fallback ? 1 : 0, pid, pd, fb, fbc, s));
-    CK(launch_scan(p, d_queries, nq, pid, D, dnp, np, fb, R, crow, cd, cs, nullptr, s));
+    CK(launch_probe_select(D, nq, h->nlist, dnp, np, dk, h->d_live.p, h->o.fallback ? 1 : 0, pid, pd, fb, fbc, s));
+    CK(launch_scan(p, d_queries, nq, pid, pd, dnp, np, fb, R, crow, cd, cs, nullptr, s));
     CK(launch_rerank(p, d_queries, nq, crow, cs, R, dk, k, mode, d_ids, d_distances, d_n_out, s));
     return HANN_OK;
 }

@@ -1,0 +1,268 @@
+// index_internal.h -- the PQIVF handle shared by the library's host files
+// (index.cu: the index and its C ABI; serve.cu: the batching server).
+#pragma once
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <shared_mutex>
+#include <string>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "hann_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace hann {
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { reset(); }
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    // Grows to at least cnt elements; contents are not kept.
+    cudaError_t reserve(size_t cnt) {
+        if (cnt <= n && p) return cudaSuccess;
+        reset();
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(cnt, 1) * sizeof(T));
+        if (e == cudaSuccess) n = std::max<size_t>(cnt, 1);
+        else p = nullptr;
+        return e;
+    }
+    void swap(DBuf& o) {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+    }
+};
+
+// xoshiro256** seeded through splitmix64: the index's own seeded source for
+// k-means seeding and empty-cluster reseeds (the reference's seededRand,
+// pqivf/index.go:20-23).
+struct Rng {
+    uint64_t s[4];
+    void seed(uint64_t x) {
+        for (int i = 0; i < 4; i++) {
+            x += 0x9e3779b97f4a7c15ull;
+            uint64_t z = x;
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+            s[i] = z ^ (z >> 31);
+        }
+    }
+    static uint64_t rotl(uint64_t v, int k) { return (v << k) | (v >> (64 - k)); }
+    uint64_t next() {
+        const uint64_t r = rotl(s[1] * 5, 7) * 9;
+        const uint64_t t = s[1] << 17;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return r;
+    }
+    int64_t intn(int64_t n) {
+        const uint64_t un = (uint64_t)n;
+        const uint64_t lim = UINT64_MAX - UINT64_MAX % un;
+        uint64_t v;
+        do v = next();
+        while (v >= lim);
+        return (int64_t)(v % un);
+    }
+    // First k entries of a uniform random permutation of [0, n).
+    std::vector<int64_t> perm_prefix(int64_t n, int64_t k) {
+        std::unordered_map<int64_t, int64_t> sw;
+        std::vector<int64_t> out((size_t)k);
+        for (int64_t i = 0; i < k; i++) {
+            const int64_t j = i + intn(n - i);
+            auto get = [&](int64_t a) {
+                auto it = sw.find(a);
+                return it == sw.end() ? a : it->second;
+            };
+            const int64_t vi = get(i), vj = get(j);
+            out[(size_t)i] = vj;
+            sw[j] = vi;
+        }
+        return out;
+    }
+};
+
+}  // namespace hann
+
+using namespace hann;
+
+// Scratch of the exact nearest-centroid search, reused across k-means
+// iterations.
+struct AssignScratch {
+    DBuf<uint16_t> xbf, cbf;
+    DBuf<float> xn2, xres, cn2, cres, cmax, cand_val;
+    DBuf<int32_t> cand_idx, ovf_idx;
+    DBuf<int64_t> ovf_rows;
+    DBuf<int> counters;  // [0] overflow rows, [1] GEMM wait errors
+    DBuf<float> ovf_x;
+    bool x_ready = false;
+};
+
+// Scratch of Add/Delete, kept on the handle so mutations allocate nothing
+// once warm (an allocator call could synchronise with searches in flight).
+struct MutationScratch {
+    DBuf<float> x, term;
+    DBuf<int32_t> asg;
+    DBuf<uint8_t> codes;
+    DBuf<int64_t> dst, ids, rows;
+    AssignScratch asc;
+    std::vector<int32_t> hasg;
+    std::vector<int64_t> add;
+    int64_t n = 0;
+    bool grow = false;
+};
+
+// Device scratch of one search stream: query staging, coarse scores, probe
+// lists, candidates and results. One per stream that searches concurrently.
+struct SearchScratch {
+    DBuf<float> q, D, probe_d, cand_d, qn2, qres;
+    DBuf<uint16_t> qbf;
+    DBuf<int32_t> probe_ids, fb, cand_row, k, np, nout;
+    DBuf<uint32_t> cand_seq;
+    DBuf<int64_t> ids;
+    DBuf<double> dist;
+    DBuf<unsigned long long> fbcount;
+};
+
+struct hann_pqivf {
+    hann_pqivf_options o{};
+    int dsub = 0, code_stride = 0;
+    std::shared_mutex mu;   // searches shared, mutations exclusive
+    std::mutex wmu;         // every writer; taken before mu
+    std::mutex run_mu;
+    MutationScratch mut;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    Rng rng;
+    bool trained = false;
+    std::atomic<int64_t> fallback_searches{0};
+
+    std::unordered_map<int64_t, std::vector<float>> pending;
+
+    int nlist = 0, pqk_eff = 0;
+    std::vector<float> h_coarse, h_codebooks;
+    std::vector<std::vector<int64_t>> list_ids;     // per list, the id of every slot
+    std::vector<std::vector<uint8_t>> list_alive;   // 0 for a deleted (tombstoned) slot
+    std::vector<int64_t> live_count;
+    int64_t dead_rows = 0;
+    std::vector<uint8_t> list_key;
+    std::vector<int64_t> cluster_counts;
+    std::unordered_map<int64_t, int32_t> id_cluster;
+    std::vector<int64_t> h_start, h_cap;
+    int64_t rows_cap = 0;
+
+    DBuf<float> d_coarse, d_codebooks, d_vectors, d_term;
+    // BF16 copy of the coarse centroids for the tensor-core preselection
+    int kp = 0;
+    bool tc = false;
+    DBuf<uint16_t> d_coarse_bf16;
+    DBuf<float> d_coarse_norm, d_cmax;
+    DBuf<int> d_err;
+    DBuf<int64_t> d_start, d_row_id;
+    DBuf<int32_t> d_len, d_live, d_row_cluster;
+    DBuf<uint8_t> d_codes;
+
+    // search scratch of the handle's own stream
+    SearchScratch main;
+    DBuf<unsigned long long> s_rows;
+
+    // stage profiling: pairs of events per stage
+    bool profile = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[4];
+    int64_t launches = 0;
+
+    int fail(int code, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char* what) {
+        return fail(e == cudaErrorMemoryAllocation ? HANN_E_NOMEM : HANN_E_CUDA, "%s: %s", what,
+                    cudaGetErrorString(e));
+    }
+    int64_t total_rows() const {
+        int64_t t = 0;
+        for (int64_t c : live_count) t += c;
+        return t;
+    }
+    ScanParams scan_params() const {
+        ScanParams p;
+        p.dim = o.dimension;
+        p.M = o.num_subquantizers;
+        p.dsub = dsub;
+        p.pqK = pqk_eff;
+        p.nlist = nlist;
+        p.code_stride = code_stride;
+        p.coarse = d_coarse.p;
+        p.codebooks = d_codebooks.p;
+        p.list_start = d_start.p;
+        p.list_len = d_len.p;
+        p.codes = d_codes.p;
+        p.term = d_term.p;
+        p.row_cluster = d_row_cluster.p;
+        p.vectors = d_vectors.p;
+        p.row_id = d_row_id.p;
+        p.kq = nullptr;
+        p.mode = 0;
+        p.rerank_fixed = o.rerank;
+        return p;
+    }
+};
+
+
+#define CK(expr)                                          \
+    do {                                                  \
+        cudaError_t _e = (expr);                          \
+        if (_e != cudaSuccess) return h->cuda_fail(_e, #expr); \
+    } while (0)
+
+template <typename T>
+inline cudaError_t upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s) {
+    cudaError_t e = b.reserve(n);
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    return cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+// Search pipeline of index.cu, usable from any stream with its own scratch.
+int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k, const int32_t* d_np,
+               int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist, int32_t* d_nout, cudaStream_t s);
+int check_searchable(hann_pqivf* h);
+int rerank_depth(const hann_pqivf* h, int kmax, int mode);
+// Mutations with the writer lock held. Without allow_relayout a mutation
+// that would move rows (a list overflowing, or tombstone compaction) changes
+// nothing and sets *needs_relayout; the rest is safe beside running searches.
+int bulk_add_locked(hann_pqivf* h, const int64_t* ids, const float* vectors, int64_t n,
+                    bool allow_relayout = true, bool* needs_relayout = nullptr);
+int bulk_delete_locked(hann_pqivf* h, const int64_t* ids, int64_t n, bool allow_relayout = true,
+                       bool* needs_relayout = nullptr);
+int add_prepare(hann_pqivf* h, const int64_t* ids, const float* vecs, int64_t n);
+int add_commit(hann_pqivf* h, const int64_t* ids);
+bool compaction_due(const hann_pqivf* h, int64_t extra);

@@ -74,9 +74,51 @@ cudaError_t launch_gather2(const float* a, const float* b, const int64_t* src, i
 cudaError_t launch_gather_cols(const float* in, int64_t ld, int off, const int64_t* src, const int32_t* dst,
                                int64_t n, int w, float* out, int64_t ldo, cudaStream_t s);
 
+// Marks rows deleted: term = +inf (never selected by a scan), row_id = -1.
+cudaError_t launch_tombstone(const int64_t* rows, int64_t n, float* term, int64_t* row_id, cudaStream_t s);
+
 // Reference-order batch distances of one query to n rows (simd_*_batch).
 cudaError_t launch_distance_rows(int metric, const float* q, const float* flat, int dim, int64_t n, double* out,
                                  cudaStream_t s);
+
+// ---- BF16 tensor-core distance GEMM (kernels_gemm.cu) ----------------------------
+
+// K padded for the GEMM (multiple of 8 BF16 = 16 bytes); candidates per row of
+// the argmin mode.
+int gemm_kpad(int dim);
+int gemm_topc();
+// FP32 rows to BF16 [n][kp] (zero padded) and, when not null, the FP32
+// squared norm of each row and the norm of its BF16 rounding error.
+cudaError_t launch_to_bf16(const float* x, int64_t n, int dim, int kp, void* out_bf16, float* sqnorm, float* resid,
+                           cudaStream_t s);
+// S[i][j] = bias[j] - 2 <a_i, b_j> for every pair (a: nrows x kp, b: ncols x kp).
+cudaError_t launch_gemm_scores(const void* a_bf16, int64_t nrows, const void* b_bf16, int ncols, int kp,
+                               const float* bias, float* out, int* err, cudaStream_t s);
+// Per row the gemm_topc() smallest scores and their columns, ascending.
+cudaError_t launch_gemm_top8(const void* a_bf16, int64_t nrows, const void* b_bf16, int ncols, int kp,
+                             const float* bias, int32_t* cand_idx, float* cand_val, int* err, cudaStream_t s);
+
+// ---- exact answers from the BF16 scores (kernels_rescore.cu) --------------------
+
+// Probe selection from BF16 scores S [nq][nlist] (rows may be overwritten):
+// the nprobe nearest lists by exact reference-order distance, ascending
+// (distance, index), with those distances; fallback flags as
+// launch_probe_select. cmax points at max ||c||.
+cudaError_t launch_probe_select_band(float* S, const float* Q, const float* qn2, const float* qres, int64_t nq,
+                                     int dim, int kp, const float* coarse, const float* cmax, int nlist,
+                                     const int32_t* nprobe,
+                                     int np_max, const int32_t* k, const int32_t* list_len, int allow_fallback,
+                                     int32_t* probe_ids, float* probe_d, int32_t* fallback,
+                                     unsigned long long* fallback_count, cudaStream_t s);
+// Exact argmin from the GEMM's 8 candidates per row; rows whose candidate
+// band overflows are appended to overflow_rows (*n_overflow counts them) and
+// left for the exact tiled kernel.
+cudaError_t launch_rescore_top8(const float* x, const float* xn2, const float* xres, int64_t n, int dim, int kp,
+                                const float* cent, int k, const float* cmax, const int32_t* cand_idx,
+                                const float* cand_val, int32_t* out_idx, int64_t* overflow_rows, int* n_overflow,
+                                cudaStream_t s);
+// out[0] = max_i sqrt(sqnorm[i]), out[1] = max_i resid[i].
+cudaError_t launch_norm_maxes(const float* sqnorm, const float* resid, int n, float* out, cudaStream_t s);
 
 // ---- search ---------------------------------------------------------------------
 
@@ -91,6 +133,8 @@ struct ScanParams {
     const int32_t* row_cluster;  // [rows]
     const float* vectors;     // [rows][dim]
     const int64_t* row_id;    // [rows]
+    const int32_t* kq;        // [nq] per-query k (sets each query's rerank depth)
+    int mode, rerank_fixed;
 };
 
 // Per query: the nprobe nearest coarse lists in ascending (distance, index)
@@ -102,14 +146,23 @@ cudaError_t launch_probe_select(const float* D, int64_t nq, int nlist, const int
                                 unsigned long long* fallback_count, cudaStream_t s);
 
 // ADC scan: per query, the R best rows by the decomposed PQ distance over the
-// probed lists (all lists for a fallback query). D is the coarse distance
-// matrix [nq][nlist]. Outputs rows (-1 padded), approximate distances and
-// candidate sequence keys; adds the rows it scanned to *rows_scanned (may be
-// null).
+// probed lists (all lists for a fallback query). probe_d [nq][np_max] holds
+// the exact coarse distance of each probed list. Outputs rows (-1 padded),
+// approximate distances and candidate sequence keys; adds the rows it
+// scanned to *rows_scanned (may be null).
 cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
-                        const float* D, const int32_t* nprobe, int np_max, const int32_t* fallback,
+                        const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback,
                         int R, int32_t* cand_row, float* cand_d, uint32_t* cand_seq,
                         unsigned long long* rows_scanned, cudaStream_t s);
+
+// The bank-conflict-free scan (kernels_scan.cu) for M a multiple of 4 up to
+// 32; launch_scan dispatches to it when it applies. Its candidates leave
+// unsorted.
+bool scan_skew_supported(int M);
+cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
+                             const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
+                             int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
+                             cudaStream_t s);
 
 // Rerank the R candidates of each query with an exact FP32 distance and emit
 // the k best: mode 0 = the reference's reconstructed-vector distance
@@ -119,5 +172,56 @@ cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, c
 cudaError_t launch_rerank(const ScanParams& p, const float* queries, int64_t nq, const int32_t* cand_row,
                           const uint32_t* cand_seq, int R, const int32_t* k, int kmax, int mode,
                           int64_t* ids, double* dist, int32_t* nout, cudaStream_t s);
+
+// ---- batched exact k-NN over a flat base (kernels_knn.cu) ------------------------
+
+constexpr int KNN_SIMT_DMAX = 256;  // register-tiled SIMT distances up to this dimension
+constexpr int KNN_TC_DMAX = 128;    // tensor-core screen up to this dimension (GEMM K)
+
+// Exact SIMT filter over base rows [c_begin, c_end) for metric 0..3: every
+// (distance, row) key below thr[qi] is appended to the candidate buffer of
+// query qi (cap entries per query; cnt keeps counting past cap). Row r of the
+// launch is query qlist[r] (all nrows queries when qlist is null).
+cudaError_t launch_knn_filter(int metric, const float* q, const int32_t* qlist, int nrows, int dim, const float* base,
+                              int64_t c_begin, int64_t c_end, const float* qnorm, const float* bnorm,
+                              const unsigned long long* thr, int cap, int32_t* cnt, int32_t* cand_id, float* cand_d,
+                              cudaStream_t s);
+// Reference-order distances of nrows queries to base rows [c_begin, c_end)
+// as FP64, out[r * ld + col - c_begin].
+cudaError_t launch_knn_matrix(int metric, const float* q, int nrows, int dim, const float* base, int64_t c_begin,
+                              int64_t c_end, const float* qnorm, const float* bnorm, double* out, int64_t ld,
+                              cudaStream_t s);
+// Folds each query's candidates into its sorted top-k list; a query whose
+// candidates overflowed is flagged in redo (and counted) and keeps its list.
+cudaError_t launch_knn_merge_exact(int nrows, const int32_t* qlist, int k, int cap, int32_t* cnt,
+                                   const int32_t* cand_id, const float* cand_d, unsigned long long* list,
+                                   int32_t* lcount, unsigned long long* thr, int32_t* redo, int* redo_count,
+                                   cudaStream_t s);
+size_t knn_merge_exact_smem(int k, int cap);
+// Tensor-core screen: filter GEMM (kernels_gemm.cu), band merge, exact final.
+cudaError_t launch_gemm_filter(const void* a_bf16, int64_t nrows, const void* b_bf16, int64_t nb, int kp,
+                               int col_begin, int col_end, const float2* cterm, const float* rthr, int cap,
+                               int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s);
+cudaError_t launch_knn_merge_band(int nrows, int k, int cap, int lcap, int32_t* cnt, const int32_t* cand_id,
+                                  const float* cand_s, const float* e2, const float* asl, unsigned long long* list,
+                                  int32_t* lcount, float* thr, int32_t* need_exact, cudaStream_t s);
+size_t knn_merge_band_smem(int lcap, int cap);
+cudaError_t launch_knn_final_band(int metric, int nrows, int k, int lcap, int dim, const float* queries,
+                                  const float* base, const float* qnorm, const float* bnorm,
+                                  const unsigned long long* list, const int32_t* lcount, const int32_t* need_exact,
+                                  int32_t* exact_list, int* exact_count, int64_t* out_ids, double* out_dist,
+                                  cudaStream_t s);
+// Sorted exact lists of rows qlist[p] (or all nrows) to ids / FP64 distances.
+cudaError_t launch_knn_emit(int nrows, int k, const unsigned long long* list, const int32_t* lcount,
+                            const int32_t* qlist, int64_t* out_ids, double* out_dist, cudaStream_t s);
+// dot_ref(x, x) of every row (the cosine kernel's norm accumulation).
+cudaError_t launch_ref_sqnorm(const float* x, int64_t n, int dim, float* out, cudaStream_t s);
+// Screen epilogue terms per base row and the maxima the error bound needs
+// (maxes: two floats as bits, zeroed by the caller).
+cudaError_t launch_knn_col_terms(const float* sqnorm, const float* resid, int64_t n, int cosine, float2* terms,
+                                 unsigned int* maxes, cudaStream_t s);
+// Per-query band constants e2 (= 2 eps) and slack scale.
+cudaError_t launch_knn_query_band(const float* qsq, const float* qres, int64_t nq, int kp, int cosine,
+                                  const unsigned int* maxes, float* e2, float* asl, cudaStream_t s);
 
 }  // namespace hann

@@ -1,0 +1,237 @@
+// kernels_rescore.cu -- exact answers from the BF16 tensor-core scores.
+//
+// The GEMM in kernels_gemm.cu ranks columns by s~(a, b) = ||b||^2 - 2<a, b>
+// computed from BF16 operands; |s~ - s| <= eps(a) with eps(a) from
+// bf16_score_eps (common.cuh). Both kernels
+// here rescore, with the reference's exact FP32 distance (common.cuh,
+// sqeuclid_ref), every column whose approximate score can still reach the
+// boundary, so their outputs equal the exact SIMT path's:
+//   * probe_select_band: the nprobe nearest lists of a query. With T~ the
+//     nprobe-th smallest approximate score, every list of the exact top
+//     nprobe has s~ <= T~ + 2 eps; all of those are rescored exactly and the
+//     best nprobe by (exact distance, index) are kept (nearestCentroids,
+//     pqivf/index.go:184-206). More than PS_MAX of them (a degenerate band)
+//     falls back to rescoring the whole row.
+//   * rescore_top8: the argmin for k-means and Add (assignPoints,
+//     pqivf/index.go:738-789). The GEMM kept each row's 8 smallest scores;
+//     if the 8th is still inside the band [s~min, s~min + 2 eps] the band may
+//     hold more columns and the row is listed for the exact tiled kernel,
+//     otherwise the exact argmin (lowest index on a tie) is among the 8.
+#include "common.cuh"
+#include "kernels.h"
+#include "select.cuh"
+
+namespace hann {
+namespace {
+
+constexpr int PB_THREADS = 256;
+constexpr int PB_MAX = 4096;
+constexpr int QMAX = 128;
+
+__global__ void __launch_bounds__(PB_THREADS) probe_select_band_kernel(
+    float* __restrict__ S, const float* __restrict__ Q, const float* __restrict__ qn2,
+    const float* __restrict__ qres, int dim, int kp, const float* __restrict__ coarse,
+    const float* __restrict__ cmax_p, int nlist, const int32_t* __restrict__ nprobe,
+    int np_max, const int32_t* __restrict__ kq, const int32_t* __restrict__ list_len, int allow_fb,
+    int32_t* __restrict__ probe_ids, float* __restrict__ probe_d, int32_t* __restrict__ fallback,
+    unsigned long long* __restrict__ fb_count, int row_in_smem) {
+    __shared__ uint32_t s_key[PB_MAX];
+    __shared__ int32_t s_idx[PB_MAX];
+    __shared__ float qv[QMAX];
+    __shared__ uint32_t s_prefix, s_rem, s_and, s_or;
+    __shared__ int s_cnt, s_cnt2;
+    __shared__ unsigned long long s_total;
+    __shared__ unsigned int whist[(PB_THREADS / 32) * 256];
+    extern __shared__ __align__(16) float srow[];
+    const int tid = threadIdx.x;
+    const int64_t q = blockIdx.x;
+    float* row = S + q * nlist;
+    if (row_in_smem) {
+        // one read of the score row; every pass below runs on shared memory
+        const float4* g4 = reinterpret_cast<const float4*>(row);
+        float4* s4 = reinterpret_cast<float4*>(srow);
+        const int n4 = (nlist & 3) == 0 ? nlist >> 2 : 0;
+        for (int i = tid; i < n4; i += PB_THREADS) s4[i] = g4[i];
+        for (int i = 4 * n4 + tid; i < nlist; i += PB_THREADS) srow[i] = row[i];
+        row = srow;
+    }
+    const int np = min(nprobe[q], nlist);
+    for (int e = tid; e < dim; e += PB_THREADS) qv[e] = Q[q * dim + e];
+    if (tid == 0) {
+        s_cnt = 0;
+        s_cnt2 = 0;
+        s_total = 0;
+    }
+    radix_nth_fast<PB_THREADS>(row, nlist, np, whist, &s_prefix, &s_rem, &s_and, &s_or);
+    const float eps = bf16_score_eps(sqrtf(qn2[q]), qres[q], cmax_p[0], cmax_p[1], kp);
+    const float tA = key_float(s_prefix);
+    // plus twice the FP32 rounding of a reference-order distance (about
+    // dim * 2^-24 of its size, covered by 2e-5 here for dim <= 128)
+    const float thr = tA + 2.0f * eps + 2e-5f * (fabsf(tA) + qn2[q]);
+    for (int c = tid; c < nlist; c += PB_THREADS) {
+        if (row[c] <= thr) {
+            const int pos = atomicAdd(&s_cnt, 1);
+            if (pos < PB_MAX) s_idx[pos] = c;
+        }
+    }
+    __syncthreads();
+    int C = s_cnt;
+    if (C > PB_MAX) {
+        // Degenerate band: rescore the whole row exactly, then select on it.
+        for (int c = tid; c < nlist; c += PB_THREADS) row[c] = sqeuclid_ref(qv, coarse + (int64_t)c * dim, dim);
+        __syncthreads();
+        radix_nth_fast<PB_THREADS>(row, nlist, np, whist, &s_prefix, &s_rem, &s_and, &s_or);
+        const uint32_t T = s_prefix;
+        for (int c = tid; c < nlist; c += PB_THREADS) {
+            const uint32_t key = float_key(row[c]);
+            if (key <= T) {
+                const int pos = atomicAdd(&s_cnt2, 1);
+                if (pos < PB_MAX) {
+                    s_key[pos] = key;
+                    s_idx[pos] = c;
+                }
+            }
+        }
+        __syncthreads();
+        C = min(s_cnt2, PB_MAX);
+    } else {
+        for (int i = tid; i < C; i += PB_THREADS)
+            s_key[i] = float_key(sqeuclid_ref(qv, coarse + (int64_t)s_idx[i] * dim, dim));
+    }
+    int P = 1;
+    while (P < C) P <<= 1;
+    for (int i = C + tid; i < P; i += PB_THREADS) {
+        s_key[i] = 0xffffffffu;
+        s_idx[i] = 0x7fffffff;
+    }
+    __syncthreads();
+    sort_ki(s_key, s_idx, P);
+    unsigned long long part = 0;
+    for (int i = tid; i < np; i += PB_THREADS) {
+        probe_ids[q * np_max + i] = s_idx[i];
+        probe_d[q * np_max + i] = key_float(s_key[i]);
+        part += (unsigned long long)list_len[s_idx[i]];
+    }
+    atomicAdd(&s_total, part);
+    __syncthreads();
+    if (tid == 0) {
+        const int fb = (allow_fb && s_total < (unsigned long long)kq[q]) ? 1 : 0;
+        fallback[q] = fb;
+        if (fb) atomicAdd(fb_count, 1ull);
+    }
+}
+
+__global__ void rescore_top8_kernel(const float* __restrict__ x, const float* __restrict__ xn2,
+                                    const float* __restrict__ xres, int64_t n, int dim, int kp,
+                                    const float* __restrict__ cent, int k, const float* __restrict__ cmax_p,
+                                    const int32_t* __restrict__ cand_idx, const float* __restrict__ cand_val,
+                                    int32_t* __restrict__ out_idx, int64_t* __restrict__ overflow_rows,
+                                    int* __restrict__ n_overflow) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float eps = bf16_score_eps(sqrtf(xn2[r]), xres[r], cmax_p[0], cmax_p[1], kp);
+    const float v0 = cand_val[r * 8];
+    const float thr = v0 + 2.0f * eps + 2e-5f * (fabsf(v0) + xn2[r]);
+    if (k > 8 && cand_val[r * 8 + 7] <= thr) {
+        const int pos = atomicAdd(n_overflow, 1);
+        overflow_rows[pos] = r;
+        return;
+    }
+    const float* xr = x + r * dim;
+    float bd = __int_as_float(0x7f800000);
+    int bi = 0x7fffffff;
+    for (int c = 0; c < 8; c++) {
+        const int idx = cand_idx[r * 8 + c];
+        if (idx < 0 || cand_val[r * 8 + c] > thr) break;
+        const float d = sqeuclid_ref(xr, cent + (int64_t)idx * dim, dim);
+        if (d < bd || (d == bd && idx < bi)) {
+            bd = d;
+            bi = idx;
+        }
+    }
+    out_idx[r] = bi == 0x7fffffff ? 0 : bi;
+}
+
+__global__ void norm_maxes_kernel(const float* __restrict__ v, const float* __restrict__ res, int n,
+                                  float* __restrict__ out) {
+    __shared__ float red[256], red2[256];
+    float m = 0.0f, m2 = 0.0f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        m = fmaxf(m, sqrtf(fmaxf(v[i], 0.0f)));
+        m2 = fmaxf(m2, res[i]);
+    }
+    red[threadIdx.x] = m;
+    red2[threadIdx.x] = m2;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + s]);
+            red2[threadIdx.x] = fmaxf(red2[threadIdx.x], red2[threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = red[0] * 1.0001f;
+        out[1] = red2[0];
+    }
+}
+
+__global__ void scatter_i32_kernel(const int32_t* __restrict__ src, const int64_t* __restrict__ rows, const int* n,
+                                   int32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < *n) out[rows[i]] = src[i];
+}
+
+}  // namespace
+
+cudaError_t launch_probe_select_band(float* S, const float* Q, const float* qn2, const float* qres, int64_t nq,
+                                     int dim, int kp, const float* coarse, const float* cmax, int nlist,
+                                     const int32_t* nprobe,
+                                     int np_max, const int32_t* k, const int32_t* list_len, int allow_fallback,
+                                     int32_t* probe_ids, float* probe_d, int32_t* fallback,
+                                     unsigned long long* fallback_count, cudaStream_t s) {
+    if (nq <= 0) return cudaSuccess;
+    if (np_max > PB_MAX || dim > QMAX) return cudaErrorInvalidValue;
+    // The score row lives in shared memory when it fits beside the 34 KiB of
+    // static buffers.
+    const size_t row_bytes = (size_t)nlist * sizeof(float);
+    const int in_smem = row_bytes <= 160 * 1024 ? 1 : 0;
+    const size_t dyn = in_smem ? row_bytes : 0;
+    // static buffers (about 34 KiB) plus the row can pass the 48 KiB default
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(probe_select_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             160 * 1024);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    probe_select_band_kernel<<<(unsigned)nq, PB_THREADS, dyn, s>>>(S, Q, qn2, qres, dim, kp, coarse, cmax, nlist,
+                                                                  nprobe,
+                                                                  np_max, k, list_len, allow_fallback, probe_ids,
+                                                                  probe_d, fallback, fallback_count, in_smem);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rescore_top8(const float* x, const float* xn2, const float* xres, int64_t n, int dim, int kp,
+                                const float* cent, int k, const float* cmax, const int32_t* cand_idx,
+                                const float* cand_val, int32_t* out_idx, int64_t* overflow_rows, int* n_overflow,
+                                cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    rescore_top8_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, xn2, xres, n, dim, kp, cent, k, cmax, cand_idx,
+                                                                   cand_val, out_idx, overflow_rows, n_overflow);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_norm_maxes(const float* sqnorm, const float* resid, int n, float* out, cudaStream_t s) {
+    norm_maxes_kernel<<<1, 256, 0, s>>>(sqnorm, resid, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_i32(const int32_t* src, const int64_t* rows, const int* n, int64_t cap, int32_t* out,
+                               cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    scatter_i32_kernel<<<(unsigned)ceil_div(cap, 256), 256, 0, s>>>(src, rows, n, out);
+    return cudaGetLastError();
+}
+
+}  // namespace hann

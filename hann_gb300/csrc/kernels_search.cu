@@ -278,7 +278,7 @@ __device__ __forceinline__ void load_code_words(const uint8_t* __restrict__ code
 // generic path for any M.
 template <int MW>
 __global__ void __launch_bounds__(SC_THREADS) scan_kernel(ScanParams p, const float* __restrict__ Q,
-                                                          const float* __restrict__ D,
+                                                          const float* __restrict__ probe_d,
                                                           const int32_t* __restrict__ probe_ids,
                                                           const int32_t* __restrict__ nprobe, int np_max,
                                                           const int32_t* __restrict__ fallback, int R, int CAPW,
@@ -317,7 +317,20 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(ScanParams p, const fl
     unsigned long long scanned = 0;
     for (int i = w; i < nl; i += SC_WARPS) {
         const int l = fb ? i : probe_ids[q * np_max + i];
-        const float base = D[q * p.nlist + l];
+        float base;
+        if (fb) {
+            // Fallback scans every list: its coarse distance, lane-parallel.
+            float part = 0.0f;
+            for (int j = lane; j < p.dim; j += 32) {
+                const float t = qv[j] - p.coarse[(int64_t)l * p.dim + j];
+                part = fmaf(t, t, part);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            base = part;
+        } else {
+            base = probe_d[q * np_max + i];
+        }
         const int64_t start = p.list_start[l];
         const int len = p.list_len[l];
         scanned += (unsigned long long)len;
@@ -404,8 +417,9 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(ScanParams p, const fl
     }
     __syncthreads();
     block_sort_cand(wdall, wsall, wrall, P);
+    const int Rq = p.kq ? min(R, rerank_depth_for(p.kq[q], p.mode, p.rerank_fixed)) : R;
     for (int i = tid; i < R; i += SC_THREADS) {
-        const bool ok = wrall[i] != 0x7fffffff;
+        const bool ok = i < Rq && wrall[i] != 0x7fffffff;
         cand_row[q * R + i] = ok ? wrall[i] : -1;
         cand_d[q * R + i] = wdall[i];
         cand_seq[q * R + i] = wsall[i];
@@ -419,10 +433,17 @@ static int cap_for(int R) {
 }
 
 cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
-                        const float* D, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
+                        const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
                         int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
                         cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
+    if (scan_skew_supported(p.M)) {
+        int capw = 128;
+        while (capw < 4 * R) capw <<= 1;
+        if ((size_t)256 * 32 * 4 + (size_t)SC_WARPS * capw * 12 + (size_t)SC_WARPS * R * 12 <= 200 * 1024)
+            return launch_scan_skew(p, queries, nq, probe_ids, probe_d, nprobe, np_max, fallback, R, cand_row,
+                                    cand_d, cand_seq, rows_scanned, s);
+    }
     const int CAPW = cap_for(R);
     int P = 1;
     while (P < SC_WARPS * R) P <<= 1;
@@ -443,7 +464,7 @@ cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, c
     }
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    void* args[] = {(void*)&p, (void*)&queries, (void*)&D, (void*)&probe_ids, (void*)&nprobe, (void*)&np_max,
+    void* args[] = {(void*)&p, (void*)&queries, (void*)&probe_d, (void*)&probe_ids, (void*)&nprobe, (void*)&np_max,
                     (void*)&fallback, (void*)&R, (void*)&CAPW, (void*)&cand_row, (void*)&cand_d, (void*)&cand_seq,
                     (void*)&rows_scanned};
     e = cudaLaunchKernel(fn, dim3((unsigned)nq), dim3(SC_THREADS), args, smem, s);
@@ -488,7 +509,7 @@ __global__ void __launch_bounds__(RR_THREADS) rerank_kernel(ScanParams p, const 
     int valid = 0;
     for (int i = tid; i < RP; i += RR_THREADS) {
         const int32_t row = i < R ? cand_row[q * R + i] : -1;
-        if (row >= 0) {
+        if (row >= 0 && p.row_id[row] >= 0) {
             float d;
             if (mode == 0) {
                 ReconRow rec{p.coarse + (int64_t)p.row_cluster[row] * p.dim, p.codebooks,

@@ -8,116 +8,19 @@
 // pqivf/index.go:816-843); the mean is rounded once to FP32.
 #include "common.cuh"
 #include "kernels.h"
+#include "tile_dist.cuh"
 
 #include <algorithm>
 
 namespace hann {
 
 // ---------------------------------------------------------------------------
-// Tiled exact distances. A block owns TP points and walks every centroid in
-// tiles of TC. Each thread owns 4 points x 4 centroids and accumulates the 16
-// pairs chain by chain in the reference's order, so all 16 pairs share each
-// shared-memory load (one float4 of points, one float4 of centroids per
-// element).
+// Tiled exact distances (tile_dist.cuh). A block owns TP points and walks
+// every centroid in tiles of TC; each thread owns 4 points x 4 centroids.
 constexpr int TD_THREADS = 256;
 constexpr int TD_TP = 128;
 constexpr int TD_TC = 32;
 constexpr int TD_DMAX = 128;
-
-struct Acc16 {
-    float v[4][4];
-};
-
-__device__ __forceinline__ void chain16(const float* __restrict__ Xs, const float* __restrict__ Cs, int tp, int tc,
-                                        int u, int l, int t16, int lim4, int s4, Acc16& acc) {
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int b = 0; b < 4; b++) acc.v[a][b] = 0.0f;
-    for (int t = 0; t < t16; t++) {
-        const int i = 16 * t + 4 * u + l;
-        const float4 xp = *reinterpret_cast<const float4*>(Xs + i * TD_TP + 4 * tp);
-        const float4 cc = *reinterpret_cast<const float4*>(Cs + i * TD_TC + 4 * tc);
-        const float xa[4] = {xp.x, xp.y, xp.z, xp.w};
-        const float cb[4] = {cc.x, cc.y, cc.z, cc.w};
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                float d = xa[a] - cb[b];
-                acc.v[a][b] = __fmaf_rn(d, d, acc.v[a][b]);
-            }
-    }
-    if (u == 0) {
-        for (int s = 0; s < s4; s++) {
-            const int i = lim4 + 4 * s + l;
-            const float4 xp = *reinterpret_cast<const float4*>(Xs + i * TD_TP + 4 * tp);
-            const float4 cc = *reinterpret_cast<const float4*>(Cs + i * TD_TC + 4 * tc);
-            const float xa[4] = {xp.x, xp.y, xp.z, xp.w};
-            const float cb[4] = {cc.x, cc.y, cc.z, cc.w};
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    float d = xa[a] - cb[b];
-                    acc.v[a][b] = __fmaf_rn(d, d, acc.v[a][b]);
-                }
-        }
-    }
-}
-
-// Reference-order distances of the thread's 16 pairs for the current tiles.
-__device__ __forceinline__ void tile_pairs(const float* __restrict__ Xs, const float* __restrict__ Cs, int tp,
-                                           int tc, int dim, float out[4][4]) {
-    const int lim4 = dim - (dim % 16);
-    const int lim = dim - (dim % 4);
-    const int t16 = lim4 / 16;
-    const int s4 = (lim - lim4) / 4;
-    Acc16 acc, c01, c2;
-    float v01[4][4], v2[4][4];
-#pragma unroll 1
-    for (int l = 0; l < 4; l++) {
-        chain16(Xs, Cs, tp, tc, 0, l, t16, lim4, s4, acc);
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) c01.v[a][b] = acc.v[a][b];
-        chain16(Xs, Cs, tp, tc, 1, l, t16, lim4, s4, acc);
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) c01.v[a][b] = __fadd_rn(c01.v[a][b], acc.v[a][b]);
-        chain16(Xs, Cs, tp, tc, 2, l, t16, lim4, s4, acc);
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) c2.v[a][b] = acc.v[a][b];
-        chain16(Xs, Cs, tp, tc, 3, l, t16, lim4, s4, acc);
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                float vl = __fadd_rn(c01.v[a][b], __fadd_rn(c2.v[a][b], acc.v[a][b]));
-                if (l == 0) v01[a][b] = vl;
-                else if (l == 1) v01[a][b] = __fadd_rn(v01[a][b], vl);
-                else if (l == 2) v2[a][b] = vl;
-                else out[a][b] = __fadd_rn(v01[a][b], __fadd_rn(v2[a][b], vl));
-            }
-    }
-    for (int i = lim; i < dim; i++) {
-        const float4 xp = *reinterpret_cast<const float4*>(Xs + i * TD_TP + 4 * tp);
-        const float4 cc = *reinterpret_cast<const float4*>(Cs + i * TD_TC + 4 * tc);
-        const float xa[4] = {xp.x, xp.y, xp.z, xp.w};
-        const float cb[4] = {cc.x, cc.y, cc.z, cc.w};
-#pragma unroll
-        for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                float d = xa[a] - cb[b];
-                out[a][b] = __fadd_rn(out[a][b], __fmul_rn(d, d));
-            }
-    }
-}
 
 // MODE 0: argmin per point. MODE 1: full distance matrix.
 // The centroid range is split over gridDim.y blocks (tiles_per_split tiles
@@ -162,7 +65,7 @@ __global__ void __launch_bounds__(TD_THREADS) tile_dist_kernel(const float* __re
         }
         __syncthreads();
         float dd[4][4];
-        tile_pairs(Xs, Cs, tp, tc, dim, dd);
+        tile_pairs<OP_SQDIFF, TD_TP, TD_TC>(Xs, Cs, tp, tc, dim, dd);
         if (MODE == 0) {
 #pragma unroll
             for (int a = 0; a < 4; a++)
@@ -600,6 +503,20 @@ cudaError_t launch_gather_cols(const float* in, int64_t ld, int off, const int64
                                int w, float* out, int64_t ldo, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     gather_cols_kernel<<<(unsigned)ceil_div(n * w, 256), 256, 0, s>>>(in, ld, off, src, dst, n, w, out, ldo);
+    return cudaGetLastError();
+}
+
+__global__ void tombstone_kernel(const int64_t* __restrict__ rows, int64_t n, float* __restrict__ term,
+                                 int64_t* __restrict__ row_id) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    term[rows[i]] = __int_as_float(0x7f800000);
+    row_id[rows[i]] = -1;
+}
+
+cudaError_t launch_tombstone(const int64_t* rows, int64_t n, float* term, int64_t* row_id, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    tombstone_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(rows, n, term, row_id);
     return cudaGetLastError();
 }
 

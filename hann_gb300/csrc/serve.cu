@@ -1,0 +1,510 @@
+// serve.cu -- continuous-batching search server on one GPU.
+//
+// Requests (a block of queries with its own k and nprobe) arrive from any
+// number of host threads. A scheduler thread packs waiting requests into
+// device batches and runs each batch on one of `slots` CUDA streams, each
+// with its own scratch (SearchScratch) and pinned staging buffers, so up to
+// `slots` batches are in flight and overlap on the device. Requests that
+// arrive while batches run are admitted into the next free slot; a batch
+// takes requests in arrival order while its queries fit max_batch_queries
+// and its device scratch fits the slot's share of the memory budget
+// (admission by device memory). Add/Delete requests are applied between
+// batches: the scheduler stops starting batches, waits for the running ones
+// and applies the mutation under the index's exclusive lock.
+//
+// Every request is an ordinary Search of its queries (pqivf/index.go:850-949)
+// with per-query k and nprobe, so its result does not depend on what it was
+// batched with.
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <thread>
+
+#include "index_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    uint64_t ticket = 0;
+    int kind = 0;  // 0 search, 1 add, 2 delete
+    int32_t nq = 0, k = 0, nprobe = 0;
+    std::vector<float> queries;
+    std::vector<int64_t> ids;  // add/delete
+    std::vector<float> vectors;
+    std::vector<int64_t> out_ids;
+    std::vector<double> out_dist;
+    std::vector<int32_t> out_n;
+    int status = 1;  // 1 pending, 0 done, <0 error
+    std::string error;
+    Clock::time_point t_submit, t_done;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    SearchScratch sc;
+    float* h_q = nullptr;  // pinned staging
+    int32_t* h_k = nullptr;
+    int32_t* h_np = nullptr;
+    int64_t* h_ids = nullptr;
+    double* h_dist = nullptr;
+    int32_t* h_n = nullptr;
+    DBuf<float> d_q;
+    DBuf<int32_t> d_k, d_np, d_n;
+    DBuf<int64_t> d_ids;
+    DBuf<double> d_dist;
+    bool busy = false;
+    int kmax = 0;
+    std::vector<std::shared_ptr<Request>> reqs;
+    std::vector<int32_t> offsets;
+};
+
+}  // namespace
+
+struct hann_server {
+    hann_pqivf* h = nullptr;
+    hann_serve_options o{};
+    std::vector<std::unique_ptr<Slot>> slots;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Request>> queue;
+    std::unordered_map<uint64_t, std::shared_ptr<Request>> tickets;
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    std::thread thr;
+    std::string err;
+    // statistics
+    std::vector<double> lat_ms;
+    int64_t queries_done = 0, requests_done = 0, batches = 0, mutations = 0;
+    int64_t peak_admitted = 0, cur_admitted = 0, relayouts = 0;
+    double mutation_ms = 0.0;
+    bool mut_drain = false;
+    Clock::time_point t_first{}, t_last{};
+    bool any = false;
+    std::shared_lock<std::shared_mutex> read_lock;  // held while batches run
+    int64_t slot_budget = 0;
+};
+
+namespace {
+
+int64_t batch_bytes(const hann_pqivf* h, int64_t nq, int kmax, int np_max, int mode) {
+    const int R = rerank_depth(h, kmax, mode);
+    const int64_t dim = h->o.dimension;
+    return nq * (h->nlist * 4 + np_max * 8 + R * 12 + dim * 4 + h->kp * 2 + 4 * 6 + kmax * 16) + 4096;
+}
+
+void complete(hann_server* s, Slot& sl) {
+    // results are in the slot's pinned buffers
+    for (size_t i = 0; i < sl.reqs.size(); i++) {
+        auto& r = sl.reqs[i];
+        const int off = sl.offsets[i];
+        r->out_ids.resize((size_t)r->nq * r->k);
+        r->out_dist.resize((size_t)r->nq * r->k);
+        r->out_n.resize((size_t)r->nq);
+        for (int q = 0; q < r->nq; q++) {
+            std::memcpy(&r->out_ids[(size_t)q * r->k], &sl.h_ids[(size_t)(off + q) * sl.kmax], sizeof(int64_t) * r->k);
+            std::memcpy(&r->out_dist[(size_t)q * r->k], &sl.h_dist[(size_t)(off + q) * sl.kmax],
+                        sizeof(double) * r->k);
+            r->out_n[q] = sl.h_n[off + q];
+        }
+        r->t_done = Clock::now();
+        r->status = 0;
+        s->lat_ms.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+        s->queries_done += r->nq;
+        s->requests_done++;
+        s->t_last = r->t_done;
+    }
+    sl.reqs.clear();
+    sl.offsets.clear();
+    sl.busy = false;
+}
+
+// Launches a batch on a free slot. Called with s->mu held and the index's
+// shared lock taken.
+int launch_batch(hann_server* s, Slot& sl, std::vector<std::shared_ptr<Request>>& take) {
+    hann_pqivf* h = s->h;
+    int64_t nq = 0;
+    int kmax = 1, np_max = 1;
+    for (auto& r : take) {
+        nq += r->nq;
+        kmax = std::max(kmax, r->k);
+        np_max = std::max(np_max, std::min(r->nprobe, h->nlist));
+    }
+    const int dim = h->o.dimension;
+    int64_t off = 0;
+    sl.reqs = take;
+    sl.offsets.clear();
+    for (auto& r : take) {
+        sl.offsets.push_back((int32_t)off);
+        std::memcpy(sl.h_q + off * dim, r->queries.data(), sizeof(float) * r->nq * dim);
+        for (int q = 0; q < r->nq; q++) {
+            sl.h_k[off + q] = r->k;
+            sl.h_np[off + q] = std::min(r->nprobe, h->nlist);
+        }
+        off += r->nq;
+    }
+    sl.kmax = kmax;
+    cudaStream_t st = sl.stream;
+    CK(cudaMemcpyAsync(sl.d_q.p, sl.h_q, sizeof(float) * nq * dim, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(sl.d_k.p, sl.h_k, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(sl.d_np.p, sl.h_np, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, st));
+    CK(sl.sc.fbcount.reserve(1));
+    CK(cudaMemsetAsync(sl.sc.fbcount.p, 0, sizeof(unsigned long long), st));
+    int rc = run_search(h, sl.sc, sl.d_q.p, nq, sl.d_k.p, sl.d_np.p, np_max, kmax, s->o.mode, sl.d_ids.p,
+                        sl.d_dist.p, sl.d_n.p, st);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(sl.h_ids, sl.d_ids.p, sizeof(int64_t) * nq * kmax, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(sl.h_dist, sl.d_dist.p, sizeof(double) * nq * kmax, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(sl.h_n, sl.d_n.p, sizeof(int32_t) * nq, cudaMemcpyDeviceToHost, st));
+    CK(cudaEventRecord(sl.done, st));
+    sl.busy = true;
+    s->batches++;
+    const int64_t b = batch_bytes(h, nq, kmax, np_max, s->o.mode);
+    s->cur_admitted += b;
+    s->peak_admitted = std::max(s->peak_admitted, s->cur_admitted);
+    return HANN_OK;
+}
+
+void fail_requests(hann_server* s, std::vector<std::shared_ptr<Request>>& rs, int code, const std::string& msg) {
+    for (auto& r : rs) {
+        r->status = code < 0 ? code : HANN_E_CUDA;
+        r->error = msg;
+    }
+}
+
+void scheduler(hann_server* s) {
+    hann_pqivf* h = s->h;
+    cudaSetDevice(h->o.device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    std::vector<int64_t> slot_bytes(s->slots.size(), 0);
+    for (;;) {
+        // 1. completions
+        bool any_busy = false;
+        for (size_t i = 0; i < s->slots.size(); i++) {
+            Slot& sl = *s->slots[i];
+            if (!sl.busy) continue;
+            const cudaError_t q = cudaEventQuery(sl.done);
+            if (q == cudaSuccess) {
+                complete(s, sl);
+                s->cur_admitted -= slot_bytes[i];
+                slot_bytes[i] = 0;
+                s->cv_done.notify_all();
+            } else if (q != cudaErrorNotReady) {
+                fail_requests(s, sl.reqs, HANN_E_CUDA, cudaGetErrorString(q));
+                sl.reqs.clear();
+                sl.busy = false;
+                s->cv_done.notify_all();
+            } else {
+                any_busy = true;
+            }
+        }
+        if (!any_busy && s->read_lock.owns_lock()) s->read_lock.unlock();
+        if (s->stop && s->queue.empty() && !any_busy) break;
+        // 2. a mutation at the head of the queue. Appends into spare capacity
+        //    and tombstone deletes move no row, so they run beside the batches
+        //    in flight (which may see them or not); batches queued after the
+        //    mutation start only once it is applied. A mutation that must move
+        //    rows (relayout) waits until nothing is in flight.
+        if (!s->queue.empty() && s->queue.front()->kind != 0) {
+            auto r = s->queue.front();
+            bool applied = false;
+            int rc = HANN_OK;
+            auto apply = [&](bool allow, bool* needs) {
+                return r->kind == 1 ? bulk_add_locked(h, r->ids.data(), r->vectors.data(), (int64_t)r->ids.size(),
+                                                      allow, needs)
+                                    : bulk_delete_locked(h, r->ids.data(), (int64_t)r->ids.size(), allow, needs);
+            };
+            const auto t0 = Clock::now();
+            if (!s->mut_drain && h->wmu.try_lock()) {
+                // never block on the writer lock while holding the read lock
+                std::lock_guard<std::mutex> wl(h->wmu, std::adopt_lock);
+                bool needs = false;
+                rc = apply(false, &needs);
+                if (needs) s->mut_drain = true;
+                else applied = true;
+            }
+            if (s->mut_drain && !any_busy) {
+                if (s->read_lock.owns_lock()) s->read_lock.unlock();
+                std::lock_guard<std::mutex> wl(h->wmu);
+                std::unique_lock<std::shared_mutex> xl(h->mu);
+                rc = apply(true, nullptr);
+                s->mut_drain = false;
+                s->relayouts++;
+                applied = true;
+            }
+            if (applied) {
+                s->queue.pop_front();
+                if (rc) r->error = h->err;
+                r->status = rc;
+                r->t_done = Clock::now();
+                s->mutations++;
+                s->mutation_ms += std::chrono::duration<double, std::milli>(r->t_done - t0).count();
+                s->cv_done.notify_all();
+                continue;
+            }
+        } else if (!s->queue.empty()) {
+            // 3. pack waiting searches into every free slot
+            for (size_t i = 0; i < s->slots.size() && !s->queue.empty() && s->queue.front()->kind == 0; i++) {
+                Slot& sl = *s->slots[i];
+                if (sl.busy) continue;
+                std::vector<std::shared_ptr<Request>> take;
+                int64_t nq = 0;
+                int kmax = 1, npm = 1;
+                while (!s->queue.empty() && s->queue.front()->kind == 0) {
+                    auto& r = s->queue.front();
+                    const int64_t nq2 = nq + r->nq;
+                    const int k2 = std::max(kmax, r->k), np2 = std::max(npm, std::min(r->nprobe, h->nlist));
+                    if (nq2 > s->o.max_batch_queries || batch_bytes(h, nq2, k2, np2, s->o.mode) > s->slot_budget) {
+                        if (take.empty()) {
+                            // a request that can never fit
+                            r->status = HANN_E_UNSUPPORTED;
+                            r->error = "request exceeds the server's per-batch query or memory limit";
+                            s->queue.pop_front();
+                            s->cv_done.notify_all();
+                            continue;
+                        }
+                        break;
+                    }
+                    nq = nq2;
+                    kmax = k2;
+                    npm = np2;
+                    take.push_back(r);
+                    s->queue.pop_front();
+                }
+                if (take.empty()) continue;
+                if (!s->read_lock.owns_lock()) s->read_lock = std::shared_lock<std::shared_mutex>(h->mu);
+                const int rc = launch_batch(s, sl, take);
+                if (rc) {
+                    fail_requests(s, take, rc, h->err);
+                    sl.reqs.clear();
+                    sl.busy = false;
+                    s->cv_done.notify_all();
+                } else {
+                    slot_bytes[i] = batch_bytes(h, nq, kmax, npm, s->o.mode);
+                    any_busy = true;
+                }
+            }
+        }
+        // 4. wait for new work or a completion (poll completions every 50 us)
+        if (any_busy) {
+            lk.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+            lk.lock();
+        } else if (s->queue.empty() && !s->stop) {
+            s->cv_work.wait_for(lk, std::chrono::milliseconds(5));
+        }
+    }
+    if (s->read_lock.owns_lock()) s->read_lock.unlock();
+}
+
+void free_slot(Slot& sl) {
+    if (sl.stream) {
+        cudaStreamSynchronize(sl.stream);
+        cudaStreamDestroy(sl.stream);
+    }
+    if (sl.done) cudaEventDestroy(sl.done);
+    cudaFreeHost(sl.h_q);
+    cudaFreeHost(sl.h_k);
+    cudaFreeHost(sl.h_np);
+    cudaFreeHost(sl.h_ids);
+    cudaFreeHost(sl.h_dist);
+    cudaFreeHost(sl.h_n);
+}
+
+}  // namespace
+
+extern "C" {
+
+void hann_serve_options_init(hann_serve_options* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->slots = 4;
+    o->max_batch_queries = 4096;
+    o->max_k = 100;
+    o->max_nprobe = 256;
+    o->mode = 1;
+    o->memory_budget = (int64_t)120 << 30;
+}
+
+int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server** out) {
+    if (!h || !opts || !out) return HANN_E_INVALID;
+    hann_serve_options o = *opts;
+    if (o.slots < 1 || o.slots > 64 || o.max_batch_queries < 1 || o.max_k < 1 || o.max_nprobe < 1 ||
+        (o.mode != 0 && o.mode != 1) || o.memory_budget <= 0)
+        return h->fail(HANN_E_INVALID, "invalid server options");
+    {
+        std::shared_lock<std::shared_mutex> lk(h->mu);
+        int rc = check_searchable(h);
+        if (rc) return rc;
+    }
+    cudaSetDevice(h->o.device);
+    auto s = std::make_unique<hann_server>();
+    s->h = h;
+    s->o = o;
+    const int np_max = std::min(o.max_nprobe, h->nlist);
+    s->slot_budget = o.memory_budget / o.slots;
+    const int64_t need = batch_bytes(h, o.max_batch_queries, o.max_k, np_max, o.mode);
+    if (need > s->slot_budget)
+        return h->fail(HANN_E_NOMEM, "memory budget %lld below %d slots x %lld bytes for %d-query batches",
+                       (long long)o.memory_budget, o.slots, (long long)need, o.max_batch_queries);
+    const int dim = h->o.dimension;
+    const int64_t Q = o.max_batch_queries, K = o.max_k;
+    for (int i = 0; i < o.slots; i++) {
+        auto sl = std::make_unique<Slot>();
+        cudaError_t e = cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl->h_q, sizeof(float) * Q * dim);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl->h_k, sizeof(int32_t) * Q);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl->h_np, sizeof(int32_t) * Q);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl->h_ids, sizeof(int64_t) * Q * K);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl->h_dist, sizeof(double) * Q * K);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl->h_n, sizeof(int32_t) * Q);
+        if (e == cudaSuccess) e = sl->d_q.reserve((size_t)Q * dim);
+        if (e == cudaSuccess) e = sl->d_k.reserve((size_t)Q);
+        if (e == cudaSuccess) e = sl->d_np.reserve((size_t)Q);
+        if (e == cudaSuccess) e = sl->d_n.reserve((size_t)Q);
+        if (e == cudaSuccess) e = sl->d_ids.reserve((size_t)Q * K);
+        if (e == cudaSuccess) e = sl->d_dist.reserve((size_t)Q * K);
+        // Size the slot's search scratch for its largest batch now, so the
+        // scheduler never calls the allocator while batches are in flight.
+        const int R = rerank_depth(h, o.max_k, o.mode);
+        if (e == cudaSuccess) e = sl->sc.D.reserve((size_t)Q * h->nlist);
+        if (e == cudaSuccess) e = sl->sc.probe_ids.reserve((size_t)Q * np_max);
+        if (e == cudaSuccess) e = sl->sc.probe_d.reserve((size_t)Q * np_max);
+        if (e == cudaSuccess) e = sl->sc.fb.reserve((size_t)Q);
+        if (e == cudaSuccess) e = sl->sc.cand_row.reserve((size_t)Q * R);
+        if (e == cudaSuccess) e = sl->sc.cand_d.reserve((size_t)Q * R);
+        if (e == cudaSuccess) e = sl->sc.cand_seq.reserve((size_t)Q * R);
+        if (e == cudaSuccess) e = sl->sc.qbf.reserve((size_t)Q * std::max(h->kp, 8));
+        if (e == cudaSuccess) e = sl->sc.qn2.reserve((size_t)Q);
+        if (e == cudaSuccess) e = sl->sc.qres.reserve((size_t)Q);
+        if (e == cudaSuccess) e = sl->sc.fbcount.reserve(1);
+        if (e != cudaSuccess) {
+            free_slot(*sl);
+            for (auto& x : s->slots) free_slot(*x);
+            return h->cuda_fail(e, "server slot allocation");
+        }
+        s->slots.push_back(std::move(sl));
+    }
+    hann_server* raw = s.release();
+    raw->thr = std::thread(scheduler, raw);
+    *out = raw;
+    return HANN_OK;
+}
+
+static int submit(hann_server* s, std::shared_ptr<Request> r, uint64_t* ticket) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return HANN_E_STATE;
+    r->ticket = s->next_ticket++;
+    r->t_submit = Clock::now();
+    if (!s->any) {
+        s->t_first = r->t_submit;
+        s->any = true;
+    }
+    s->tickets[r->ticket] = r;
+    s->queue.push_back(r);
+    s->cv_work.notify_one();
+    if (ticket) *ticket = r->ticket;
+    return HANN_OK;
+}
+
+int hann_serve_submit(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe, uint64_t* ticket) {
+    if (!s || !queries || nq <= 0) return HANN_E_INVALID;
+    if (k <= 0 || k > s->o.max_k) return HANN_E_INVALID;
+    if (nprobe <= 0) nprobe = s->h->o.candidate_clusters;
+    if (nprobe > s->o.max_nprobe) nprobe = s->o.max_nprobe;
+    auto r = std::make_shared<Request>();
+    r->kind = 0;
+    r->nq = nq;
+    r->k = k;
+    r->nprobe = nprobe;
+    r->queries.assign(queries, queries + (size_t)nq * s->h->o.dimension);
+    return submit(s, r, ticket);
+}
+
+int hann_serve_submit_add(hann_server* s, const int64_t* ids, const float* vectors, int64_t n, uint64_t* ticket) {
+    if (!s || n < 0 || (n > 0 && (!ids || !vectors))) return HANN_E_INVALID;
+    auto r = std::make_shared<Request>();
+    r->kind = 1;
+    r->ids.assign(ids, ids + n);
+    r->vectors.assign(vectors, vectors + n * s->h->o.dimension);
+    return submit(s, r, ticket);
+}
+
+int hann_serve_submit_delete(hann_server* s, const int64_t* ids, int64_t n, uint64_t* ticket) {
+    if (!s || n < 0 || (n > 0 && !ids)) return HANN_E_INVALID;
+    auto r = std::make_shared<Request>();
+    r->kind = 2;
+    r->ids.assign(ids, ids + n);
+    return submit(s, r, ticket);
+}
+
+int hann_serve_wait(hann_server* s, uint64_t ticket, int64_t* ids, double* distances, int32_t* n_out,
+                    int32_t timeout_ms, double* latency_ms) {
+    if (!s) return HANN_E_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return HANN_E_NOT_FOUND;
+    auto r = it->second;
+    const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 1000000000 : timeout_ms);
+    while (r->status == 1) {
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && r->status == 1) {
+            s->err = "timed out waiting for the request";
+            return HANN_E_STATE;
+        }
+    }
+    s->tickets.erase(it);
+    if (r->status < 0) {
+        s->err = r->error;
+        return r->status;
+    }
+    if (r->kind == 0) {
+        if (ids) std::memcpy(ids, r->out_ids.data(), sizeof(int64_t) * r->out_ids.size());
+        if (distances) std::memcpy(distances, r->out_dist.data(), sizeof(double) * r->out_dist.size());
+        if (n_out) std::memcpy(n_out, r->out_n.data(), sizeof(int32_t) * r->out_n.size());
+    }
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    return HANN_OK;
+}
+
+int hann_serve_stats(hann_server* s, hann_serve_statistics* out) {
+    if (!s || !out) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->requests = s->requests_done;
+    out->queries = s->queries_done;
+    out->batches = s->batches;
+    out->mutations = s->mutations;
+    out->peak_admitted_bytes = s->peak_admitted;
+    out->relayouts = s->relayouts;
+    out->mutation_ms = s->mutation_ms;
+    std::vector<double> l = s->lat_ms;
+    if (!l.empty()) {
+        std::sort(l.begin(), l.end());
+        auto pct = [&](double p) { return l[std::min(l.size() - 1, (size_t)(p * (l.size() - 1) + 0.5))]; };
+        out->p50_ms = pct(0.50);
+        out->p99_ms = pct(0.99);
+        const double span = std::chrono::duration<double>(s->t_last - s->t_first).count();
+        out->queries_per_s = span > 0 ? s->queries_done / span : 0.0;
+    }
+    return HANN_OK;
+}
+
+const char* hann_serve_last_error(const hann_server* s) { return s ? s->err.c_str() : ""; }
+
+int hann_serve_stop(hann_server* s) {
+    if (!s) return HANN_E_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->thr.joinable()) s->thr.join();
+    for (auto& sl : s->slots) free_slot(*sl);
+    delete s;
+    return HANN_OK;
+}
+
+}  // extern "C"

@@ -155,6 +155,49 @@ int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float* d_queries
 /* Index.Stats (core/index.go:41; pqivf/index.go:953-966). */
 int hann_pqivf_stats(hann_pqivf* h, hann_pqivf_index_stats* out);
 
+/* ---- continuous-batching server -------------------------------------------
+ * No single reference counterpart: the reference serves concurrent Search
+ * calls under its RWMutex (pqivf/index.go:37, 850-853) from a goroutine pool
+ * (example/run_datasets.go:84-120). Here requests from any host thread are
+ * packed into device batches that run on `slots` CUDA streams at once;
+ * requests arriving meanwhile join the next free slot; a batch is admitted
+ * only while its device scratch fits the slot's share of memory_budget.
+ * Add/Delete requests take effect before any batch queued after them starts;
+ * when they move no row (appends into spare capacity, tombstone deletes)
+ * they run beside the batches already in flight, which may or may not see
+ * them. Each request's result equals a Search of its queries alone. */
+typedef struct hann_server hann_server;
+typedef struct {
+    int32_t slots;             /* batches in flight (streams); default 4 */
+    int32_t max_batch_queries; /* queries per device batch; default 4096 */
+    int32_t max_k;             /* largest k a request may ask; default 100 */
+    int32_t max_nprobe;        /* nprobe is clamped to this; default 256 */
+    int32_t mode;              /* 0 PQ distances (parity), 1 exact rerank; default 1 */
+    int64_t memory_budget;     /* device bytes for batch scratch; default 120 GiB */
+} hann_serve_options;
+typedef struct {
+    int64_t requests, queries, batches, mutations, peak_admitted_bytes;
+    double p50_ms, p99_ms, queries_per_s;
+    int64_t relayouts;  /* mutations that had to wait for the batches in flight */
+    double mutation_ms; /* host time spent applying mutations */
+} hann_serve_statistics;
+
+void hann_serve_options_init(hann_serve_options* opts);
+int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server** out);
+/* Queues nq queries (copied) with one k and nprobe; returns a ticket. */
+int hann_serve_submit(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe, uint64_t* ticket);
+/* Queues a BulkAdd / BulkDelete applied between batches. */
+int hann_serve_submit_add(hann_server* s, const int64_t* ids, const float* vectors, int64_t n, uint64_t* ticket);
+int hann_serve_submit_delete(hann_server* s, const int64_t* ids, int64_t n, uint64_t* ticket);
+/* Waits for a ticket (timeout_ms < 0: no limit) and copies its results:
+ * ids/distances [nq*k], n_out [nq]; latency_ms = submit to completion. */
+int hann_serve_wait(hann_server* s, uint64_t ticket, int64_t* ids, double* distances, int32_t* n_out,
+                    int32_t timeout_ms, double* latency_ms);
+int hann_serve_stats(hann_server* s, hann_serve_statistics* out);
+const char* hann_serve_last_error(const hann_server* s);
+/* Finishes the queued work, then releases the server. */
+int hann_serve_stop(hann_server* s);
+
 /* ---- persisted state (Save/Load, pqivf/index.go:969-1101) ----------------
  * The binding encodes/decodes the reference's gob stream itself and moves
  * the arrays through these calls. */

@@ -1,0 +1,28 @@
+/*
+ * hann_gb300_diag.h -- diagnostic entry points of libhann_gb300.so. They have
+ * no counterpart in the reference; tests use them to check single kernels
+ * against a host computation. Host buffers; 0 or a negative HANN_E_* status.
+ */
+#ifndef HANN_GB300_DIAG_H
+#define HANN_GB300_DIAG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The BF16 tensor-core distance GEMM (tcgen05, TMA-fed): for rows a [n][dim]
+ * and columns b [m][dim] (dim <= 128), scores s[i][j] = ||b_j||^2 - 2 <a_i, b_j>
+ * with a and b rounded to BF16, FP32 accumulation and ||b_j||^2 from the FP32
+ * rows; and per row the 8 smallest scores with their columns, ascending.
+ * `scores` may be NULL. */
+int hann_gpu_bf16_scores(const float* a, int64_t n, const float* b, int32_t m, int32_t dim, float* scores,
+                         int32_t* top_idx, float* top_val);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HANN_GB300_DIAG_H */
