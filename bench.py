@@ -63,6 +63,14 @@ def parse():
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="served-stream phase length (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=5000.0, help="Poisson request arrivals per second")
+    ap.add_argument("--knn", type=int, default=1, help="run the batched exact k-NN section (1M x 128, top-100)")
+    ap.add_argument("--knn-n", type=int, default=1_000_000)
+    ap.add_argument("--knn-nq", type=int, default=10_000)
+    ap.add_argument("--knn-steps", type=int, default=3)
+    ap.add_argument("--knn-only", action="store_true", help="run only the k-NN section and print its line")
+    ap.add_argument("--knn-variants", type=str,
+                    default="squared_euclidean/tensor,cosine/tensor,manhattan/exact,squared_euclidean/exact,"
+                            "cosine/exact")
     return ap.parse_args()
 
 
@@ -277,6 +285,9 @@ def main():
     ge.build()
     import hann_gb300 as hg
 
+    if args.knn_only:
+        print(json.dumps({"knn": knn_section(args, torch, dev)}), flush=True)
+        return 0
     x, q = make_data(args, torch, dev)
     idx, xh, train_s = build_index(args, x, torch)
     q_host = q.cpu().numpy()
@@ -422,6 +433,14 @@ def main():
             log("served stream failed:", e)
             served = {"error": str(e)}
 
+    knn = None
+    if args.knn and rank == 0:
+        try:
+            knn = knn_section(args, torch, dev)
+        except Exception as e:  # pragma: no cover
+            log("knn section failed:", e)
+            knn = {"error": str(e)}
+
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -448,6 +467,7 @@ def main():
             "gpu_launches": launches,
             "clocks": clocks,
             "served_stream": served,
+            "knn": knn,
         }
         if served and "p50_ms" in served:
             line["p50_ms"] = served["p50_ms"]
@@ -459,6 +479,113 @@ def main():
 
         dist.destroy_process_group()
     return 0
+
+
+def knn_histogram_data(torch, dev, n, dim, seed):
+    """Non-negative integers 0-255, 70% zeros, nonzeros geometric with mean
+    20 (quantized-histogram-like vectors)."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    u = torch.rand(n, dim, device=dev, generator=g, dtype=torch.float64)
+    geo = torch.floor(torch.log1p(-u) / np.log1p(-1.0 / 20.0)) + 1.0
+    x = torch.clamp(geo, max=255.0).to(torch.float32)
+    x[torch.rand(n, dim, device=dev, generator=g) < 0.7] = 0.0
+    return x
+
+
+def knn_section(args, torch, dev):
+    """Batched exact k-NN: 1,000,000 x 128 histogram-like base, 10,000
+    queries, top-100 under squared Euclidean, cosine (tensor-core screen +
+    exact FP32 rescore, and the plain FP32 SIMT path) and Manhattan (FP32
+    SIMT). Per variant: queries/s with inputs resident in HBM, recall@100
+    and the largest relative distance error against an FP64 brute force of
+    the first 100 queries, and for the screen how many queries fell back to
+    the exact path."""
+    import hann_gb300 as hg
+
+    n, dim, nq, k = args.knn_n, 128, args.knn_nq, 100
+    base = knn_histogram_data(torch, dev, n, dim, args.seed + 7)
+    q = knn_histogram_data(torch, dev, nq, dim, args.seed + 8)
+    idx = hg.KNN(base.cpu().numpy())
+    ids = torch.empty(nq, k, dtype=torch.int64, device=dev)
+    dist = torch.empty(nq, k, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    nr = min(100, nq)
+    b64 = base.double()
+    q64 = q[:nr].double()
+    gt = {}
+    for metric in ("squared_euclidean", "cosine", "manhattan"):
+        if metric == "manhattan":
+            d = torch.cdist(q64, b64, p=1)
+        else:
+            dot = q64 @ b64.T
+            if metric == "squared_euclidean":
+                d = (q64 * q64).sum(1, keepdim=True) - 2 * dot + (b64 * b64).sum(1)[None, :]
+            else:
+                qn = q64.norm(dim=1, keepdim=True)
+                bn = b64.norm(dim=1)[None, :]
+                den = qn * bn
+                d = torch.where(den == 0, torch.ones_like(dot), 1 - torch.clamp(dot / torch.where(den == 0, 1, den),
+                                                                                  -1, 1))
+        # (distance, id) order: stable sort on distance keeps ids ascending
+        dd, order = torch.sort(d, dim=1, stable=True)
+        gt[metric] = (order[:, :k].cpu().numpy(), dd[:, :k].cpu().numpy())
+    del b64
+    out = {"workload": f"{n} x {dim} histogram-like (0-255, 70% zeros, geometric mean 20), {nq} queries, top-{k}"}
+    variants = [tuple(v.split("/")) for v in args.knn_variants.split(",") if v]
+    for metric, method in variants:
+        def run():
+            idx.search_device(q.data_ptr(), nq, k, ids.data_ptr(), dist.data_ptr(), metric, method,
+                              stream.cuda_stream)
+        before = idx.stats()
+        run()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.knn_steps):
+            run()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms = t0.elapsed_time(t1) / args.knn_steps
+        after = idx.stats()
+        got_i = ids[:nr].cpu().numpy()
+        got_d = dist[:nr].cpu().numpy()
+        gi, gd = gt[metric]
+        rec = float(np.mean([len(set(got_i[i]) & set(gi[i])) / k for i in range(nr)]))
+        rel = float(np.max(np.abs(got_d - gd) / np.maximum(np.abs(gd), 1e-30)))
+        key = f"{metric}/{method}"
+        out[key] = {"queries_per_s": nq / (ms / 1e3), "ms": round(ms, 3), "recall_at_100_vs_fp64": round(rec, 5),
+                    "max_rel_dist_err_vs_fp64": rel,
+                    "fallback_queries_per_run": (after["fallback_queries"] - before["fallback_queries"])
+                    / (args.knn_steps + 1)}
+        log("knn", key, out[key])
+    # the screen must give exactly the exact path's answer
+    for metric in ("squared_euclidean", "cosine") if len(variants) == 5 else ():
+        idx.search_device(q.data_ptr(), nq, k, ids.data_ptr(), dist.data_ptr(), metric, "tensor", stream.cuda_stream)
+        a = (ids.clone(), dist.clone())
+        idx.search_device(q.data_ptr(), nq, k, ids.data_ptr(), dist.data_ptr(), metric, "exact", stream.cuda_stream)
+        out[f"{metric}/tensor_equals_exact"] = bool(torch.equal(a[0], ids) and torch.equal(a[1], dist))
+    # host (e2e) form of the screened squared Euclidean
+    qh = q.cpu().numpy()
+    idx.search(qh, k, "squared_euclidean", "tensor")
+    t = time.perf_counter()
+    idx.search(qh, k, "squared_euclidean", "tensor")
+    out["squared_euclidean/tensor_e2e_queries_per_s"] = nq / (time.perf_counter() - t)
+    # CPU: the oracle's restatement of the reference batch kernels on a sample
+    if not args.no_cpu_baseline:
+        import oracle
+
+        oracle.build()
+        bh = base.cpu().numpy()
+        sample = 8
+        t = time.perf_counter()
+        oracle.knn(qh[:sample], bh, k, "squared_euclidean", nthreads=os.cpu_count() or 1)
+        el = time.perf_counter() - t
+        out["cpu_port_queries_per_s"] = sample / el
+        out["cpu_port_sample"] = f"{sample} queries x {n} rows, squared Euclidean, {os.cpu_count()} threads"
+    idx.close()
+    return out
 
 
 def serve_stream(args, idx, q_host, gt, nr):

@@ -95,6 +95,8 @@ EXPORTED = (
     "hann_pqivf_search_batch", "hann_pqivf_search_batch_device", "hann_pqivf_stats", "hann_pqivf_export_layout",
     "hann_pqivf_export", "hann_pqivf_import", "hann_gpu_distance_batch", "hann_pqivf_set_profiling",
     "hann_pqivf_stage_times", "hann_pqivf_list_lengths", "hann_pqivf_search_batch_device_noalloc",
+    "hann_gpu_distance_matrix", "hann_knn_new", "hann_knn_free", "hann_knn_last_error", "hann_knn_search",
+    "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn",
 )
 
 
@@ -137,6 +139,21 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
         L.hann_pqivf_list_lengths.argtypes = [_P, _P]
+        L.hann_gpu_distance_matrix.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64,
+                                               ctypes.c_int32, _P]
+        L.hann_knn_new.argtypes = [_P, ctypes.c_int64, ctypes.c_int32]
+        L.hann_knn_new.restype = _P
+        L.hann_knn_free.argtypes = [_P]
+        L.hann_knn_free.restype = None
+        L.hann_knn_last_error.argtypes = [_P]
+        L.hann_knn_last_error.restype = ctypes.c_char_p
+        L.hann_knn_search.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P,
+                                      _P]
+        L.hann_knn_search_device.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int64, ctypes.c_int32,
+                                             ctypes.c_int32, _P, _P, _P]
+        L.hann_knn_get_stats.argtypes = [_P, _P]
+        L.hann_gpu_knn.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64, ctypes.c_int32,
+                                   ctypes.c_int32, ctypes.c_int32, _P, _P]
         if path is None:
             _lib = L
         return L
@@ -546,6 +563,103 @@ def distance_batch(metric: int, query, flat) -> np.ndarray:
     if rc != HANN_OK:
         raise HannError(rc, "distance batch failed")
     return out
+
+
+def distance_matrix(metric, queries, base) -> np.ndarray:
+    """Every query against every base row, the values of distance_batch."""
+    L = load_library()
+    m = _metric_id(metric)
+    x = np.ascontiguousarray(base, dtype=np.float32)
+    dim = x.shape[1] if x.ndim == 2 else 0
+    q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, dim) if dim else \
+        np.zeros((len(queries), 0), np.float32)
+    out = np.zeros((q.shape[0], x.shape[0]), dtype=np.float64)
+    rc = L.hann_gpu_distance_matrix(m, _ptr(q), q.shape[0], _ptr(x), x.shape[0], dim, _ptr(out))
+    if rc != HANN_OK:
+        raise HannError(rc, "distance matrix failed")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# batched exact k-NN over a flat base (testutil.BruteForceKNN,
+# internal/testutil/data.go:66-93, for many queries at once)
+
+METRICS = {"squared_euclidean": 0, "euclidean": 1, "manhattan": 2, "cosine": 3}
+KNN_METHODS = {"auto": 0, "exact": 1, "tensor": 2}
+
+
+def _metric_id(metric) -> int:
+    return METRICS[metric] if isinstance(metric, str) else int(metric)
+
+
+class _KnnStats(ctypes.Structure):
+    _fields_ = [("queries", ctypes.c_int64), ("exact_queries", ctypes.c_int64), ("tensor_queries", ctypes.c_int64),
+                ("fallback_queries", ctypes.c_int64), ("chunks", ctypes.c_int64), ("redo_chunks", ctypes.c_int64)]
+
+
+class KNN:
+    """A flat base resident on the GPU, searched in batches. Results are
+    ordered by (distance, row) with the reference's FP32 distances, so they
+    equal testutil.BruteForceKNN over the same rows (ids = row numbers)."""
+
+    def __init__(self, base):
+        self._L = load_library()
+        x = np.ascontiguousarray(base, dtype=np.float32)
+        if x.ndim != 2:
+            raise ValueError("base must be [n][dim]")
+        self.n, self.dim = x.shape
+        self._h = self._L.hann_knn_new(_ptr(x), self.n, self.dim)
+        if not self._h:
+            raise HannError(HANN_E_CUDA, "hann_knn_new failed")
+
+    def close(self):
+        if self._h:
+            self._L.hann_knn_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != HANN_OK:
+            raise HannError(rc, self._L.hann_knn_last_error(self._h).decode())
+
+    def search(self, queries, k: int, metric="squared_euclidean", method="auto"):
+        """(ids int64 [nq][k], dist float64 [nq][k]); slots past n hold -1 / +inf."""
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self.dim) if self.dim else \
+            np.zeros((len(queries), 0), np.float32)
+        nq = q.shape[0]
+        ids = np.zeros((nq, k), dtype=np.int64)
+        dist = np.zeros((nq, k), dtype=np.float64)
+        self._check(self._L.hann_knn_search(self._h, _metric_id(metric), _ptr(q), nq, int(k),
+                                            KNN_METHODS.get(method, method) if isinstance(method, str) else method,
+                                            _ptr(ids), _ptr(dist)))
+        return ids, dist
+
+    def search_device(self, q_ptr: int, nq: int, k: int, ids_ptr: int, dist_ptr: int, metric="squared_euclidean",
+                      method="auto", stream: int = 0):
+        """Device buffers (raw pointers, e.g. torch tensor data_ptr())."""
+        self._check(self._L.hann_knn_search_device(self._h, _metric_id(metric), ctypes.c_void_p(q_ptr), nq, int(k),
+                                                   KNN_METHODS[method] if isinstance(method, str) else method,
+                                                   ctypes.c_void_p(ids_ptr), ctypes.c_void_p(dist_ptr),
+                                                   ctypes.c_void_p(stream)))
+
+    def stats(self) -> dict:
+        st = _KnnStats()
+        self._check(self._L.hann_knn_get_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in _KnnStats._fields_}
+
+
+def knn(queries, base, k: int, metric="squared_euclidean", method="auto"):
+    """One-shot batched k-NN (copies base to the GPU, searches, frees)."""
+    idx = KNN(base)
+    try:
+        return idx.search(queries, k, metric, method)
+    finally:
+        idx.close()
 
 
 # ---------------------------------------------------------------------------

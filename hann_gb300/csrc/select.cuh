@@ -11,7 +11,7 @@ __device__ __forceinline__ bool ki_less(uint32_t ka, int32_t ia, uint32_t kb, in
     return ka < kb || (ka == kb && ia < ib);
 }
 
-__device__ void sort_ki(uint32_t* key, int32_t* idx, int P) {
+__device__ __forceinline__ void sort_ki(uint32_t* key, int32_t* idx, int P) {
     for (int kk = 2; kk <= P; kk <<= 1) {
         for (int j = kk >> 1; j > 0; j >>= 1) {
             for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -42,7 +42,7 @@ __device__ void sort_ki(uint32_t* key, int32_t* idx, int P) {
 // one warp scans the 256 bins. whist holds THREADS/32 x 256 counters; the
 // block must have exactly THREADS threads.
 template <int THREADS>
-__device__ void radix_nth_fast(const float* __restrict__ row, int len, int n, unsigned int* whist, uint32_t* s_prefix,
+__device__ __forceinline__ void radix_nth_fast(const float* __restrict__ row, int len, int n, unsigned int* whist, uint32_t* s_prefix,
                                uint32_t* s_rem, uint32_t* s_and, uint32_t* s_or) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     constexpr int NW = THREADS / 32;
@@ -127,7 +127,7 @@ __device__ void radix_nth_fast(const float* __restrict__ row, int len, int n, un
 }
 
 // Bitonic sort of P (a power of two) 64-bit keys in shared memory, ascending.
-__device__ void sort_u64(unsigned long long* key, int P) {
+__device__ __forceinline__ void sort_u64(unsigned long long* key, int P) {
     for (int kk = 2; kk <= P; kk <<= 1) {
         for (int j = kk >> 1; j > 0; j >>= 1) {
             for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -148,11 +148,14 @@ __device__ void sort_u64(unsigned long long* key, int P) {
 
 // The n-th smallest (1-based, 1 <= n <= len) of the 64-bit keys in
 // shared memory, returned to every thread. Digits of 8 bits from the
-// highest bit where the keys differ; one shared histogram per pass.
-// hist holds 256 counters; the scalars live in shared memory.
-__device__ unsigned long long radix_nth_u64(const unsigned long long* keys, int len, int n, unsigned int* hist,
-                                  unsigned long long* s_and, unsigned long long* s_or,
-                                  unsigned long long* s_prefix, unsigned int* s_rem) {
+// highest bit where the keys differ; one shared histogram per pass; once the
+// chosen digit holds a single key, that key is the answer.
+// hist holds 256 counters; the scalars live in shared memory (*s_and holds
+// the chosen digit's count after each pass).
+__device__ __forceinline__ unsigned long long radix_nth_u64(const unsigned long long* keys, int len, int n,
+                                                            unsigned int* hist, unsigned long long* s_and,
+                                                            unsigned long long* s_or,
+                                                            unsigned long long* s_prefix, unsigned int* s_rem) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         *s_and = ~0ull;
@@ -184,6 +187,7 @@ __device__ unsigned long long radix_nth_u64(const unsigned long long* keys, int 
             if ((k & himask) == prefix) atomicAdd(&hist[(unsigned)(k >> lo) & dmask], 1u);
         }
         __syncthreads();
+        uint32_t chosen = 0;
         if (w == 0) {
             uint32_t cnt[8], tot = 0;
 #pragma unroll
@@ -199,19 +203,33 @@ __device__ unsigned long long radix_nth_u64(const unsigned long long* keys, int 
             }
             const uint32_t excl = incl - tot;
             const uint32_t rem = *s_rem;
-            if (excl < rem && rem <= incl) {
+            const bool mine = excl < rem && rem <= incl;
+            if (mine) {
                 uint32_t cum = excl;
                 for (int j = 0; j < 8; j++) {
                     if (cum + cnt[j] >= rem) {
                         *s_prefix = prefix | ((unsigned long long)(lane * 8 + j) << lo);
                         *s_rem = rem - cum;
+                        chosen = cnt[j];
                         break;
                     }
                     cum += cnt[j];
                 }
             }
+            chosen = __reduce_max_sync(0xffffffffu, mine ? chosen : 0u);
+            if (lane == 0) *s_and = chosen;
         }
         __syncthreads();
+        // (*s_and is rewritten only after the next pass's first barrier)
+        if (lo > 0 && *s_and == 1ull) {
+            // a single key carries the chosen prefix: it is the answer
+            const unsigned long long pm = ~0ull << lo, pf = *s_prefix;
+            __syncthreads();
+            for (int i = threadIdx.x; i < len; i += blockDim.x)
+                if ((keys[i] & pm) == pf) *s_prefix = keys[i];
+            __syncthreads();
+            return *s_prefix;
+        }
     }
     return *s_prefix;
 }

@@ -239,6 +239,54 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* layout, const floa
 int hann_gpu_distance_batch(int32_t metric, const float* query, const float* flat, size_t dim, size_t n,
                             double* out);
 
+/* Many queries at once: out[q * n + i] = distance(queries[q], base[i]), the
+ * same values as hann_gpu_distance_batch row by row. Host buffers. */
+int hann_gpu_distance_matrix(int32_t metric, const float* queries, int64_t nq, const float* base, int64_t n,
+                             int32_t dim, double* out);
+
+/* ---- batched exact k-NN over a flat base ---------------------------------
+ * testutil.BruteForceKNN (internal/testutil/data.go:66-93) for a batch of
+ * queries: per query the k rows of base with the smallest distance under the
+ * metric, ascending by (distance, row), each distance the value
+ * hann_gpu_distance_batch returns for that pair. Row numbers stand for the
+ * reference's ids (0..n-1); slots past n are id -1, distance +inf. k is in
+ * [1, 4096], n below 2^31.
+ * method: HANN_KNN_EXACT computes every distance in FP32 in the reference's
+ * summation order; HANN_KNN_TENSOR (squared Euclidean, Euclidean, cosine; dim
+ * <= 128) screens with a BF16 tensor-core GEMM, then rescores exactly every
+ * row whose screened score lies within the GEMM's error bound of the k-th --
+ * the results are identical to HANN_KNN_EXACT; HANN_KNN_AUTO picks the tensor
+ * screen where it applies. */
+#define HANN_KNN_AUTO 0
+#define HANN_KNN_EXACT 1
+#define HANN_KNN_TENSOR 2
+
+typedef struct hann_knn hann_knn;
+typedef struct hann_knn_stats {
+    int64_t queries;          /* queries answered */
+    int64_t exact_queries;    /* answered by the exact path as requested */
+    int64_t tensor_queries;   /* answered through the tensor-core screen */
+    int64_t fallback_queries; /* screened queries whose band overflowed and ran exactly */
+    int64_t chunks;           /* base chunks walked */
+    int64_t redo_chunks;      /* chunks rerun in pieces after a candidate overflow */
+} hann_knn_stats;
+
+/* Copies the flat base [n][dim] (host) to the device. NULL on failure. */
+hann_knn* hann_knn_new(const float* base, int64_t n, int32_t dim);
+void hann_knn_free(hann_knn* h);
+const char* hann_knn_last_error(const hann_knn* h);
+/* Host buffers: queries [nq][dim], ids [nq][k], dist [nq][k]. */
+int hann_knn_search(hann_knn* h, int32_t metric, const float* queries, int64_t nq, int32_t k, int32_t method,
+                    int64_t* ids, double* dist);
+/* Device buffers, work enqueued on `stream` (a cudaStream_t; NULL = the
+ * handle's own); returns once the results are complete. */
+int hann_knn_search_device(hann_knn* h, int32_t metric, const float* queries, int64_t nq, int32_t k, int32_t method,
+                           int64_t* ids, double* dist, void* stream);
+int hann_knn_get_stats(hann_knn* h, hann_knn_stats* out);
+/* One-shot form: copies base, searches, frees. */
+int hann_gpu_knn(int32_t metric, const float* queries, int64_t nq, const float* base, int64_t n, int32_t dim,
+                 int32_t k, int32_t method, int64_t* ids, double* dist);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,6 +84,8 @@ def lib():
                 _i32p, _u8p, _i32p, _f32p, ctypes.c_int64, _i32p, _i32p, ctypes.c_int, ctypes.c_int,
                 _i64p, _f64p, _i32p, _i32p, ctypes.c_int]
             L.hann_oracle_probe.argtypes = [ctypes.c_int, ctypes.c_int, _f32p, _f32p, ctypes.c_int, _i32p]
+            L.hann_oracle_knn.argtypes = [ctypes.c_int, _f32p, ctypes.c_int64, _f32p, ctypes.c_int64, ctypes.c_int,
+                                          ctypes.c_int, _i64p, _f64p, ctypes.c_int]
             _lib = L
     return _lib
 
@@ -131,6 +133,26 @@ def batch(metric: int, q, flat) -> np.ndarray:
     if n:
         lib().hann_oracle_batch(metric, _p(q, _f32p), _p(flat, _f32p), dim, n, _p(out, _f64p))
     return out
+
+
+METRICS = {"squared_euclidean": 0, "euclidean": 1, "manhattan": 2, "cosine": 3}
+
+
+def knn(queries, base, k: int, metric="squared_euclidean", nthreads: int = 1):
+    """testutil.BruteForceKNN (internal/testutil/data.go:66-93) per query over
+    the tier's FP32 batch distances; ids are row numbers. Returns (ids int64
+    [nq][k], dist float64 [nq][k]); slots past n hold -1 / +inf."""
+    m = METRICS[metric] if isinstance(metric, str) else int(metric)
+    base = _f32(base)
+    n, dim = base.shape if base.ndim == 2 else (0, 0)
+    q = _f32(queries).reshape(-1, dim) if dim else np.zeros((np.asarray(queries).shape[0], 0), np.float32)
+    nq = q.shape[0]
+    ids = np.zeros((nq, k), dtype=np.int64)
+    dist = np.zeros((nq, k), dtype=np.float64)
+    if nq:
+        lib().hann_oracle_knn(m, _p(q, _f32p), nq, _p(base, _f32p), n, dim, k, _p(ids, _i64p), _p(dist, _f64p),
+                              nthreads)
+    return ids, dist
 
 
 def assign(data, centroids, nthreads: int = 1) -> np.ndarray:

@@ -520,3 +520,43 @@ void hann_oracle_probe(int dim, int nlist, const float* coarse, const float* q, 
     for (int i = 0; i < np; i++) out[i] = pr[i].c;
     free(pr);
 }
+
+/* ---------------------------------------------------------------------- */
+/* testutil.BruteForceKNN (internal/testutil/data.go:66-93) for a batch of
+ * queries over a flat base whose row numbers are the ids: every distance as
+ * the tier's batch kernel returns it (FP32 widened to double; an empty
+ * vector has distance 0, core/distance.go:23-25), sorted by (distance, id),
+ * the first k kept; slots past n get id -1 and distance +inf. */
+struct knn_item { double d; int64_t id; };
+static int cmp_knn(const void* x, const void* y) {
+    const struct knn_item* a = (const struct knn_item*)x;
+    const struct knn_item* b = (const struct knn_item*)y;
+    if (a->d < b->d) return -1;
+    if (a->d > b->d) return 1;
+    return (a->id > b->id) - (a->id < b->id);
+}
+struct knn_ctx { int metric; const float* q; const float* base; int64_t n; int dim; int k; int64_t* ids; double* dist; };
+static void knn_range(void* p, int64_t b, int64_t e) {
+    struct knn_ctx* c = (struct knn_ctx*)p;
+    struct knn_item* it = (struct knn_item*)malloc(sizeof(struct knn_item) * (size_t)(c->n > 0 ? c->n : 1));
+    double* dd = (double*)malloc(sizeof(double) * (size_t)(c->n > 0 ? c->n : 1));
+    for (int64_t qi = b; qi < e; qi++) {
+        if (c->dim > 0) hann_oracle_batch(c->metric, c->q + (size_t)qi * c->dim, c->base, (size_t)c->dim, (size_t)c->n, dd);
+        for (int64_t i = 0; i < c->n; i++) {
+            it[i].d = c->dim > 0 ? dd[i] : 0.0;
+            it[i].id = i;
+        }
+        qsort(it, (size_t)c->n, sizeof(struct knn_item), cmp_knn);
+        for (int j = 0; j < c->k; j++) {
+            c->ids[qi * c->k + j] = j < c->n ? it[j].id : -1;
+            c->dist[qi * c->k + j] = j < c->n ? it[j].d : INFINITY;
+        }
+    }
+    free(it);
+    free(dd);
+}
+void hann_oracle_knn(int metric, const float* q, int64_t nq, const float* base, int64_t n, int dim, int k,
+                     int64_t* ids, double* dist, int nthreads) {
+    struct knn_ctx c = {metric, q, base, n, dim, k, ids, dist};
+    parallel_for(nq, nthreads, knn_range, &c);
+}
