@@ -112,6 +112,8 @@ static int prepare_coarse(hann_pqivf* h) {
     CK(launch_to_bf16(h->d_coarse.p, h->nlist, h->o.dimension, h->kp, h->d_coarse_bf16.p, h->d_coarse_norm.p,
                       cres.p, h->stream));
     CK(launch_norm_maxes(h->d_coarse_norm.p, cres.p, h->nlist, h->d_cmax.p, h->stream));
+    CK(h->d_coarse_terms.reserve((size_t)h->nlist));
+    CK(launch_sq_terms(h->d_coarse_norm.p, h->nlist, h->d_coarse_terms.p, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return HANN_OK;
 }
@@ -560,6 +562,10 @@ int rerank_depth(const hann_pqivf* h, int kmax, int mode) { return rerank_depth_
 
 // Runs the device search for nq queries already in d_q; k/nprobe per query
 // in device arrays d_k/d_np. Outputs to device buffers.
+constexpr int SCREEN_MIN_LISTS = 2048;  // below this the full score matrix is cheaper
+constexpr int PROBE_CAP = 4096;         // screened-probe candidates per query and chunk
+constexpr int PROBE_FIRST = 1024;       // first centroid chunk (every list enters the band)
+
 int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k,
                       const int32_t* d_np, int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist,
                       int32_t* d_nout, cudaStream_t s) {
@@ -592,9 +598,66 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
         else h->ev[stage].back().second = e;
         return cudaEventRecord(e, s);
     };
+    // Screened probe: the BF16 GEMM walks the centroids in chunks growing
+    // fourfold and keeps per query only the lists whose screened score can
+    // still reach its np-th (the band merge of the batched k-NN,
+    // kernels_knn.cu); probe_final rescores the band exactly. Same lists and
+    // distances as probe_select_band on the full score matrix.
+    const bool screened = h->tc && h->nlist >= SCREEN_MIN_LISTS;
+    const int lcap = std::max(1024, 2 * np_max);
+    if (screened) {
+        CK(sc.pe2.reserve((size_t)chunk));
+        CK(sc.pasl.reserve((size_t)chunk));
+        CK(sc.pthr.reserve((size_t)chunk));
+        CK(sc.pcnt.reserve((size_t)chunk));
+        CK(sc.plcount.reserve((size_t)chunk));
+        CK(sc.pneed.reserve((size_t)chunk));
+        CK(sc.pcand_id.reserve((size_t)chunk * PROBE_CAP));
+        CK(sc.pcand_s.reserve((size_t)chunk * PROBE_CAP));
+        CK(sc.pband.reserve((size_t)chunk * lcap));
+    }
     for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
         const int64_t nc = std::min(chunk, nq - q0);
         const float* qp = d_q + q0 * h->o.dimension;
+        if (screened) {
+            CK(mark(0, true));
+            CK(launch_to_bf16(qp, nc, h->o.dimension, h->kp, sc.qbf.p, sc.qn2.p, sc.qres.p, s));
+            CK(launch_knn_query_band(sc.qn2.p, sc.qres.p, nc, h->kp, 0,
+                                     reinterpret_cast<const unsigned int*>(h->d_cmax.p), sc.pe2.p, sc.pasl.p, s));
+            CK(cudaMemsetAsync(sc.pcnt.p, 0, sizeof(int32_t) * nc, s));
+            CK(cudaMemsetAsync(sc.plcount.p, 0, sizeof(int32_t) * nc, s));
+            CK(cudaMemsetAsync(sc.pneed.p, 0, sizeof(int32_t) * nc, s));
+            CK(launch_fill_f32(sc.pthr.p, nc, INFINITY, s));
+            int launches = 3;
+            for (int b = 0, w = std::min(h->nlist, PROBE_FIRST); b < h->nlist; w = 3 * b) {
+                const int e = std::min(h->nlist, b + w);
+                CK(launch_gemm_filter(sc.qbf.p, nc, h->d_coarse_bf16.p, h->nlist, h->kp, b, e,
+                                      h->d_coarse_terms.p, sc.pthr.p, PROBE_CAP, sc.pcnt.p, sc.pcand_id.p,
+                                      sc.pcand_s.p, h->d_err.p, s));
+                CK(launch_knn_merge_band((int)nc, np_max, d_np + q0, PROBE_CAP, lcap, sc.pcnt.p, sc.pcand_id.p,
+                                         sc.pcand_s.p, sc.pe2.p, sc.pasl.p, sc.pband.p, sc.plcount.p, sc.pthr.p,
+                                         sc.pneed.p, s));
+                launches += 2;
+                b = e;
+            }
+            CK(mark(0, false));
+            CK(mark(1, true));
+            CK(launch_probe_final(qp, nc, h->o.dimension, h->d_coarse.p, h->nlist, d_np + q0, np_max, d_k + q0,
+                                  h->d_live.p, h->o.fallback ? 1 : 0, lcap, sc.pband.p, sc.plcount.p, sc.pneed.p,
+                                  sc.D.p, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, sc.fbcount.p, s));
+            CK(mark(1, false));
+            CK(mark(2, true));
+            p.kq = d_k + q0;
+            CK(launch_scan(p, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R,
+                           sc.cand_row.p, sc.cand_d.p, sc.cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
+            CK(mark(2, false));
+            CK(mark(3, true));
+            CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+                             d_dist + q0 * kmax, d_nout + q0, s));
+            CK(mark(3, false));
+            h->launches += launches + 3;
+            continue;
+        }
         CK(mark(0, true));
         if (h->tc) {
             CK(launch_to_bf16(qp, nc, h->o.dimension, h->kp, sc.qbf.p, sc.qn2.p, sc.qres.p, s));

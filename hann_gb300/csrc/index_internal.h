@@ -143,6 +143,10 @@ struct SearchScratch {
     DBuf<int64_t> ids;
     DBuf<double> dist;
     DBuf<unsigned long long> fbcount;
+    // screened probe (band lists per query)
+    DBuf<float> pe2, pasl, pthr, pcand_s;
+    DBuf<int32_t> pcnt, pcand_id, plcount, pneed;
+    DBuf<unsigned long long> pband;
 };
 
 struct hann_pqivf {
@@ -178,6 +182,7 @@ struct hann_pqivf {
     bool tc = false;
     DBuf<uint16_t> d_coarse_bf16;
     DBuf<float> d_coarse_norm, d_cmax;
+    DBuf<float2> d_coarse_terms;  // (||c||^2, -2) per centroid, the screen's epilogue terms
     DBuf<int> d_err;
     DBuf<int64_t> d_start, d_row_id;
     DBuf<int32_t> d_len, d_live, d_row_cluster;

@@ -117,6 +117,16 @@ cudaError_t launch_rescore_top8(const float* x, const float* xn2, const float* x
                                 const float* cent, int k, const float* cmax, const int32_t* cand_idx,
                                 const float* cand_val, int32_t* out_idx, int64_t* overflow_rows, int* n_overflow,
                                 cudaStream_t s);
+// Final step of the screened probe (kernels_rescore.cu): exact rescoring of
+// each query's band list, the np nearest lists ascending, fallback flags.
+// Queries flagged need_exact select on their whole exact row (Drow scratch,
+// nlist floats per query).
+cudaError_t launch_probe_final(const float* Q, int64_t nq, int dim, const float* coarse, int nlist,
+                               const int32_t* nprobe, int np_max, const int32_t* k, const int32_t* list_len,
+                               int allow_fallback, int lcap, const unsigned long long* band, const int32_t* lcount,
+                               const int32_t* need_exact, float* Drow, int32_t* probe_ids, float* probe_d,
+                               int32_t* fallback, unsigned long long* fallback_count, cudaStream_t s);
+
 // out[0] = max_i sqrt(sqnorm[i]), out[1] = max_i resid[i].
 cudaError_t launch_norm_maxes(const float* sqnorm, const float* resid, int n, float* out, cudaStream_t s);
 
@@ -202,9 +212,10 @@ size_t knn_merge_exact_smem(int k, int cap);
 cudaError_t launch_gemm_filter(const void* a_bf16, int64_t nrows, const void* b_bf16, int64_t nb, int kp,
                                int col_begin, int col_end, const float2* cterm, const float* rthr, int cap,
                                int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s);
-cudaError_t launch_knn_merge_band(int nrows, int k, int cap, int lcap, int32_t* cnt, const int32_t* cand_id,
-                                  const float* cand_s, const float* e2, const float* asl, unsigned long long* list,
-                                  int32_t* lcount, float* thr, int32_t* need_exact, cudaStream_t s);
+cudaError_t launch_knn_merge_band(int nrows, int k, const int32_t* krow, int cap, int lcap, int32_t* cnt,
+                                  const int32_t* cand_id, const float* cand_s, const float* e2, const float* asl,
+                                  unsigned long long* list, int32_t* lcount, float* thr, int32_t* need_exact,
+                                  cudaStream_t s);
 size_t knn_merge_band_smem(int lcap, int cap);
 cudaError_t launch_knn_final_band(int metric, int nrows, int k, int lcap, int dim, const float* queries,
                                   const float* base, const float* qnorm, const float* bnorm,
@@ -220,6 +231,9 @@ cudaError_t launch_ref_sqnorm(const float* x, int64_t n, int dim, float* out, cu
 // (maxes: two floats as bits, zeroed by the caller).
 cudaError_t launch_knn_col_terms(const float* sqnorm, const float* resid, int64_t n, int cosine, float2* terms,
                                  unsigned int* maxes, cudaStream_t s);
+cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
+// (sqnorm[i], -2): squared-Euclidean screen terms.
+cudaError_t launch_sq_terms(const float* sqnorm, int64_t n, float2* terms, cudaStream_t s);
 // Per-query band constants e2 (= 2 eps) and slack scale.
 cudaError_t launch_knn_query_band(const float* qsq, const float* qres, int64_t nq, int kp, int cosine,
                                   const unsigned int* maxes, float* e2, float* asl, cudaStream_t s);

@@ -45,7 +45,8 @@ constexpr uint32_t SPIN_LIMIT = 1u << 22;
 constexpr int A_BYTES = KB_MAX * BM * 128;           // 32 KiB
 constexpr int B_STAGE_BYTES = KB_MAX * BN * 128;     // 64 KiB
 constexpr int TR_BYTES = 4 * 32 * 33 * 4;               // epilogue transpose tiles
-constexpr int SMEM_BYTES = 1024 + A_BYTES + STAGES * B_STAGE_BYTES + 256 + TR_BYTES;
+constexpr int CT_BYTES = 4 * 2 * BN * 8;                // per-warp column terms, two tiles
+constexpr int SMEM_BYTES = 1024 + A_BYTES + STAGES * B_STAGE_BYTES + 256 + TR_BYTES + CT_BYTES;
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -114,19 +115,19 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+// 64 columns of the warp's 32 lanes into v[0..64): two 32-column loads in
+// flight, then one wait, all in one asm statement so no use of v can be
+// scheduled before the wait.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
+    uint32_t r[64];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%"
-        "19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr)
+        : "memory");
 #pragma unroll
-    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 64; i++) v[i] = __uint_as_float(r[i]);
 }
 
 // MODE 0: write the score matrix S[row][col] (ld = ncols).
@@ -159,6 +160,7 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
     int* s_abort = reinterpret_cast<int*>(bars + 10);
     float* trans = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(bars) + 256);
+    float2* cts = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(trans) + TR_BYTES);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row0 = blockIdx.x * BM;
@@ -230,9 +232,14 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
             }
         }
     } else {
-        // Epilogue: warp w drains tensor-memory lanes 32*(w%4) .. +31.
+        // Epilogue: warp w drains tensor-memory lanes 32*(w%4) .. +31, one
+        // row per lane. Each warp stages the tile's per-column terms (bias,
+        // scale) in its own shared-memory slice, fetched one tile ahead, so
+        // the 256 columns are read as broadcasts instead of 256 global loads
+        // per lane; the accumulator comes out 64 columns per wait.
         const int quarter = warp & 3;
         const int row = row0 + quarter * 32 + lane;
+        float2* wct = cts + quarter * 2 * BN;  // [2][BN]
         float best_v[TOPC];
         int best_i[TOPC];
 #pragma unroll
@@ -241,47 +248,73 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
             best_i[c] = -1;
         }
         const float rt = (MODE == 2 && row < nrows) ? rthr[row] : -__int_as_float(0x7f800000);
+        // invalid columns: +inf scores (modes 0, 1), NaN (mode 2, never passes)
+        const float2 pad = MODE == 2 ? make_float2(__int_as_float(0x7fc00000), 0.0f)
+                                     : make_float2(__int_as_float(0x7f800000), 0.0f);
+        float2 pre[BN / 32];
+        auto fetch = [&](int t) {
+            const int colb = col_begin + (t0 + t) * BN;
+#pragma unroll
+            for (int j = 0; j < BN / 32; j++) {
+                const int col = colb + 32 * j + lane;
+                if (col < ncols) pre[j] = MODE == 2 ? __ldg(cterm + col) : make_float2(__ldg(bias + col), -2.0f);
+                else pre[j] = pad;
+            }
+        };
+        if (ntiles > 0) fetch(0);
         for (int t = 0; t < ntiles; t++) {
             const int buf = t & 1;
-            if (!mbar_wait(&tfull[buf], (t >> 1) & 1, err)) break;
+            float2* ct = wct + buf * BN;
+#pragma unroll
+            for (int j = 0; j < BN / 32; j++) ct[32 * j + lane] = pre[j];
+            __syncwarp();
+            if (t + 1 < ntiles) fetch(t + 1);
+            // a warp leaves together when a wait runs out
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], (t >> 1) & 1, err));
+            if (!ok) break;
             tc_fence_after();
             const int col0 = col_begin + (t0 + t) * BN;
-            for (int c = 0; c < BN; c += 32) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN + c), v);
-                const int cb = col0 + c;
+            for (int c = 0; c < BN; c += 64) {
+                float v[64];
+                const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN + c);
+                tmem_ld64(ta, v);
                 if (MODE == 0) {
-                    // Transpose the warp's 32 rows x 32 columns through shared
+                    // Transpose 32 rows x 32 columns at a time through shared
                     // memory so each store writes 128 contiguous bytes of a row.
                     float* tw = trans + quarter * 32 * 33;
-                    const float bl = cb + lane < ncols ? __ldg(bias + cb + lane) : 0.0f;
-#pragma unroll
-                    for (int i = 0; i < 32; i++) tw[lane * 33 + i] = v[i];
-                    __syncwarp();
                     const int rbase = row0 + quarter * 32;
-                    for (int rr = 0; rr < 32; rr++) {
-                        if (rbase + rr < nrows && cb + lane < ncols)
-                            out[(int64_t)(rbase + rr) * ncols + cb + lane] = bl - 2.0f * tw[rr * 33 + lane];
-                    }
-                    __syncwarp();
-                } else if (MODE == 2) {
-                    float sc[32];
-                    unsigned pass = 0;
 #pragma unroll
-                    for (int i = 0; i < 32; i++) {
-                        const int col = cb + i;
-                        const float2 tt = col < ncols ? __ldg(cterm + col) : make_float2(0.0f, 0.0f);
-                        sc[i] = __fmaf_rn(tt.y, v[i], tt.x);
-                        if (col < ncols && sc[i] <= rt) pass |= 1u << i;
+                    for (int h = 0; h < 2; h++) {
+                        const int cb = col0 + c + 32 * h;
+                        const float bl = ct[c + 32 * h + lane].x;
+#pragma unroll
+                        for (int i = 0; i < 32; i++) tw[lane * 33 + i] = v[32 * h + i];
+                        __syncwarp();
+                        if (cb + lane < ncols) {
+                            for (int rr = 0; rr < 32; rr++) {
+                                if (rbase + rr < nrows)
+                                    out[(int64_t)(rbase + rr) * ncols + cb + lane] =
+                                        __fmaf_rn(-2.0f, tw[rr * 33 + lane], bl);
+                            }
+                        }
+                        __syncwarp();
+                    }
+                } else if (MODE == 2) {
+                    unsigned long long pass = 0;
+#pragma unroll
+                    for (int i = 0; i < 64; i++) {
+                        const float2 tt = ct[c + i];
+                        if (__fmaf_rn(tt.y, v[i], tt.x) <= rt) pass |= 1ull << i;
                     }
                     if (pass) {
-                        int pos = atomicAdd(&cnt[row], __popc(pass));
+                        int pos = atomicAdd(&cnt[row], __popcll(pass));
 #pragma unroll
-                        for (int i = 0; i < 32; i++) {
-                            if (pass & (1u << i)) {
+                        for (int i = 0; i < 64; i++) {
+                            if (pass & (1ull << i)) {
                                 if (pos < cap) {
-                                    cand_idx[(int64_t)row * cap + pos] = cb + i;
-                                    cand_val[(int64_t)row * cap + pos] = sc[i];
+                                    const float2 tt = ct[c + i];
+                                    cand_idx[(int64_t)row * cap + pos] = col0 + c + i;
+                                    cand_val[(int64_t)row * cap + pos] = __fmaf_rn(tt.y, v[i], tt.x);
                                 }
                                 pos++;
                             }
@@ -289,14 +322,13 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
                     }
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 32; i++) {
-                        const int col = cb + i;
-                        const float sc = col < ncols ? __ldg(bias + min(col, ncols - 1)) - 2.0f * v[i]
-                                                     : __int_as_float(0x7f800000);
+                    for (int i = 0; i < 64; i++) {
+                        const float2 tt = ct[c + i];
+                        const float sc = __fmaf_rn(tt.y, v[i], tt.x);
                         if (sc < best_v[TOPC - 1]) {
                             // insert into the ascending list
                             float cv = sc;
-                            int ci = col;
+                            int ci = col0 + c + i;
 #pragma unroll
                             for (int p = 0; p < TOPC; p++) {
                                 if (cv < best_v[p]) {

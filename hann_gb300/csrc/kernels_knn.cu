@@ -249,8 +249,10 @@ __global__ void __launch_bounds__(KM_THREADS) knn_merge_exact_kernel(
 // reference's distance, covered by the relative slack).
 // A list that would exceed lcap, or a candidate buffer that overflowed,
 // sends the query to the exact SIMT path (need_exact) and stops its screen.
+// krow (optional) gives a per-row k, capped at k.
 __global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
-    int k, int cap, int lcap, int32_t* __restrict__ cnt, const int32_t* __restrict__ cand_id,
+    int k, const int32_t* __restrict__ krow, int cap, int lcap, int32_t* __restrict__ cnt,
+    const int32_t* __restrict__ cand_id,
     const float* __restrict__ cand_s, const float* __restrict__ e2, const float* __restrict__ asl,
     unsigned long long* __restrict__ list, int32_t* __restrict__ lcount, float* __restrict__ thr,
     int32_t* __restrict__ need_exact) {
@@ -271,14 +273,15 @@ __global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
         return;
     }
     const int L = lcount[r];
+    const int kr = krow ? max(1, min(krow[r], k)) : k;
     for (int i = threadIdx.x; i < L; i += KM_THREADS) keys[i] = list[r * lcap + i];
     for (int i = threadIdx.x; i < c; i += KM_THREADS)
         keys[L + i] = dkey(cand_s[r * cap + i], (uint32_t)cand_id[r * cap + i]);
     const int T = L + c;
     __syncthreads();
     float t_new = __int_as_float(0x7f800000);
-    if (T >= k) {
-        const unsigned long long K = radix_nth_u64(keys, T, k, hist, &s_and, &s_or, &s_prefix, &s_rem);
+    if (T >= kr) {
+        const unsigned long long K = radix_nth_u64(keys, T, kr, hist, &s_and, &s_or, &s_prefix, &s_rem);
         const float tk = key_float((uint32_t)(K >> 32));
         t_new = tk + e2[r] + 2e-5f * (fabsf(tk) + asl[r]);
     }
@@ -548,15 +551,16 @@ cudaError_t launch_knn_merge_exact(int nrows, const int32_t* qlist, int k, int c
 
 size_t knn_merge_band_smem(int lcap, int cap) { return (size_t)(lcap + cap) * sizeof(unsigned long long); }
 
-cudaError_t launch_knn_merge_band(int nrows, int k, int cap, int lcap, int32_t* cnt, const int32_t* cand_id,
-                                  const float* cand_s, const float* e2, const float* asl, unsigned long long* list,
-                                  int32_t* lcount, float* thr, int32_t* need_exact, cudaStream_t s) {
+cudaError_t launch_knn_merge_band(int nrows, int k, const int32_t* krow, int cap, int lcap, int32_t* cnt,
+                                  const int32_t* cand_id, const float* cand_s, const float* e2, const float* asl,
+                                  unsigned long long* list, int32_t* lcount, float* thr, int32_t* need_exact,
+                                  cudaStream_t s) {
     if (nrows <= 0) return cudaSuccess;
     const size_t smem = knn_merge_band_smem(lcap, cap);
     cudaError_t e = set_smem_attr((const void*)knn_merge_band_kernel, smem);
     if (e != cudaSuccess) return e;
-    knn_merge_band_kernel<<<(unsigned)nrows, KM_THREADS, smem, s>>>(k, cap, lcap, cnt, cand_id, cand_s, e2, asl, list,
-                                                                    lcount, thr, need_exact);
+    knn_merge_band_kernel<<<(unsigned)nrows, KM_THREADS, smem, s>>>(k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl,
+                                                                    list, lcount, thr, need_exact);
     return cudaGetLastError();
 }
 
@@ -617,6 +621,29 @@ cudaError_t launch_knn_col_terms(const float* sqnorm, const float* resid, int64_
                                  unsigned int* maxes, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     knn_col_terms_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(sqnorm, resid, n, cosine, terms, maxes);
+    return cudaGetLastError();
+}
+
+namespace {
+__global__ void fill_f32_kernel(float* __restrict__ p, int64_t n, float v) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+__global__ void sq_terms_kernel(const float* __restrict__ sqnorm, int64_t n, float2* __restrict__ terms) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) terms[i] = make_float2(sqnorm[i], -2.0f);
+}
+}  // namespace
+
+cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    fill_f32_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(p, n, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sq_terms(const float* sqnorm, int64_t n, float2* terms, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    sq_terms_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(sqnorm, n, terms);
     return cudaGetLastError();
 }
 

@@ -121,6 +121,106 @@ __global__ void __launch_bounds__(PB_THREADS) probe_select_band_kernel(
     }
 }
 
+// Final step of the screened probe. Per query, the band list (every list
+// whose screened score can still reach the np-th) is rescored with the
+// reference-order FP32 distance and the best np by (distance, list) are
+// written ascending. A query whose band overflowed (need_exact) computes its
+// whole exact row into Drow (global scratch, nlist per query) and selects on
+// it, ties at the cut taken in list order. Also sets the fallback flag like
+// probe_select_band.
+__global__ void __launch_bounds__(PB_THREADS) probe_final_kernel(
+    const float* __restrict__ Q, int dim, const float* __restrict__ coarse, int nlist,
+    const int32_t* __restrict__ nprobe, int np_max, const int32_t* __restrict__ kq,
+    const int32_t* __restrict__ list_len, int allow_fb, int lcap, const unsigned long long* __restrict__ band,
+    const int32_t* __restrict__ lcount, const int32_t* __restrict__ need_exact, float* __restrict__ Drow,
+    int32_t* __restrict__ probe_ids, float* __restrict__ probe_d, int32_t* __restrict__ fallback,
+    unsigned long long* __restrict__ fb_count) {
+    extern __shared__ __align__(16) unsigned long long keys[];  // [lcap + P]
+    __shared__ float qv[QMAX];
+    __shared__ unsigned int hist[256];
+    __shared__ unsigned int whist[(PB_THREADS / 32) * 256];
+    __shared__ unsigned long long s_and, s_or, s_prefix;
+    __shared__ uint32_t s_p32, s_rem, s_a32, s_o32;
+    __shared__ int s_pos, s_wsum[PB_THREADS / 32];
+    __shared__ unsigned long long s_total;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t q = blockIdx.x;
+    const int np = min(nprobe[q], nlist);
+    for (int e = tid; e < dim; e += PB_THREADS) qv[e] = Q[q * dim + e];
+    if (tid == 0) {
+        s_pos = 0;
+        s_total = 0;
+    }
+    __syncthreads();
+    int P = 1;
+    while (P < np) P <<= 1;
+    unsigned long long* out;
+    if (need_exact[q]) {
+        float* row = Drow + q * nlist;
+        for (int c = tid; c < nlist; c += PB_THREADS) row[c] = sqeuclid_ref(qv, coarse + (int64_t)c * dim, dim);
+        __syncthreads();
+        radix_nth_fast<PB_THREADS>(row, nlist, np, whist, &s_p32, &s_rem, &s_a32, &s_o32);
+        const uint32_t T = s_p32, rem = s_rem;
+        out = keys;
+        // below the cut: order-free
+        for (int c = tid; c < nlist; c += PB_THREADS) {
+            const uint32_t key = float_key(row[c]);
+            if (key < T) out[atomicAdd(&s_pos, 1)] = ((unsigned long long)key << 32) | (uint32_t)c;
+        }
+        // at the cut: the first rem lists in list order
+        uint32_t taken = 0;
+        for (int c0 = 0; c0 < nlist && taken < rem; c0 += PB_THREADS) {
+            const int c = c0 + tid;
+            const bool eq = c < nlist && float_key(row[c]) == T;
+            const unsigned b = __ballot_sync(0xffffffffu, eq);
+            if (lane == 0) s_wsum[w] = __popc(b);
+            __syncthreads();
+            uint32_t before = 0, tot = 0;
+            for (int ww = 0; ww < PB_THREADS / 32; ww++) {
+                if (ww < w) before += s_wsum[ww];
+                tot += s_wsum[ww];
+            }
+            const uint32_t rank = taken + before + __popc(b & ((1u << lane) - 1u));
+            if (eq && rank < rem) out[atomicAdd(&s_pos, 1)] = ((unsigned long long)T << 32) | (uint32_t)c;
+            taken += tot;
+            __syncthreads();
+        }
+    } else {
+        const int L = lcount[q];
+        for (int i = tid; i < L; i += PB_THREADS) {
+            const uint32_t c = (uint32_t)(band[q * lcap + i] & 0xffffffffull);
+            keys[i] = ((unsigned long long)float_key(sqeuclid_ref(qv, coarse + (int64_t)c * dim, dim)) << 32) | c;
+        }
+        __syncthreads();
+        out = keys + L;
+        if (L > np) {
+            const unsigned long long K = radix_nth_u64(keys, L, np, hist, &s_and, &s_or, &s_prefix, &s_p32);
+            for (int i = tid; i < L; i += PB_THREADS)
+                if (keys[i] <= K) out[atomicAdd(&s_pos, 1)] = keys[i];
+        } else {
+            for (int i = tid; i < L; i += PB_THREADS) out[i] = keys[i];
+        }
+    }
+    __syncthreads();
+    for (int i = np + tid; i < P; i += PB_THREADS) out[i] = ~0ull;
+    __syncthreads();
+    if (P > 1) sort_u64(out, P);
+    unsigned long long part = 0;
+    for (int i = tid; i < np; i += PB_THREADS) {
+        const int c = (int)(out[i] & 0xffffffffull);
+        probe_ids[q * np_max + i] = c;
+        probe_d[q * np_max + i] = key_float((uint32_t)(out[i] >> 32));
+        part += (unsigned long long)list_len[c];
+    }
+    atomicAdd(&s_total, part);
+    __syncthreads();
+    if (tid == 0) {
+        const int fb = (allow_fb && s_total < (unsigned long long)kq[q]) ? 1 : 0;
+        fallback[q] = fb;
+        if (fb) atomicAdd(fb_count, 1ull);
+    }
+}
+
 __global__ void rescore_top8_kernel(const float* __restrict__ x, const float* __restrict__ xn2,
                                     const float* __restrict__ xres, int64_t n, int dim, int kp,
                                     const float* __restrict__ cent, int k, const float* __restrict__ cmax_p,
@@ -209,6 +309,28 @@ cudaError_t launch_probe_select_band(float* S, const float* Q, const float* qn2,
                                                                   nprobe,
                                                                   np_max, k, list_len, allow_fallback, probe_ids,
                                                                   probe_d, fallback, fallback_count, in_smem);
+    return cudaGetLastError();
+}
+
+size_t probe_final_smem(int lcap, int np_max) {
+    int P = 1;
+    while (P < np_max) P <<= 1;
+    return (size_t)(lcap + P) * sizeof(unsigned long long);
+}
+
+cudaError_t launch_probe_final(const float* Q, int64_t nq, int dim, const float* coarse, int nlist,
+                               const int32_t* nprobe, int np_max, const int32_t* k, const int32_t* list_len,
+                               int allow_fallback, int lcap, const unsigned long long* band, const int32_t* lcount,
+                               const int32_t* need_exact, float* Drow, int32_t* probe_ids, float* probe_d,
+                               int32_t* fallback, unsigned long long* fallback_count, cudaStream_t s) {
+    if (nq <= 0) return cudaSuccess;
+    if (np_max > PB_MAX || dim > QMAX || lcap < np_max) return cudaErrorInvalidValue;
+    const size_t smem = probe_final_smem(lcap, np_max);
+    cudaError_t e = cudaFuncSetAttribute(probe_final_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    probe_final_kernel<<<(unsigned)nq, PB_THREADS, smem, s>>>(Q, dim, coarse, nlist, nprobe, np_max, k, list_len,
+                                                              allow_fallback, lcap, band, lcount, need_exact, Drow,
+                                                              probe_ids, probe_d, fallback, fallback_count);
     return cudaGetLastError();
 }
 
