@@ -62,7 +62,8 @@ def parse():
     ap.add_argument("--profile-region", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="served-stream phase length (0 = skip)")
-    ap.add_argument("--serve-rate", type=float, default=5000.0, help="Poisson request arrivals per second")
+    ap.add_argument("--serve-rate", type=str, default="2000,5000",
+                    help="Poisson request arrivals per second, one served-stream phase per value")
     ap.add_argument("--knn", type=int, default=1, help="run the batched exact k-NN section (1M x 128, top-100)")
     ap.add_argument("--knn-n", type=int, default=1_000_000)
     ap.add_argument("--knn-nq", type=int, default=10_000)
@@ -432,11 +433,14 @@ def main():
 
     served = None
     if args.serve_seconds > 0:
-        try:
-            served = serve_stream(args, idx, q_host, gt, nr)
-        except Exception as e:  # pragma: no cover
-            log("served stream failed:", e)
-            served = {"error": str(e)}
+        served = []
+        for rate in [float(r) for r in args.serve_rate.split(",") if r]:
+            try:
+                served.append(serve_stream(args, idx, q_host, gt, nr, rate))
+                log("served", served[-1])
+            except Exception as e:  # pragma: no cover
+                log("served stream failed:", e)
+                served.append({"offered_requests_per_s": rate, "error": str(e)})
 
     knn = None
     if args.knn and rank == 0:
@@ -474,9 +478,9 @@ def main():
             "served_stream": served,
             "knn": knn,
         }
-        if served and "p50_ms" in served:
-            line["p50_ms"] = served["p50_ms"]
-            line["p99_ms"] = served["p99_ms"]
+        if served and "p50_ms" in served[0]:
+            line["p50_ms"] = served[0]["p50_ms"]
+            line["p99_ms"] = served[0]["p99_ms"]
         print(json.dumps(line), flush=True)
     idx.close()
     if ws > 1:
@@ -593,8 +597,8 @@ def knn_section(args, torch, dev):
     return out
 
 
-def serve_stream(args, idx, q_host, gt, nr):
-    """The served stream: Poisson arrivals at --serve-rate requests/s, each a
+def serve_stream(args, idx, q_host, gt, nr, rate):
+    """The served stream: Poisson arrivals at `rate` requests/s, each a
     block of 1-512 queries (log-uniform), k uniform in [1, 100], nprobe
     log-uniform in [8, 256]; BulkAdd of 1,000-vector chunks and Deletes of
     random ids, each at 1% of the request rate, applied between batches.
@@ -637,7 +641,7 @@ def serve_stream(args, idx, q_host, gt, nr):
         if now < t_next:
             time.sleep(min(t_next - now, 0.001))
             continue
-        t_next += rng.exponential(1.0 / args.serve_rate)
+        t_next += rng.exponential(1.0 / rate)
         u = rng.random()
         if u < 0.01:
             # random unit vectors: far from every query, so they do not
@@ -672,7 +676,7 @@ def serve_stream(args, idx, q_host, gt, nr):
             tot += 10
     return {"requests": int(st["requests"]), "queries": int(st["queries"]), "batches": int(st["batches"]),
             "mutations": int(st["mutations"]), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-            "queries_per_s": st["queries_per_s"], "offered_requests_per_s": args.serve_rate,
+            "queries_per_s": st["queries_per_s"], "offered_requests_per_s": rate,
             "recall_at_10_k_ge_10": hits / tot if tot else None,
             "peak_admitted_bytes": int(st["peak_admitted_bytes"]), "relayouts": int(st["relayouts"]),
             "mutation_ms_total": round(st["mutation_ms"], 1),

@@ -16,7 +16,8 @@ static thread_local std::string g_new_error;
 
 
 // Capacity for a list that must hold `len` rows.
-static int64_t list_capacity(int64_t len) { return round_up(len + len / 8 + 32, 32); }
+// Slots for a list of len rows: a quarter more, plus 32.
+static int64_t list_capacity(int64_t len) { return round_up(len + len / 4 + 32, 32); }
 
 // ---------------------------------------------------------------------------
 // Device layout management.
@@ -24,7 +25,10 @@ static int64_t list_capacity(int64_t len) { return round_up(len + len / 8 + 32, 
 // Lays the lists out afresh with capacities caps[], moving the live rows.
 // With move_rows false it only allocates (the caller fills the rows).
 // Deleted (tombstoned) slots are dropped while the live rows move, so a
-// relayout also compacts the lists.
+// relayout also compacts the lists. The rows move on the device, list by
+// list; the host only renumbers the lists that held tombstones. The previous
+// arrays are kept as the next relayout's destination, so a relayout of an
+// index that does not grow allocates nothing.
 static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_rows = true) {
     const int dim = h->o.dimension;
     std::vector<int64_t> start(h->nlist);
@@ -34,47 +38,44 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
         total += round_up(caps[l], 32);
     }
     if (total >= (int64_t)1 << 31) return h->fail(HANN_E_UNSUPPORTED, "more than 2^31 stored rows");
-    DBuf<float> vec, term;
-    DBuf<int64_t> rid;
-    DBuf<int32_t> rcl;
-    DBuf<uint8_t> codes;
-    CK(vec.reserve((size_t)total * dim));
-    CK(term.reserve((size_t)total));
-    CK(rid.reserve((size_t)total));
-    CK(rcl.reserve((size_t)total));
-    CK(codes.reserve((size_t)total * h->code_stride));
+    CK(h->s_vectors.reserve((size_t)total * dim));
+    CK(h->s_term.reserve((size_t)total));
+    CK(h->s_row_id.reserve((size_t)total));
+    CK(h->s_row_cluster.reserve((size_t)total));
+    CK(h->s_codes.reserve((size_t)total * h->code_stride));
     if (move_rows && h->rows_cap > 0) {
-        std::vector<int64_t> src, dst;
+        std::vector<int64_t> src(h->nlist);
+        std::vector<int32_t> len(h->nlist), cmp(h->nlist);
         for (int l = 0; l < h->nlist; l++) {
-            const int64_t len = (int64_t)h->list_ids[l].size();
+            src[l] = h->h_start[l];
+            len[l] = (int32_t)h->list_ids[l].size();
+            cmp[l] = h->live_count[l] != (int64_t)h->list_ids[l].size();
+            if (!cmp[l]) continue;
             int64_t w = 0;
-            for (int64_t j = 0; j < len; j++) {
+            for (size_t j = 0; j < h->list_ids[l].size(); j++) {
                 if (!h->list_alive[l][j]) continue;
-                src.push_back(h->h_start[l] + j);
-                dst.push_back(start[l] + w);
-                h->list_ids[l][w] = h->list_ids[l][j];
-                w++;
+                h->list_ids[l][w++] = h->list_ids[l][j];
             }
             h->list_ids[l].resize(w);
             h->list_alive[l].assign(w, 1);
         }
         h->dead_rows = 0;
         DBuf<int64_t> dsrc, ddst;
+        DBuf<int32_t> dlen, dcmp;
         CK(upload(dsrc, src.data(), src.size(), h->stream));
-        CK(upload(ddst, dst.data(), dst.size(), h->stream));
-        const int64_t n = (int64_t)src.size();
-        CK(launch_copy_words(h->d_vectors.p, dsrc.p, vec.p, ddst.p, n, dim, h->stream));
-        CK(launch_copy_words(h->d_term.p, dsrc.p, term.p, ddst.p, n, 1, h->stream));
-        CK(launch_copy_words(h->d_row_id.p, dsrc.p, rid.p, ddst.p, n, 2, h->stream));
-        CK(launch_copy_words(h->d_row_cluster.p, dsrc.p, rcl.p, ddst.p, n, 1, h->stream));
-        CK(launch_copy_words(h->d_codes.p, dsrc.p, codes.p, ddst.p, n, h->code_stride / 4, h->stream));
+        CK(upload(ddst, start.data(), start.size(), h->stream));
+        CK(upload(dlen, len.data(), len.size(), h->stream));
+        CK(upload(dcmp, cmp.data(), cmp.size(), h->stream));
+        CK(launch_relayout_lists(h->nlist, dsrc.p, dlen.p, ddst.p, dcmp.p, dim, h->code_stride / 4, h->d_vectors.p,
+                                 h->s_vectors.p, h->d_codes.p, h->s_codes.p, h->d_term.p, h->s_term.p,
+                                 h->d_row_id.p, h->s_row_id.p, h->d_row_cluster.p, h->s_row_cluster.p, h->stream));
         CK(cudaStreamSynchronize(h->stream));
     }
-    h->d_vectors.swap(vec);
-    h->d_term.swap(term);
-    h->d_row_id.swap(rid);
-    h->d_row_cluster.swap(rcl);
-    h->d_codes.swap(codes);
+    h->d_vectors.swap(h->s_vectors);
+    h->d_term.swap(h->s_term);
+    h->d_row_id.swap(h->s_row_id);
+    h->d_row_cluster.swap(h->s_row_cluster);
+    h->d_codes.swap(h->s_codes);
     h->h_start = start;
     h->h_cap.assign(h->nlist, 0);
     for (int l = 0; l < h->nlist; l++) h->h_cap[l] = round_up(caps[l], 32);
@@ -214,9 +215,11 @@ int add_commit(hann_pqivf* h, const int64_t* ids) {
     if (m.grow) {
         // one relayout that also drops every tombstone
         std::vector<int64_t> caps(h->nlist);
+        // every list gets its headroom back; lists that overflowed double
         for (int l = 0; l < h->nlist; l++) {
             const int64_t live = h->live_count[l] + m.add[l];
-            caps[l] = std::max(h->h_cap[l], live > h->h_cap[l] ? list_capacity(live + live / 2) : (int64_t)0);
+            const int64_t need = (int64_t)h->list_ids[l].size() + m.add[l];
+            caps[l] = std::max(h->h_cap[l], need > h->h_cap[l] ? list_capacity(2 * live) : list_capacity(live));
         }
         int rc = relayout(h, caps);
         if (rc) return rc;

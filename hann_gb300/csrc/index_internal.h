@@ -187,6 +187,11 @@ struct hann_pqivf {
     DBuf<int64_t> d_start, d_row_id;
     DBuf<int32_t> d_len, d_live, d_row_cluster;
     DBuf<uint8_t> d_codes;
+    // the previous row arrays, kept for the next relayout to reuse
+    DBuf<float> s_vectors, s_term;
+    DBuf<int64_t> s_row_id;
+    DBuf<int32_t> s_row_cluster;
+    DBuf<uint8_t> s_codes;
 
     // search scratch of the handle's own stream
     SearchScratch main;

@@ -183,6 +183,14 @@ cudaError_t launch_rerank(const ScanParams& p, const float* queries, int64_t nq,
                           const uint32_t* cand_seq, int R, const int32_t* k, int kmax, int mode,
                           int64_t* ids, double* dist, int32_t* nout, cudaStream_t s);
 
+// Moves every list's slots to a new layout (one block per list), dropping
+// tombstones (row id -1) in the lists flagged compact.
+cudaError_t launch_relayout_lists(int nlist, const int64_t* src_start, const int32_t* src_len,
+                                  const int64_t* dst_start, const int32_t* compact, int dim, int cwords,
+                                  const float* vin, float* vout, const void* cin, void* cout, const float* tin,
+                                  float* tout, const int64_t* rin, int64_t* rout, const int32_t* clin, int32_t* clout,
+                                  cudaStream_t s);
+
 // ---- batched exact k-NN over a flat base (kernels_knn.cu) ------------------------
 
 constexpr int KNN_SIMT_DMAX = 256;  // register-tiled SIMT distances up to this dimension

@@ -514,6 +514,70 @@ __global__ void tombstone_kernel(const int64_t* __restrict__ rows, int64_t n, fl
     row_id[rows[i]] = -1;
 }
 
+// One block per list: the list's slots [src, src + len) move, in order, to
+// [dst, ...); with compact set only live slots (row id >= 0) move, so the
+// tombstones disappear. Rows go 256 at a time: the block ranks the live
+// slots with ballots, then copies the chunk's vector and code words with
+// consecutive threads on consecutive words.
+__global__ void __launch_bounds__(256) relayout_lists_kernel(
+    const int64_t* __restrict__ src_start, const int32_t* __restrict__ src_len, const int64_t* __restrict__ dst_start,
+    const int32_t* __restrict__ compact, int dim, int cwords, const float* __restrict__ vin, float* __restrict__ vout,
+    const uint32_t* __restrict__ cin, uint32_t* __restrict__ cout, const float* __restrict__ tin,
+    float* __restrict__ tout, const int64_t* __restrict__ rin, int64_t* __restrict__ rout,
+    const int32_t* __restrict__ clin, int32_t* __restrict__ clout) {
+    __shared__ int pos[256];
+    __shared__ int wcnt[8];
+    const int l = blockIdx.x, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t src = src_start[l], dst = dst_start[l];
+    const int len = src_len[l];
+    const bool cmp = compact[l] != 0;
+    int out = 0;
+    for (int c0 = 0; c0 < len; c0 += 256) {
+        const int j = c0 + tid;
+        const bool live = j < len && (!cmp || rin[src + j] >= 0);
+        const unsigned b = __ballot_sync(0xffffffffu, live);
+        if (lane == 0) wcnt[w] = __popc(b);
+        __syncthreads();
+        int before = 0, tot = 0;
+        for (int ww = 0; ww < 8; ww++) {
+            if (ww < w) before += wcnt[ww];
+            tot += wcnt[ww];
+        }
+        const int p = live ? out + before + __popc(b & ((1u << lane) - 1u)) : -1;
+        pos[tid] = p;
+        if (live) {
+            tout[dst + p] = tin[src + j];
+            rout[dst + p] = rin[src + j];
+            clout[dst + p] = clin[src + j];
+        }
+        __syncthreads();
+        const int rows = min(256, len - c0);
+        for (int e = tid; e < rows * dim; e += 256) {
+            const int r = e / dim, i = e - r * dim;
+            if (pos[r] >= 0) vout[(dst + pos[r]) * dim + i] = vin[(src + c0 + r) * dim + i];
+        }
+        for (int e = tid; e < rows * cwords; e += 256) {
+            const int r = e / cwords, i = e - r * cwords;
+            if (pos[r] >= 0) cout[(dst + pos[r]) * cwords + i] = cin[(src + c0 + r) * cwords + i];
+        }
+        out += tot;
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_relayout_lists(int nlist, const int64_t* src_start, const int32_t* src_len,
+                                  const int64_t* dst_start, const int32_t* compact, int dim, int cwords,
+                                  const float* vin, float* vout, const void* cin, void* cout, const float* tin,
+                                  float* tout, const int64_t* rin, int64_t* rout, const int32_t* clin, int32_t* clout,
+                                  cudaStream_t s) {
+    if (nlist <= 0) return cudaSuccess;
+    relayout_lists_kernel<<<(unsigned)nlist, 256, 0, s>>>(src_start, src_len, dst_start, compact, dim, cwords, vin,
+                                                         vout, static_cast<const uint32_t*>(cin),
+                                                         static_cast<uint32_t*>(cout), tin, tout, rin, rout, clin,
+                                                         clout);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tombstone(const int64_t* rows, int64_t n, float* term, int64_t* row_id, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     tombstone_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(rows, n, term, row_id);
