@@ -43,6 +43,18 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
     CK(h->s_row_id.reserve((size_t)total));
     CK(h->s_row_cluster.reserve((size_t)total));
     CK(h->s_codes.reserve((size_t)total * h->code_stride));
+    // scan words: each list's region rounded up to whole groups of rows
+    const bool sw = scan_skew_supported(h->o.num_subquantizers);
+    std::vector<int64_t> swstart(h->nlist);
+    int64_t swtotal = 0;
+    if (sw) {
+        const int G = scan_group_rows(h->o.num_subquantizers);
+        for (int l = 0; l < h->nlist; l++) {
+            swstart[l] = swtotal;
+            swtotal += round_up(round_up(caps[l], 32), G);
+        }
+        CK(h->s_scanw.reserve((size_t)swtotal * scan_words_per_row(h->o.num_subquantizers)));
+    }
     if (move_rows && h->rows_cap > 0) {
         std::vector<int64_t> src(h->nlist);
         std::vector<int32_t> len(h->nlist), cmp(h->nlist);
@@ -76,11 +88,17 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
     h->d_row_id.swap(h->s_row_id);
     h->d_row_cluster.swap(h->s_row_cluster);
     h->d_codes.swap(h->s_codes);
+    if (sw) h->d_scanw.swap(h->s_scanw);
+    h->scanw_dirty = true;  // rebuilt by upload_lens, which every caller runs next
     h->h_start = start;
     h->h_cap.assign(h->nlist, 0);
     for (int l = 0; l < h->nlist; l++) h->h_cap[l] = round_up(caps[l], 32);
     h->rows_cap = total;
     CK(upload(h->d_start, h->h_start.data(), h->h_start.size(), h->stream));
+    if (sw) {
+        h->h_swstart = swstart;
+        CK(upload(h->d_swstart, h->h_swstart.data(), h->h_swstart.size(), h->stream));
+    }
     CK(cudaStreamSynchronize(h->stream));
     return HANN_OK;
 }
@@ -93,6 +111,11 @@ static int upload_lens(hann_pqivf* h) {
     }
     CK(upload(h->d_len, len.data(), len.size(), h->stream));
     CK(upload(h->d_live, live.data(), live.size(), h->stream));
+    if (h->scanw_dirty && h->rows_cap > 0) {
+        CK(launch_scan_words_lists(h->d_codes.p, h->code_stride, h->o.num_subquantizers, h->d_start.p, h->d_len.p,
+                                   h->d_swstart.p, h->nlist, h->d_scanw.p, h->stream));
+        h->scanw_dirty = false;
+    }
     CK(cudaStreamSynchronize(h->stream));
     return HANN_OK;
 }
@@ -242,6 +265,8 @@ int add_commit(hann_pqivf* h, const int64_t* ids) {
     CK(launch_copy_words(m.codes.p, nullptr, h->d_codes.p, m.dst.p, n, h->code_stride / 4, h->stream));
     CK(launch_copy_words(m.ids.p, nullptr, h->d_row_id.p, m.dst.p, n, 2, h->stream));
     CK(launch_copy_words(m.asg.p, nullptr, h->d_row_cluster.p, m.dst.p, n, 1, h->stream));
+    CK(launch_scan_words_rows(h->d_codes.p, h->code_stride, h->o.num_subquantizers, h->d_start.p, h->d_swstart.p,
+                              m.dst.p, m.asg.p, n, h->d_scanw.p, h->stream));
     // the term last: a row becomes selectable only once it is complete
     CK(launch_copy_words(m.term.p, nullptr, h->d_term.p, m.dst.p, n, 1, h->stream));
     CK(cudaStreamSynchronize(h->stream));

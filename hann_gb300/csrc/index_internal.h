@@ -187,11 +187,16 @@ struct hann_pqivf {
     DBuf<int64_t> d_start, d_row_id;
     DBuf<int32_t> d_len, d_live, d_row_cluster;
     DBuf<uint8_t> d_codes;
+    DBuf<uint16_t> d_scanw;   // scan words, rebuilt from the codes when rows are placed
+    DBuf<int64_t> d_swstart;  // first scan-word slot of each list
+    std::vector<int64_t> h_swstart;
+    bool scanw_dirty = false;
     // the previous row arrays, kept for the next relayout to reuse
     DBuf<float> s_vectors, s_term;
     DBuf<int64_t> s_row_id;
     DBuf<int32_t> s_row_cluster;
     DBuf<uint8_t> s_codes;
+    DBuf<uint16_t> s_scanw;
 
     // search scratch of the handle's own stream
     SearchScratch main;
@@ -233,6 +238,8 @@ struct hann_pqivf {
         p.list_start = d_start.p;
         p.list_len = d_len.p;
         p.codes = d_codes.p;
+        p.scanw = scan_skew_supported(o.num_subquantizers) ? d_scanw.p : nullptr;
+        p.sw_start = d_swstart.p;
         p.term = d_term.p;
         p.row_cluster = d_row_cluster.p;
         p.vectors = d_vectors.p;

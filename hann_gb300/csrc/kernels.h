@@ -139,6 +139,8 @@ struct ScanParams {
     const int64_t* list_start;  // [nlist] first row of each list
     const int32_t* list_len;    // [nlist]
     const uint8_t* codes;     // [rows][code_stride]
+    const uint16_t* scanw;    // table offsets per row (kernels_scan.cu), blocked by groups of rows
+    const int64_t* sw_start;  // [nlist] first scan-word slot of each list
     const float* term;        // [rows]
     const int32_t* row_cluster;  // [rows]
     const float* vectors;     // [rows][dim]
@@ -169,6 +171,17 @@ cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, c
 // 32; launch_scan dispatches to it when it applies. Its candidates leave
 // unsorted.
 bool scan_skew_supported(int M);
+int scan_words_per_row(int M);
+int scan_group_rows(int M);
+size_t scan_skew_smem(int R);
+// Scan words (kernels_scan.cu) of every slot of every list, or of the rows at
+// positions rows[i] in lists cluster[i].
+cudaError_t launch_scan_words_lists(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+                                    const int32_t* list_len, const int64_t* sw_start, int nlist, uint16_t* scanw,
+                                    cudaStream_t s);
+cudaError_t launch_scan_words_rows(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+                                   const int64_t* sw_start, const int64_t* rows, const int32_t* cluster, int64_t n,
+                                   uint16_t* scanw, cudaStream_t s);
 cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
                              const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
                              int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,

@@ -1,22 +1,30 @@
 // kernels_scan.cu -- bank-conflict-free ADC list scan with warp radix
-// selection, for M a multiple of 4 and at most 32 (the row's codes fill whole
-// 32-bit words). Other M use scan_kernel in kernels_search.cu.
+// selection, for M up to 32. Larger M use scan_kernel in kernels_search.cu.
 //
 // Same distance as scan_kernel: ||q-c||^2 + term + sum_m T[m][code_m].
 //
-// Lookup table without bank conflicts. The table is stored as 256 rows of 32
-// words, entry (m, j) at row j, bank (copy * M + m); when M divides 32 it is
-// replicated 32 / M times. Lane l walks the subquantizers in the rotated order
-// m_s = (s + l mod M) mod M and uses copy (l / M) mod copies, so in any step
-// the 32 lanes read 32 distinct banks (M | 32), or at most two lanes share a
-// bank (M = 24). The lane rotates its row's code bytes by l mod M once per row
-// (word selects and funnel shifts) so step s reads byte s.
+// Lookup table without bank conflicts. The table is 256 rows of 32 words,
+// entry (m, j) at row j, bank (c * M + m) for every copy c < 32 / M. A warp
+// takes G = M * (32 / M) rows of a list at a time; lane l (l < G) owns rows
+// whose position in the list is l mod G, uses copy c = l / M, and walks the
+// subquantizers in the rotated order m_s = (s + l) mod M, so in every step
+// the G lanes read G distinct banks.
+//
+// Scan words. Rather than its code bytes, each row stores for every step s
+// the byte offset of its table entry, (code_{m_s} * 32 + c * M + m_s) * 4,
+// as a 16-bit word ("scan words", built from the codes whenever rows are
+// placed; see launch_scan_words_*). A lookup is then one shift or mask, one
+// shared load and one add. The words of G consecutive rows are stored plane
+// by plane, so a warp step reads them with contiguous 16-byte loads: the
+// scan is bound by the L1 data pipe's wavefronts (table reads plus these
+// loads), and contiguous loads take the fewest.
 //
 // Selection without sorting. Each warp appends rows below the block-wide
 // threshold to its buffer; a full buffer is cut back to its R smallest keys
-// by a ballot radix select, whose R-th key lowers the threshold. At the end
-// warp 0 selects the query's R best from the warps' survivors. Candidates
-// leave unsorted: the rerank sorts them by exact distance.
+// by a radix select on 8-bit digits (warp-private histogram), whose R-th key
+// lowers the threshold. At the end warp 0 selects the query's R best from the
+// warps' survivors. Candidates leave unsorted: the rerank sorts them by exact
+// distance.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -27,11 +35,14 @@ constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint32_t KEY_INF = 0xff800000u;  // float_key(+inf)
+constexpr int SCAN_FLAT_LISTS = 128;        // probe lists held for the balanced schedule
 
 // Keeps the `R` smallest keys of entries [0, count) (ties at the cut broken
-// by position), compacted in place to [0, R). Returns the R-th smallest key
-// through *kth. Warp-synchronous.
-__device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count, int R, uint32_t* kth) {
+// by position), compacted in place to [0, R). Returns through *kth a key at
+// or above the R-th smallest (exactly it unless the digit holding the cut
+// came out whole). hist: the warp's 256 counters. Warp-synchronous.
+__device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count, int R, uint32_t* kth,
+                           uint32_t* hist) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     if (count <= R) {
@@ -58,20 +69,64 @@ __device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count
     const int top = 31 - __clz(diff);
     uint32_t prefix = top == 31 ? 0u : (band & (0xffffffffu << (top + 1)));
     uint32_t need = (uint32_t)R;
-    for (int bit = top; bit >= 0; bit--) {
-        const uint32_t hi = bit == 31 ? 0u : (0xffffffffu << (bit + 1));
-        int c0 = 0;
+    int L = 0;  // bits below the resolved prefix
+    for (int hi = top; hi >= 0; hi -= 8) {
+        const int lo = hi >= 7 ? hi - 7 : 0;
+        const uint32_t himask = hi == 31 ? 0u : (0xffffffffu << (hi + 1));
+        const uint32_t dmask = (1u << (hi - lo + 1)) - 1u;
+#pragma unroll
+        for (int b = 0; b < 8; b++) hist[b * 32 + lane] = 0;
+        __syncwarp();
         for (int ch = 0; ch < nch; ch++) {
             const int i = ch * 32 + lane;
-            const uint32_t kk = i < count ? key[i] : 0xffffffffu;
-            const bool m = i < count && (kk & hi) == prefix && !((kk >> bit) & 1u);
-            c0 += __popc(__ballot_sync(FULL, m));
+            uint32_t bin = 0xffffffffu;
+            if (i < count) {
+                const uint32_t kk = key[i];
+                if ((kk & himask) == prefix) bin = (kk >> lo) & dmask;
+            }
+            const unsigned peers = __match_any_sync(FULL, bin);
+            if (bin != 0xffffffffu && lane == __ffs(peers) - 1) hist[bin] += __popc(peers);
+            __syncwarp();
         }
-        if ((uint32_t)c0 < need) {
-            need -= (uint32_t)c0;
-            prefix |= 1u << bit;
+        // lane owns bins [8 lane, 8 lane + 8)
+        uint32_t cnt[8], tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            cnt[j] = hist[lane * 8 + j];
+            tot += cnt[j];
         }
+        uint32_t incl = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const uint32_t excl = incl - tot;
+        const bool mine = excl < need && need <= incl;
+        uint32_t pick = 0, below = 0, inbin = 0;
+        if (mine) {
+            uint32_t cum = excl;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                if (cum < need && need <= cum + cnt[j]) {
+                    pick = (uint32_t)(lane * 8 + j);
+                    below = cum;
+                    inbin = cnt[j];
+                }
+                cum += cnt[j];
+            }
+        }
+        const int owner = __ffs(__ballot_sync(FULL, mine)) - 1;
+        pick = __shfl_sync(FULL, pick, owner);
+        below = __shfl_sync(FULL, below, owner);
+        inbin = __shfl_sync(FULL, inbin, owner);
+        __syncwarp();
+        prefix |= pick << lo;
+        need -= below;
+        L = lo;
+        if (inbin == need) break;  // the whole digit is kept
     }
+    const uint32_t pk = L == 0 ? prefix : (prefix >> L);
     int out = 0, eq_taken = 0;
     for (int ch = 0; ch < nch; ch++) {
         const int i = ch * 32 + lane;
@@ -79,8 +134,9 @@ __device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count
         const uint32_t kk = in ? key[i] : 0xffffffffu;
         const uint32_t ss = in ? seq[i] : 0u;
         const int32_t rr = in ? row[i] : 0;
-        const bool lt_k = in && kk < prefix;
-        const bool eq = in && kk == prefix;
+        const uint32_t kp = L == 0 ? kk : (kk >> L);
+        const bool lt_k = in && kp < pk;
+        const bool eq = in && kp == pk;
         const unsigned beq = __ballot_sync(FULL, eq);
         const bool keep = lt_k || (eq && (uint32_t)(eq_taken + __popc(beq & lt)) < need);
         const unsigned bk = __ballot_sync(FULL, keep);
@@ -95,35 +151,12 @@ __device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count
         eq_taken += __popc(beq);
         __syncwarp();
     }
-    *kth = prefix;
+    *kth = L == 0 ? prefix : (prefix | ((1u << L) - 1u));
     return out;
 }
 
-template <int MW>
-__device__ __forceinline__ void rotate_bytes(uint32_t (&w)[MW], int a, int b) {
-    // words left by a (0 <= a < MW), then bytes by b (0..3)
-#pragma unroll
-    for (int t = 0; (1 << t) < MW; t++) {
-        const int sh = (1 << t) % MW;
-        if ((a >> t) & 1) {
-            uint32_t tmp[MW];
-#pragma unroll
-            for (int i = 0; i < MW; i++) tmp[i] = w[(i + sh) % MW];
-#pragma unroll
-            for (int i = 0; i < MW; i++) w[i] = tmp[i];
-        }
-    }
-    if (b) {
-        uint32_t tmp[MW];
-#pragma unroll
-        for (int i = 0; i < MW; i++) tmp[i] = __funnelshift_r(w[i], w[(i + 1) % MW], 8 * b);
-#pragma unroll
-        for (int i = 0; i < MW; i++) w[i] = tmp[i];
-    }
-}
-
-template <int MW>
-__global__ void __launch_bounds__(THREADS) scan_skew_kernel(ScanParams p, const float* __restrict__ Q,
+template <int MP>
+__global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, const float* __restrict__ Q,
                                                             const float* __restrict__ probe_d,
                                                             const int32_t* __restrict__ probe_ids,
                                                             const int32_t* __restrict__ nprobe, int np_max,
@@ -132,18 +165,24 @@ __global__ void __launch_bounds__(THREADS) scan_skew_kernel(ScanParams p, const 
                                                             float* __restrict__ cand_d,
                                                             uint32_t* __restrict__ cand_seq,
                                                             unsigned long long* __restrict__ rows_scanned) {
-    constexpr int M = 4 * MW;
-    constexpr int COPIES = (32 % M == 0) ? 32 / M : 1;
+    // MP: scan words per row (M rounded up to 8); G rows per warp step
+    __shared__ __align__(16) float lut[256 * 32];
     extern __shared__ __align__(16) unsigned char smraw[];
-    float* lut = reinterpret_cast<float*>(smraw);  // [256][32]
-    uint32_t* wkey = reinterpret_cast<uint32_t*>(lut + 256 * 32);
+    uint32_t* wkey = reinterpret_cast<uint32_t*>(smraw);
     uint32_t* wseq = wkey + WARPS * CAPW;
     int32_t* wrow = reinterpret_cast<int32_t*>(wseq + WARPS * CAPW);
     uint32_t* mkey = reinterpret_cast<uint32_t*>(wrow + WARPS * CAPW);  // [WARPS * R] merge region
     uint32_t* mseq = mkey + WARPS * R;
     int32_t* mrow = reinterpret_cast<int32_t*>(mseq + WARPS * R);
+    uint32_t* whist = reinterpret_cast<uint32_t*>(mrow + WARPS * R);   // [WARPS][256]
     __shared__ uint32_t s_tau;
     __shared__ int s_wcount[WARPS];
+    __shared__ int s_lstart[SCAN_FLAT_LISTS], s_lsw[SCAN_FLAT_LISTS];
+    __shared__ int s_llen[SCAN_FLAT_LISTS], s_lsteps[SCAN_FLAT_LISTS + 1];
+    __shared__ float s_lbase[SCAN_FLAT_LISTS];
+    const int M = p.M;
+    const int copies = 32 / M;
+    const int G = 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int64_t q = blockIdx.x;
     const float* qv = Q + q * p.dim;
@@ -151,40 +190,32 @@ __global__ void __launch_bounds__(THREADS) scan_skew_kernel(ScanParams p, const 
     for (int e = tid; e < 256 * 32; e += THREADS) {
         const int j = e >> 5, bk = e & 31;
         float v = 0.0f;
-        if (bk < COPIES * M && j < p.pqK) {
+        if (bk < copies * M && j < p.pqK) {
             const int m = bk % M;
             const float* cw = p.codebooks + ((int64_t)m * p.pqK + j) * p.dsub;
             const float* qm = qv + m * p.dsub;
-            float s = 0.0f;
-            for (int t = 0; t < p.dsub; t++) s = fmaf(qm[t], cw[t], s);
-            v = -2.0f * s;
+            float acc = 0.0f;
+            for (int t = 0; t < p.dsub; t++) acc = fmaf(qm[t], cw[t], acc);
+            v = -2.0f * acc;
         }
         lut[e] = v;
-    }
-    // Lane constants: rotation r = lane mod M and the byte offset of each step's bank.
-    const int r = lane % M;
-    const int cb = (COPIES > 1 ? (lane / M) % COPIES : 0) * M;
-    uint32_t boff[M];
-#pragma unroll
-    for (int s = 0; s < M; s++) {
-        int m = s + r;
-        if (m >= M) m -= M;
-        boff[s] = (uint32_t)((cb + m) << 2);
     }
     __syncthreads();
     const unsigned char* lutb = reinterpret_cast<const unsigned char*>(lut);
     uint32_t* key = wkey + w * CAPW;
     uint32_t* seq = wseq + w * CAPW;
     int32_t* row = wrow + w * CAPW;
+    uint32_t* hist = whist + w * 256;
     const bool fb = fallback[q] != 0;
     const int nl = fb ? p.nlist : min(nprobe[q], p.nlist);
     const unsigned ltm = (1u << lane) - 1u;
+    const bool act = lane < G;
     int count = 0;
     unsigned long long scanned = 0;
-    // The warp walks its lists chunk by chunk (32 rows, one per lane) and
-    // loads the next chunk -- in the same list or the next one -- before it
-    // computes the current, so each lane keeps two rows in flight.
-    auto list_meta = [&](int i, int64_t& start, int& len, float& base) {
+    // The warp walks its lists G rows at a time and loads the next step's
+    // rows -- in the same list or the next one -- before it computes the
+    // current, so each lane keeps two rows in flight.
+    auto list_meta = [&](int i, int64_t& start, int64_t& sws, int& len, float& base) {
         const int l = fb ? i : probe_ids[q * np_max + i];
         if (fb) {
             float part = 0.0f;
@@ -199,93 +230,171 @@ __global__ void __launch_bounds__(THREADS) scan_skew_kernel(ScanParams p, const 
             base = probe_d[q * np_max + i];
         }
         start = p.list_start[l];
+        sws = p.sw_start[l];
         len = p.list_len[l];
     };
-    auto load_row = [&](int64_t grow, uint32_t (&cw)[MW], float& term) {
-        const uint8_t* cp = p.codes + grow * p.code_stride;
-        if constexpr (MW % 2 == 0) {
+    // Scan words of one step: G rows, stored as MP / 8 planes of G
+    // consecutive 16-byte chunks, so the warp's loads are contiguous.
+    auto load_row = [&](int64_t sws, int step, int64_t grow, uint4 (&sw)[MP / 8], float& term) {
+        const uint4* sp = reinterpret_cast<const uint4*>(p.scanw) + sws * (MP / 8) + (int64_t)step * G * (MP / 8) + lane;
 #pragma unroll
-            for (int t = 0; t < MW / 2; t++) {
-                const uint2 v = __ldg(reinterpret_cast<const uint2*>(cp) + t);
-                cw[2 * t] = v.x;
-                cw[2 * t + 1] = v.y;
-            }
-        } else {
-#pragma unroll
-            for (int t = 0; t < MW; t++) cw[t] = __ldg(reinterpret_cast<const uint32_t*>(cp) + t);
-        }
+        for (int t = 0; t < MP / 8; t++) sw[t] = __ldg(sp + t * G);
         term = __ldg(p.term + grow);
     };
-    int ci = w, cr0 = 0, clen = 0;
-    int64_t cstart = 0;
-    float cbase = 0.0f;
-    while (ci < nl) {
-        list_meta(ci, cstart, clen, cbase);
-        scanned += (unsigned long long)clen;
-        if (clen > 0) break;
-        ci += WARPS;
-    }
-    uint32_t ncw[MW];
-    float nterm = 0.0f;
+    // four partial sums keep the adds off one long dependency chain
+    auto lookup = [&](const uint4 (&sw)[MP / 8], float acc) {
+        const uint32_t* wv = reinterpret_cast<const uint32_t*>(sw);
+        float part[4] = {acc, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int t = 0; t < MW; t++) ncw[t] = 0;
-    if (ci < nl && lane < clen) load_row(cstart + lane, ncw, nterm);
-    while (ci < nl) {
-        uint32_t cw[MW];
-#pragma unroll
-        for (int t = 0; t < MW; t++) cw[t] = ncw[t];
-        const float term = nterm;
-        const int i = ci;
-        const bool valid = cr0 + lane < clen;
-        const int64_t grow = cstart + cr0 + lane;
-        const float base = cbase;
-        // advance, then prefetch the next chunk
-        cr0 += 32;
-        if (cr0 >= clen) {
-            cr0 = 0;
-            ci += WARPS;
-            while (ci < nl) {
-                list_meta(ci, cstart, clen, cbase);
-                scanned += (unsigned long long)clen;
-                if (clen > 0) break;
-                ci += WARPS;
-            }
+        for (int s2 = 0; s2 < MP / 2; s2++) {
+            const uint32_t word = wv[s2];
+            if (2 * s2 < M) part[(2 * s2) & 3] += *reinterpret_cast<const float*>(lutb + (word & 0xffffu));
+            if (2 * s2 + 1 < M) part[(2 * s2 + 1) & 3] += *reinterpret_cast<const float*>(lutb + (word >> 16));
         }
-        if (ci < nl && cr0 + lane < clen) load_row(cstart + cr0 + lane, ncw, nterm);
-        uint32_t k = KEY_INF;
-        if (valid) {
-            rotate_bytes<MW>(cw, r >> 2, r & 3);
-            float acc = base + term;
-#pragma unroll
-            for (int s = 0; s < M; s++) {
-                const uint32_t code = (cw[s >> 2] >> (8 * (s & 3))) & 255u;
-                acc += *reinterpret_cast<const float*>(lutb + (code << 7) + boff[s]);
-            }
-            k = float_key(acc);
-        }
+        return float_key((part[0] + part[1]) + (part[2] + part[3]));
+    };
+    auto offer = [&](uint32_t k, int li, int64_t grow) {
         const bool pass = k < *(volatile uint32_t*)&s_tau;
         const unsigned bal = __ballot_sync(FULL, pass);
         if (bal) {
             const int pos = count + __popc(bal & ltm);
             if (pass) {
                 key[pos] = k;
-                seq[pos] = (uint32_t)i;
+                seq[pos] = (uint32_t)li;
                 row[pos] = (int32_t)grow;
             }
             count += __popc(bal);
             if (count > CAPW - 32) {
                 __syncwarp();
                 uint32_t kth;
-                count = warp_select(key, seq, row, count, R, &kth);
+                count = warp_select(key, seq, row, count, R, &kth, hist);
                 if (lane == 0) atomicMin(&s_tau, kth);
                 __syncwarp();
+            }
+        }
+    };
+    if (!fb && nl <= SCAN_FLAT_LISTS) {
+        // Balanced schedule: the probed lists' steps (G rows each) are
+        // numbered in probe order and warp w takes steps w, w + WARPS, ...,
+        // two at a time, so every warp gets the same number of rows to
+        // within one step whatever the list sizes.
+        for (int i = tid; i < nl; i += THREADS) {
+            const int l = probe_ids[q * np_max + i];
+            s_lstart[i] = (int)p.list_start[l];
+            s_lsw[i] = (int)p.sw_start[l];
+            const int len = p.list_len[l];
+            s_llen[i] = len;
+            s_lbase[i] = probe_d[q * np_max + i];
+            s_lsteps[i] = (len + G - 1) / G;
+        }
+        __syncthreads();
+        if (w == 0) {
+            // exclusive prefix of the step counts into s_lsteps (in place)
+            int carry = 0;
+            for (int b = 0; b < nl; b += 32) {
+                const int i = b + lane;
+                const int v = i < nl ? s_lsteps[i] : 0;
+                int incl = v;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                if (i < nl) s_lsteps[i] = carry + incl - v;
+                carry += __shfl_sync(FULL, incl, 31);
+            }
+            if (lane == 0) s_lsteps[nl] = carry;
+            if (lane == 0 && rows_scanned) {
+                unsigned long long tot = 0;
+                for (int i = 0; i < nl; i++) tot += (unsigned long long)s_llen[i];
+                scanned = tot;
+            }
+        }
+        __syncthreads();
+        const int total = s_lsteps[nl];
+        int lc = 0;  // list cursor, monotonic over the warp's units
+        auto place = [&](int u, int& li, int64_t& g, bool& v) {
+            v = false;
+            li = 0;
+            g = 0;
+            if (u >= total) return;
+            while (s_lsteps[lc + 1] <= u) lc++;
+            li = lc;
+            const int r = (u - s_lsteps[lc]) * G + lane;
+            v = act && r < s_llen[lc];
+            g = (int64_t)s_lstart[lc] + r;
+        };
+        auto fetch = [&](int u, int li, int64_t g, uint4 (&sw)[MP / 8], float& term) {
+            load_row(s_lsw[li], u - s_lsteps[li], g, sw, term);
+        };
+        // units u (A) and u + WARPS (B) are computed while u + 2 WARPS and
+        // u + 3 WARPS load
+        int la, lb;
+        int64_t ga, gb;
+        bool va, vb;
+        uint4 sa[MP / 8], sb[MP / 8];
+        float ta = 0.0f, tb = 0.0f;
+        place(w, la, ga, va);
+        if (va) fetch(w, la, ga, sa, ta);
+        place(w + WARPS, lb, gb, vb);
+        if (vb) fetch(w + WARPS, lb, gb, sb, tb);
+        for (int u = w; u < total; u += 2 * WARPS) {
+            int na, nb;
+            int64_t gna, gnb;
+            bool vna, vnb;
+            uint4 sna[MP / 8], snb[MP / 8];
+            float tna = 0.0f, tnb = 0.0f;
+            place(u + 2 * WARPS, na, gna, vna);
+            if (vna) fetch(u + 2 * WARPS, na, gna, sna, tna);
+            place(u + 3 * WARPS, nb, gnb, vnb);
+            if (vnb) fetch(u + 3 * WARPS, nb, gnb, snb, tnb);
+            const uint32_t ka = va ? lookup(sa, s_lbase[la] + ta) : KEY_INF;
+            const uint32_t kb = vb ? lookup(sb, s_lbase[lb] + tb) : KEY_INF;
+            offer(ka, la, ga);
+            if (u + WARPS < total) offer(kb, lb, gb);
+            la = na;
+            lb = nb;
+            ga = gna;
+            gb = gnb;
+            va = vna;
+            vb = vnb;
+            ta = tna;
+            tb = tnb;
+#pragma unroll
+            for (int t = 0; t < MP / 8; t++) {
+                sa[t] = sna[t];
+                sb[t] = snb[t];
+            }
+        }
+    } else {
+        // Fallback queries and very long probe lists: every WARPS-th list per
+        // warp, the next step loaded before the current is computed.
+        for (int li = w; li < nl; li += WARPS) {
+            int64_t start, sws;
+            int len;
+            float base;
+            list_meta(li, start, sws, len, base);
+            scanned += (unsigned long long)len;
+            uint4 sa[MP / 8], sb[MP / 8];
+            float ta = 0.0f, tb = 0.0f;
+            bool va = act && lane < len;
+            if (va) load_row(sws, 0, start + lane, sa, ta);
+            for (int st = 0; st * G < len; st += 2) {
+                const int r0 = st * G;
+                const bool vb = act && r0 + G + lane < len;
+                if (vb) load_row(sws, st + 1, start + r0 + G + lane, sb, tb);
+                offer(va ? lookup(sa, base + ta) : KEY_INF, li, start + r0 + lane);
+                if (r0 + G >= len) break;
+                va = act && r0 + 2 * G + lane < len;
+                if (va) load_row(sws, st + 2, start + r0 + 2 * G + lane, sa, ta);
+                offer(vb ? lookup(sb, base + tb) : KEY_INF, li, start + r0 + G + lane);
             }
         }
     }
     __syncwarp();
     {
         uint32_t kth;
-        count = warp_select(key, seq, row, count, R, &kth);
+        count = warp_select(key, seq, row, count, R, &kth, hist);
         if (lane == 0) {
             s_wcount[w] = count;
             if (rows_scanned) atomicAdd(rows_scanned, scanned);
@@ -306,7 +415,7 @@ __global__ void __launch_bounds__(THREADS) scan_skew_kernel(ScanParams p, const 
     if (w == 0) {
         uint32_t kth;
         const int Rq = p.kq ? min(R, rerank_depth_for(p.kq[q], p.mode, p.rerank_fixed)) : R;
-        const int kept = warp_select(mkey, mseq, mrow, total, Rq, &kth);
+        const int kept = warp_select(mkey, mseq, mrow, total, Rq, &kth, hist);
         for (int i = lane; i < R; i += 32) {
             const bool ok = i < kept;
             cand_row[q * R + i] = ok ? mrow[i] : -1;
@@ -316,28 +425,80 @@ __global__ void __launch_bounds__(THREADS) scan_skew_kernel(ScanParams p, const 
     }
 }
 
+// Scan words of rows: for the row at position pos of its list (group
+// pos / G, lane l = pos mod G, copy c = l / M, rotation r = l mod M), word s
+// is the table offset of subquantizer m = (s + r) mod M: (code_m * 32 + c * M
+// + m) * 4; words past M are zero. A list's words start at slot sw_start
+// (MP words per slot); group g of G rows holds MP / 8 planes of G 8-word
+// chunks: word s of lane l sits at ((g * MP / 8 + s / 8) * G + l) * 8 + s % 8.
+__device__ __forceinline__ void write_scan_words(const uint8_t* __restrict__ codes, int M, int MP, int pos,
+                                                 uint16_t* __restrict__ list_words) {
+    const int copies = 32 / M, G = 32;
+    const int g = pos / G, l = pos - g * G, c = (l / M) % copies, r = l % M;
+    for (int s = 0; s < MP; s++) {
+        uint16_t v = 0;
+        if (s < M) {
+            int m = s + r;
+            if (m >= M) m -= M;
+            v = (uint16_t)(((int)codes[m] * 32 + c * M + m) * 4);
+        }
+        list_words[((int64_t)(g * (MP / 8) + s / 8) * G + l) * 8 + (s & 7)] = v;
+    }
+}
+
+// One block per list: every slot in [start, start + len).
+__global__ void scan_words_lists_kernel(const uint8_t* __restrict__ codes, int code_stride, int M, int MP,
+                                        const int64_t* __restrict__ list_start, const int32_t* __restrict__ list_len,
+                                        const int64_t* __restrict__ sw_start, uint16_t* __restrict__ scanw) {
+    const int l = blockIdx.x;
+    const int64_t start = list_start[l];
+    const int len = list_len[l];
+    uint16_t* words = scanw + sw_start[l] * MP;
+    for (int j = threadIdx.x; j < len; j += blockDim.x) write_scan_words(codes + (start + j) * code_stride, M, MP, j, words);
+}
+
+// Rows at positions rows[i] of list cluster[i].
+__global__ void scan_words_rows_kernel(const uint8_t* __restrict__ codes, int code_stride, int M, int MP,
+                                       const int64_t* __restrict__ list_start, const int64_t* __restrict__ sw_start,
+                                       const int64_t* __restrict__ rows, const int32_t* __restrict__ cluster,
+                                       int64_t n, uint16_t* __restrict__ scanw) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t g = rows[i];
+    const int c = cluster[i];
+    write_scan_words(codes + g * code_stride, M, MP, (int)(g - list_start[c]), scanw + sw_start[c] * MP);
+}
+
 }  // namespace
 
-bool scan_skew_supported(int M) { return M % 4 == 0 && M >= 4 && M <= 32; }
+bool scan_skew_supported(int M) { return M >= 1 && M <= 32; }
+int scan_words_per_row(int M) { return (M + 7) / 8 * 8; }
+int scan_group_rows(int) { return 32; }
+
+int scan_skew_capw(int R) {
+    int c = 128;
+    while (c < 2 * R + 64) c <<= 1;
+    return c;
+}
+
+size_t scan_skew_smem(int R) {
+    return (size_t)WARPS * scan_skew_capw(R) * 12 + (size_t)WARPS * R * 12 + (size_t)WARPS * 256 * 4;
+}
 
 cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
                              const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
                              int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
                              cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
-    int CAPW = 128;
-    while (CAPW < 4 * R) CAPW <<= 1;
-    const size_t smem = (size_t)256 * 32 * sizeof(float) + (size_t)WARPS * CAPW * 12 + (size_t)WARPS * R * 12;
+    if (!scan_skew_supported(p.M) || !p.scanw) return cudaErrorInvalidValue;
+    int CAPW = scan_skew_capw(R);
+    const size_t smem = scan_skew_smem(R);
     const void* fn;
-    switch (p.M / 4) {
-    case 1: fn = (const void*)scan_skew_kernel<1>; break;
-    case 2: fn = (const void*)scan_skew_kernel<2>; break;
-    case 3: fn = (const void*)scan_skew_kernel<3>; break;
-    case 4: fn = (const void*)scan_skew_kernel<4>; break;
-    case 5: fn = (const void*)scan_skew_kernel<5>; break;
-    case 6: fn = (const void*)scan_skew_kernel<6>; break;
-    case 7: fn = (const void*)scan_skew_kernel<7>; break;
-    case 8: fn = (const void*)scan_skew_kernel<8>; break;
+    switch (scan_words_per_row(p.M) / 8) {
+    case 1: fn = (const void*)scan_skew_kernel<8>; break;
+    case 2: fn = (const void*)scan_skew_kernel<16>; break;
+    case 3: fn = (const void*)scan_skew_kernel<24>; break;
+    case 4: fn = (const void*)scan_skew_kernel<32>; break;
     default: return cudaErrorInvalidValue;
     }
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -347,6 +508,24 @@ cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t 
                     (void*)&rows_scanned};
     e = cudaLaunchKernel(fn, dim3((unsigned)nq), dim3(THREADS), args, smem, s);
     if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_words_lists(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+                                    const int32_t* list_len, const int64_t* sw_start, int nlist, uint16_t* scanw,
+                                    cudaStream_t s) {
+    if (nlist <= 0 || !scan_skew_supported(M)) return cudaSuccess;
+    scan_words_lists_kernel<<<(unsigned)nlist, 128, 0, s>>>(codes, code_stride, M, scan_words_per_row(M),
+                                                            list_start, list_len, sw_start, scanw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan_words_rows(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+                                   const int64_t* sw_start, const int64_t* rows, const int32_t* cluster, int64_t n,
+                                   uint16_t* scanw, cudaStream_t s) {
+    if (n <= 0 || !scan_skew_supported(M)) return cudaSuccess;
+    scan_words_rows_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(codes, code_stride, M, scan_words_per_row(M),
+                                                                      list_start, sw_start, rows, cluster, n, scanw);
     return cudaGetLastError();
 }
 

@@ -437,13 +437,9 @@ cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, c
                         int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
                         cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
-    if (scan_skew_supported(p.M)) {
-        int capw = 128;
-        while (capw < 4 * R) capw <<= 1;
-        if ((size_t)256 * 32 * 4 + (size_t)SC_WARPS * capw * 12 + (size_t)SC_WARPS * R * 12 <= 200 * 1024)
-            return launch_scan_skew(p, queries, nq, probe_ids, probe_d, nprobe, np_max, fallback, R, cand_row,
-                                    cand_d, cand_seq, rows_scanned, s);
-    }
+    if (scan_skew_supported(p.M) && p.scanw && scan_skew_smem(R) + 32 * 1024 <= 200 * 1024)
+        return launch_scan_skew(p, queries, nq, probe_ids, probe_d, nprobe, np_max, fallback, R, cand_row, cand_d,
+                                cand_seq, rows_scanned, s);
     const int CAPW = cap_for(R);
     int P = 1;
     while (P < SC_WARPS * R) P <<= 1;
