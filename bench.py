@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--knn-nq", type=int, default=10_000)
     ap.add_argument("--knn-steps", type=int, default=3)
     ap.add_argument("--knn-only", action="store_true", help="run only the k-NN section and print its line")
+    ap.add_argument("--train-bench", type=int, default=1,
+                    help="run the training section (1M x 128, coarse 4096, 16 x 256 PQ, 25 iterations)")
+    ap.add_argument("--train-only", action="store_true", help="run only the training section")
     ap.add_argument("--knn-variants", type=str,
                     default="squared_euclidean/tensor,cosine/tensor,manhattan/exact,squared_euclidean/exact,"
                             "cosine/exact")
@@ -289,6 +292,9 @@ def main():
     if args.knn_only:
         print(json.dumps({"knn": knn_section(args, torch, dev)}), flush=True)
         return 0
+    if args.train_only:
+        print(json.dumps({"train": train_section(args, torch, dev)}), flush=True)
+        return 0
     x, q = make_data(args, torch, dev)
     idx, xh, train_s = build_index(args, x, torch)
     q_host = q.cpu().numpy()
@@ -407,6 +413,23 @@ def main():
     h2d = nq * args.dim * 4 + nq * 4 * 2
     d2h = nq * args.k * (8 + 8) + nq * 4
 
+    # the plain FP32 GPU path: the same search with every coarse distance on
+    # the FP32 SIMT kernels (no tensor-core preselection); same results
+    idx.SetPlainFP32(True)
+    for _ in range(max(1, args.warmup // 2)):
+        step()
+    torch.cuda.synchronize()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(args.steps):
+        step()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_fp32_qps = nq * args.steps / (p0.elapsed_time(p1) / 1000.0)
+    plain_same = bool(np.array_equal(ids_d.cpu().numpy(), ids_t))
+    idx.SetPlainFP32(False)
+
     # one-query-per-call path (plain, one launch sequence per query)
     nplain = 200
     t0 = time.perf_counter()
@@ -442,6 +465,14 @@ def main():
                 log("served stream failed:", e)
                 served.append({"offered_requests_per_s": rate, "error": str(e)})
 
+    train = None
+    if args.train_bench and rank == 0:
+        try:
+            train = train_section(args, torch, dev)
+        except Exception as e:  # pragma: no cover
+            log("train section failed:", e)
+            train = {"error": str(e)}
+
     knn = None
     if args.knn and rank == 0:
         try:
@@ -468,6 +499,7 @@ def main():
             "stage_ms_per_step": [round(v / args.steps, 4) for v in stage_ms],
             "train_s": round(train_s, 2),
             "plain_one_query_per_call_qps": plain_qps,
+            "plain_fp32_gpu_qps": plain_fp32_qps, "plain_fp32_same_ids": plain_same,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "kernel": "scan_skew_kernel",
                          "bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
@@ -477,6 +509,7 @@ def main():
             "clocks": clocks,
             "served_stream": served,
             "knn": knn,
+            "train": train,
         }
         if served and "p50_ms" in served[0]:
             line["p50_ms"] = served[0]["p50_ms"]
@@ -488,6 +521,54 @@ def main():
 
         dist.destroy_process_group()
     return 0
+
+
+def train_section(args, torch, dev):
+    """PQIVF training at scale: 1,000,000 x 128 float32 from a Gaussian
+    mixture of 2,000 anisotropic clusters (per-cluster diagonal scales
+    log-uniform in [0.05, 1]); coarse 4,096, 16 x 256 PQ (8 dims each), 25
+    k-means iterations. Trains twice -- tensor-core assignment with exact
+    boundary rescoring, and the plain FP32 SIMT assignment -- and reports
+    wall time, time per iteration and the coarse inertia evaluated in FP64.
+    Both must give the same index."""
+    import hann_gb300 as hg
+
+    n, dim, k, iters = 1_000_000, 128, 4096, 25
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 11)
+    centers = torch.randn(2000, dim, device=dev, generator=g) * 2.0
+    scales = torch.exp(torch.rand(2000, dim, device=dev, generator=g) * (np.log(1.0) - np.log(0.05))
+                       + np.log(0.05))
+    lab = torch.randint(0, 2000, (n,), device=dev, generator=g)
+    x = centers[lab] + torch.randn(n, dim, device=dev, generator=g) * scales[lab]
+    xh = x.cpu().numpy()
+    ids = np.arange(n, dtype=np.int64)
+    out = {"workload": f"{n} x {dim} anisotropic Gaussian mixture (2000 clusters), coarse {k}, 16 x 256 PQ, "
+                       f"{iters} k-means iterations"}
+    states = {}
+    for name, plain in (("tensor_core", False), ("plain_fp32", True)):
+        idx = hg.New(dim, hg.WithCoarseK(k), hg.WithNumSubquantizers(16), hg.WithPQK(256),
+                     hg.WithKMeansIters(iters), hg.WithPlainFP32(plain))
+        idx.BulkAddArrays(ids, xh)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        idx.Train()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t
+        st = idx.export_state()
+        cent = torch.from_numpy(st["coarse"]).to(dev).double()
+        lab_of = torch.from_numpy(np.repeat(np.arange(k), st["list_len"])).to(dev)
+        rows = torch.from_numpy(st["ids"]).to(dev)
+        d = x[rows].double() - cent[lab_of]
+        inertia = float((d * d).sum().item())
+        out[name] = {"train_s": round(el, 3), "s_per_iteration": round(el / iters, 4), "inertia_fp64": inertia}
+        states[name] = st
+        log("train", name, out[name])
+        idx.close()
+    a, b = states["tensor_core"], states["plain_fp32"]
+    out["identical_index"] = bool(all(np.array_equal(a[key], b[key]) for key in ("coarse", "list_len", "ids",
+                                                                                "codes")))
+    return out
 
 
 def knn_histogram_data(torch, dev, n, dim, seed):

@@ -66,7 +66,7 @@ class _Options(ctypes.Structure):
                 ("num_subquantizers", ctypes.c_int32), ("pq_k", ctypes.c_int32),
                 ("kmeans_iters", ctypes.c_int32), ("candidate_clusters", ctypes.c_int32),
                 ("fallback", ctypes.c_int32), ("seed", ctypes.c_uint64), ("device", ctypes.c_int32),
-                ("rerank", ctypes.c_int32)]
+                ("rerank", ctypes.c_int32), ("plain_fp32", ctypes.c_int32)]
 
 
 class _Stats(ctypes.Structure):
@@ -96,7 +96,7 @@ EXPORTED = (
     "hann_pqivf_export", "hann_pqivf_import", "hann_gpu_distance_batch", "hann_pqivf_set_profiling",
     "hann_pqivf_stage_times", "hann_pqivf_list_lengths", "hann_pqivf_search_batch_device_noalloc",
     "hann_gpu_distance_matrix", "hann_knn_new", "hann_knn_free", "hann_knn_last_error", "hann_knn_search",
-    "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn",
+    "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn", "hann_pqivf_set_plain_fp32",
 )
 
 
@@ -137,6 +137,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_import.argtypes = [_P, ctypes.POINTER(_Layout)] + [_P] * 11
         L.hann_gpu_distance_batch.argtypes = [ctypes.c_int32, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
         L.hann_pqivf_list_lengths.argtypes = [_P, _P]
         L.hann_gpu_distance_matrix.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64,
@@ -188,6 +189,12 @@ def WithCandidateClusters(n: int):
 
 def WithBruteForceFallback(allow: bool):
     return lambda o: setattr(o, "fallback", 1 if allow else 0)
+
+
+def WithPlainFP32(on: bool = True):
+    """Every assignment and probe on the FP32 SIMT kernels (no tensor-core
+    preselection); the results are the same."""
+    return lambda o: setattr(o, "plain_fp32", 1 if on else 0)
 
 
 def WithSeed(seed: int):
@@ -384,6 +391,10 @@ class Index:
         self._check(self._L.hann_pqivf_search_batch_device(
             self._h, ctypes.c_void_p(d_queries), int(nq), int(k), int(nprobe), int(mode), ctypes.c_void_p(d_ids),
             ctypes.c_void_p(d_dist), ctypes.c_void_p(d_nout), ctypes.c_void_p(stream)))
+
+    def SetPlainFP32(self, on: bool) -> None:
+        """Switch the FP32 SIMT-only mode (same results, no tensor cores)."""
+        self._check(self._L.hann_pqivf_set_plain_fp32(self._h, 1 if on else 0))
 
     def SetProfiling(self, on: bool) -> None:
         self._check(self._L.hann_pqivf_set_profiling(self._h, 1 if on else 0))

@@ -123,7 +123,7 @@ static int upload_lens(hann_pqivf* h) {
 // BF16 centroids, their FP32 squared norms and the largest norm, for the
 // tensor-core preselection (dimensions up to 128).
 static int prepare_coarse(hann_pqivf* h) {
-    h->tc = h->o.dimension <= 128 && h->nlist > 0;
+    h->tc = !h->o.plain_fp32 && h->o.dimension <= 128 && h->nlist > 0;
     if (!h->tc) return HANN_OK;
     h->kp = gemm_kpad(h->o.dimension);
     CK(h->d_coarse_bf16.reserve((size_t)h->nlist * h->kp));
@@ -151,7 +151,7 @@ static int assign_rows(hann_pqivf* h, AssignScratch& sc, const float* x, int64_t
                        int k, int32_t* out_idx) {
     cudaStream_t s = h->stream;
     if (n <= 0) return HANN_OK;
-    if (dim > 128) {
+    if (dim > 128 || h->o.plain_fp32) {
         DBuf<unsigned long long> keys;
         CK(keys.reserve((size_t)n));
         CK(launch_assign_exact(x, n, dim, cent, k, out_idx, nullptr, keys.p, s));
@@ -1105,6 +1105,15 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
     CK(sc.fbcount.reserve(1));
     CK(cudaStreamSynchronize(s));
     return run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
+}
+
+int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on) {
+    if (!h) return HANN_E_INVALID;
+    std::unique_lock<std::mutex> w(h->wmu);
+    std::unique_lock<std::shared_mutex> g(h->mu);
+    h->o.plain_fp32 = on ? 1 : 0;
+    if (!h->trained) return HANN_OK;
+    return prepare_coarse(h);
 }
 
 int hann_pqivf_set_profiling(hann_pqivf* h, int32_t on) {

@@ -51,6 +51,8 @@ typedef struct {
     uint64_t seed;              /* plays HANN_SEED's role (core/utils.go:12-20) */
     int32_t device;             /* CUDA device ordinal */
     int32_t rerank;             /* candidates rescored exactly per query; 0 = automatic */
+    int32_t plain_fp32;         /* 1: no tensor-core preselection; every assignment and probe runs the
+                                   FP32 SIMT kernels (same results, for comparison); 0 = default */
 } hann_pqivf_options;
 
 /* Defaults of pqivf.New for the given dimension (pqivf/index.go:106-157). */
@@ -121,6 +123,10 @@ int hann_pqivf_search_batch(hann_pqivf* h, const float* queries, int64_t nq, con
 int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k, int32_t nprobe,
                                    int32_t mode, int64_t* d_ids, double* d_distances, int32_t* d_n_out,
                                    void* stream);
+
+/* Switches the plain-FP32 mode of hann_pqivf_options at run time (no
+ * reference counterpart; results do not change). */
+int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on);
 
 /* Diagnostics (no reference counterpart). With profiling on, every search
  * stage is bracketed by CUDA events on the stream it runs on and the list

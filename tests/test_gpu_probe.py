@@ -52,3 +52,30 @@ def test_screened_probe_tied_centroids(built, gpu):
     q[:40] = st["coarse"][100]
     compare(idx, q, 10, 50)
     compare(idx, q, 5, 3000)
+
+
+def test_plain_fp32_mode_gives_identical_index_and_results(built, gpu):
+    """The SIMT-only mode trains the same index and answers the same."""
+    import hann_gb300 as hg
+    rng = np.random.default_rng(31)
+    x, _ = gaussian_mixture(rng, 12000, 48, 300, 0.4)
+    q, _ = gaussian_mixture(np.random.default_rng(32), 100, 48, 300, 0.4)
+    a = hg.New(48, hg.WithCoarseK(2048), hg.WithNumSubquantizers(8), hg.WithPQK(16), hg.WithKMeansIters(3))
+    b = hg.New(48, hg.WithCoarseK(2048), hg.WithNumSubquantizers(8), hg.WithPQK(16), hg.WithKMeansIters(3),
+               hg.WithPlainFP32(True))
+    for idx in (a, b):
+        idx.BulkAddArrays(np.arange(len(x), dtype=np.int64), x)
+        idx.Train()
+    sa, sb = a.export_state(), b.export_state()
+    for key in ("coarse", "codebooks", "list_len", "ids", "codes"):
+        np.testing.assert_array_equal(sa[key], sb[key], err_msg=key)
+    for mode in (0, 1):
+        ra = a.SearchBatch(q, 10, nprobe=40, mode=mode)
+        rb = b.SearchBatch(q, 10, nprobe=40, mode=mode)
+        for u, v in zip(ra, rb):
+            np.testing.assert_array_equal(u, v)
+    a.SetPlainFP32(True)
+    rc = a.SearchBatch(q, 10, nprobe=40, mode=1)
+    rb = b.SearchBatch(q, 10, nprobe=40, mode=1)
+    for u, v in zip(rc, rb):
+        np.testing.assert_array_equal(u, v)
