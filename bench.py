@@ -501,7 +501,7 @@ def main():
             "plain_one_query_per_call_qps": plain_qps,
             "plain_fp32_gpu_qps": plain_fp32_qps, "plain_fp32_same_ids": plain_same,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": "scan_skew_kernel",
+                         "frac": achieved / peak, "traffic": scan_traffic(args), "kernel": "scan_skew_kernel",
                          "bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
             "cpu_baseline": cb,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -676,6 +676,19 @@ def knn_section(args, torch, dev):
         out["cpu_port_sample"] = f"{sample} queries x {n} rows, squared Euclidean, {os.cpu_count()} threads"
     idx.close()
     return out
+
+
+def scan_traffic(args):
+    """DRAM bytes (read + write) of one scan launch on this workload, from the
+    1-pass ncu capture kept in profiles/ (ncu cannot run inside the bench)."""
+    path = os.path.join(HERE, "profiles", "scan_skew_kernel_10Mx96_dram.json")
+    if not os.path.exists(path) or (args.n, args.dim, args.nlist, args.nq) != (10_000_000, 96, 16384, 10_000):
+        return None
+    try:
+        rec = json.load(open(path))
+        return float(rec["dram_bytes_read_per_launch"]) + float(rec["dram_bytes_write_per_launch"])
+    except Exception:
+        return None
 
 
 def serve_stream(args, idx, q_host, gt, nr, rate):

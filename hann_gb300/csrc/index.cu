@@ -592,7 +592,7 @@ int rerank_depth(const hann_pqivf* h, int kmax, int mode) { return rerank_depth_
 // in device arrays d_k/d_np. Outputs to device buffers.
 constexpr int SCREEN_MIN_LISTS = 2048;  // below this the full score matrix is cheaper
 constexpr int PROBE_CAP = 4096;         // screened-probe candidates per query and chunk
-constexpr int PROBE_FIRST = 1024;       // first centroid chunk (every list enters the band)
+constexpr int PROBE_FIRST = 256;        // first centroid chunk at least (every list enters the band)
 
 int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k,
                       const int32_t* d_np, int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist,
@@ -626,11 +626,12 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
         else h->ev[stage].back().second = e;
         return cudaEventRecord(e, s);
     };
-    // Screened probe: the BF16 GEMM walks the centroids in chunks growing
-    // fourfold and keeps per query only the lists whose screened score can
-    // still reach its np-th (the band merge of the batched k-NN,
-    // kernels_knn.cu); probe_final rescores the band exactly. Same lists and
-    // distances as probe_select_band on the full score matrix.
+    // Screened probe: the BF16 GEMM walks the centroids in chunks, each
+    // making the walked prefix eight times longer, and keeps per query only
+    // the lists whose screened score can still reach its np-th (the band
+    // merge of the batched k-NN, kernels_knn.cu); probe_final rescores the
+    // band exactly. Same lists and distances as probe_select_band on the
+    // full score matrix.
     const bool screened = h->tc && h->nlist >= SCREEN_MIN_LISTS;
     const int lcap = std::max(1024, 2 * np_max);
     if (screened) {
@@ -643,6 +644,8 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
         CK(sc.pcand_id.reserve((size_t)chunk * PROBE_CAP));
         CK(sc.pcand_s.reserve((size_t)chunk * PROBE_CAP));
         CK(sc.pband.reserve((size_t)chunk * lcap));
+        CK(sc.qorder.reserve((size_t)chunk));
+        CK(sc.order_scratch.reserve((size_t)h->nlist));
     }
     for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
         const int64_t nc = std::min(chunk, nq - q0);
@@ -657,7 +660,9 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
             CK(cudaMemsetAsync(sc.pneed.p, 0, sizeof(int32_t) * nc, s));
             CK(launch_fill_f32(sc.pthr.p, nc, INFINITY, s));
             int launches = 3;
-            for (int b = 0, w = std::min(h->nlist, PROBE_FIRST); b < h->nlist; w = 3 * b) {
+            const int first = std::min(h->nlist,
+                                       std::min(PROBE_CAP, std::max(PROBE_FIRST, (int)round_up(2 * (int64_t)np_max, 256))));
+            for (int b = 0, w = first; b < h->nlist; w = 7 * b) {
                 const int e = std::min(h->nlist, b + w);
                 CK(launch_gemm_filter(sc.qbf.p, nc, h->d_coarse_bf16.p, h->nlist, h->kp, b, e,
                                       h->d_coarse_terms.p, sc.pthr.p, PROBE_CAP, sc.pcnt.p, sc.pcand_id.p,
@@ -673,17 +678,20 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
             CK(launch_probe_final(qp, nc, h->o.dimension, h->d_coarse.p, h->nlist, d_np + q0, np_max, d_k + q0,
                                   h->d_live.p, h->o.fallback ? 1 : 0, lcap, sc.pband.p, sc.plcount.p, sc.pneed.p,
                                   sc.D.p, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, sc.fbcount.p, s));
+            CK(launch_probe_order(sc.probe_ids.p, nc, np_max, h->nlist, sc.order_scratch.p, sc.qorder.p, s));
             CK(mark(1, false));
             CK(mark(2, true));
             p.kq = d_k + q0;
+            p.qorder = sc.qorder.p;
             CK(launch_scan(p, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R,
                            sc.cand_row.p, sc.cand_d.p, sc.cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
             CK(mark(2, false));
             CK(mark(3, true));
             CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
                              d_dist + q0 * kmax, d_nout + q0, s));
+            p.qorder = nullptr;
             CK(mark(3, false));
-            h->launches += launches + 3;
+            h->launches += launches + 6;
             continue;
         }
         CK(mark(0, true));

@@ -147,6 +147,7 @@ struct SearchScratch {
     DBuf<float> pe2, pasl, pthr, pcand_s;
     DBuf<int32_t> pcnt, pcand_id, plcount, pneed;
     DBuf<unsigned long long> pband;
+    DBuf<int32_t> qorder, order_scratch;  // L2-friendly query order for scan and rerank
 };
 
 struct hann_pqivf {
@@ -239,6 +240,7 @@ struct hann_pqivf {
         p.list_len = d_len.p;
         p.codes = d_codes.p;
         p.scanw = scan_skew_supported(o.num_subquantizers) ? d_scanw.p : nullptr;
+        p.qorder = nullptr;
         p.sw_start = d_swstart.p;
         p.term = d_term.p;
         p.row_cluster = d_row_cluster.p;

@@ -146,6 +146,7 @@ struct ScanParams {
     const float* vectors;     // [rows][dim]
     const int64_t* row_id;    // [rows]
     const int32_t* kq;        // [nq] per-query k (sets each query's rerank depth)
+    const int32_t* qorder;    // optional: block b works on query qorder[b] (L2-friendly order)
     int mode, rerank_fixed;
 };
 
@@ -195,6 +196,12 @@ cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t 
 cudaError_t launch_rerank(const ScanParams& p, const float* queries, int64_t nq, const int32_t* cand_row,
                           const uint32_t* cand_seq, int R, const int32_t* k, int kmax, int mode,
                           int64_t* ids, double* dist, int32_t* nout, cudaStream_t s);
+
+// Query order for the scan and rerank: queries grouped by their first
+// probed list (a counting sort), so blocks that run at the same time read
+// overlapping lists and more of the list reads hit L2. scratch: nlist ints.
+cudaError_t launch_probe_order(const int32_t* probe_ids, int64_t nq, int np_max, int nlist, int32_t* scratch,
+                               int32_t* order, cudaStream_t s);
 
 // Moves every list's slots to a new layout (one block per list), dropping
 // tombstones (row id -1) in the lists flagged compact.

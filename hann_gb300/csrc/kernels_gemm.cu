@@ -444,9 +444,8 @@ cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat
     const int ntiles = (int)ceil_div(ncols - col_begin, BN);
     int splits = 1;
     if (MODE == 0) splits = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, ceil_div(4 * 152, mtiles)));
-    // filter mode: about eight waves, each CTA at least eight tiles
-    if (MODE == 2)
-        splits = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ntiles, 8), ceil_div(8 * 152, mtiles)));
+    // filter mode: about eight waves of CTAs, as many as the column tiles allow
+    if (MODE == 2) splits = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, ceil_div(8 * 152, mtiles)));
     const int per = (int)ceil_div(ntiles, splits);
     splits = (int)ceil_div(ntiles, per);
     dist_gemm_kernel<MODE><<<dim3((unsigned)mtiles, (unsigned)splits), THREADS, SMEM_BYTES, s>>>(

@@ -79,16 +79,10 @@ __global__ void __launch_bounds__(KF_THREADS) knn_filter_kernel(
     const int tid = threadIdx.x;
     const int tp = tid & 31, tc = tid >> 5;
     const int r0 = blockIdx.x * KF_TP;
-    for (int e = tid; e < KF_TP * dim; e += KF_THREADS) {
-        const int p = e / dim, i = e - p * dim;
-        const int r = r0 + p;
-        float v = 0.0f;
-        if (r < nrows) {
-            const int64_t qi = qlist ? qlist[r] : r;
-            v = queries[qi * dim + i];
-        }
-        Xs[i * KF_TP + p] = v;
-    }
+    stage_tile<KF_TP, KF_THREADS>(Xs, dim, min(KF_TP, nrows - r0), [&](int p) {
+        const int64_t qi = qlist ? qlist[r0 + p] : r0 + p;
+        return queries + qi * dim;
+    });
     unsigned long long t_row[4];
     float qn[4];
     int64_t qrow[4];
@@ -109,10 +103,8 @@ __global__ void __launch_bounds__(KF_THREADS) knn_filter_kernel(
     const int64_t cb1 = min(c_end, cb0 + (int64_t)tiles_per_split * KF_TC);
     for (int64_t c0 = cb0; c0 < cb1; c0 += KF_TC) {
         __syncthreads();
-        for (int e = tid; e < KF_TC * dim; e += KF_THREADS) {
-            const int c = e / dim, i = e - c * dim;
-            Cs[i * KF_TC + c] = (c0 + c < cb1) ? base[(c0 + c) * dim + i] : 0.0f;
-        }
+        stage_tile<KF_TC, KF_THREADS>(Cs, dim, (int)min((int64_t)KF_TC, cb1 - c0),
+                                      [&](int c) { return base + (c0 + c) * dim; });
         __syncthreads();
         float dd[4][4];
         tile_pairs<OP, KF_TP, KF_TC>(Xs, Cs, tp, tc, dim, dd);

@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
     const int copies = 32 / M;
     const int G = 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int64_t q = blockIdx.x;
+    const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const float* qv = Q + q * p.dim;
     if (tid == 0) s_tau = KEY_INF;
     for (int e = tid; e < 256 * 32; e += THREADS) {
@@ -469,7 +469,56 @@ __global__ void scan_words_rows_kernel(const uint8_t* __restrict__ codes, int co
     write_scan_words(codes + g * code_stride, M, MP, (int)(g - list_start[c]), scanw + sw_start[c] * MP);
 }
 
+__global__ void order_count_kernel(const int32_t* __restrict__ probe_ids, int64_t nq, int np_max,
+                                   int32_t* __restrict__ cnt) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nq) atomicAdd(&cnt[probe_ids[q * np_max]], 1);
+}
+
+// Exclusive prefix of cnt[0..n) in place, one block.
+__global__ void order_scan_kernel(int32_t* __restrict__ cnt, int n) {
+    __shared__ int32_t part[1024];
+    const int t = threadIdx.x;
+    const int per = (n + 1023) / 1024;
+    int sum = 0;
+    for (int i = t * per; i < min(n, (t + 1) * per); i++) sum += cnt[i];
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int v = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - sum;
+    for (int i = t * per; i < min(n, (t + 1) * per); i++) {
+        const int c = cnt[i];
+        cnt[i] = run;
+        run += c;
+    }
+}
+
+// Each query takes the next slot of its first list's range. The order
+// within a list is whatever the atomics give; a query's result does not
+// depend on which block runs it.
+__global__ void order_scatter_kernel(const int32_t* __restrict__ probe_ids, int64_t nq, int np_max,
+                                     int32_t* __restrict__ cursor, int32_t* __restrict__ order) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nq) order[atomicAdd(&cursor[probe_ids[q * np_max]], 1)] = (int32_t)q;
+}
+
 }  // namespace
+
+cudaError_t launch_probe_order(const int32_t* probe_ids, int64_t nq, int np_max, int nlist, int32_t* scratch,
+                               int32_t* order, cudaStream_t s) {
+    if (nq <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(int32_t) * (size_t)nlist, s);
+    if (e != cudaSuccess) return e;
+    order_count_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(probe_ids, nq, np_max, scratch);
+    order_scan_kernel<<<1, 1024, 0, s>>>(scratch, nlist);
+    order_scatter_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(probe_ids, nq, np_max, scratch, order);
+    return cudaGetLastError();
+}
 
 bool scan_skew_supported(int M) { return M >= 1 && M <= 32; }
 int scan_words_per_row(int M) { return (M + 7) / 8 * 8; }

@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(ScanParams p, const fl
     __shared__ uint32_t s_tau;
     __shared__ int s_wcount[SC_WARPS];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int64_t q = blockIdx.x;
+    const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const float* qv = Q + q * p.dim;
     if (tid == 0) s_tau = float_key(F_INF);
     for (int e = tid; e < p.M * 256; e += SC_THREADS) {
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(RR_THREADS) rerank_kernel(ScanParams p, const 
     uint32_t* cs = reinterpret_cast<uint32_t*>(cd + RP);
     int32_t* cr = reinterpret_cast<int32_t*>(cs + RP);
     __shared__ int s_valid;
-    const int64_t q = blockIdx.x;
+    const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const int tid = threadIdx.x;
     if (tid == 0) s_valid = 0;
     for (int e = tid; e < p.dim; e += RR_THREADS) qv[e] = Q[q * p.dim + e];

@@ -43,11 +43,8 @@ __global__ void __launch_bounds__(TD_THREADS) tile_dist_kernel(const float* __re
     const int tid = threadIdx.x;
     const int tp = tid & 31, tc = tid >> 5;
     const int64_t p0 = (int64_t)blockIdx.x * TD_TP;
-    for (int e = tid; e < TD_TP * dim; e += TD_THREADS) {
-        const int p = e / dim, i = e - p * dim;
-        const int64_t gp = p0 + p;
-        Xs[i * TD_TP + p] = gp < n ? x[gp * dim + i] : 0.0f;
-    }
+    stage_tile<TD_TP, TD_THREADS>(Xs, dim, (int)min((int64_t)TD_TP, n - p0),
+                                  [&](int r) { return x + (p0 + r) * dim; });
     float best_d[4];
     int best_i[4];
 #pragma unroll
@@ -59,10 +56,8 @@ __global__ void __launch_bounds__(TD_THREADS) tile_dist_kernel(const float* __re
     const int c_end = min(k, c_begin + tiles_per_split * TD_TC);
     for (int c0 = c_begin; c0 < c_end; c0 += TD_TC) {
         __syncthreads();
-        for (int e = tid; e < TD_TC * dim; e += TD_THREADS) {
-            const int c = e / dim, i = e - c * dim;
-            Cs[i * TD_TC + c] = (c0 + c < k) ? cent[(int64_t)(c0 + c) * dim + i] : 0.0f;
-        }
+        stage_tile<TD_TC, TD_THREADS>(Cs, dim, min(TD_TC, k - c0),
+                                      [&](int r) { return cent + (int64_t)(c0 + r) * dim; });
         __syncthreads();
         float dd[4][4];
         tile_pairs<OP_SQDIFF, TD_TP, TD_TC>(Xs, Cs, tp, tc, dim, dd);

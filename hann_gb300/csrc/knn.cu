@@ -21,7 +21,7 @@ namespace {
 constexpr int KNN_QB = 8192;       // queries per block of work
 constexpr int KNN_CAP = 8192;      // candidate buffer per query and chunk
 constexpr int KNN_KMAX = 4096;     // largest k
-constexpr int64_t KNN_GROW = 4;    // chunk growth factor
+constexpr int64_t KNN_GROW = 8;    // chunk growth factor
 
 __global__ void knn_init_rows_kernel(const int32_t* __restrict__ qlist, int nsel, int32_t* __restrict__ lcount,
                                      unsigned long long* __restrict__ thr, int32_t* __restrict__ cnt) {
@@ -89,10 +89,13 @@ struct hann_knn {
 
 namespace {
 
-// Chunk boundaries of the base walk: [0, min(n, CAP)), then growing by KNN_GROW.
-std::vector<int64_t> chunk_bounds(int64_t n) {
+// Chunk boundaries of the base walk: a first chunk of `first` rows (at most
+// CAP: every row of it enters the candidate buffer), then chunks that make
+// the walked prefix grow KNN_GROW-fold, so about k * (KNN_GROW - 1) rows per
+// query pass each later chunk.
+std::vector<int64_t> chunk_bounds(int64_t n, int k) {
     std::vector<int64_t> b{0};
-    int64_t c = std::min<int64_t>(n, KNN_CAP);
+    int64_t c = std::min<int64_t>(n, std::min<int64_t>(KNN_CAP, std::max<int64_t>(1024, round_up(8 * (int64_t)k, 256))));
     while (b.back() < n) {
         b.push_back(std::min<int64_t>(n, b.back() + c));
         c = b.back() * (KNN_GROW - 1);
@@ -154,7 +157,7 @@ int reserve_block(hann_knn* h, int64_t qb, int k, int nchunks) {
 int knn_exact(hann_knn* h, int metric, const float* q, int nrows, const int32_t* qlist, int nsel, int k,
               int64_t* ids, double* dist, cudaStream_t s) {
     if (nsel <= 0) return HANN_OK;
-    const std::vector<int64_t> cb = chunk_bounds(h->n);
+    const std::vector<int64_t> cb = chunk_bounds(h->n, k);
     const int nch = (int)cb.size() - 1;
     if (metric == HANN_METRIC_COSINE) {
         int rc = prepare_bnorm(h, s);
@@ -225,7 +228,7 @@ int knn_screen(hann_knn* h, int metric, const float* q, int nrows, int k, int64_
     CK(cudaMemsetAsync(h->counters.p, 0, 2 * sizeof(int), s));
     knn_fill_f32_kernel<<<(unsigned)ceil_div(nrows, 256), 256, 0, s>>>(h->thr_f.p, nrows, INFINITY);
     CK(cudaGetLastError());
-    const std::vector<int64_t> cb = chunk_bounds(h->n);
+    const std::vector<int64_t> cb = chunk_bounds(h->n, k);
     const int nch = (int)cb.size() - 1;
     for (int c = 0; c < nch; c++) {
         CK(launch_gemm_filter(h->q_bf.p, nrows, h->base_bf.p, h->n, h->kp, (int)cb[c], (int)cb[c + 1],
@@ -271,7 +274,7 @@ int knn_run(hann_knn* h, int metric, const float* q, int64_t nq, int k, int meth
         CK(cudaStreamSynchronize(s));
         return HANN_OK;
     }
-    const int nch = (int)chunk_bounds(h->n).size() - 1;
+    const int nch = (int)chunk_bounds(h->n, k).size() - 1;
     for (int64_t q0 = 0; q0 < nq; q0 += KNN_QB) {
         const int nr = (int)std::min<int64_t>(KNN_QB, nq - q0);
         int rc = reserve_block(h, nr, k, nch);

@@ -138,4 +138,31 @@ __device__ __forceinline__ void tile_pairs(const float* __restrict__ Xs, const f
     }
 }
 
+// Stage rows [0, valid) of a row-major matrix (leading dimension dim) into
+// an element-major tile T[i * TR + r] (TR rows wide), zero past `valid`
+// (valid >= 1). Consecutive threads take consecutive rows, so the
+// shared-memory stores are conflict-free; when dim is a multiple of 4 and
+// the rows are 16-byte aligned each thread moves a float4. src(r) gives the
+// global row pointer of tile row r (all rows share one base).
+template <int TR, int THREADS, typename RowPtr>
+__device__ __forceinline__ void stage_tile(float* __restrict__ T, int dim, int valid, RowPtr src) {
+    if ((dim & 3) == 0 && (reinterpret_cast<uintptr_t>(src(0)) & 15) == 0) {
+        const int d4 = dim >> 2;
+        for (int e = threadIdx.x; e < TR * d4; e += THREADS) {
+            const int r = e % TR, i4 = e / TR;
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (r < valid) v = *reinterpret_cast<const float4*>(src(r) + 4 * i4);
+            T[(4 * i4 + 0) * TR + r] = v.x;
+            T[(4 * i4 + 1) * TR + r] = v.y;
+            T[(4 * i4 + 2) * TR + r] = v.z;
+            T[(4 * i4 + 3) * TR + r] = v.w;
+        }
+    } else {
+        for (int e = threadIdx.x; e < TR * dim; e += THREADS) {
+            const int r = e % TR, i = e / TR;
+            T[i * TR + r] = r < valid ? src(r)[i] : 0.0f;
+        }
+    }
+}
+
 }  // namespace hann
