@@ -38,14 +38,24 @@ constexpr int BN = 256;       // columns per tile (MMA N)
 constexpr int BKE = 64;       // bf16 elements per 128-byte swizzle row
 constexpr int KB_MAX = 2;     // K <= 128
 constexpr int STAGES = 2;
-constexpr int THREADS = 192;
+// Warp 0 loads, warp 1 issues the MMAs, then EW epilogue warps per quarter
+// of the accumulator's 128 lanes: one for the top-8 mode (a row's running
+// list stays in one thread), two for the score and filter modes, each
+// taking half of a tile's columns, so two warps per SM sub-partition hide
+// each other's load latency.
+template <int MODE>
+struct Epi {
+    static constexpr int EW = MODE == 1 ? 1 : 2;
+    static constexpr int THREADS = 64 + 128 * EW;
+    static constexpr int CW = 256 / EW;  // columns per epilogue warp
+};
 constexpr int TOPC = 8;       // argmin mode: candidates kept per row
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
 
 constexpr int A_BYTES = KB_MAX * BM * 128;           // 32 KiB
 constexpr int B_STAGE_BYTES = KB_MAX * BN * 128;     // 64 KiB
-constexpr int TR_BYTES = 4 * 32 * 33 * 4;               // epilogue transpose tiles
-constexpr int CT_BYTES = 4 * 2 * BN * 8;                // per-warp column terms, two tiles
+constexpr int TR_BYTES = 8 * 32 * 33 * 4;               // epilogue transpose tiles (up to 8 warps)
+constexpr int CT_BYTES = 4 * 2 * BN * 8;                // column terms of two tiles, split over the warps
 constexpr int SMEM_BYTES = 1024 + A_BYTES + STAGES * B_STAGE_BYTES + 256 + TR_BYTES + CT_BYTES;
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -138,7 +148,7 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
 //         buffer (cand_idx / cand_val, cap entries, count in cnt[row]; the
 //         count keeps growing past cap so the caller sees the overflow).
 template <int MODE>
-__global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
+__global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
                                                               const __grid_constant__ CUtensorMap map_b, int nrows,
                                                               int ncols, int kp, int tiles_per_split,
                                                               const float* __restrict__ bias,
@@ -177,7 +187,7 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
         }
         for (int b = 0; b < 2; b++) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], 4);
+            mbar_init(&tempty[b], 4 * Epi<MODE>::EW);
         }
         mbar_init(afull, 1);
         *s_abort = 0;
@@ -237,9 +247,11 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
         // scale) in its own shared-memory slice, fetched one tile ahead, so
         // the 256 columns are read as broadcasts instead of 256 global loads
         // per lane; the accumulator comes out 64 columns per wait.
-        const int quarter = warp & 3;
+        constexpr int CW = Epi<MODE>::CW;
+        // tcgen05.ld lets warp w read only TMEM lanes 32 (w % 4) .. + 31
+        const int ew = warp - 2, quarter = warp & 3, cbeg = (ew >> 2) * CW;
         const int row = row0 + quarter * 32 + lane;
-        float2* wct = cts + quarter * 2 * BN;  // [2][BN]
+        float2* wct = cts + ew * 2 * CW;  // [2][CW]: this warp's columns of two tiles
         float best_v[TOPC];
         int best_i[TOPC];
 #pragma unroll
@@ -251,11 +263,11 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
         // invalid columns: +inf scores (modes 0, 1), NaN (mode 2, never passes)
         const float2 pad = MODE == 2 ? make_float2(__int_as_float(0x7fc00000), 0.0f)
                                      : make_float2(__int_as_float(0x7f800000), 0.0f);
-        float2 pre[BN / 32];
+        float2 pre[CW / 32];
         auto fetch = [&](int t) {
-            const int colb = col_begin + (t0 + t) * BN;
+            const int colb = col_begin + (t0 + t) * BN + cbeg;
 #pragma unroll
-            for (int j = 0; j < BN / 32; j++) {
+            for (int j = 0; j < CW / 32; j++) {
                 const int col = colb + 32 * j + lane;
                 if (col < ncols) pre[j] = MODE == 2 ? __ldg(cterm + col) : make_float2(__ldg(bias + col), -2.0f);
                 else pre[j] = pad;
@@ -264,24 +276,24 @@ __global__ void __launch_bounds__(THREADS, 1) dist_gemm_kernel(const __grid_cons
         if (ntiles > 0) fetch(0);
         for (int t = 0; t < ntiles; t++) {
             const int buf = t & 1;
-            float2* ct = wct + buf * BN;
+            float2* ct = wct + buf * CW;
 #pragma unroll
-            for (int j = 0; j < BN / 32; j++) ct[32 * j + lane] = pre[j];
+            for (int j = 0; j < CW / 32; j++) ct[32 * j + lane] = pre[j];
             __syncwarp();
             if (t + 1 < ntiles) fetch(t + 1);
             // a warp leaves together when a wait runs out
             const bool ok = __all_sync(0xffffffffu, mbar_wait(&tfull[buf], (t >> 1) & 1, err));
             if (!ok) break;
             tc_fence_after();
-            const int col0 = col_begin + (t0 + t) * BN;
-            for (int c = 0; c < BN; c += 64) {
+            const int col0 = col_begin + (t0 + t) * BN + cbeg;
+            for (int c = 0; c < CW; c += 64) {
                 float v[64];
-                const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN + c);
+                const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN + cbeg + c);
                 tmem_ld64(ta, v);
                 if (MODE == 0) {
                     // Transpose 32 rows x 32 columns at a time through shared
                     // memory so each store writes 128 contiguous bytes of a row.
-                    float* tw = trans + quarter * 32 * 33;
+                    float* tw = trans + ew * 32 * 33;
                     const int rbase = row0 + quarter * 32;
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
@@ -448,7 +460,7 @@ cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat
     if (MODE == 2) splits = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, ceil_div(8 * 152, mtiles)));
     const int per = (int)ceil_div(ntiles, splits);
     splits = (int)ceil_div(ntiles, per);
-    dist_gemm_kernel<MODE><<<dim3((unsigned)mtiles, (unsigned)splits), THREADS, SMEM_BYTES, s>>>(
+    dist_gemm_kernel<MODE><<<dim3((unsigned)mtiles, (unsigned)splits), Epi<MODE>::THREADS, SMEM_BYTES, s>>>(
         ma, mb, (int)nrows, ncols, kp, per, bias, out, cand_idx, cand_val, err, col_begin, cterm, rthr, cap, cnt);
     return cudaGetLastError();
 }
