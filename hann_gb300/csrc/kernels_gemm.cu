@@ -147,6 +147,8 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
 //         column with score <= rthr[row] is appended to the row's candidate
 //         buffer (cand_idx / cand_val, cap entries, count in cnt[row]; the
 //         count keeps growing past cap so the caller sees the overflow).
+//         cmode 0: cterm[col].y is -2 for every column; cmode 1: cterm[col].x
+//         is 0 for every column (so one float per column is staged).
 template <int MODE>
 __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
                                                               const __grid_constant__ CUtensorMap map_b, int nrows,
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                                                               float* __restrict__ out, int32_t* __restrict__ cand_idx,
                                                               float* __restrict__ cand_val, int* __restrict__ err,
                                                               int col_begin, const float2* __restrict__ cterm,
-                                                              const float* __restrict__ rthr, int cap,
+                                                              int cmode, const float* __restrict__ rthr, int cap,
                                                               int32_t* __restrict__ cnt) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -251,7 +253,9 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
         // tcgen05.ld lets warp w read only TMEM lanes 32 (w % 4) .. + 31
         const int ew = warp - 2, quarter = warp & 3, cbeg = (ew >> 2) * CW;
         const int row = row0 + quarter * 32 + lane;
-        float2* wct = cts + ew * 2 * CW;  // [2][CW]: this warp's columns of two tiles
+        // this warp's columns of two tiles: the bias (scores b - 2v) or, in
+        // filter mode 1, the scale (scores w v)
+        float* wct = reinterpret_cast<float*>(cts) + ew * 2 * CW;
         float best_v[TOPC];
         int best_i[TOPC];
 #pragma unroll
@@ -261,22 +265,31 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
         }
         const float rt = (MODE == 2 && row < nrows) ? rthr[row] : -__int_as_float(0x7f800000);
         // invalid columns: +inf scores (modes 0, 1), NaN (mode 2, never passes)
-        const float2 pad = MODE == 2 ? make_float2(__int_as_float(0x7fc00000), 0.0f)
-                                     : make_float2(__int_as_float(0x7f800000), 0.0f);
-        float2 pre[CW / 32];
+        const float pad = MODE == 2 ? __int_as_float(0x7fc00000) : __int_as_float(0x7f800000);
+        const bool scaled = MODE == 2 && cmode == 1;
+        float pre[CW / 32];
         auto fetch = [&](int t) {
             const int colb = col_begin + (t0 + t) * BN + cbeg;
 #pragma unroll
             for (int j = 0; j < CW / 32; j++) {
                 const int col = colb + 32 * j + lane;
-                if (col < ncols) pre[j] = MODE == 2 ? __ldg(cterm + col) : make_float2(__ldg(bias + col), -2.0f);
-                else pre[j] = pad;
+                if (col < ncols) {
+                    if (MODE == 2) {
+                        const float2 tt = __ldg(cterm + col);
+                        pre[j] = scaled ? tt.y : tt.x;
+                    } else {
+                        pre[j] = __ldg(bias + col);
+                    }
+                } else {
+                    pre[j] = pad;
+                }
             }
         };
+        auto score = [&](float tc, float v) { return scaled ? __fmul_rn(tc, v) : __fmaf_rn(-2.0f, v, tc); };
         if (ntiles > 0) fetch(0);
         for (int t = 0; t < ntiles; t++) {
             const int buf = t & 1;
-            float2* ct = wct + buf * CW;
+            float* ct = wct + buf * CW;
 #pragma unroll
             for (int j = 0; j < CW / 32; j++) ct[32 * j + lane] = pre[j];
             __syncwarp();
@@ -298,7 +311,7 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
                         const int cb = col0 + c + 32 * h;
-                        const float bl = ct[c + 32 * h + lane].x;
+                        const float bl = ct[c + 32 * h + lane];
 #pragma unroll
                         for (int i = 0; i < 32; i++) tw[lane * 33 + i] = v[32 * h + i];
                         __syncwarp();
@@ -312,11 +325,15 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                         __syncwarp();
                     }
                 } else if (MODE == 2) {
+                    const float4* ct4 = reinterpret_cast<const float4*>(ct + c);
                     unsigned long long pass = 0;
 #pragma unroll
-                    for (int i = 0; i < 64; i++) {
-                        const float2 tt = ct[c + i];
-                        if (__fmaf_rn(tt.y, v[i], tt.x) <= rt) pass |= 1ull << i;
+                    for (int i4 = 0; i4 < 16; i4++) {
+                        const float4 tt = ct4[i4];
+                        if (score(tt.x, v[4 * i4 + 0]) <= rt) pass |= 1ull << (4 * i4 + 0);
+                        if (score(tt.y, v[4 * i4 + 1]) <= rt) pass |= 1ull << (4 * i4 + 1);
+                        if (score(tt.z, v[4 * i4 + 2]) <= rt) pass |= 1ull << (4 * i4 + 2);
+                        if (score(tt.w, v[4 * i4 + 3]) <= rt) pass |= 1ull << (4 * i4 + 3);
                     }
                     if (pass) {
                         int pos = atomicAdd(&cnt[row], __popcll(pass));
@@ -324,9 +341,8 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                         for (int i = 0; i < 64; i++) {
                             if (pass & (1ull << i)) {
                                 if (pos < cap) {
-                                    const float2 tt = ct[c + i];
                                     cand_idx[(int64_t)row * cap + pos] = col0 + c + i;
-                                    cand_val[(int64_t)row * cap + pos] = __fmaf_rn(tt.y, v[i], tt.x);
+                                    cand_val[(int64_t)row * cap + pos] = score(ct[c + i], v[i]);
                                 }
                                 pos++;
                             }
@@ -335,8 +351,7 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                 } else {
 #pragma unroll
                     for (int i = 0; i < 64; i++) {
-                        const float2 tt = ct[c + i];
-                        const float sc = __fmaf_rn(tt.y, v[i], tt.x);
+                        const float sc = __fmaf_rn(-2.0f, v[i], ct[c + i]);
                         if (sc < best_v[TOPC - 1]) {
                             // insert into the ascending list
                             float cv = sc;
@@ -434,8 +449,8 @@ cudaError_t make_map(CUtensorMap* m, const void* ptr, int64_t rows, int kp, int 
 template <int MODE>
 cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat16* b, int ncols, int kp,
                         const float* bias, float* out, int32_t* cand_idx, float* cand_val, int* err, cudaStream_t s,
-                        int col_begin = 0, const float2* cterm = nullptr, const float* rthr = nullptr, int cap = 0,
-                        int32_t* cnt = nullptr) {
+                        int col_begin = 0, const float2* cterm = nullptr, int cmode = 0, const float* rthr = nullptr,
+                        int cap = 0, int32_t* cnt = nullptr) {
     if (nrows <= 0 || ncols <= col_begin) return cudaSuccess;
     if (kp <= 0 || kp > KB_MAX * BKE || (kp & 7)) return cudaErrorInvalidValue;
     if (nrows > ((int64_t)1 << 31) - BM) return cudaErrorInvalidValue;
@@ -461,20 +476,21 @@ cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat
     const int per = (int)ceil_div(ntiles, splits);
     splits = (int)ceil_div(ntiles, per);
     dist_gemm_kernel<MODE><<<dim3((unsigned)mtiles, (unsigned)splits), Epi<MODE>::THREADS, SMEM_BYTES, s>>>(
-        ma, mb, (int)nrows, ncols, kp, per, bias, out, cand_idx, cand_val, err, col_begin, cterm, rthr, cap, cnt);
+        ma, mb, (int)nrows, ncols, kp, per, bias, out, cand_idx, cand_val, err, col_begin, cterm, cmode, rthr, cap,
+        cnt);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_gemm_filter(const void* a_bf16, int64_t nrows, const void* b_bf16, int64_t nb, int kp,
-                               int col_begin, int col_end, const float2* cterm, const float* rthr, int cap,
+                               int col_begin, int col_end, const float2* cterm, int cmode, const float* rthr, int cap,
                                int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s) {
     // the tensor map spans all nb rows of b; the CTAs cover [col_begin, col_end)
     if (col_end > nb) return cudaErrorInvalidValue;
     return launch_gemm<2>(static_cast<const __nv_bfloat16*>(a_bf16), nrows, static_cast<const __nv_bfloat16*>(b_bf16),
-                          (int)col_end, kp, nullptr, nullptr, cand_id, cand_s, err, s, col_begin, cterm, rthr, cap,
-                          cnt);
+                          (int)col_end, kp, nullptr, nullptr, cand_id, cand_s, err, s, col_begin, cterm, cmode, rthr,
+                          cap, cnt);
 }
 
 int gemm_kpad(int dim) { return (dim + 7) / 8 * 8; }
