@@ -40,14 +40,15 @@ constexpr int KB_MAX = 2;     // K <= 128
 constexpr int STAGES = 2;
 // Warp 0 loads, warp 1 issues the MMAs, then EW epilogue warps per quarter
 // of the accumulator's 128 lanes: one for the top-8 mode (a row's running
-// list stays in one thread), two for the score and filter modes, each
-// taking half of a tile's columns, so two warps per SM sub-partition hide
-// each other's load latency.
+// list stays in one thread), two for the score mode and four for the filter
+// mode, each taking its share of a tile's columns, so several warps per SM
+// sub-partition hide each other's latency.
 template <int MODE>
 struct Epi {
-    static constexpr int EW = MODE == 1 ? 1 : 2;
+    static constexpr int EW = MODE == 1 ? 1 : (MODE == 2 ? 4 : 2);
     static constexpr int THREADS = 64 + 128 * EW;
     static constexpr int CW = 256 / EW;  // columns per epilogue warp
+    static constexpr int LDC = MODE == 2 ? 32 : 64;  // accumulator columns per TMEM load
 };
 constexpr int TOPC = 8;       // argmin mode: candidates kept per row
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
@@ -124,6 +125,20 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 columns of the warp's 32 lanes into v[0..32), load and wait in one asm
+// statement.
+__device__ __forceinline__ void tmem_ld32w(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
 
 // 64 columns of the warp's 32 lanes into v[0..64): two 32-column loads in
 // flight, then one wait, all in one asm statement so no use of v can be
@@ -299,10 +314,12 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
             if (!ok) break;
             tc_fence_after();
             const int col0 = col_begin + (t0 + t) * BN + cbeg;
-            for (int c = 0; c < CW; c += 64) {
-                float v[64];
+            constexpr int LDC = Epi<MODE>::LDC;
+            for (int c = 0; c < CW; c += LDC) {
+                float v[LDC];
                 const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * BN + cbeg + c);
-                tmem_ld64(ta, v);
+                if constexpr (LDC == 64) tmem_ld64(ta, *reinterpret_cast<float(*)[64]>(v));
+                else tmem_ld32w(ta, v);
                 if (MODE == 0) {
                     // Transpose 32 rows x 32 columns at a time through shared
                     // memory so each store writes 128 contiguous bytes of a row.
@@ -328,7 +345,7 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                     const float4* ct4 = reinterpret_cast<const float4*>(ct + c);
                     unsigned long long pass = 0;
 #pragma unroll
-                    for (int i4 = 0; i4 < 16; i4++) {
+                    for (int i4 = 0; i4 < LDC / 4; i4++) {
                         const float4 tt = ct4[i4];
                         if (score(tt.x, v[4 * i4 + 0]) <= rt) pass |= 1ull << (4 * i4 + 0);
                         if (score(tt.y, v[4 * i4 + 1]) <= rt) pass |= 1ull << (4 * i4 + 1);
@@ -338,7 +355,7 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                     if (pass) {
                         int pos = atomicAdd(&cnt[row], __popcll(pass));
 #pragma unroll
-                        for (int i = 0; i < 64; i++) {
+                        for (int i = 0; i < LDC; i++) {
                             if (pass & (1ull << i)) {
                                 if (pos < cap) {
                                     cand_idx[(int64_t)row * cap + pos] = col0 + c + i;
