@@ -39,16 +39,17 @@ constexpr int BKE = 64;       // bf16 elements per 128-byte swizzle row
 constexpr int KB_MAX = 2;     // K <= 128
 constexpr int STAGES = 2;
 // Warp 0 loads, warp 1 issues the MMAs, then EW epilogue warps per quarter
-// of the accumulator's 128 lanes: one for the top-8 mode (a row's running
-// list stays in one thread), two for the score mode and four for the filter
-// mode, each taking its share of a tile's columns, so several warps per SM
-// sub-partition hide each other's latency.
+// of the accumulator's 128 lanes: two for the score mode, four for the
+// top-8 and filter modes, each taking its share of a tile's columns, so
+// several warps per SM sub-partition hide each other's latency. In the top-8
+// mode each warp keeps a list over its columns and the lists of a row are
+// merged at the end.
 template <int MODE>
 struct Epi {
-    static constexpr int EW = MODE == 1 ? 1 : (MODE == 2 ? 4 : 2);
+    static constexpr int EW = MODE == 0 ? 2 : 4;
     static constexpr int THREADS = 64 + 128 * EW;
     static constexpr int CW = 256 / EW;  // columns per epilogue warp
-    static constexpr int LDC = MODE == 2 ? 32 : 64;  // accumulator columns per TMEM load
+    static constexpr int LDC = MODE == 0 ? 64 : 32;  // accumulator columns per TMEM load
 };
 constexpr int TOPC = 8;       // argmin mode: candidates kept per row
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
@@ -367,7 +368,7 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                     }
                 } else {
 #pragma unroll
-                    for (int i = 0; i < 64; i++) {
+                    for (int i = 0; i < LDC; i++) {
                         const float sc = __fmaf_rn(-2.0f, v[i], ct[c + i]);
                         if (sc < best_v[TOPC - 1]) {
                             // insert into the ascending list
@@ -392,11 +393,43 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
             __syncwarp();
             if (lane == 0) mbar_arrive(&tempty[buf]);
         }
-        if (MODE == 1 && row < nrows) {
+        if (MODE == 1) {
+            // every epilogue warp reaches this point, also after a timed-out wait
+            constexpr int EW = Epi<MODE>::EW;
+            float* lv = trans;                                           // [4 EW][32][TOPC]
+            int* li = reinterpret_cast<int*>(trans + 4 * EW * 32 * TOPC);  // same shape
 #pragma unroll
             for (int c = 0; c < TOPC; c++) {
-                cand_idx[(int64_t)row * TOPC + c] = best_i[c];
-                cand_val[(int64_t)row * TOPC + c] = best_v[c];
+                lv[(ew * 32 + lane) * TOPC + c] = best_v[c];
+                li[(ew * 32 + lane) * TOPC + c] = best_i[c];
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(128 * EW) : "memory");
+            if (ew < 4 && row < nrows) {
+                // merge the row's other lists in, ties to the lower column
+                for (int h = 1; h < EW; h++) {
+                    const int src = ((ew + 4 * h) * 32 + lane) * TOPC;
+                    for (int c = 0; c < TOPC; c++) {
+                        float cv = lv[src + c];
+                        int ci = li[src + c];
+                        if (ci < 0) break;
+#pragma unroll
+                        for (int p = 0; p < TOPC; p++) {
+                            if (cv < best_v[p] || (cv == best_v[p] && (unsigned)ci < (unsigned)best_i[p])) {
+                                const float tv = best_v[p];
+                                const int ti = best_i[p];
+                                best_v[p] = cv;
+                                best_i[p] = ci;
+                                cv = tv;
+                                ci = ti;
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < TOPC; c++) {
+                    cand_idx[(int64_t)row * TOPC + c] = best_i[c];
+                    cand_val[(int64_t)row * TOPC + c] = best_v[c];
+                }
             }
         }
     }
