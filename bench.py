@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=8.0, help="served-stream phase length (0 = skip)")
     ap.add_argument("--serve-rate", type=str, default="2000,5000",
                     help="Poisson request arrivals per second, one served-stream phase per value")
+    ap.add_argument("--serve-batch-probes", type=int, default=32768,
+                    help="served stream: bound on a batch's summed nprobe (0 = none)")
     ap.add_argument("--knn", type=int, default=1, help="run the batched exact k-NN section (1M x 128, top-100)")
     ap.add_argument("--knn-n", type=int, default=1_000_000)
     ap.add_argument("--knn-nq", type=int, default=10_000)
@@ -706,7 +708,7 @@ def serve_stream(args, idx, q_host, gt, nr, rate):
 
     rng = np.random.default_rng(args.seed + 7)
     srv = hg.Server(idx, slots=4, max_batch_queries=8192, max_k=100, max_nprobe=256, mode=1,
-                    memory_budget=120 << 30)
+                    memory_budget=120 << 30, max_batch_probes=args.serve_batch_probes)
     pending = qmod.Queue()
     results = []
     stop = threading.Event()
@@ -775,7 +777,8 @@ def serve_stream(args, idx, q_host, gt, nr, rate):
             "peak_admitted_bytes": int(st["peak_admitted_bytes"]), "relayouts": int(st["relayouts"]),
             "mutation_ms_total": round(st["mutation_ms"], 1),
             "stream": "Poisson arrivals; 1-512 queries/request log-uniform; k U[1,100]; nprobe log-U[8,256]; "
-                      "BulkAdd 1000-vector chunks and Deletes at 1% of the request rate; exact rerank"}
+                      "BulkAdd 1000-vector chunks and Deletes at 1% of the request rate; exact rerank",
+            "max_batch_probes": args.serve_batch_probes}
 
 
 def workload_config(args, nprobe, mode, rec):

@@ -679,7 +679,8 @@ def knn(queries, base, k: int, metric="squared_euclidean", method="auto"):
 
 class _ServeOptions(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_int32), ("max_batch_queries", ctypes.c_int32), ("max_k", ctypes.c_int32),
-                ("max_nprobe", ctypes.c_int32), ("mode", ctypes.c_int32), ("memory_budget", ctypes.c_int64)]
+                ("max_nprobe", ctypes.c_int32), ("mode", ctypes.c_int32), ("memory_budget", ctypes.c_int64),
+                ("max_batch_probes", ctypes.c_int64)]
 
 
 class _ServeStats(ctypes.Structure):
@@ -716,12 +717,12 @@ class Server:
     (ids [nq, k], distances [nq, k], counts [nq], latency_ms)."""
 
     def __init__(self, index: Index, slots=4, max_batch_queries=4096, max_k=100, max_nprobe=256,
-                 mode=MODE_EXACT_RERANK, memory_budget=120 << 30):
+                 mode=MODE_EXACT_RERANK, memory_budget=120 << 30, max_batch_probes=0):
         L = _serve_lib()
         o = _ServeOptions()
         L.hann_serve_options_init(ctypes.byref(o))
         o.slots, o.max_batch_queries, o.max_k, o.max_nprobe = slots, max_batch_queries, max_k, max_nprobe
-        o.mode, o.memory_budget = mode, memory_budget
+        o.mode, o.memory_budget, o.max_batch_probes = mode, memory_budget, max_batch_probes
         h = _P()
         rc = L.hann_serve_start(index.handle, ctypes.byref(o), ctypes.byref(h))
         if rc != HANN_OK:

@@ -594,16 +594,13 @@ constexpr int SCREEN_MIN_LISTS = 2048;  // below this the full score matrix is c
 constexpr int PROBE_CAP = 4096;         // screened-probe candidates per query and chunk
 constexpr int PROBE_FIRST = 256;        // first centroid chunk at least (every list enters the band)
 
-int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k,
-                      const int32_t* d_np, int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist,
-                      int32_t* d_nout, cudaStream_t s) {
+
+// Every scratch buffer run_search needs for nq queries (in chunks of at most
+// 2^28 / nlist), reserved up front; a server calls it once per slot at start
+// so no batch ever reaches the allocator.
+int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_max, int kmax, int mode) {
     const int R = rerank_depth(h, kmax, mode);
-    if (R > 480) return h->fail(HANN_E_UNSUPPORTED, "k (%d) above this build's limit of 448", kmax);
     np_max = std::min(np_max, h->nlist);
-    if (np_max > 4096) return h->fail(HANN_E_UNSUPPORTED, "more than 4096 probed lists per query");
-    ScanParams p = h->scan_params();
-    p.mode = mode;
-    p.rerank_fixed = h->o.rerank;
     const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)1 << 28) / std::max(1, h->nlist)));
     CK(sc.D.reserve((size_t)chunk * h->nlist));
     if (h->tc) {
@@ -617,6 +614,37 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
     CK(sc.cand_row.reserve((size_t)chunk * R));
     CK(sc.cand_d.reserve((size_t)chunk * R));
     CK(sc.cand_seq.reserve((size_t)chunk * R));
+    CK(sc.fbcount.reserve(1));
+    if (h->tc && h->nlist >= SCREEN_MIN_LISTS) {
+        const int lcap = std::max(1024, 2 * np_max);
+        CK(sc.pe2.reserve((size_t)chunk));
+        CK(sc.pasl.reserve((size_t)chunk));
+        CK(sc.pthr.reserve((size_t)chunk));
+        CK(sc.pcnt.reserve((size_t)chunk));
+        CK(sc.plcount.reserve((size_t)chunk));
+        CK(sc.pneed.reserve((size_t)chunk));
+        CK(sc.pcand_id.reserve((size_t)chunk * PROBE_CAP));
+        CK(sc.pcand_s.reserve((size_t)chunk * PROBE_CAP));
+        CK(sc.pband.reserve((size_t)chunk * lcap));
+        CK(sc.qorder.reserve((size_t)chunk));
+        CK(sc.order_scratch.reserve((size_t)h->nlist));
+    }
+    return HANN_OK;
+}
+
+int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k,
+                      const int32_t* d_np, int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist,
+                      int32_t* d_nout, cudaStream_t s) {
+    const int R = rerank_depth(h, kmax, mode);
+    if (R > 480) return h->fail(HANN_E_UNSUPPORTED, "k (%d) above this build's limit of 448", kmax);
+    np_max = std::min(np_max, h->nlist);
+    if (np_max > 4096) return h->fail(HANN_E_UNSUPPORTED, "more than 4096 probed lists per query");
+    ScanParams p = h->scan_params();
+    p.mode = mode;
+    p.rerank_fixed = h->o.rerank;
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)1 << 28) / std::max(1, h->nlist)));
+    int rrc = reserve_search_scratch(h, sc, nq, np_max, kmax, mode);
+    if (rrc) return rrc;
     auto mark = [&](int stage, bool begin) -> cudaError_t {
         if (!h->profile) return cudaSuccess;
         cudaEvent_t e;
@@ -634,19 +662,6 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
     // full score matrix.
     const bool screened = h->tc && h->nlist >= SCREEN_MIN_LISTS;
     const int lcap = std::max(1024, 2 * np_max);
-    if (screened) {
-        CK(sc.pe2.reserve((size_t)chunk));
-        CK(sc.pasl.reserve((size_t)chunk));
-        CK(sc.pthr.reserve((size_t)chunk));
-        CK(sc.pcnt.reserve((size_t)chunk));
-        CK(sc.plcount.reserve((size_t)chunk));
-        CK(sc.pneed.reserve((size_t)chunk));
-        CK(sc.pcand_id.reserve((size_t)chunk * PROBE_CAP));
-        CK(sc.pcand_s.reserve((size_t)chunk * PROBE_CAP));
-        CK(sc.pband.reserve((size_t)chunk * lcap));
-        CK(sc.qorder.reserve((size_t)chunk));
-        CK(sc.order_scratch.reserve((size_t)h->nlist));
-    }
     for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
         const int64_t nc = std::min(chunk, nq - q0);
         const float* qp = d_q + q0 * h->o.dimension;

@@ -274,6 +274,7 @@ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k, const int32_t* d_np,
                int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist, int32_t* d_nout, cudaStream_t s);
 int check_searchable(hann_pqivf* h);
+int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_max, int kmax, int mode);
 int rerank_depth(const hann_pqivf* h, int kmax, int mode);
 // Mutations with the writer lock held. Without allow_relayout a mutation
 // that would move rows (a list overflowing, or tombstone compaction) changes

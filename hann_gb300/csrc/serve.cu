@@ -6,11 +6,17 @@
 // with its own scratch (SearchScratch) and pinned staging buffers, so up to
 // `slots` batches are in flight and overlap on the device. Requests that
 // arrive while batches run are admitted into the next free slot; a batch
-// takes requests in arrival order while its queries fit max_batch_queries
-// and its device scratch fits the slot's share of the memory budget
-// (admission by device memory). Add/Delete requests are applied between
-// batches: the scheduler stops starting batches, waits for the running ones
-// and applies the mutation under the index's exclusive lock.
+// takes requests in arrival order while its queries fit max_batch_queries,
+// its summed nprobe fits max_batch_probes (when set) and its device scratch
+// fits the slot's share of the memory budget
+// (admission by device memory). Add/Delete requests go, in order, to a
+// mutation thread that applies them beside the running batches: an append
+// into spare capacity and a tombstone delete move no row, so batches in
+// flight see each mutation either not at all or whole. Only a mutation that
+// must move rows (a relayout) stops the scheduler from starting batches;
+// the mutation thread then waits for the running ones and applies it under
+// the index's exclusive lock. A search sees every mutation whose ticket was
+// waited for before the search was submitted.
 //
 // Every request is an ordinary Search of its queries (pqivf/index.go:850-949)
 // with per-query k and nprobe, so its result does not depend on what it was
@@ -81,7 +87,14 @@ struct hann_server {
     int64_t queries_done = 0, requests_done = 0, batches = 0, mutations = 0;
     int64_t peak_admitted = 0, cur_admitted = 0, relayouts = 0;
     double mutation_ms = 0.0;
-    bool mut_drain = false;
+    // mutation thread: its FIFO, and the drain handshake for relayouts
+    std::deque<std::shared_ptr<Request>> mqueue;
+    std::condition_variable cv_mut;
+    std::thread mthr;
+    bool drain_wanted = false;  // set by the mutation thread; the scheduler stops launching
+    bool drained = false;       // set by the scheduler once nothing is in flight
+    bool mstop = false;
+    bool sched_done = false;    // the scheduler has exited: nothing runs any more
     Clock::time_point t_first{}, t_last{};
     bool any = false;
     std::shared_lock<std::shared_mutex> read_lock;  // held while batches run
@@ -175,6 +188,62 @@ void fail_requests(hann_server* s, std::vector<std::shared_ptr<Request>>& rs, in
     }
 }
 
+// Applies Add/Delete requests in submission order. An append or tombstone
+// delete runs under the writer lock beside the scheduler's batches; one that
+// needs a relayout asks the scheduler to drain, then runs under the index's
+// exclusive lock.
+void mutator(hann_server* s) {
+    hann_pqivf* h = s->h;
+    cudaSetDevice(h->o.device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        s->cv_mut.wait(lk, [&] { return s->mstop || !s->mqueue.empty(); });
+        if (s->mqueue.empty()) break;
+        auto r = s->mqueue.front();
+        lk.unlock();
+        auto apply = [&](bool allow, bool* needs) {
+            return r->kind == 1 ? bulk_add_locked(h, r->ids.data(), r->vectors.data(), (int64_t)r->ids.size(), allow,
+                                                  needs)
+                                : bulk_delete_locked(h, r->ids.data(), (int64_t)r->ids.size(), allow, needs);
+        };
+        const auto t0 = Clock::now();
+        bool needs = false, relaid = false;
+        int rc;
+        {
+            std::lock_guard<std::mutex> wl(h->wmu);
+            rc = apply(false, &needs);
+        }
+        if (needs) {
+            lk.lock();
+            s->drain_wanted = true;
+            s->drained = s->sched_done;
+            s->cv_work.notify_one();
+            s->cv_mut.wait(lk, [&] { return s->drained; });
+            lk.unlock();
+            {
+                std::lock_guard<std::mutex> wl(h->wmu);
+                std::unique_lock<std::shared_mutex> xl(h->mu);
+                rc = apply(true, nullptr);
+            }
+            relaid = true;
+        }
+        lk.lock();
+        if (relaid) {
+            s->drain_wanted = false;
+            s->drained = false;
+            s->relayouts++;
+            s->cv_work.notify_one();
+        }
+        s->mqueue.pop_front();
+        if (rc) r->error = h->err;
+        r->status = rc;
+        r->t_done = Clock::now();
+        s->mutations++;
+        s->mutation_ms += std::chrono::duration<double, std::milli>(r->t_done - t0).count();
+        s->cv_done.notify_all();
+    }
+}
+
 void scheduler(hann_server* s) {
     hann_pqivf* h = s->h;
     cudaSetDevice(h->o.device);
@@ -203,47 +272,18 @@ void scheduler(hann_server* s) {
         }
         if (!any_busy && s->read_lock.owns_lock()) s->read_lock.unlock();
         if (s->stop && s->queue.empty() && !any_busy) break;
-        // 2. a mutation at the head of the queue. Appends into spare capacity
-        //    and tombstone deletes move no row, so they run beside the batches
-        //    in flight (which may see them or not); batches queued after the
-        //    mutation start only once it is applied. A mutation that must move
-        //    rows (relayout) waits until nothing is in flight.
-        if (!s->queue.empty() && s->queue.front()->kind != 0) {
-            auto r = s->queue.front();
-            bool applied = false;
-            int rc = HANN_OK;
-            auto apply = [&](bool allow, bool* needs) {
-                return r->kind == 1 ? bulk_add_locked(h, r->ids.data(), r->vectors.data(), (int64_t)r->ids.size(),
-                                                      allow, needs)
-                                    : bulk_delete_locked(h, r->ids.data(), (int64_t)r->ids.size(), allow, needs);
-            };
-            const auto t0 = Clock::now();
-            if (!s->mut_drain && h->wmu.try_lock()) {
-                // never block on the writer lock while holding the read lock
-                std::lock_guard<std::mutex> wl(h->wmu, std::adopt_lock);
-                bool needs = false;
-                rc = apply(false, &needs);
-                if (needs) s->mut_drain = true;
-                else applied = true;
-            }
-            if (s->mut_drain && !any_busy) {
+        // 2. mutations at the head of the queue go to the mutation thread
+        while (!s->queue.empty() && s->queue.front()->kind != 0) {
+            s->mqueue.push_back(s->queue.front());
+            s->queue.pop_front();
+            s->cv_mut.notify_one();
+        }
+        // a relayout waits for the batches in flight; none start meanwhile
+        if (s->drain_wanted) {
+            if (!any_busy && !s->drained) {
                 if (s->read_lock.owns_lock()) s->read_lock.unlock();
-                std::lock_guard<std::mutex> wl(h->wmu);
-                std::unique_lock<std::shared_mutex> xl(h->mu);
-                rc = apply(true, nullptr);
-                s->mut_drain = false;
-                s->relayouts++;
-                applied = true;
-            }
-            if (applied) {
-                s->queue.pop_front();
-                if (rc) r->error = h->err;
-                r->status = rc;
-                r->t_done = Clock::now();
-                s->mutations++;
-                s->mutation_ms += std::chrono::duration<double, std::milli>(r->t_done - t0).count();
-                s->cv_done.notify_all();
-                continue;
+                s->drained = true;
+                s->cv_mut.notify_one();
             }
         } else if (!s->queue.empty()) {
             // 3. pack waiting searches into every free slot
@@ -251,12 +291,14 @@ void scheduler(hann_server* s) {
                 Slot& sl = *s->slots[i];
                 if (sl.busy) continue;
                 std::vector<std::shared_ptr<Request>> take;
-                int64_t nq = 0;
+                int64_t nq = 0, probes = 0;
                 int kmax = 1, npm = 1;
                 while (!s->queue.empty() && s->queue.front()->kind == 0) {
                     auto& r = s->queue.front();
                     const int64_t nq2 = nq + r->nq;
                     const int k2 = std::max(kmax, r->k), np2 = std::max(npm, std::min(r->nprobe, h->nlist));
+                    const int64_t pr2 = probes + (int64_t)r->nq * std::min(r->nprobe, h->nlist);
+                    if (!take.empty() && s->o.max_batch_probes > 0 && pr2 > s->o.max_batch_probes) break;
                     if (nq2 > s->o.max_batch_queries || batch_bytes(h, nq2, k2, np2, s->o.mode) > s->slot_budget) {
                         if (take.empty()) {
                             // a request that can never fit
@@ -271,6 +313,7 @@ void scheduler(hann_server* s) {
                     nq = nq2;
                     kmax = k2;
                     npm = np2;
+                    probes = pr2;
                     take.push_back(r);
                     s->queue.pop_front();
                 }
@@ -289,7 +332,9 @@ void scheduler(hann_server* s) {
             }
         }
         // 4. wait for new work or a completion (poll completions every 50 us)
-        if (any_busy) {
+        if (s->drain_wanted && s->drained) {
+            s->cv_work.wait_for(lk, std::chrono::milliseconds(1));
+        } else if (any_busy) {
             lk.unlock();
             std::this_thread::sleep_for(std::chrono::microseconds(50));
             lk.lock();
@@ -298,6 +343,10 @@ void scheduler(hann_server* s) {
         }
     }
     if (s->read_lock.owns_lock()) s->read_lock.unlock();
+    // nothing runs any more: a pending relayout may go ahead
+    s->sched_done = true;
+    s->drained = true;
+    s->cv_mut.notify_one();
 }
 
 void free_slot(Slot& sl) {
@@ -369,18 +418,8 @@ int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server*
         if (e == cudaSuccess) e = sl->d_dist.reserve((size_t)Q * K);
         // Size the slot's search scratch for its largest batch now, so the
         // scheduler never calls the allocator while batches are in flight.
-        const int R = rerank_depth(h, o.max_k, o.mode);
-        if (e == cudaSuccess) e = sl->sc.D.reserve((size_t)Q * h->nlist);
-        if (e == cudaSuccess) e = sl->sc.probe_ids.reserve((size_t)Q * np_max);
-        if (e == cudaSuccess) e = sl->sc.probe_d.reserve((size_t)Q * np_max);
-        if (e == cudaSuccess) e = sl->sc.fb.reserve((size_t)Q);
-        if (e == cudaSuccess) e = sl->sc.cand_row.reserve((size_t)Q * R);
-        if (e == cudaSuccess) e = sl->sc.cand_d.reserve((size_t)Q * R);
-        if (e == cudaSuccess) e = sl->sc.cand_seq.reserve((size_t)Q * R);
-        if (e == cudaSuccess) e = sl->sc.qbf.reserve((size_t)Q * std::max(h->kp, 8));
-        if (e == cudaSuccess) e = sl->sc.qn2.reserve((size_t)Q);
-        if (e == cudaSuccess) e = sl->sc.qres.reserve((size_t)Q);
-        if (e == cudaSuccess) e = sl->sc.fbcount.reserve(1);
+        if (e == cudaSuccess && reserve_search_scratch(h, sl->sc, Q, np_max, o.max_k, o.mode) != HANN_OK)
+            e = cudaErrorMemoryAllocation;
         if (e != cudaSuccess) {
             free_slot(*sl);
             for (auto& x : s->slots) free_slot(*x);
@@ -390,6 +429,7 @@ int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server*
     }
     hann_server* raw = s.release();
     raw->thr = std::thread(scheduler, raw);
+    raw->mthr = std::thread(mutator, raw);
     *out = raw;
     return HANN_OK;
 }
@@ -502,6 +542,12 @@ int hann_serve_stop(hann_server* s) {
         s->cv_work.notify_all();
     }
     if (s->thr.joinable()) s->thr.join();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->mstop = true;
+        s->cv_mut.notify_all();
+    }
+    if (s->mthr.joinable()) s->mthr.join();
     for (auto& sl : s->slots) free_slot(*sl);
     delete s;
     return HANN_OK;

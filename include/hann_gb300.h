@@ -180,6 +180,8 @@ typedef struct {
     int32_t max_nprobe;        /* nprobe is clamped to this; default 256 */
     int32_t mode;              /* 0 PQ distances (parity), 1 exact rerank; default 1 */
     int64_t memory_budget;     /* device bytes for batch scratch; default 120 GiB */
+    int64_t max_batch_probes;  /* sum over a batch's queries of nprobe, a bound on its scan work (and so on the
+                                  latency of every request in it); 0 = no bound; default 0 */
 } hann_serve_options;
 typedef struct {
     int64_t requests, queries, batches, mutations, peak_admitted_bytes;
@@ -192,7 +194,9 @@ void hann_serve_options_init(hann_serve_options* opts);
 int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server** out);
 /* Queues nq queries (copied) with one k and nprobe; returns a ticket. */
 int hann_serve_submit(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe, uint64_t* ticket);
-/* Queues a BulkAdd / BulkDelete applied between batches. */
+/* Queues a BulkAdd / BulkDelete, applied in order beside the running
+ * batches; a search submitted after the mutation's ticket was waited for
+ * sees it. */
 int hann_serve_submit_add(hann_server* s, const int64_t* ids, const float* vectors, int64_t n, uint64_t* ticket);
 int hann_serve_submit_delete(hann_server* s, const int64_t* ids, int64_t n, uint64_t* ticket);
 /* Waits for a ticket (timeout_ms < 0: no limit) and copies its results:

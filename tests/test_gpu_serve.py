@@ -55,23 +55,55 @@ def test_each_result_equals_alone(index, mode):
 
 
 def test_mutations_between_batches(index):
+    """A search sees every mutation whose ticket was waited for before it
+    was submitted."""
     idx, x, rng = index
     newv = (x[:5] + 1e-3).astype(np.float32)
     with hg.Server(idx, slots=2, max_batch_queries=256, max_k=10, max_nprobe=16) as srv:
-        t1 = srv.submit(newv, 1, 16)
-        ta = srv.submit_add(np.arange(900000, 900005), newv)
-        t2 = srv.submit(newv, 1, 16)
-        td = srv.submit_delete([900000, 900001])
-        t3 = srv.submit(newv, 1, 16)
-        r1, _, r2, r3 = srv.wait(t1), srv.wait(ta), srv.wait(t2), srv.wait(t3)
-        srv.wait(td)
+        r1 = srv.wait(srv.submit(newv, 1, 16))
+        srv.wait(srv.submit_add(np.arange(900000, 900005), newv))
+        r2 = srv.wait(srv.submit(newv, 1, 16))
+        srv.wait(srv.submit_delete([900000, 900001]))
+        r3 = srv.wait(srv.submit(newv, 1, 16))
         assert srv.stats()["mutations"] == 2
     # before the add: the originals; after it: the added copies (exact rerank
     # distance 0); after the delete: originals for the first two again
+    assert not np.isin(r1[0][:, 0], np.arange(900000, 900005)).any()
     assert (r2[0][:, 0] == np.arange(900000, 900005)).all()
     assert (r3[0][:2, 0] != np.arange(900000, 900002)).all()
     assert (r3[0][2:, 0] == np.arange(900002, 900005)).all()
     idx.BulkDelete(list(range(900000, 900005)))
+
+
+def test_mutations_beside_running_batches(index):
+    """Searches and mutations submitted without waiting all complete; every
+    search returns full, sorted results; once all are waited for, a search
+    sees every mutation."""
+    idx, x, rng = index
+    added = []
+    with hg.Server(idx, slots=3, max_batch_queries=512, max_k=10, max_nprobe=16) as srv:
+        tickets = []
+        for i in range(40):
+            q = rng.normal(size=(int(rng.integers(1, 64)), x.shape[1])).astype(np.float32)
+            tickets.append((0, srv.submit(q, 10, 16)))
+            if i % 5 == 0:
+                ids = np.arange(950000 + 10 * i, 950000 + 10 * i + 10)
+                v = (x[rng.integers(0, len(x), 10)] + 1e-3).astype(np.float32)
+                added.append((ids, v))
+                tickets.append((1, srv.submit_add(ids, v)))
+            if i % 7 == 3 and added:
+                tickets.append((2, srv.submit_delete(added[0][0][:3])))
+        for kind, t in tickets:
+            r = srv.wait(t)
+            if kind == 0:
+                ids, dist, n, _ = r
+                assert (n == 10).all()
+                assert (np.diff(dist, axis=1) >= 0).all()
+        ids0, v0 = added[-1]
+        r = srv.wait(srv.submit(v0, 1, 16))
+        assert (r[0][:, 0] == ids0).all()
+    # BulkDelete skips the ids already deleted (pqivf/index.go:365-367)
+    idx.BulkDelete([int(i) for ids, _ in added for i in ids])
 
 
 def test_admission_by_memory_budget(index):
