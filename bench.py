@@ -566,6 +566,18 @@ def train_section(args, torch, dev):
         out[name] = {"train_s": round(el, 3), "s_per_iteration": round(el / iters, 4), "inertia_fp64": inertia}
         states[name] = st
         log("train", name, out[name])
+        if not plain and args.serve_seconds > 0:
+            # the served stream on this 1M x 128 index as well
+            try:
+                nq_s = 1000
+                lab_q = torch.randint(0, 2000, (nq_s,), device=dev, generator=g)
+                qs = centers[lab_q] + torch.randn(nq_s, dim, device=dev, generator=g) * scales[lab_q]
+                gt = ground_truth(torch, x, qs, 10)
+                out["served_stream_1Mx128"] = serve_stream(args, idx, qs.cpu().numpy(), gt, nq_s, 2000.0,
+                                                           n_ids=n, seconds=min(4.0, args.serve_seconds))
+                log("served 1Mx128", out["served_stream_1Mx128"])
+            except Exception as e:  # pragma: no cover
+                out["served_stream_1Mx128"] = {"error": str(e)}
         idx.close()
     a, b = states["tensor_core"], states["plain_fp32"]
     out["identical_index"] = bool(all(np.array_equal(a[key], b[key]) for key in ("coarse", "list_len", "ids",
@@ -693,7 +705,7 @@ def scan_traffic(args):
         return None
 
 
-def serve_stream(args, idx, q_host, gt, nr, rate):
+def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
     """The served stream: Poisson arrivals at `rate` requests/s, each a
     block of 1-512 queries (log-uniform), k uniform in [1, 100], nprobe
     log-uniform in [8, 256]; BulkAdd of 1,000-vector chunks and Deletes of
@@ -732,7 +744,7 @@ def serve_stream(args, idx, q_host, gt, nr, rate):
     sent = 0
     while True:
         now = time.perf_counter()
-        if now - t0 > args.serve_seconds:
+        if now - t0 > (seconds or args.serve_seconds):
             break
         if now < t_next:
             time.sleep(min(t_next - now, 0.001))
@@ -749,7 +761,7 @@ def serve_stream(args, idx, q_host, gt, nr, rate):
             pending.put((1, srv.submit_add(ids, chunk), None))
             continue
         if u < 0.02:
-            pending.put((2, srv.submit_delete(rng.integers(0, args.n, 100)), None))
+            pending.put((2, srv.submit_delete(rng.integers(0, n_ids or args.n, 100)), None))
             continue
         nq = int(np.exp(rng.uniform(0, np.log(512))))
         k = int(rng.integers(1, 101))
