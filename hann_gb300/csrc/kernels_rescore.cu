@@ -121,6 +121,58 @@ __global__ void __launch_bounds__(PB_THREADS) probe_select_band_kernel(
     }
 }
 
+constexpr int PFW_CAP = 256;  // band lists up to this length finish on one warp
+constexpr int PFW_WARPS = 8;
+
+// One warp per query when its band holds at most PFW_CAP lists (the usual
+// case: about nprobe plus a few): the same result as probe_final_kernel
+// without block barriers. Other queries are left to probe_final_kernel.
+__global__ void __launch_bounds__(PFW_WARPS * 32) probe_final_warp_kernel(
+    const float* __restrict__ Q, int64_t nq, int dim, const float* __restrict__ coarse, int nlist,
+    const int32_t* __restrict__ nprobe, int np_max, const int32_t* __restrict__ kq,
+    const int32_t* __restrict__ list_len, int allow_fb, int lcap, const unsigned long long* __restrict__ band,
+    const int32_t* __restrict__ lcount, const int32_t* __restrict__ need_exact, int32_t* __restrict__ probe_ids,
+    float* __restrict__ probe_d, int32_t* __restrict__ fallback, unsigned long long* __restrict__ fb_count) {
+    __shared__ float qv_all[PFW_WARPS][QMAX];
+    __shared__ unsigned long long keys_all[PFW_WARPS][PFW_CAP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t q = (int64_t)blockIdx.x * PFW_WARPS + w;
+    if (q >= nq) return;
+    const int L = lcount[q];
+    if (need_exact[q] || L > PFW_CAP) return;
+    float* qv = qv_all[w];
+    unsigned long long* keys = keys_all[w];
+    for (int e = lane; e < dim; e += 32) qv[e] = Q[q * dim + e];
+    __syncwarp();
+    const int np = min(nprobe[q], nlist);
+    int P = 1;
+    while (P < L) P <<= 1;
+    for (int i = lane; i < P; i += 32) {
+        unsigned long long key = ~0ull;
+        if (i < L) {
+            const uint32_t c = (uint32_t)(band[q * lcap + i] & 0xffffffffull);
+            key = ((unsigned long long)float_key(sqeuclid_ref(qv, coarse + (int64_t)c * dim, dim)) << 32) | c;
+        }
+        keys[i] = key;
+    }
+    __syncwarp();
+    warp_sort_u64(keys, P);
+    unsigned long long part = 0;
+    for (int i = lane; i < np; i += 32) {
+        const int c = (int)(keys[i] & 0xffffffffull);
+        probe_ids[q * np_max + i] = c;
+        probe_d[q * np_max + i] = key_float((uint32_t)(keys[i] >> 32));
+        part += (unsigned long long)list_len[c];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) {
+        const int fb = (allow_fb && part < (unsigned long long)kq[q]) ? 1 : 0;
+        fallback[q] = fb;
+        if (fb) atomicAdd(fb_count, 1ull);
+    }
+}
+
 // Final step of the screened probe. Per query, the band list (every list
 // whose screened score can still reach the np-th) is rescored with the
 // reference-order FP32 distance and the best np by (distance, list) are
@@ -145,6 +197,7 @@ __global__ void __launch_bounds__(PB_THREADS) probe_final_kernel(
     __shared__ unsigned long long s_total;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int64_t q = blockIdx.x;
+    if (!need_exact[q] && lcount[q] <= PFW_CAP) return;  // done by probe_final_warp_kernel
     const int np = min(nprobe[q], nlist);
     for (int e = tid; e < dim; e += PB_THREADS) qv[e] = Q[q * dim + e];
     if (tid == 0) {
@@ -328,6 +381,9 @@ cudaError_t launch_probe_final(const float* Q, int64_t nq, int dim, const float*
     const size_t smem = probe_final_smem(lcap, np_max);
     cudaError_t e = cudaFuncSetAttribute(probe_final_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    probe_final_warp_kernel<<<(unsigned)ceil_div(nq, PFW_WARPS), PFW_WARPS * 32, 0, s>>>(
+        Q, nq, dim, coarse, nlist, nprobe, np_max, k, list_len, allow_fallback, lcap, band, lcount, need_exact,
+        probe_ids, probe_d, fallback, fallback_count);
     probe_final_kernel<<<(unsigned)nq, PB_THREADS, smem, s>>>(Q, dim, coarse, nlist, nprobe, np_max, k, list_len,
                                                               allow_fallback, lcap, band, lcount, need_exact, Drow,
                                                               probe_ids, probe_d, fallback, fallback_count);

@@ -484,6 +484,66 @@ struct ReconRow {
 };
 
 constexpr int RR_THREADS = 256;
+constexpr int RW_MAX = 128;  // candidates per query up to which one warp reranks a query
+
+// One warp per query for small candidate sets (RP <= RW_MAX): the same
+// computation as rerank_kernel without block barriers, eight queries per
+// block.
+__global__ void __launch_bounds__(RR_THREADS) rerank_warp_kernel(ScanParams p, const float* __restrict__ Q, int64_t nq,
+                                                                 const int32_t* __restrict__ cand_row,
+                                                                 const uint32_t* __restrict__ cand_seq, int R, int RP,
+                                                                 const int32_t* __restrict__ kq, int kmax, int mode,
+                                                                 int64_t* __restrict__ ids, double* __restrict__ dist,
+                                                                 int32_t* __restrict__ nout) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t qi = (int64_t)blockIdx.x * (RR_THREADS / 32) + w;
+    if (qi >= nq) return;
+    const int64_t q = p.qorder ? p.qorder[qi] : qi;
+    float* qv = reinterpret_cast<float*>(smraw) + (int64_t)w * (p.dim + 3 * RP);
+    float* cd = qv + p.dim;
+    uint32_t* cs = reinterpret_cast<uint32_t*>(cd + RP);
+    int32_t* cr = reinterpret_cast<int32_t*>(cs + RP);
+    for (int e = lane; e < p.dim; e += 32) qv[e] = Q[q * p.dim + e];
+    __syncwarp();
+    int valid = 0;
+    for (int i = lane; i < RP; i += 32) {
+        const int32_t row = i < R ? cand_row[q * R + i] : -1;
+        if (row >= 0 && p.row_id[row] >= 0) {
+            float d;
+            if (mode == 0) {
+                ReconRow rec{p.coarse + (int64_t)p.row_cluster[row] * p.dim, p.codebooks,
+                             p.codes + (int64_t)row * p.code_stride, p.dsub, p.pqK};
+                d = sqeuclid_ref(qv, rec, p.dim);
+            } else {
+                d = sqeuclid_ref(qv, p.vectors + (int64_t)row * p.dim, p.dim);
+            }
+            cd[i] = d;
+            cs[i] = cand_seq[q * R + i];
+            cr[i] = row;
+            valid++;
+        } else {
+            cd[i] = F_INF;
+            cs[i] = 0xffffffffu;
+            cr[i] = 0x7fffffff;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) valid += __shfl_xor_sync(0xffffffffu, valid, o);
+    __syncwarp();
+    warp_sort_cand(cd, cs, cr, RP);
+    const int k = min(kq[q], valid);
+    for (int i = lane; i < kmax; i += 32) {
+        if (i < k) {
+            ids[q * kmax + i] = p.row_id[cr[i]];
+            dist[q * kmax + i] = sqrt((double)cd[i]);
+        } else {
+            ids[q * kmax + i] = -1;
+            dist[q * kmax + i] = 0.0;
+        }
+    }
+    if (lane == 0) nout[q] = k;
+}
 
 __global__ void __launch_bounds__(RR_THREADS) rerank_kernel(ScanParams p, const float* __restrict__ Q,
                                                             const int32_t* __restrict__ cand_row,
@@ -546,6 +606,21 @@ cudaError_t launch_rerank(const ScanParams& p, const float* queries, int64_t nq,
     if (nq <= 0) return cudaSuccess;
     int RP = 1;
     while (RP < R) RP <<= 1;
+    if (RP <= RW_MAX) {
+        const size_t wsm = (size_t)(RR_THREADS / 32) * ((size_t)p.dim * sizeof(float) + (size_t)RP * 12);
+        if (wsm <= 160 * 1024) {
+            static bool attr = false;
+            if (!attr) {
+                cudaError_t e = cudaFuncSetAttribute(rerank_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     160 * 1024);
+                if (e != cudaSuccess) return e;
+                attr = true;
+            }
+            rerank_warp_kernel<<<(unsigned)ceil_div(nq, RR_THREADS / 32), RR_THREADS, wsm, s>>>(
+                p, queries, nq, cand_row, cand_seq, R, RP, k, kmax, mode, ids, dist, nout);
+            return cudaGetLastError();
+        }
+    }
     const size_t smem = (size_t)p.dim * sizeof(float) + (size_t)RP * 12;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(rerank_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -146,6 +146,28 @@ __device__ __forceinline__ void sort_u64(unsigned long long* key, int P) {
     }
 }
 
+// Warp-synchronous bitonic sort of P (a power of two) 64-bit keys in the
+// warp's shared memory, ascending.
+__device__ __forceinline__ void warp_sort_u64(unsigned long long* key, int P) {
+    const int lane = threadIdx.x & 31;
+    for (int kk = 2; kk <= P; kk <<= 1) {
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int i = lane; i < P; i += 32) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const bool up = (i & kk) == 0;
+                    const unsigned long long a = key[i], b = key[ixj];
+                    if (up == (b < a)) {
+                        key[i] = b;
+                        key[ixj] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
 // The n-th smallest (1-based, 1 <= n <= len) of the 64-bit keys in
 // shared memory, returned to every thread. Digits of 8 bits from the
 // highest bit where the keys differ; one shared histogram per pass; once the
