@@ -57,6 +57,59 @@ __device__ __forceinline__ float sqeuclid_ref(PA a, PB b, int n) {
     return sum;
 }
 
+// sqeuclid_ref with b read as float4 (b 16-byte aligned, as every row of a
+// row-major matrix with dim % 4 == 0 is): same arithmetic, same order, fewer
+// and wider loads.
+template <typename PA>
+__device__ __forceinline__ float sqeuclid_ref_v4(PA a, const float* __restrict__ b, int n) {
+    float acc[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int l = 0; l < 4; l++) acc[u][l] = 0.0f;
+    const float4* b4 = reinterpret_cast<const float4*>(b);
+    int i = 0;
+    const int lim4 = n - (n % 16);
+    for (; i < lim4; i += 16) {
+        float bb[16];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const float4 v = __ldg(b4 + (i >> 2) + u);
+            bb[4 * u + 0] = v.x;
+            bb[4 * u + 1] = v.y;
+            bb[4 * u + 2] = v.z;
+            bb[4 * u + 3] = v.w;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                float d = a[i + 4 * u + l] - bb[4 * u + l];
+                acc[u][l] = __fmaf_rn(d, d, acc[u][l]);
+            }
+    }
+    const int lim = n - (n % 4);
+    for (; i < lim; i += 4) {
+        const float4 v = __ldg(b4 + (i >> 2));
+        const float bb[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int l = 0; l < 4; l++) {
+            float d = a[i + l] - bb[l];
+            acc[0][l] = __fmaf_rn(d, d, acc[0][l]);
+        }
+    }
+    float v[4];
+#pragma unroll
+    for (int l = 0; l < 4; l++)
+        v[l] = __fadd_rn(__fadd_rn(acc[0][l], acc[1][l]), __fadd_rn(acc[2][l], acc[3][l]));
+    float sum = __fadd_rn(__fadd_rn(v[0], v[1]), __fadd_rn(v[2], v[3]));
+    for (; i < n; i++) {
+        float d = a[i] - b[i];
+        sum = __fadd_rn(sum, __fmul_rn(d, d));
+    }
+    return sum;
+}
+
 // Reference-order Manhattan distance (core/simd_kernels.inc.h:115-149, NEON).
 template <typename PA, typename PB>
 __device__ __forceinline__ float manhattan_ref(PA a, PB b, int n) {

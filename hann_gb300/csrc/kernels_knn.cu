@@ -54,8 +54,8 @@ __device__ __forceinline__ unsigned long long dkey(float d, uint32_t row) {
 
 template <int METRIC>
 __device__ __forceinline__ float metric_ref(const float* q, const float* b, int dim, float qn, float bn) {
-    if (METRIC == 0) return sqeuclid_ref(q, b, dim);
-    if (METRIC == 1) return __fsqrt_rn(sqeuclid_ref(q, b, dim));
+    if (METRIC == 0) return (dim & 3) == 0 ? sqeuclid_ref_v4(q, b, dim) : sqeuclid_ref(q, b, dim);
+    if (METRIC == 1) return __fsqrt_rn((dim & 3) == 0 ? sqeuclid_ref_v4(q, b, dim) : sqeuclid_ref(q, b, dim));
     if (METRIC == 2) return manhattan_ref(q, b, dim);
     return cosine_from_parts(dot_ref(q, b, dim), qn, bn);
 }

@@ -151,7 +151,9 @@ __global__ void __launch_bounds__(PFW_WARPS * 32) probe_final_warp_kernel(
         unsigned long long key = ~0ull;
         if (i < L) {
             const uint32_t c = (uint32_t)(band[q * lcap + i] & 0xffffffffull);
-            key = ((unsigned long long)float_key(sqeuclid_ref(qv, coarse + (int64_t)c * dim, dim)) << 32) | c;
+            const float* cr = coarse + (int64_t)c * dim;
+            const float d = (dim & 3) == 0 ? sqeuclid_ref_v4(qv, cr, dim) : sqeuclid_ref(qv, cr, dim);
+            key = ((unsigned long long)float_key(d) << 32) | c;
         }
         keys[i] = key;
     }

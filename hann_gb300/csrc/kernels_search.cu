@@ -515,6 +515,8 @@ __global__ void __launch_bounds__(RR_THREADS) rerank_warp_kernel(ScanParams p, c
                 ReconRow rec{p.coarse + (int64_t)p.row_cluster[row] * p.dim, p.codebooks,
                              p.codes + (int64_t)row * p.code_stride, p.dsub, p.pqK};
                 d = sqeuclid_ref(qv, rec, p.dim);
+            } else if ((p.dim & 3) == 0) {
+                d = sqeuclid_ref_v4(qv, p.vectors + (int64_t)row * p.dim, p.dim);
             } else {
                 d = sqeuclid_ref(qv, p.vectors + (int64_t)row * p.dim, p.dim);
             }
