@@ -298,7 +298,8 @@ __global__ void rescore_top8_kernel(const float* __restrict__ x, const float* __
     for (int c = 0; c < 8; c++) {
         const int idx = cand_idx[r * 8 + c];
         if (idx < 0 || cand_val[r * 8 + c] > thr) break;
-        const float d = sqeuclid_ref(xr, cent + (int64_t)idx * dim, dim);
+        const float* cr = cent + (int64_t)idx * dim;
+        const float d = (dim & 3) == 0 ? sqeuclid_ref_v4(xr, cr, dim) : sqeuclid_ref(xr, cr, dim);
         if (d < bd || (d == bd && idx < bi)) {
             bd = d;
             bi = idx;
