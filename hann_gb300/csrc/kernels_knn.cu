@@ -300,6 +300,55 @@ __global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
     }
 }
 
+constexpr int MW_MAX = 512;  // band list + candidates up to which one warp merges a row
+constexpr int MW_WARPS = 8;
+
+// One warp per row when the row's band list and new candidates together
+// hold at most MW_MAX keys (the probe's usual case): the same merge as
+// knn_merge_band_kernel without block barriers. A row it merges has its
+// candidate count reset, so the block kernel launched after it skips the
+// row; rows it leaves (larger, or flagged) go to the block kernel.
+__global__ void __launch_bounds__(MW_WARPS * 32) knn_merge_band_warp_kernel(
+    int nrows, int k, const int32_t* __restrict__ krow, int cap, int lcap, int32_t* __restrict__ cnt,
+    const int32_t* __restrict__ cand_id, const float* __restrict__ cand_s, const float* __restrict__ e2,
+    const float* __restrict__ asl, unsigned long long* __restrict__ list, int32_t* __restrict__ lcount,
+    float* __restrict__ thr, const int32_t* __restrict__ need_exact) {
+    __shared__ unsigned long long keys_all[MW_WARPS][MW_MAX];
+    __shared__ unsigned int hist_all[MW_WARPS][256];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t r = (int64_t)blockIdx.x * MW_WARPS + w;
+    if (r >= nrows) return;
+    const int c = cnt[r];
+    const int L = lcount[r];
+    if (c == 0 || need_exact[r] || c > cap || L + c > MW_MAX) return;
+    unsigned long long* keys = keys_all[w];
+    const int kr = krow ? max(1, min(krow[r], k)) : k;
+    for (int i = lane; i < L; i += 32) keys[i] = list[r * lcap + i];
+    for (int i = lane; i < c; i += 32) keys[L + i] = dkey(cand_s[r * cap + i], (uint32_t)cand_id[r * cap + i]);
+    const int T = L + c;
+    __syncwarp();
+    float t_new = __int_as_float(0x7f800000);
+    if (T >= kr) {
+        const unsigned long long K = warp_radix_nth_u64(keys, T, kr, hist_all[w]);
+        const float tk = key_float((uint32_t)(K >> 32));
+        t_new = tk + e2[r] + 2e-5f * (fabsf(tk) + asl[r]);
+    }
+    int m = 0;
+    for (int i0 = 0; i0 < T; i0 += 32) {
+        const int i = i0 + lane;
+        const unsigned long long key = i < T ? keys[i] : 0ull;
+        const bool keep = i < T && key_float((uint32_t)(key >> 32)) <= t_new;
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        if (keep) list[r * lcap + m + __popc(b & ((1u << lane) - 1u))] = key;
+        m += __popc(b);
+    }
+    if (lane == 0) {
+        lcount[r] = m;  // m <= T <= MW_MAX <= lcap
+        thr[r] = t_new;
+        cnt[r] = 0;
+    }
+}
+
 // Exact rescoring of each query's band and the final top k, written as
 // (id, distance). Queries flagged need_exact are appended to exact_list.
 template <int METRIC>
@@ -551,6 +600,9 @@ cudaError_t launch_knn_merge_band(int nrows, int k, const int32_t* krow, int cap
     const size_t smem = knn_merge_band_smem(lcap, cap);
     cudaError_t e = set_smem_attr((const void*)knn_merge_band_kernel, smem);
     if (e != cudaSuccess) return e;
+    if (lcap >= MW_MAX)
+        knn_merge_band_warp_kernel<<<(unsigned)ceil_div(nrows, MW_WARPS), MW_WARPS * 32, 0, s>>>(
+            nrows, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact);
     knn_merge_band_kernel<<<(unsigned)nrows, KM_THREADS, smem, s>>>(k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl,
                                                                     list, lcount, thr, need_exact);
     return cudaGetLastError();

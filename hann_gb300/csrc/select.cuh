@@ -146,6 +146,94 @@ __device__ __forceinline__ void sort_u64(unsigned long long* key, int P) {
     }
 }
 
+// The n-th smallest (1-based, 1 <= n <= len) of the 64-bit keys in the
+// warp's shared memory, warp-synchronous: 8-bit digits from the highest bit
+// where the keys differ, one warp-private histogram of 256 counters; once
+// the chosen digit holds a single key, that key is the answer.
+__device__ __forceinline__ unsigned long long warp_radix_nth_u64(const unsigned long long* keys, int len, int n,
+                                                                 unsigned int* hist) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long a = ~0ull, o = 0ull;
+    for (int i = lane; i < len; i += 32) {
+        a &= keys[i];
+        o |= keys[i];
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        a &= __shfl_xor_sync(0xffffffffu, a, s);
+        o |= __shfl_xor_sync(0xffffffffu, o, s);
+    }
+    const unsigned long long diff = a ^ o;
+    if (diff == 0) return a;
+    const int top = 63 - __clzll((long long)diff);
+    unsigned long long prefix = top == 63 ? 0ull : (a & (~0ull << (top + 1)));
+    uint32_t rem = (uint32_t)n;
+    for (int hi = top; hi >= 0; hi -= 8) {
+        const int lo = hi >= 7 ? hi - 7 : 0;
+        const unsigned long long himask = hi == 63 ? 0ull : (~0ull << (hi + 1));
+        const unsigned dmask = (1u << (hi - lo + 1)) - 1u;
+#pragma unroll
+        for (int b = 0; b < 8; b++) hist[b * 32 + lane] = 0;
+        __syncwarp();
+        for (int i0 = 0; i0 < len; i0 += 32) {
+            const int i = i0 + lane;
+            unsigned bin = 0xffffffffu;
+            if (i < len) {
+                const unsigned long long k = keys[i];
+                if ((k & himask) == prefix) bin = (unsigned)(k >> lo) & dmask;
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, bin);
+            if (bin != 0xffffffffu && lane == __ffs(peers) - 1) hist[bin] += __popc(peers);
+            __syncwarp();
+        }
+        uint32_t cnt[8], tot = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            cnt[j] = hist[lane * 8 + j];
+            tot += cnt[j];
+        }
+        uint32_t incl = tot;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, s);
+            if (lane >= s) incl += t;
+        }
+        const uint32_t excl = incl - tot;
+        const bool mine = excl < rem && rem <= incl;
+        uint32_t pick = 0, below = 0, inbin = 0;
+        if (mine) {
+            uint32_t cum = excl;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                if (cum < rem && rem <= cum + cnt[j]) {
+                    pick = (uint32_t)(lane * 8 + j);
+                    below = cum;
+                    inbin = cnt[j];
+                }
+                cum += cnt[j];
+            }
+        }
+        const int owner = __ffs(__ballot_sync(0xffffffffu, mine)) - 1;
+        pick = __shfl_sync(0xffffffffu, pick, owner);
+        below = __shfl_sync(0xffffffffu, below, owner);
+        inbin = __shfl_sync(0xffffffffu, inbin, owner);
+        __syncwarp();
+        prefix |= (unsigned long long)pick << lo;
+        rem -= below;
+        if (lo > 0 && inbin == 1) {
+            // a single key carries the chosen prefix: it is the answer
+            const unsigned long long pm = ~0ull << lo;
+            unsigned long long found = 0ull;
+            for (int i = lane; i < len; i += 32)
+                if ((keys[i] & pm) == prefix) found = keys[i];
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) found |= __shfl_xor_sync(0xffffffffu, found, s);
+            return found;
+        }
+    }
+    return prefix;
+}
+
 // Warp-synchronous bitonic sort of P (a power of two) 64-bit keys in the
 // warp's shared memory, ascending.
 __device__ __forceinline__ void warp_sort_u64(unsigned long long* key, int P) {
