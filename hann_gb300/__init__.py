@@ -97,6 +97,7 @@ EXPORTED = (
     "hann_pqivf_stage_times", "hann_pqivf_list_lengths", "hann_pqivf_search_batch_device_noalloc",
     "hann_gpu_distance_matrix", "hann_knn_new", "hann_knn_free", "hann_knn_last_error", "hann_knn_search",
     "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn", "hann_pqivf_set_plain_fp32",
+    "hann_serve_submit_priority", "hann_serve_cancel",
 )
 
 
@@ -699,6 +700,9 @@ def _serve_lib():
     L.hann_serve_start.argtypes = [_P, ctypes.POINTER(_ServeOptions), ctypes.POINTER(_P)]
     L.hann_serve_submit.argtypes = [_P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                     ctypes.POINTER(ctypes.c_uint64)]
+    L.hann_serve_submit_priority.argtypes = [_P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)]
+    L.hann_serve_cancel.argtypes = [_P, ctypes.c_uint64]
     L.hann_serve_submit_add.argtypes = [_P, _P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
     L.hann_serve_submit_delete.argtypes = [_P, _P, ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
     L.hann_serve_wait.argtypes = [_P, ctypes.c_uint64, _P, _P, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
@@ -735,13 +739,29 @@ class Server:
         if rc != HANN_OK:
             raise HannError(rc, self._L.hann_serve_last_error(self._h).decode())
 
-    def submit(self, queries, k: int, nprobe: int = 0) -> int:
+    def submit(self, queries, k: int, nprobe: int = 0, priority: int = 0) -> int:
+        """Queue a search; priority 1 goes ahead of every normal one still queued."""
         q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self._dim)
         t = ctypes.c_uint64(0)
-        self._check(self._L.hann_serve_submit(self._h, _ptr(q), q.shape[0], int(k), int(nprobe), ctypes.byref(t)))
+        if priority:
+            self._check(self._L.hann_serve_submit_priority(self._h, _ptr(q), q.shape[0], int(k), int(nprobe),
+                                                           int(priority), ctypes.byref(t)))
+        else:
+            self._check(self._L.hann_serve_submit(self._h, _ptr(q), q.shape[0], int(k), int(nprobe),
+                                                  ctypes.byref(t)))
         with self._meta_lock:
             self._meta[t.value] = (q.shape[0], int(k))
         return t.value
+
+    def cancel(self, ticket: int) -> bool:
+        """Withdraw a queued search: True if it had not started (its wait then
+        raises), False if it already runs or finished."""
+        rc = self._L.hann_serve_cancel(self._h, ctypes.c_uint64(ticket))
+        if rc == HANN_OK:
+            return True
+        if rc == HANN_E_STATE:
+            return False
+        raise HannError(rc, "unknown ticket")
 
     def submit_add(self, ids, matrix) -> int:
         ids = np.ascontiguousarray(ids, dtype=np.int64)

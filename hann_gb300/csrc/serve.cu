@@ -43,6 +43,7 @@ struct Request {
     std::vector<int64_t> out_ids;
     std::vector<double> out_dist;
     std::vector<int32_t> out_n;
+    int priority = 0;  // 1: taken before every normal request still queued
     int status = 1;  // 1 pending, 0 done, <0 error
     std::string error;
     Clock::time_point t_submit, t_done;
@@ -77,6 +78,7 @@ struct hann_server {
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<std::shared_ptr<Request>> queue;
+    std::deque<std::shared_ptr<Request>> queue_hi;  // high-priority searches, taken first
     std::unordered_map<uint64_t, std::shared_ptr<Request>> tickets;
     uint64_t next_ticket = 1;
     bool stop = false;
@@ -271,7 +273,7 @@ void scheduler(hann_server* s) {
             }
         }
         if (!any_busy && s->read_lock.owns_lock()) s->read_lock.unlock();
-        if (s->stop && s->queue.empty() && !any_busy) break;
+        if (s->stop && s->queue.empty() && s->queue_hi.empty() && !any_busy) break;
         // 2. mutations at the head of the queue go to the mutation thread
         while (!s->queue.empty() && s->queue.front()->kind != 0) {
             s->mqueue.push_back(s->queue.front());
@@ -285,16 +287,21 @@ void scheduler(hann_server* s) {
                 s->drained = true;
                 s->cv_mut.notify_one();
             }
-        } else if (!s->queue.empty()) {
-            // 3. pack waiting searches into every free slot
-            for (size_t i = 0; i < s->slots.size() && !s->queue.empty() && s->queue.front()->kind == 0; i++) {
+        } else if (!s->queue.empty() || !s->queue_hi.empty()) {
+            // 3. pack waiting searches into every free slot, high priority first
+            auto next = [&]() -> std::deque<std::shared_ptr<Request>>* {
+                if (!s->queue_hi.empty()) return &s->queue_hi;
+                if (!s->queue.empty() && s->queue.front()->kind == 0) return &s->queue;
+                return nullptr;
+            };
+            for (size_t i = 0; i < s->slots.size() && next(); i++) {
                 Slot& sl = *s->slots[i];
                 if (sl.busy) continue;
                 std::vector<std::shared_ptr<Request>> take;
                 int64_t nq = 0, probes = 0;
                 int kmax = 1, npm = 1;
-                while (!s->queue.empty() && s->queue.front()->kind == 0) {
-                    auto& r = s->queue.front();
+                while (auto* qq = next()) {
+                    auto& r = qq->front();
                     const int64_t nq2 = nq + r->nq;
                     const int k2 = std::max(kmax, r->k), np2 = std::max(npm, std::min(r->nprobe, h->nlist));
                     const int64_t pr2 = probes + (int64_t)r->nq * std::min(r->nprobe, h->nlist);
@@ -304,7 +311,7 @@ void scheduler(hann_server* s) {
                             // a request that can never fit
                             r->status = HANN_E_UNSUPPORTED;
                             r->error = "request exceeds the server's per-batch query or memory limit";
-                            s->queue.pop_front();
+                            qq->pop_front();
                             s->cv_done.notify_all();
                             continue;
                         }
@@ -315,7 +322,7 @@ void scheduler(hann_server* s) {
                     npm = np2;
                     probes = pr2;
                     take.push_back(r);
-                    s->queue.pop_front();
+                    qq->pop_front();
                 }
                 if (take.empty()) continue;
                 if (!s->read_lock.owns_lock()) s->read_lock = std::shared_lock<std::shared_mutex>(h->mu);
@@ -338,7 +345,7 @@ void scheduler(hann_server* s) {
             lk.unlock();
             std::this_thread::sleep_for(std::chrono::microseconds(50));
             lk.lock();
-        } else if (s->queue.empty() && !s->stop) {
+        } else if (s->queue.empty() && s->queue_hi.empty() && !s->stop) {
             s->cv_work.wait_for(lk, std::chrono::milliseconds(5));
         }
     }
@@ -444,7 +451,8 @@ static int submit(hann_server* s, std::shared_ptr<Request> r, uint64_t* ticket) 
         s->any = true;
     }
     s->tickets[r->ticket] = r;
-    s->queue.push_back(r);
+    if (r->kind == 0 && r->priority > 0) s->queue_hi.push_back(r);
+    else s->queue.push_back(r);
     s->cv_work.notify_one();
     if (ticket) *ticket = r->ticket;
     return HANN_OK;
@@ -462,6 +470,44 @@ int hann_serve_submit(hann_server* s, const float* queries, int32_t nq, int32_t 
     r->nprobe = nprobe;
     r->queries.assign(queries, queries + (size_t)nq * s->h->o.dimension);
     return submit(s, r, ticket);
+}
+
+int hann_serve_submit_priority(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe,
+                               int32_t priority, uint64_t* ticket) {
+    if (!s || !queries || nq <= 0) return HANN_E_INVALID;
+    if (k <= 0 || k > s->o.max_k) return HANN_E_INVALID;
+    if (nprobe <= 0) nprobe = s->h->o.candidate_clusters;
+    if (nprobe > s->o.max_nprobe) nprobe = s->o.max_nprobe;
+    auto r = std::make_shared<Request>();
+    r->kind = 0;
+    r->nq = nq;
+    r->k = k;
+    r->nprobe = nprobe;
+    r->priority = priority > 0 ? 1 : 0;
+    r->queries.assign(queries, queries + (size_t)nq * s->h->o.dimension);
+    return submit(s, r, ticket);
+}
+
+int hann_serve_cancel(hann_server* s, uint64_t ticket) {
+    if (!s) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return HANN_E_NOT_FOUND;
+    auto r = it->second;
+    for (auto* qq : {&s->queue_hi, &s->queue}) {
+        for (auto q = qq->begin(); q != qq->end(); ++q) {
+            if (q->get() != r.get()) continue;
+            if (r->kind != 0) break;  // mutations are not cancelled
+            qq->erase(q);
+            r->status = HANN_E_STATE;
+            r->error = "request cancelled";
+            r->t_done = Clock::now();
+            s->cv_done.notify_all();
+            return HANN_OK;
+        }
+    }
+    s->err = "request already started or finished";
+    return HANN_E_STATE;
 }
 
 int hann_serve_submit_add(hann_server* s, const int64_t* ids, const float* vectors, int64_t n, uint64_t* ticket) {

@@ -194,6 +194,15 @@ void hann_serve_options_init(hann_serve_options* opts);
 int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server** out);
 /* Queues nq queries (copied) with one k and nprobe; returns a ticket. */
 int hann_serve_submit(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe, uint64_t* ticket);
+/* hann_serve_submit with a priority: 1 puts the request ahead of every
+ * normal-priority search still queued (no reference counterpart). */
+int hann_serve_submit_priority(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe,
+                               int32_t priority, uint64_t* ticket);
+/* Withdraws a search that has not started: HANN_OK and the ticket's wait
+ * returns HANN_E_STATE ("request cancelled"); HANN_E_STATE when it already
+ * runs or finished (its wait returns the results); HANN_E_NOT_FOUND for an
+ * unknown ticket. Mutations are not cancelled (no reference counterpart). */
+int hann_serve_cancel(hann_server* s, uint64_t ticket);
 /* Queues a BulkAdd / BulkDelete, applied in order beside the running
  * batches; a search submitted after the mutation's ticket was waited for
  * sees it. */

@@ -121,3 +121,29 @@ def test_admission_by_memory_budget(index):
         assert st["requests"] == 12
     finally:
         srv.stop()
+
+
+def test_priority_and_cancel(index):
+    """A high-priority search returns the same results as a normal one; a
+    cancelled search either had not started (its wait raises) or had (its
+    wait returns its results)."""
+    idx, x, rng = index
+    q = rng.normal(size=(40, x.shape[1])).astype(np.float32)
+    with hg.Server(idx, slots=1, max_batch_queries=64, max_k=10, max_nprobe=16) as srv:
+        normal = [srv.submit(q, 10, 16) for _ in range(12)]
+        hi = srv.submit(q, 10, 16, priority=1)
+        victim = srv.submit(q, 10, 16)
+        cancelled = srv.cancel(victim)
+        r_hi = srv.wait(hi)
+        r_n = srv.wait(normal[-1])
+        np.testing.assert_array_equal(r_hi[0], r_n[0])
+        np.testing.assert_array_equal(r_hi[1], r_n[1])
+        if cancelled:
+            with pytest.raises(hg.HannError, match="cancelled"):
+                srv.wait(victim)
+        else:
+            assert (srv.wait(victim)[2] == 10).all()
+        for t in normal[:-1]:
+            srv.wait(t)
+        with pytest.raises(hg.HannError):
+            srv.cancel(123456789)
