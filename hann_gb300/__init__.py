@@ -97,7 +97,7 @@ EXPORTED = (
     "hann_pqivf_stage_times", "hann_pqivf_list_lengths", "hann_pqivf_search_batch_device_noalloc",
     "hann_gpu_distance_matrix", "hann_knn_new", "hann_knn_free", "hann_knn_last_error", "hann_knn_search",
     "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn", "hann_pqivf_set_plain_fp32",
-    "hann_serve_submit_priority", "hann_serve_cancel",
+    "hann_serve_submit_priority", "hann_serve_cancel", "hann_pqivf_set_candidate_clusters",
 )
 
 
@@ -139,6 +139,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_gpu_distance_batch.argtypes = [ctypes.c_int32, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
         L.hann_pqivf_list_lengths.argtypes = [_P, _P]
         L.hann_gpu_distance_matrix.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64,
@@ -392,6 +393,44 @@ class Index:
         self._check(self._L.hann_pqivf_search_batch_device(
             self._h, ctypes.c_void_p(d_queries), int(nq), int(k), int(nprobe), int(mode), ctypes.c_void_p(d_ids),
             ctypes.c_void_p(d_dist), ctypes.c_void_p(d_nout), ctypes.c_void_p(stream)))
+
+    def SetCandidateClusters(self, n: int) -> None:
+        """The default nprobe of Search (WithCandidateClusters on a live index)."""
+        self._check(self._L.hann_pqivf_set_candidate_clusters(self._h, int(n)))
+
+    def TuneCandidateClusters(self, queries, k: int, target_recall: float, ladder=None, mode: int = 1,
+                              ground_truth=None, apply: bool = True):
+        """The smallest nprobe of `ladder` whose recall@k on `queries` reaches
+        `target_recall` against exact k-NN over the stored vectors (computed on
+        the GPU by the batched exact k-NN unless ground_truth ids are given).
+        Returns (nprobe, {nprobe: recall}); with apply, the index's default
+        nprobe becomes the chosen value. When no value reaches the target the
+        largest is chosen."""
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self._dim)
+        if ground_truth is None:
+            st = self.export_state()
+            flat = np.ascontiguousarray(st["vectors"], dtype=np.float32)
+            rows, _ = knn(q, flat, k, "squared_euclidean")
+            ground_truth = np.where(rows >= 0, np.asarray(st["ids"])[np.maximum(rows, 0)], -1)
+        gt = np.asarray(ground_truth)
+        nlist = self.DeviceStats()["nlist"]
+        if ladder is None:
+            ladder = [p for p in (1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096) if p <= nlist]
+            if not ladder or ladder[-1] != min(nlist, 4096):
+                ladder.append(min(nlist, 4096))
+        rec = {}
+        chosen = ladder[-1]
+        for p in ladder:
+            ids, _, n = self.SearchBatch(q, k, nprobe=p, mode=mode)
+            hits = sum(len(set(ids[i, :n[i]].tolist()) & set(gt[i][gt[i] >= 0].tolist())) for i in range(len(q)))
+            tot = int((gt >= 0).sum())
+            rec[p] = hits / tot if tot else 1.0
+            if rec[p] >= target_recall:
+                chosen = p
+                break
+        if apply:
+            self.SetCandidateClusters(chosen)
+        return chosen, rec
 
     def SetPlainFP32(self, on: bool) -> None:
         """Switch the FP32 SIMT-only mode (same results, no tensor cores)."""

@@ -1130,6 +1130,15 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
     return run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
 }
 
+int hann_pqivf_set_candidate_clusters(hann_pqivf* h, int32_t n) {
+    if (!h) return HANN_E_INVALID;
+    if (n <= 0) return h->fail(HANN_E_INVALID, "candidate clusters must be positive");
+    std::unique_lock<std::mutex> w(h->wmu);
+    std::unique_lock<std::shared_mutex> g(h->mu);
+    h->o.candidate_clusters = n;
+    return HANN_OK;
+}
+
 int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on) {
     if (!h) return HANN_E_INVALID;
     std::unique_lock<std::mutex> w(h->wmu);

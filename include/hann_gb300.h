@@ -124,6 +124,10 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
                                    int32_t mode, int64_t* d_ids, double* d_distances, int32_t* d_n_out,
                                    void* stream);
 
+/* Sets the default nprobe (WithCandidateClusters, pqivf/index.go:86-94) of a
+ * live index, e.g. to the value a recall-target tuning picked. */
+int hann_pqivf_set_candidate_clusters(hann_pqivf* h, int32_t n);
+
 /* Switches the plain-FP32 mode of hann_pqivf_options at run time (no
  * reference counterpart; results do not change). */
 int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on);

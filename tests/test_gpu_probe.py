@@ -79,3 +79,24 @@ def test_plain_fp32_mode_gives_identical_index_and_results(built, gpu):
     rb = b.SearchBatch(q, 10, nprobe=40, mode=1)
     for u, v in zip(rc, rb):
         np.testing.assert_array_equal(u, v)
+
+
+def test_tune_candidate_clusters(built, gpu):
+    """The tuned nprobe is the smallest of the ladder whose recall@10 against
+    exact k-NN over the stored vectors reaches the target, and it becomes the
+    index's default nprobe."""
+    import hann_gb300 as hg
+    idx, q = build(12000, 32, 512, 41)
+    chosen, rec = idx.TuneCandidateClusters(q[:64], 10, 0.9)
+    assert rec[chosen] >= 0.9 or chosen == max(rec)
+    assert all(r < 0.9 for p, r in rec.items() if p < chosen)
+    # exact k-NN from the same stored vectors gives the same ground truth
+    st = idx.export_state()
+    rows, _ = hg.knn(q[:64], st["vectors"], 10)
+    gt = np.asarray(st["ids"])[rows]
+    chosen2, rec2 = idx.TuneCandidateClusters(q[:64], 10, 0.9, ground_truth=gt, apply=False)
+    assert chosen2 == chosen and rec2 == rec
+    # the default nprobe now is `chosen`: Search without nprobe equals nprobe=chosen
+    a = idx.SearchBatch(q[:8], 10, mode=1)
+    b = idx.SearchBatch(q[:8], 10, nprobe=chosen, mode=1)
+    np.testing.assert_array_equal(a[0], b[0])
