@@ -330,9 +330,43 @@ __global__ void pq_accumulate_kernel(const float* __restrict__ res, int64_t n, i
     if (i == 0) atomicAdd(reinterpret_cast<unsigned long long*>(&counts[(int64_t)m * pqK + c]), 1ull);
 }
 
+// One subquantizer's sums, accumulated per block in shared memory (FP64)
+// and added to the global sums once per block: every codeword is hit by
+// thousands of points, so direct global atomics serialise on it.
+__global__ void pq_accumulate_smem_kernel(const float* __restrict__ res, int64_t n, int M, int dsub,
+                                          const int32_t* __restrict__ codes, int pqK, int m,
+                                          double* __restrict__ sums, int64_t* __restrict__ counts) {
+    extern __shared__ __align__(16) double psum[];  // [pqK * dsub], then pqK counts
+    unsigned long long* pcnt = reinterpret_cast<unsigned long long*>(psum + pqK * dsub);
+    for (int i = threadIdx.x; i < pqK * dsub; i += blockDim.x) psum[i] = 0.0;
+    for (int i = threadIdx.x; i < pqK; i += blockDim.x) pcnt[i] = 0ull;
+    __syncthreads();
+    const int dim = M * dsub;
+    const int64_t per = ceil_div(n, gridDim.x);
+    const int64_t p0 = blockIdx.x * per, p1 = min(n, p0 + per);
+    for (int64_t e = p0 * dsub + threadIdx.x; e < p1 * dsub; e += blockDim.x) {
+        const int64_t p = e / dsub;
+        const int i = (int)(e - p * dsub);
+        const int c = codes[p * M + m];
+        atomicAdd(&psum[c * dsub + i], (double)res[p * dim + m * dsub + i]);
+        if (i == 0) atomicAdd(&pcnt[c], 1ull);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < pqK * dsub; i += blockDim.x)
+        if (psum[i] != 0.0) atomicAdd(&sums[(int64_t)m * pqK * dsub + i], psum[i]);
+    for (int i = threadIdx.x; i < pqK; i += blockDim.x)
+        if (pcnt[i]) atomicAdd(reinterpret_cast<unsigned long long*>(&counts[(int64_t)m * pqK + i]), pcnt[i]);
+}
+
 cudaError_t launch_pq_accumulate(const float* res, int64_t n, int M, int dsub, const int32_t* codes, int pqK,
                                  int m_begin, int m_end, double* sums, int64_t* counts, cudaStream_t s) {
     if (n <= 0 || m_end <= m_begin) return cudaSuccess;
+    const size_t smem = (size_t)pqK * dsub * sizeof(double) + (size_t)pqK * sizeof(unsigned long long);
+    if (m_end - m_begin == 1 && smem <= 48 * 1024 && n >= 4096) {
+        const unsigned blocks = (unsigned)std::min<int64_t>(4 * 152, ceil_div(n, 1024));
+        pq_accumulate_smem_kernel<<<blocks, 256, smem, s>>>(res, n, M, dsub, codes, pqK, m_begin, sums, counts);
+        return cudaGetLastError();
+    }
     const int64_t total = n * (int64_t)(m_end - m_begin) * dsub;
     pq_accumulate_kernel<<<(unsigned)ceil_div(total, 256), 256, 0, s>>>(res, n, M, dsub, codes, pqK, m_begin,
                                                                        m_end - m_begin, sums, counts);
@@ -406,17 +440,90 @@ __global__ void __launch_bounds__(256) encode_kernel(const float* __restrict__ x
     }
 }
 
+// encode_kernel with the sub-vector length known at compile time: each
+// residual sub-vector (FP32 x - c, as the reference's residual) is formed once
+// in registers instead of at every codeword.
+template <int DSUB>
+__global__ void __launch_bounds__(256) encode_fixed_kernel(const float* __restrict__ x,
+                                                           const int64_t* __restrict__ rows,
+                                                           const int32_t* __restrict__ cluster, int64_t n, int dim,
+                                                           const float* __restrict__ coarse,
+                                                           const float* __restrict__ cb, int M, int pqK,
+                                                           uint8_t* __restrict__ codes, int code_stride,
+                                                           float* __restrict__ term) {
+    extern __shared__ __align__(16) float scb[];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    const int64_t p = live ? (rows ? rows[i] : i) : 0;
+    const int cl = live ? cluster[p] : 0;
+    const float* xp = x + p * dim;
+    const float* cp = coarse + (int64_t)cl * dim;
+    float tsum = 0.0f;
+    for (int m = 0; m < M; m++) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < pqK * DSUB; e += blockDim.x) scb[e] = cb[(int64_t)m * pqK * DSUB + e];
+        __syncthreads();
+        if (!live) continue;
+        float r[DSUB];
+#pragma unroll
+        for (int e = 0; e < DSUB; e++) r[e] = xp[m * DSUB + e] - cp[m * DSUB + e];
+        float bd = sqeuclid_ref(r, scb, DSUB);
+        int bi = 0;
+        for (int j = 1; j < pqK; j++) {
+            const float d = sqeuclid_ref(r, scb + j * DSUB, DSUB);
+            if (d < bd) {
+                bd = d;
+                bi = j;
+            }
+        }
+        codes[p * code_stride + m] = (uint8_t)bi;
+        const float* w = scb + bi * DSUB;
+        for (int e = 0; e < DSUB; e++) tsum += w[e] * (w[e] + 2.0f * cp[m * DSUB + e]);
+    }
+    if (live) {
+        for (int m = M; m < code_stride; m++) codes[p * code_stride + m] = 0;
+        term[p] = tsum;
+    }
+}
+
 cudaError_t launch_encode(const float* x, const int64_t* rows, const int32_t* cluster, int64_t n, int dim,
                           const float* coarse, const float* codebooks, int M, int pqK, uint8_t* codes,
                           int code_stride, float* term, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    const size_t smem = (size_t)pqK * (dim / M) * sizeof(float);
+    const int dsub = dim / M;
+    const size_t smem = (size_t)pqK * dsub * sizeof(float);
+    const unsigned grid = (unsigned)ceil_div(n, 256);
+    if (smem <= 48 * 1024) {
+        switch (dsub) {
+        case 1:
+            encode_fixed_kernel<1><<<grid, 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK,
+                                                          codes, code_stride, term);
+            return cudaGetLastError();
+        case 2:
+            encode_fixed_kernel<2><<<grid, 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK,
+                                                          codes, code_stride, term);
+            return cudaGetLastError();
+        case 4:
+            encode_fixed_kernel<4><<<grid, 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK,
+                                                          codes, code_stride, term);
+            return cudaGetLastError();
+        case 8:
+            encode_fixed_kernel<8><<<grid, 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK,
+                                                          codes, code_stride, term);
+            return cudaGetLastError();
+        case 16:
+            encode_fixed_kernel<16><<<grid, 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK,
+                                                          codes, code_stride, term);
+            return cudaGetLastError();
+        default: break;
+        }
+    }
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(encode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    encode_kernel<<<(unsigned)ceil_div(n, 256), 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK,
-                                                                codes, code_stride, term);
+    encode_kernel<<<grid, 256, smem, s>>>(x, rows, cluster, n, dim, coarse, codebooks, M, pqK, codes, code_stride,
+                                          term);
     return cudaGetLastError();
 }
 
