@@ -787,7 +787,8 @@ def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
             "queries_per_s": st["queries_per_s"], "offered_requests_per_s": rate,
             "recall_at_10_k_ge_10": hits / tot if tot else None,
             "peak_admitted_bytes": int(st["peak_admitted_bytes"]), "relayouts": int(st["relayouts"]),
-            "mutation_ms_total": round(st["mutation_ms"], 1),
+            "mutation_ms_total": round(st["mutation_ms"], 1), "relayout_drain_ms_total": round(st["drain_ms"], 1),
+            "relayout_ms_total": round(st["relayout_ms"], 1), "relayout_max_ms": round(st["relayout_max_ms"], 1),
             "stream": "Poisson arrivals; 1-512 queries/request log-uniform; k U[1,100]; nprobe log-U[8,256]; "
                       "BulkAdd 1000-vector chunks and Deletes at 1% of the request rate; exact rerank",
             "max_batch_probes": args.serve_batch_probes}

@@ -727,7 +727,8 @@ class _ServeStats(ctypes.Structure):
     _fields_ = [("requests", ctypes.c_int64), ("queries", ctypes.c_int64), ("batches", ctypes.c_int64),
                 ("mutations", ctypes.c_int64), ("peak_admitted_bytes", ctypes.c_int64), ("p50_ms", ctypes.c_double),
                 ("p99_ms", ctypes.c_double), ("queries_per_s", ctypes.c_double), ("relayouts", ctypes.c_int64),
-                ("mutation_ms", ctypes.c_double)]
+                ("mutation_ms", ctypes.c_double), ("drain_ms", ctypes.c_double), ("relayout_ms", ctypes.c_double),
+                ("relayout_max_ms", ctypes.c_double)]
 
 
 def _serve_lib():

@@ -123,6 +123,13 @@ static int upload_lens(hann_pqivf* h) {
 // BF16 centroids, their FP32 squared norms and the largest norm, for the
 // tensor-core preselection (dimensions up to 128).
 static int prepare_coarse(hann_pqivf* h) {
+    if (h->nlist > 0 && h->pqk_eff > 0) {
+        const size_t ncb = (size_t)h->o.num_subquantizers * h->pqk_eff * h->dsub;
+        CK(h->d_codebooks_t.reserve(ncb));
+        CK(launch_transpose_codebooks(h->d_codebooks.p, h->o.num_subquantizers, h->pqk_eff, h->dsub,
+                                      h->d_codebooks_t.p, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
     h->tc = !h->o.plain_fp32 && h->o.dimension <= 128 && h->nlist > 0;
     if (!h->tc) return HANN_OK;
     h->kp = gemm_kpad(h->o.dimension);

@@ -178,6 +178,7 @@ struct hann_pqivf {
     int64_t rows_cap = 0;
 
     DBuf<float> d_coarse, d_codebooks, d_vectors, d_term;
+    DBuf<float> d_codebooks_t;  // [pqK][M][dsub], the scan's table-build layout
     // BF16 copy of the coarse centroids for the tensor-core preselection
     int kp = 0;
     bool tc = false;
@@ -236,6 +237,7 @@ struct hann_pqivf {
         p.code_stride = code_stride;
         p.coarse = d_coarse.p;
         p.codebooks = d_codebooks.p;
+        p.codebooks_t = d_codebooks_t.p;
         p.list_start = d_start.p;
         p.list_len = d_len.p;
         p.codes = d_codes.p;

@@ -136,6 +136,7 @@ struct ScanParams {
     int dim, M, dsub, pqK, nlist, code_stride;
     const float* coarse;      // [nlist][dim]
     const float* codebooks;   // [M][pqK][dsub]
+    const float* codebooks_t; // [pqK][M][dsub]: codeword j of every subquantizer in one row
     const int64_t* list_start;  // [nlist] first row of each list
     const int32_t* list_len;    // [nlist]
     const uint8_t* codes;     // [rows][code_stride]
@@ -183,6 +184,8 @@ cudaError_t launch_scan_words_lists(const uint8_t* codes, int code_stride, int M
 cudaError_t launch_scan_words_rows(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
                                    const int64_t* sw_start, const int64_t* rows, const int32_t* cluster, int64_t n,
                                    uint16_t* scanw, cudaStream_t s);
+// Codebooks [M][pqK][dsub] -> [pqK][M][dsub] (the scan's table-build layout).
+cudaError_t launch_transpose_codebooks(const float* cb, int M, int pqK, int dsub, float* out, cudaStream_t s);
 cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
                              const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
                              int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,

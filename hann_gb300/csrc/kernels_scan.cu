@@ -25,6 +25,8 @@
 // lowers the threshold. At the end warp 0 selects the query's R best from the
 // warps' survivors. Candidates leave unsorted: the rerank sorts them by exact
 // distance.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -187,18 +189,38 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
     const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const float* qv = Q + q * p.dim;
     if (tid == 0) s_tau = KEY_INF;
-    for (int e = tid; e < 256 * 32; e += THREADS) {
-        const int j = e >> 5, bk = e & 31;
-        float v = 0.0f;
-        if (bk < copies * M && j < p.pqK) {
-            const int m = bk % M;
-            const float* cw = p.codebooks + ((int64_t)m * p.pqK + j) * p.dsub;
-            const float* qm = qv + m * p.dsub;
-            float acc = 0.0f;
-            for (int t = 0; t < p.dsub; t++) acc = fmaf(qm[t], cw[t], acc);
-            v = -2.0f * acc;
+    {
+        // Lane l fills bank l of table rows w, w + WARPS, ...: subquantizer
+        // m = l % M. Codeword j of every subquantizer sits in one row of the
+        // transposed codebooks, so a warp's loads for one table row are one
+        // contiguous read (the [M][pqK] layout spread them over M rows 1 KB+
+        // apart).
+        const bool own = lane < copies * M;
+        const int m = lane % M;
+        const float* qm = qv + m * p.dsub;
+        const bool v4 = (p.dsub & 3) == 0 &&
+                        ((reinterpret_cast<uintptr_t>(qv) | reinterpret_cast<uintptr_t>(p.codebooks_t)) & 15) == 0;
+        for (int j = w; j < 256; j += WARPS) {
+            float v = 0.0f;
+            if (own && j < p.pqK) {
+                const float* cw = p.codebooks_t + ((int64_t)j * M + m) * p.dsub;
+                float acc = 0.0f;
+                if (v4) {
+                    for (int t = 0; t < p.dsub; t += 4) {
+                        const float4 a = __ldg(reinterpret_cast<const float4*>(qm + t));
+                        const float4 b = __ldg(reinterpret_cast<const float4*>(cw + t));
+                        acc = fmaf(a.x, b.x, acc);
+                        acc = fmaf(a.y, b.y, acc);
+                        acc = fmaf(a.z, b.z, acc);
+                        acc = fmaf(a.w, b.w, acc);
+                    }
+                } else {
+                    for (int t = 0; t < p.dsub; t++) acc = fmaf(qm[t], cw[t], acc);
+                }
+                v = -2.0f * acc;
+            }
+            lut[j * 32 + lane] = v;
         }
-        lut[e] = v;
     }
     __syncthreads();
     const unsigned char* lutb = reinterpret_cast<const unsigned char*>(lut);
@@ -507,7 +529,28 @@ __global__ void order_scatter_kernel(const int32_t* __restrict__ probe_ids, int6
     if (q < nq) order[atomicAdd(&cursor[probe_ids[q * np_max]], 1)] = (int32_t)q;
 }
 
+__global__ void transpose_codebooks_kernel(const float* __restrict__ cb, int M, int pqK, int dsub,
+                                           float* __restrict__ out) {
+    const int64_t total = (int64_t)M * pqK * dsub;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int t = (int)(e % dsub);
+        const int64_t r = e / dsub;
+        const int m = (int)(r % M);
+        const int j = (int)(r / M);
+        out[e] = cb[((int64_t)m * pqK + j) * dsub + t];
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_transpose_codebooks(const float* cb, int M, int pqK, int dsub, float* out, cudaStream_t s) {
+    const int64_t total = (int64_t)M * pqK * dsub;
+    if (total <= 0) return cudaSuccess;
+    transpose_codebooks_kernel<<<(unsigned)std::min<int64_t>(ceil_div(total, 256), 1024), 256, 0, s>>>(cb, M, pqK,
+                                                                                                      dsub, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_probe_order(const int32_t* probe_ids, int64_t nq, int np_max, int nlist, int32_t* scratch,
                                int32_t* order, cudaStream_t s) {

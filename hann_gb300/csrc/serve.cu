@@ -88,7 +88,7 @@ struct hann_server {
     std::vector<double> lat_ms;
     int64_t queries_done = 0, requests_done = 0, batches = 0, mutations = 0;
     int64_t peak_admitted = 0, cur_admitted = 0, relayouts = 0;
-    double mutation_ms = 0.0;
+    double mutation_ms = 0.0, drain_ms = 0.0, relayout_ms = 0.0, relayout_max_ms = 0.0;
     // mutation thread: its FIFO, and the drain handshake for relayouts
     std::deque<std::shared_ptr<Request>> mqueue;
     std::condition_variable cv_mut;
@@ -210,6 +210,7 @@ void mutator(hann_server* s) {
         };
         const auto t0 = Clock::now();
         bool needs = false, relaid = false;
+        Clock::time_point t1, t2, t3;
         int rc;
         {
             std::lock_guard<std::mutex> wl(h->wmu);
@@ -220,13 +221,16 @@ void mutator(hann_server* s) {
             s->drain_wanted = true;
             s->drained = s->sched_done;
             s->cv_work.notify_one();
+            t1 = Clock::now();
             s->cv_mut.wait(lk, [&] { return s->drained; });
             lk.unlock();
+            t2 = Clock::now();
             {
                 std::lock_guard<std::mutex> wl(h->wmu);
                 std::unique_lock<std::shared_mutex> xl(h->mu);
                 rc = apply(true, nullptr);
             }
+            t3 = Clock::now();
             relaid = true;
         }
         lk.lock();
@@ -234,6 +238,10 @@ void mutator(hann_server* s) {
             s->drain_wanted = false;
             s->drained = false;
             s->relayouts++;
+            s->drain_ms += std::chrono::duration<double, std::milli>(t2 - t1).count();
+            s->relayout_ms += std::chrono::duration<double, std::milli>(t3 - t2).count();
+            s->relayout_max_ms =
+                std::max(s->relayout_max_ms, std::chrono::duration<double, std::milli>(t3 - t1).count());
             s->cv_work.notify_one();
         }
         s->mqueue.pop_front();
@@ -566,6 +574,9 @@ int hann_serve_stats(hann_server* s, hann_serve_statistics* out) {
     out->peak_admitted_bytes = s->peak_admitted;
     out->relayouts = s->relayouts;
     out->mutation_ms = s->mutation_ms;
+    out->drain_ms = s->drain_ms;
+    out->relayout_ms = s->relayout_ms;
+    out->relayout_max_ms = s->relayout_max_ms;
     std::vector<double> l = s->lat_ms;
     if (!l.empty()) {
         std::sort(l.begin(), l.end());

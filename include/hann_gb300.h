@@ -192,6 +192,9 @@ typedef struct {
     double p50_ms, p99_ms, queries_per_s;
     int64_t relayouts;  /* mutations that had to wait for the batches in flight */
     double mutation_ms; /* host time spent applying mutations */
+    double drain_ms;    /* of which waiting for the batches in flight before relayouts */
+    double relayout_ms; /* of which applying relayouts (no batch starts meanwhile) */
+    double relayout_max_ms; /* the longest single drain + relayout */
 } hann_serve_statistics;
 
 void hann_serve_options_init(hann_serve_options* opts);
