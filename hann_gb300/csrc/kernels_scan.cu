@@ -37,6 +37,7 @@ constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint32_t KEY_INF = 0xff800000u;  // float_key(+inf)
+#define INF __int_as_float(0x7f800000)
 constexpr int SCAN_FLAT_LISTS = 128;        // probe lists held for the balanced schedule
 
 // Keeps the `R` smallest keys of entries [0, count) (ties at the cut broken
@@ -157,7 +158,7 @@ __device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count
     return out;
 }
 
-template <int MP>
+template <int MP, int MX>
 __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, const float* __restrict__ Q,
                                                             const float* __restrict__ probe_d,
                                                             const int32_t* __restrict__ probe_ids,
@@ -167,7 +168,8 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
                                                             float* __restrict__ cand_d,
                                                             uint32_t* __restrict__ cand_seq,
                                                             unsigned long long* __restrict__ rows_scanned) {
-    // MP: scan words per row (M rounded up to 8); G rows per warp step
+    // MP: scan words per row (M rounded up to 8); MX: M when it equals MP
+    // (known at compile time), else 0. G rows per warp step.
     __shared__ __align__(16) float lut[256 * 32];
     extern __shared__ __align__(16) unsigned char smraw[];
     uint32_t* wkey = reinterpret_cast<uint32_t*>(smraw);
@@ -178,17 +180,21 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
     int32_t* mrow = reinterpret_cast<int32_t*>(mseq + WARPS * R);
     uint32_t* whist = reinterpret_cast<uint32_t*>(mrow + WARPS * R);   // [WARPS][256]
     __shared__ uint32_t s_tau;
+    __shared__ int s_big;
     __shared__ int s_wcount[WARPS];
     __shared__ int s_lstart[SCAN_FLAT_LISTS], s_lsw[SCAN_FLAT_LISTS];
     __shared__ int s_llen[SCAN_FLAT_LISTS], s_lsteps[SCAN_FLAT_LISTS + 1];
     __shared__ float s_lbase[SCAN_FLAT_LISTS];
-    const int M = p.M;
+    const int M = MX > 0 ? MX : p.M;
     const int copies = 32 / M;
     const int G = 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const float* qv = Q + q * p.dim;
-    if (tid == 0) s_tau = KEY_INF;
+    if (tid == 0) {
+        s_tau = KEY_INF;
+        s_big = 0;
+    }
     {
         // Lane l fills bank l of table rows w, w + WARPS, ...: subquantizer
         // m = l % M. Codeword j of every subquantizer sits in one row of the
@@ -295,11 +301,13 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             }
         }
     };
-    if (!fb && nl <= SCAN_FLAT_LISTS) {
+    bool flat = !fb && nl <= SCAN_FLAT_LISTS;
+    if (flat) {
         // Balanced schedule: the probed lists' steps (G rows each) are
-        // numbered in probe order and warp w takes steps w, w + WARPS, ...,
-        // two at a time, so every warp gets the same number of rows to
-        // within one step whatever the list sizes.
+        // numbered in probe order and split into equal contiguous ranges,
+        // one per warp, so every warp gets the same number of rows to within
+        // one step whatever the list sizes. Lists of nearly 2^24 rows (whose
+        // positions do not fit a step's tag) take the list-by-list walk.
         for (int i = tid; i < nl; i += THREADS) {
             const int l = probe_ids[q * np_max + i];
             s_lstart[i] = (int)p.list_start[l];
@@ -308,8 +316,12 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             s_llen[i] = len;
             s_lbase[i] = probe_d[q * np_max + i];
             s_lsteps[i] = (len + G - 1) / G;
+            if (len > (1 << 24) - G) s_big = 1;
         }
         __syncthreads();
+        flat = s_big == 0;
+    }
+    if (flat) {
         if (w == 0) {
             // exclusive prefix of the step counts into s_lsteps (in place)
             int carry = 0;
@@ -333,59 +345,107 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             }
         }
         __syncthreads();
+        // Warp w takes the contiguous steps [ub, ue) of the probe-order
+        // numbering (every warp within one step of the same count) and walks
+        // them with a cursor held in registers: list, its boundary, the
+        // lane's row in it and the scan-word pointer. Three steps are in
+        // flight: a step's words are loaded two steps before it is computed.
         const int total = s_lsteps[nl];
-        int lc = 0;  // list cursor, monotonic over the warp's units
-        auto place = [&](int u, int& li, int64_t& g, bool& v) {
-            v = false;
-            li = 0;
-            g = 0;
-            if (u >= total) return;
-            while (s_lsteps[lc + 1] <= u) lc++;
-            li = lc;
-            const int r = (u - s_lsteps[lc]) * G + lane;
-            v = act && r < s_llen[lc];
-            g = (int64_t)s_lstart[lc] + r;
-        };
-        auto fetch = [&](int u, int li, int64_t g, uint4 (&sw)[MP / 8], float& term) {
-            load_row(s_lsw[li], u - s_lsteps[li], g, sw, term);
-        };
-        // units u (A) and u + WARPS (B) are computed while u + 2 WARPS and
-        // u + 3 WARPS load
-        int la, lb;
-        int64_t ga, gb;
-        bool va, vb;
-        uint4 sa[MP / 8], sb[MP / 8];
-        float ta = 0.0f, tb = 0.0f;
-        place(w, la, ga, va);
-        if (va) fetch(w, la, ga, sa, ta);
-        place(w + WARPS, lb, gb, vb);
-        if (vb) fetch(w + WARPS, lb, gb, sb, tb);
-        for (int u = w; u < total; u += 2 * WARPS) {
-            int na, nb;
-            int64_t gna, gnb;
-            bool vna, vnb;
-            uint4 sna[MP / 8], snb[MP / 8];
-            float tna = 0.0f, tnb = 0.0f;
-            place(u + 2 * WARPS, na, gna, vna);
-            if (vna) fetch(u + 2 * WARPS, na, gna, sna, tna);
-            place(u + 3 * WARPS, nb, gnb, vnb);
-            if (vnb) fetch(u + 3 * WARPS, nb, gnb, snb, tnb);
-            const uint32_t ka = va ? lookup(sa, s_lbase[la] + ta) : KEY_INF;
-            const uint32_t kb = vb ? lookup(sb, s_lbase[lb] + tb) : KEY_INF;
-            offer(ka, la, ga);
-            if (u + WARPS < total) offer(kb, lb, gb);
-            la = na;
-            lb = nb;
-            ga = gna;
-            gb = gnb;
-            va = vna;
-            vb = vnb;
-            ta = tna;
-            tb = tnb;
+        const int per = total / WARPS, rem = total % WARPS;
+        const int ub = w * per + min(w, rem);
+        const int n = per + (w < rem ? 1 : 0);
+        if (n > 0) {
+            int cl;
+            {
+                int lo = 0, hi = nl - 1;  // the last list starting at or before ub
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_lsteps[mid] <= ub) lo = mid;
+                    else hi = mid - 1;
+                }
+                cl = lo;
+            }
+            const uint4* sw4 = reinterpret_cast<const uint4*>(p.scanw);
+            int cu = ub, cend = s_lsteps[cl + 1], crow = (ub - s_lsteps[cl]) * G + lane;
+            int clen = s_llen[cl];
+            const float* cterm = p.term + s_lstart[cl];
+            const uint4* csw = sw4 + ((int64_t)s_lsw[cl] + (int64_t)(ub - s_lsteps[cl]) * G) * (MP / 8) + lane;
+            // A step in flight: its words, its term (+inf past the list's end,
+            // where the words are not initialised and the lookup is skipped)
+            // and tag = probe position << 24 | row position in the list.
+            auto load_step = [&](uint4 (&sw)[MP / 8], float& term, int& tag) {
 #pragma unroll
-            for (int t = 0; t < MP / 8; t++) {
-                sa[t] = sna[t];
-                sb[t] = snb[t];
+                for (int t = 0; t < MP / 8; t++) sw[t] = __ldg(csw + t * G);
+                term = crow < clen ? __ldg(cterm + crow) : INF;
+                tag = (cl << 24) | crow;
+                cu++;
+                if (cu < cend) {
+                    crow += G;
+                    csw += G * (MP / 8);
+                } else if (cu < ub + n) {
+                    do {
+                        cl++;
+                    } while (s_lsteps[cl + 1] <= cu);
+                    cend = s_lsteps[cl + 1];
+                    crow = lane;
+                    clen = s_llen[cl];
+                    cterm = p.term + s_lstart[cl];
+                    csw = sw4 + (int64_t)s_lsw[cl] * (MP / 8) + lane;
+                }
+            };
+            auto compute = [&](const uint4 (&sw)[MP / 8], float term, int tag) {
+                const int li = tag >> 24;
+                const uint32_t k = term < INF ? lookup(sw, s_lbase[li] + term) : KEY_INF;
+                return k;
+            };
+            auto offer_tag = [&](uint32_t k, int tag) {
+                const bool pass = k < *(volatile uint32_t*)&s_tau;
+                const unsigned bal = __ballot_sync(FULL, pass);
+                if (bal) {
+                    const int pos = count + __popc(bal & ltm);
+                    if (pass) {
+                        const int li = tag >> 24;
+                        key[pos] = k;
+                        seq[pos] = (uint32_t)li;
+                        row[pos] = s_lstart[li] + (tag & 0xffffff);
+                    }
+                    count += __popc(bal);
+                    if (count > CAPW - 32) {
+                        __syncwarp();
+                        uint32_t kth;
+                        count = warp_select(key, seq, row, count, R, &kth, hist);
+                        if (lane == 0) atomicMin(&s_tau, kth);
+                        __syncwarp();
+                    }
+                }
+            };
+            uint4 sa[MP / 8], sb[MP / 8], sc[MP / 8];
+            float ta = 0.0f, tb = 0.0f, tc = 0.0f;
+            int ga = 0, gb = 0, gc = 0;
+            load_step(sa, ta, ga);
+            if (n > 1) load_step(sb, tb, gb);
+            if (n > 2) load_step(sc, tc, gc);
+            for (int i = 0; i < n; i += 3) {
+                {
+                    const uint32_t k = compute(sa, ta, ga);
+                    const int g0 = ga;
+                    if (i + 3 < n) load_step(sa, ta, ga);
+                    offer_tag(k, g0);
+                }
+                if (i + 1 >= n) break;
+                {
+                    const uint32_t k = compute(sb, tb, gb);
+                    const int g0 = gb;
+                    if (i + 4 < n) load_step(sb, tb, gb);
+                    offer_tag(k, g0);
+                }
+                if (i + 2 >= n) break;
+                {
+                    const uint32_t k = compute(sc, tc, gc);
+                    const int g0 = gc;
+                    if (i + 5 < n) load_step(sc, tc, gc);
+                    offer_tag(k, g0);
+                }
             }
         }
     } else {
@@ -586,12 +646,19 @@ cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t 
     int CAPW = scan_skew_capw(R);
     const size_t smem = scan_skew_smem(R);
     const void* fn;
-    switch (scan_words_per_row(p.M) / 8) {
-    case 1: fn = (const void*)scan_skew_kernel<8>; break;
-    case 2: fn = (const void*)scan_skew_kernel<16>; break;
-    case 3: fn = (const void*)scan_skew_kernel<24>; break;
-    case 4: fn = (const void*)scan_skew_kernel<32>; break;
-    default: return cudaErrorInvalidValue;
+    switch (p.M) {
+    case 8: fn = (const void*)scan_skew_kernel<8, 8>; break;
+    case 16: fn = (const void*)scan_skew_kernel<16, 16>; break;
+    case 24: fn = (const void*)scan_skew_kernel<24, 24>; break;
+    case 32: fn = (const void*)scan_skew_kernel<32, 32>; break;
+    default:
+        switch (scan_words_per_row(p.M) / 8) {
+        case 1: fn = (const void*)scan_skew_kernel<8, 0>; break;
+        case 2: fn = (const void*)scan_skew_kernel<16, 0>; break;
+        case 3: fn = (const void*)scan_skew_kernel<24, 0>; break;
+        case 4: fn = (const void*)scan_skew_kernel<32, 0>; break;
+        default: return cudaErrorInvalidValue;
+        }
     }
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
