@@ -49,7 +49,7 @@ struct Epi {
     static constexpr int EW = MODE == 0 ? 2 : 4;
     static constexpr int THREADS = 64 + 128 * EW;
     static constexpr int CW = 256 / EW;  // columns per epilogue warp
-    static constexpr int LDC = MODE == 0 ? 64 : 32;  // accumulator columns per TMEM load
+    static constexpr int LDC = MODE == 0 ? 64 : 32;  // accumulator columns per TMEM wait
 };
 constexpr int TOPC = 8;       // argmin mode: candidates kept per row
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
@@ -343,15 +343,27 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                         __syncwarp();
                     }
                 } else if (MODE == 2) {
+                    // Most rows pass no column of a tile: test the minimum
+                    // score first (fminf skips the NaN pads) and build the
+                    // pass mask, with the same scores, only when it passes.
                     const float4* ct4 = reinterpret_cast<const float4*>(ct + c);
-                    unsigned long long pass = 0;
+                    float mn = __int_as_float(0x7f800000);
 #pragma unroll
                     for (int i4 = 0; i4 < LDC / 4; i4++) {
                         const float4 tt = ct4[i4];
-                        if (score(tt.x, v[4 * i4 + 0]) <= rt) pass |= 1ull << (4 * i4 + 0);
-                        if (score(tt.y, v[4 * i4 + 1]) <= rt) pass |= 1ull << (4 * i4 + 1);
-                        if (score(tt.z, v[4 * i4 + 2]) <= rt) pass |= 1ull << (4 * i4 + 2);
-                        if (score(tt.w, v[4 * i4 + 3]) <= rt) pass |= 1ull << (4 * i4 + 3);
+                        mn = fminf(mn, fminf(fminf(score(tt.x, v[4 * i4 + 0]), score(tt.y, v[4 * i4 + 1])),
+                                             fminf(score(tt.z, v[4 * i4 + 2]), score(tt.w, v[4 * i4 + 3]))));
+                    }
+                    unsigned long long pass = 0;
+                    if (mn <= rt) {
+#pragma unroll
+                        for (int i4 = 0; i4 < LDC / 4; i4++) {
+                            const float4 tt = ct4[i4];
+                            if (score(tt.x, v[4 * i4 + 0]) <= rt) pass |= 1ull << (4 * i4 + 0);
+                            if (score(tt.y, v[4 * i4 + 1]) <= rt) pass |= 1ull << (4 * i4 + 1);
+                            if (score(tt.z, v[4 * i4 + 2]) <= rt) pass |= 1ull << (4 * i4 + 2);
+                            if (score(tt.w, v[4 * i4 + 3]) <= rt) pass |= 1ull << (4 * i4 + 3);
+                        }
                     }
                     if (pass) {
                         int pos = atomicAdd(&cnt[row], __popcll(pass));
