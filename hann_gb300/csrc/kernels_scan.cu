@@ -158,7 +158,7 @@ __device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count
     return out;
 }
 
-template <int MP, int MX>
+template <int MP, int MX, int DEPTH>
 __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, const float* __restrict__ Q,
                                                             const float* __restrict__ probe_d,
                                                             const int32_t* __restrict__ probe_ids,
@@ -345,11 +345,10 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             }
         }
         __syncthreads();
-        // Warp w takes the contiguous steps [ub, ue) of the probe-order
+        // Warp w takes n contiguous steps from ub in the probe-order
         // numbering (every warp within one step of the same count) and walks
         // them with a cursor held in registers: list, its boundary, the
-        // lane's row in it and the scan-word pointer. Three steps are in
-        // flight: a step's words are loaded two steps before it is computed.
+        // lane's row in it and the scan-word pointer.
         const int total = s_lsteps[nl];
         const int per = total / WARPS, rem = total % WARPS;
         const int ub = w * per + min(w, rem);
@@ -419,31 +418,24 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
                     }
                 }
             };
-            uint4 sa[MP / 8], sb[MP / 8], sc[MP / 8];
-            float ta = 0.0f, tb = 0.0f, tc = 0.0f;
-            int ga = 0, gb = 0, gc = 0;
-            load_step(sa, ta, ga);
-            if (n > 1) load_step(sb, tb, gb);
-            if (n > 2) load_step(sc, tc, gc);
-            for (int i = 0; i < n; i += 3) {
-                {
-                    const uint32_t k = compute(sa, ta, ga);
-                    const int g0 = ga;
-                    if (i + 3 < n) load_step(sa, ta, ga);
-                    offer_tag(k, g0);
-                }
-                if (i + 1 >= n) break;
-                {
-                    const uint32_t k = compute(sb, tb, gb);
-                    const int g0 = gb;
-                    if (i + 4 < n) load_step(sb, tb, gb);
-                    offer_tag(k, g0);
-                }
-                if (i + 2 >= n) break;
-                {
-                    const uint32_t k = compute(sc, tc, gc);
-                    const int g0 = gc;
-                    if (i + 5 < n) load_step(sc, tc, gc);
+            // DEPTH steps in a ring: a step's words are loaded DEPTH - 1
+            // steps before it is computed. Two: a deeper ring spills
+            // registers at three blocks per SM, and the spills cost more
+            // than the latency it hides (2.06 ms against 2.43 ms for three
+            // and 4.19 ms for four on the 10M x 96 search).
+            uint4 sw[DEPTH][MP / 8];
+            float tm[DEPTH];
+            int tg[DEPTH];
+#pragma unroll
+            for (int d = 0; d < DEPTH; d++)
+                if (d < n) load_step(sw[d], tm[d], tg[d]);
+            for (int i = 0; i < n; i += DEPTH) {
+#pragma unroll
+                for (int d = 0; d < DEPTH; d++) {
+                    if (i + d >= n) break;
+                    const uint32_t k = compute(sw[d], tm[d], tg[d]);
+                    const int g0 = tg[d];
+                    if (i + d + DEPTH < n) load_step(sw[d], tm[d], tg[d]);
                     offer_tag(k, g0);
                 }
             }
@@ -647,16 +639,16 @@ cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t 
     const size_t smem = scan_skew_smem(R);
     const void* fn;
     switch (p.M) {
-    case 8: fn = (const void*)scan_skew_kernel<8, 8>; break;
-    case 16: fn = (const void*)scan_skew_kernel<16, 16>; break;
-    case 24: fn = (const void*)scan_skew_kernel<24, 24>; break;
-    case 32: fn = (const void*)scan_skew_kernel<32, 32>; break;
+    case 8: fn = (const void*)scan_skew_kernel<8, 8, 2>; break;
+    case 16: fn = (const void*)scan_skew_kernel<16, 16, 2>; break;
+    case 24: fn = (const void*)scan_skew_kernel<24, 24, 2>; break;
+    case 32: fn = (const void*)scan_skew_kernel<32, 32, 2>; break;
     default:
         switch (scan_words_per_row(p.M) / 8) {
-        case 1: fn = (const void*)scan_skew_kernel<8, 0>; break;
-        case 2: fn = (const void*)scan_skew_kernel<16, 0>; break;
-        case 3: fn = (const void*)scan_skew_kernel<24, 0>; break;
-        case 4: fn = (const void*)scan_skew_kernel<32, 0>; break;
+        case 1: fn = (const void*)scan_skew_kernel<8, 0, 2>; break;
+        case 2: fn = (const void*)scan_skew_kernel<16, 0, 2>; break;
+        case 3: fn = (const void*)scan_skew_kernel<24, 0, 2>; break;
+        case 4: fn = (const void*)scan_skew_kernel<32, 0, 2>; break;
         default: return cudaErrorInvalidValue;
         }
     }
