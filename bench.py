@@ -566,6 +566,31 @@ def train_section(args, torch, dev):
         out[name] = {"train_s": round(el, 3), "s_per_iteration": round(el / iters, 4), "inertia_fp64": inertia}
         states[name] = st
         log("train", name, out[name])
+        if not plain:
+            # binary snapshot of this index: write, read back into a new
+            # handle, and the same answers
+            try:
+                import tempfile
+                with tempfile.TemporaryDirectory() as td:
+                    path = os.path.join(td, "index.snap")
+                    t = time.perf_counter()
+                    idx.SaveSnapshot(path)
+                    t_save = time.perf_counter() - t
+                    size = os.path.getsize(path)
+                    other = hg.New(dim)
+                    t = time.perf_counter()
+                    other.LoadSnapshot(path)
+                    torch.cuda.synchronize()
+                    t_load = time.perf_counter() - t
+                qs_ = x[:256].cpu().numpy()
+                same = all(np.array_equal(u, v) for u, v in zip(idx.SearchBatch(qs_, 10, nprobe=16, mode=1),
+                                                                 other.SearchBatch(qs_, 10, nprobe=16, mode=1)))
+                other.close()
+                out["snapshot"] = {"bytes": size, "save_s": round(t_save, 3), "load_s": round(t_load, 3),
+                                   "same_results": bool(same)}
+                log("snapshot", out["snapshot"])
+            except Exception as e:  # pragma: no cover
+                out["snapshot"] = {"error": str(e)}
         if not plain and args.serve_seconds > 0:
             # the served stream on this 1M x 128 index as well
             try:

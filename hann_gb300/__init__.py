@@ -98,6 +98,7 @@ EXPORTED = (
     "hann_gpu_distance_matrix", "hann_knn_new", "hann_knn_free", "hann_knn_last_error", "hann_knn_search",
     "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn", "hann_pqivf_set_plain_fp32",
     "hann_serve_submit_priority", "hann_serve_cancel", "hann_pqivf_set_candidate_clusters",
+    "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot",
 )
 
 
@@ -140,6 +141,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_save_snapshot.argtypes = [_P, ctypes.c_char_p]
+        L.hann_pqivf_load_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
         L.hann_pqivf_list_lengths.argtypes = [_P, _P]
         L.hann_gpu_distance_matrix.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64,
@@ -508,6 +511,19 @@ class Index:
         data = r.read() if hasattr(r, "read") else bytes(r)
         ser = gob.decode_pqivf(data)
         self.import_state(gob_to_state(ser, self._opts))
+
+    def SaveSnapshot(self, path) -> None:
+        """Write the binary snapshot (the gob stream's content as flat arrays;
+        fast for large indexes)."""
+        self._check(self._L.hann_pqivf_save_snapshot(self._h, os.fsencode(path)))
+
+    def LoadSnapshot(self, path) -> None:
+        """Replace the index with a binary snapshot (sizes and checksum are
+        checked first; a bad file leaves the index as it was)."""
+        self._check(self._L.hann_pqivf_load_snapshot(self._h, os.fsencode(path)))
+        lay = _Layout()
+        self._check(self._L.hann_pqivf_export_layout(self._h, ctypes.byref(lay)))
+        self._dim = lay.dimension
 
 
 # ---------------------------------------------------------------------------

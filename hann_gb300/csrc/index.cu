@@ -1283,6 +1283,20 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
+    return import_locked(h, L, coarse, codebooks, list_len, list_key, cluster_counts, ids, vectors, codes, nullptr,
+                         has_codes, pending_ids, pending_vectors);
+}
+
+}  // extern "C"
+
+// The import behind hann_pqivf_import and the snapshot loader (all locks
+// held). Codes come as the reference's ints (codes32, with has_codes) or as
+// bytes (codes8, M per row); codes out of range are recomputed from the
+// vectors.
+int import_locked(hann_pqivf* h, const hann_pqivf_layout* L, const float* coarse, const float* codebooks,
+                  const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
+                  const int64_t* ids, const float* vectors, const int32_t* codes32, const uint8_t* codes8,
+                  const uint8_t* has_codes, const int64_t* pending_ids, const float* pending_vectors) {
     // GobDecode's parameter checks (pqivf/index.go:1035-1045).
     if (L->dimension <= 0) return h->fail(HANN_E_INVALID, "serialized index has invalid dimension %d", L->dimension);
     if (L->num_subquantizers <= 0 || L->dimension % L->num_subquantizers != 0)
@@ -1365,7 +1379,7 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
             rcl[r] = l;
             bool ok = has_codes == nullptr || has_codes[r];
             for (int m = 0; ok && m < M; m++) {
-                const int32_t c = codes[r * M + m];
+                const int32_t c = codes8 ? (int32_t)codes8[r * M + m] : codes32[r * M + m];
                 if (c < 0 || c >= h->pqk_eff) ok = false;
                 else cbytes[(size_t)r * h->code_stride + m] = (uint8_t)c;
             }
@@ -1395,6 +1409,8 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
     CK(cudaStreamSynchronize(h->stream));
     return upload_lens(h);
 }
+
+extern "C" {
 
 int hann_gpu_distance_batch(int32_t metric, const float* query, const float* flat, size_t dim, size_t n,
                             double* out) {

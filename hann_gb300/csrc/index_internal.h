@@ -288,3 +288,9 @@ int bulk_delete_locked(hann_pqivf* h, const int64_t* ids, int64_t n, bool allow_
 int add_prepare(hann_pqivf* h, const int64_t* ids, const float* vecs, int64_t n);
 int add_commit(hann_pqivf* h, const int64_t* ids);
 bool compaction_due(const hann_pqivf* h, int64_t extra);
+// Replaces the handle's state (every lock held); codes as ints (codes32) or
+// bytes (codes8), M per row.
+int import_locked(hann_pqivf* h, const hann_pqivf_layout* L, const float* coarse, const float* codebooks,
+                  const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
+                  const int64_t* ids, const float* vectors, const int32_t* codes32, const uint8_t* codes8,
+                  const uint8_t* has_codes, const int64_t* pending_ids, const float* pending_vectors);

@@ -252,6 +252,14 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* layout, const floa
                       const int64_t* ids, const float* vectors, const int32_t* codes, const uint8_t* has_codes,
                       const int64_t* pending_ids, const float* pending_vectors);
 
+/* Binary snapshot of the whole index (the content of Save/Load's gob
+ * stream, pqivf/index.go:969-1101, as flat arrays with byte codes and a
+ * checksum; layout in hann_gb300/csrc/snapshot.cu). Save lets searches run
+ * and holds mutations; Load replaces the handle's state after checking the
+ * file's sizes and checksum, and leaves the index unchanged when they fail. */
+int hann_pqivf_save_snapshot(hann_pqivf* h, const char* path);
+int hann_pqivf_load_snapshot(hann_pqivf* h, const char* path);
+
 /* ---- distance layer (core/simd_distance.h:30-33, core/metric.go:64-99) ----
  * metric: 0 squared Euclidean, 1 Euclidean, 2 Manhattan, 3 cosine. */
 #define HANN_METRIC_SQEUCLID 0
