@@ -744,60 +744,77 @@ def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
     import hann_gb300 as hg
 
     rng = np.random.default_rng(args.seed + 7)
-    srv = hg.Server(idx, slots=4, max_batch_queries=8192, max_k=100, max_nprobe=256, mode=1,
-                    memory_budget=120 << 30, max_batch_probes=args.serve_batch_probes)
-    pending = qmod.Queue()
-    results = []
-    stop = threading.Event()
-
-    def waiter():
-        while True:
-            item = pending.get()
-            if item is None:
-                return
-            kind, t, meta = item
-            r = srv.wait(t, timeout_ms=120000)
-            if kind == 0:
-                results.append((meta, r))
-
-    ws = [threading.Thread(target=waiter, daemon=True) for _ in range(4)]
-    for w in ws:
-        w.start()
+    dur = seconds or args.serve_seconds
+    # The whole arrival schedule is drawn before the clock starts, and
+    # Python's thread switch interval is shortened for the run, so the
+    # submitting thread keeps to the schedule (a waiter holding the
+    # interpreter for a whole 5 ms switch interval used to delay it, and the
+    # delayed arrivals then came as one burst). Latency is the server's own,
+    # from submit to completion.
+    sched = []
+    t = 0.0
     next_id = 50_000_000
-    t0 = time.perf_counter()
-    t_next = t0
-    sent = 0
     while True:
-        now = time.perf_counter()
-        if now - t0 > (seconds or args.serve_seconds):
+        t += rng.exponential(1.0 / rate)
+        if t > dur:
             break
-        if now < t_next:
-            time.sleep(min(t_next - now, 0.001))
-            continue
-        t_next += rng.exponential(1.0 / rate)
         u = rng.random()
         if u < 0.01:
             # random unit vectors: far from every query, so they do not
             # disturb the recall measured against the original ground truth
             chunk = rng.standard_normal((1000, q_host.shape[1])).astype(np.float32)
             chunk /= np.linalg.norm(chunk, axis=1, keepdims=True)
-            ids = np.arange(next_id, next_id + 1000)
+            sched.append((t, 1, (np.arange(next_id, next_id + 1000), chunk)))
             next_id += 1000
-            pending.put((1, srv.submit_add(ids, chunk), None))
-            continue
-        if u < 0.02:
-            pending.put((2, srv.submit_delete(rng.integers(0, n_ids or args.n, 100)), None))
-            continue
-        nq = int(np.exp(rng.uniform(0, np.log(512))))
-        k = int(rng.integers(1, 101))
-        npb = int(np.exp(rng.uniform(np.log(8), np.log(256))))
-        rows = rng.integers(0, nr, nq)
-        pending.put((0, srv.submit(q_host[rows], k, npb), (rows, k)))
-        sent += 1
+        elif u < 0.02:
+            sched.append((t, 2, rng.integers(0, n_ids or args.n, 100)))
+        else:
+            nq = int(np.exp(rng.uniform(0, np.log(512))))
+            k = int(rng.integers(1, 101))
+            npb = int(np.exp(rng.uniform(np.log(8), np.log(256))))
+            rows = rng.integers(0, nr, nq)
+            sched.append((t, 0, (k, npb, rows)))
+    srv = hg.Server(idx, slots=4, max_batch_queries=8192, max_k=100, max_nprobe=256, mode=1,
+                    memory_budget=120 << 30, max_batch_probes=args.serve_batch_probes)
+    pending = qmod.Queue()
+    results = []
+
+    def waiter():
+        while True:
+            item = pending.get()
+            if item is None:
+                return
+            kind, tk, meta = item
+            r = srv.wait(tk, timeout_ms=120000)
+            if kind == 0:
+                results.append((meta, r))
+
+    old_switch = sys.getswitchinterval()
+    sys.setswitchinterval(2e-4)
+    ws = [threading.Thread(target=waiter, daemon=True) for _ in range(2)]
+    for w in ws:
+        w.start()
+    late = []
+    t0 = time.perf_counter()
+    for ta, kind, payload in sched:
+        while True:
+            now = time.perf_counter() - t0
+            if now >= ta:
+                break
+            time.sleep(min(ta - now, 0.0005))
+        late.append(now - ta)
+        if kind == 1:
+            pending.put((1, srv.submit_add(*payload), None))
+        elif kind == 2:
+            pending.put((2, srv.submit_delete(payload), None))
+        else:
+            k, npb, rows = payload
+            pending.put((0, srv.submit(q_host[rows], k, npb), (rows, k)))
     for _ in ws:
         pending.put(None)
     for w in ws:
         w.join()
+    sys.setswitchinterval(old_switch)
     st = srv.stats()
     srv.stop()
     hits = tot = 0
@@ -812,6 +829,7 @@ def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
             "queries_per_s": st["queries_per_s"], "offered_requests_per_s": rate,
             "recall_at_10_k_ge_10": hits / tot if tot else None,
             "peak_admitted_bytes": int(st["peak_admitted_bytes"]), "relayouts": int(st["relayouts"]),
+            "submit_late_ms_p99": round(1000.0 * float(np.percentile(late, 99)), 3) if late else None,
             "mutation_ms_total": round(st["mutation_ms"], 1), "relayout_drain_ms_total": round(st["drain_ms"], 1),
             "relayout_ms_total": round(st["relayout_ms"], 1), "relayout_max_ms": round(st["relayout_max_ms"], 1),
             "stream": "Poisson arrivals; 1-512 queries/request log-uniform; k U[1,100]; nprobe log-U[8,256]; "
