@@ -184,3 +184,37 @@ def test_exact_rerank_distances(config1):
             want = np.sqrt(np.float64(oracle.sqeuclid(q[i], config1["x"][pos[int(ids[i, j])]])))
             assert d[i, j] == want
         assert (np.diff(d[i, :n[i]]) >= 0).all()
+
+
+@pytest.mark.parametrize("M", [24, 12, 32, 6, 48, 16])
+def test_search_parity_by_subquantizers(M):
+    """Every scan-kernel shape (M = 24 as the 10M x 96 bench, M not dividing
+    32, M = 32, the general M > 32 kernel) against the oracle, both in
+    parity mode and with the exact rerank, on unit-norm 96-d data."""
+    rng = np.random.default_rng(500 + M)
+    x, centers = gaussian_mixture(rng, 12000, 96, 40, 0.35)
+    x = (x / np.linalg.norm(x, axis=1, keepdims=True)).astype(np.float32)
+    q = centers[rng.integers(0, 40, 200)] + 0.35 * rng.standard_normal((200, 96))
+    q = (q / np.linalg.norm(q, axis=1, keepdims=True)).astype(np.float32)
+    idx = hg.New(96, hg.WithCoarseK(48), hg.WithNumSubquantizers(M), hg.WithPQK(64), hg.WithKMeansIters(4))
+    idx.BulkAddArrays(np.arange(len(x), dtype=np.int64), x)
+    idx.Train()
+    ora = state_to_oracle(idx.export_state())
+    for nprobe, k in ((4, 10), (13, 37)):
+        g = idx.SearchBatch(q, k, nprobe=nprobe)
+        o = ora.search(q, k, nprobe, nthreads=NT)
+        assert_same_results(*g, *o[:3])
+    # exact rerank: rows of the probed lists, exact distances, ascending
+    ids, dist, n = idx.SearchBatch(q[:50], 10, nprobe=8, mode=1)
+    st = idx.export_state()
+    starts = np.concatenate([[0], np.cumsum(st["list_len"])])
+    vec_of = dict(zip(st["ids"].tolist(), range(len(st["ids"]))))
+    for i in range(50):
+        rows = np.concatenate([np.arange(starts[l], starts[l + 1]) for l in ora.probe(q[i], 8)])
+        allowed = set(st["ids"][rows].tolist())
+        got = ids[i, :n[i]]
+        assert set(got.tolist()) <= allowed
+        assert (np.diff(dist[i, :n[i]]) >= 0).all()
+        for j, id_ in enumerate(got):
+            want = np.sqrt(oracle.sqeuclid(q[i], st["vectors"][vec_of[int(id_)]]))
+            assert abs(dist[i, j] - want) <= 1e-6 * max(want, 1e-12)
