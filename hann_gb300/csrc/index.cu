@@ -688,7 +688,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
                 const int e = std::min(h->nlist, b + w);
                 CK(launch_gemm_filter(sc.qbf.p, nc, h->d_coarse_bf16.p, h->nlist, h->kp, b, e,
                                       h->d_coarse_terms.p, 0, sc.pthr.p, PROBE_CAP, sc.pcnt.p, sc.pcand_id.p,
-                                      sc.pcand_s.p, h->d_err.p, s));
+                                      sc.pcand_s.p, h->d_err.p, s, b == 0));
                 CK(launch_knn_merge_band((int)nc, np_max, d_np + q0, PROBE_CAP, lcap, sc.pcnt.p, sc.pcand_id.p,
                                          sc.pcand_s.p, sc.pe2.p, sc.pasl.p, sc.pband.p, sc.plcount.p, sc.pthr.p,
                                          sc.pneed.p, s));

@@ -241,9 +241,13 @@ cudaError_t launch_knn_merge_exact(int nrows, const int32_t* qlist, int k, int c
 size_t knn_merge_exact_smem(int k, int cap);
 // Tensor-core screen: filter GEMM (kernels_gemm.cu), band merge, exact final.
 // cmode 0: cterm = (bias, -2) (squared scores); cmode 1: cterm = (0, scale).
+// first: every row's threshold is +inf (the first chunk, counts zero), so
+// every column is kept: they are written in column order without atomics
+// (when the chunk fits cap).
 cudaError_t launch_gemm_filter(const void* a_bf16, int64_t nrows, const void* b_bf16, int64_t nb, int kp,
                                int col_begin, int col_end, const float2* cterm, int cmode, const float* rthr, int cap,
-                               int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s);
+                               int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s,
+                               bool first = false);
 cudaError_t launch_knn_merge_band(int nrows, int k, const int32_t* krow, int cap, int lcap, int32_t* cnt,
                                   const int32_t* cand_id, const float* cand_s, const float* e2, const float* asl,
                                   unsigned long long* list, int32_t* lcount, float* thr, int32_t* need_exact,

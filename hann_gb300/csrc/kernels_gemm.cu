@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                                                               float* __restrict__ cand_val, int* __restrict__ err,
                                                               int col_begin, const float2* __restrict__ cterm,
                                                               int cmode, const float* __restrict__ rthr, int cap,
-                                                              int32_t* __restrict__ cnt) {
+                                                              int32_t* __restrict__ cnt, int dense) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sA = base;
@@ -341,6 +341,37 @@ __global__ void __launch_bounds__(Epi<MODE>::THREADS, 1) dist_gemm_kernel(const 
                             }
                         }
                         __syncwarp();
+                    }
+                } else if (MODE == 2 && dense) {
+                    // First chunk (every threshold +inf, every column kept):
+                    // column col_begin + i goes to slot i, four at a time,
+                    // and the row's count is the chunk's width.
+                    if (row < nrows) {
+                        const int width = ncols - col_begin;
+                        const int pos0 = col0 + c - col_begin;
+                        int32_t* ri = cand_idx + (int64_t)row * cap;
+                        float* rv = cand_val + (int64_t)row * cap;
+#pragma unroll
+                        for (int i4 = 0; i4 < LDC / 4; i4++) {
+                            const int pos = pos0 + 4 * i4;
+                            if (pos + 3 < width) {
+                                *reinterpret_cast<int4*>(ri + pos) =
+                                    make_int4(col0 + c + 4 * i4, col0 + c + 4 * i4 + 1, col0 + c + 4 * i4 + 2,
+                                              col0 + c + 4 * i4 + 3);
+                                *reinterpret_cast<float4*>(rv + pos) = make_float4(
+                                    score(ct[c + 4 * i4], v[4 * i4]), score(ct[c + 4 * i4 + 1], v[4 * i4 + 1]),
+                                    score(ct[c + 4 * i4 + 2], v[4 * i4 + 2]), score(ct[c + 4 * i4 + 3], v[4 * i4 + 3]));
+                            } else {
+#pragma unroll
+                                for (int u = 0; u < 4; u++) {
+                                    if (pos + u < width) {
+                                        ri[pos + u] = col0 + c + 4 * i4 + u;
+                                        rv[pos + u] = score(ct[c + 4 * i4 + u], v[4 * i4 + u]);
+                                    }
+                                }
+                            }
+                        }
+                        if (blockIdx.y == 0 && t == 0 && cbeg == 0 && c == 0) cnt[row] = width;
                     }
                 } else if (MODE == 2) {
                     // Most rows pass no column of a tile: test the minimum
@@ -512,7 +543,7 @@ template <int MODE>
 cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat16* b, int ncols, int kp,
                         const float* bias, float* out, int32_t* cand_idx, float* cand_val, int* err, cudaStream_t s,
                         int col_begin = 0, const float2* cterm = nullptr, int cmode = 0, const float* rthr = nullptr,
-                        int cap = 0, int32_t* cnt = nullptr) {
+                        int cap = 0, int32_t* cnt = nullptr, int dense = 0) {
     if (nrows <= 0 || ncols <= col_begin) return cudaSuccess;
     if (kp <= 0 || kp > KB_MAX * BKE || (kp & 7)) return cudaErrorInvalidValue;
     if (nrows > ((int64_t)1 << 31) - BM) return cudaErrorInvalidValue;
@@ -539,7 +570,7 @@ cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat
     splits = (int)ceil_div(ntiles, per);
     dist_gemm_kernel<MODE><<<dim3((unsigned)mtiles, (unsigned)splits), Epi<MODE>::THREADS, SMEM_BYTES, s>>>(
         ma, mb, (int)nrows, ncols, kp, per, bias, out, cand_idx, cand_val, err, col_begin, cterm, cmode, rthr, cap,
-        cnt);
+        cnt, dense);
     return cudaGetLastError();
 }
 
@@ -547,12 +578,13 @@ cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat
 
 cudaError_t launch_gemm_filter(const void* a_bf16, int64_t nrows, const void* b_bf16, int64_t nb, int kp,
                                int col_begin, int col_end, const float2* cterm, int cmode, const float* rthr, int cap,
-                               int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s) {
+                               int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s, bool first) {
     // the tensor map spans all nb rows of b; the CTAs cover [col_begin, col_end)
     if (col_end > nb) return cudaErrorInvalidValue;
+    const int dense = first && col_end - col_begin <= cap ? 1 : 0;
     return launch_gemm<2>(static_cast<const __nv_bfloat16*>(a_bf16), nrows, static_cast<const __nv_bfloat16*>(b_bf16),
                           (int)col_end, kp, nullptr, nullptr, cand_id, cand_s, err, s, col_begin, cterm, cmode, rthr,
-                          cap, cnt);
+                          cap, cnt, dense);
 }
 
 int gemm_kpad(int dim) { return (dim + 7) / 8 * 8; }

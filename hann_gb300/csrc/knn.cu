@@ -233,7 +233,7 @@ int knn_screen(hann_knn* h, int metric, const float* q, int nrows, int k, int64_
     for (int c = 0; c < nch; c++) {
         CK(launch_gemm_filter(h->q_bf.p, nrows, h->base_bf.p, h->n, h->kp, (int)cb[c], (int)cb[c + 1],
                               h->cterm[cos].p, cos, h->thr_f.p, KNN_CAP, h->cnt.p, h->cand_id.p, h->cand_v.p,
-                              h->counters.p + 1, s));
+                              h->counters.p + 1, s, c == 0));
         CK(launch_knn_merge_band(nrows, k, nullptr, KNN_CAP, lcap, h->cnt.p, h->cand_id.p, h->cand_v.p, h->e2.p, h->asl.p,
                                  h->list.p, h->lcount.p, h->thr_f.p, h->need_exact.p, s));
     }
