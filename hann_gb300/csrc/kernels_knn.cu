@@ -300,28 +300,39 @@ __global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
     }
 }
 
-constexpr int MW_MAX = 512;  // band list + candidates up to which one warp merges a row
+// Warp merge capacities: band list + candidates up to which one warp merges
+// a row. The small form (8 warps a block) serves the probe's bands; rows of
+// a k-NN with k > 32 carry about 8 k keys after a chunk, for the large form
+// (4 warps a block, 16 KB of keys each).
+constexpr int MW_MAX = 512;
 constexpr int MW_WARPS = 8;
+constexpr int MW_MAX_L = 2048;
+constexpr int MW_WARPS_L = 4;
+template <int CAPK, int WARPS>
+constexpr size_t merge_warp_smem() {
+    return (size_t)WARPS * CAPK * sizeof(unsigned long long) + (size_t)WARPS * 256 * sizeof(unsigned int);
+}
 
 // One warp per row when the row's band list and new candidates together
-// hold at most MW_MAX keys (the probe's usual case): the same merge as
-// knn_merge_band_kernel without block barriers. A row it merges has its
-// candidate count reset, so the block kernel launched after it skips the
-// row; rows it leaves (larger, or flagged) go to the block kernel.
-__global__ void __launch_bounds__(MW_WARPS * 32) knn_merge_band_warp_kernel(
+// hold at most CAPK keys: the same merge as knn_merge_band_kernel without
+// block barriers. A row it merges has its candidate count reset, so the
+// block kernel launched after it skips the row; rows it leaves (larger, or
+// flagged) go to the block kernel.
+template <int CAPK, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) knn_merge_band_warp_kernel(
     int nrows, int k, const int32_t* __restrict__ krow, int cap, int lcap, int32_t* __restrict__ cnt,
     const int32_t* __restrict__ cand_id, const float* __restrict__ cand_s, const float* __restrict__ e2,
     const float* __restrict__ asl, unsigned long long* __restrict__ list, int32_t* __restrict__ lcount,
     float* __restrict__ thr, const int32_t* __restrict__ need_exact) {
-    __shared__ unsigned long long keys_all[MW_WARPS][MW_MAX];
-    __shared__ unsigned int hist_all[MW_WARPS][256];
+    extern __shared__ __align__(16) unsigned long long mw_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t r = (int64_t)blockIdx.x * MW_WARPS + w;
+    unsigned int* hist = reinterpret_cast<unsigned int*>(mw_smem + WARPS * CAPK) + w * 256;
+    const int64_t r = (int64_t)blockIdx.x * WARPS + w;
     if (r >= nrows) return;
     const int c = cnt[r];
     const int L = lcount[r];
-    if (c == 0 || need_exact[r] || c > cap || L + c > MW_MAX) return;
-    unsigned long long* keys = keys_all[w];
+    if (c == 0 || need_exact[r] || c > cap || L + c > CAPK) return;
+    unsigned long long* keys = mw_smem + w * CAPK;
     const int kr = krow ? max(1, min(krow[r], k)) : k;
     for (int i = lane; i < L; i += 32) keys[i] = list[r * lcap + i];
     for (int i = lane; i < c; i += 32) keys[L + i] = dkey(cand_s[r * cap + i], (uint32_t)cand_id[r * cap + i]);
@@ -329,7 +340,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) knn_merge_band_warp_kernel(
     __syncwarp();
     float t_new = __int_as_float(0x7f800000);
     if (T >= kr) {
-        const unsigned long long K = warp_radix_nth_u64(keys, T, kr, hist_all[w]);
+        const unsigned long long K = warp_radix_nth_u64(keys, T, kr, hist);
         const float tk = key_float((uint32_t)(K >> 32));
         t_new = tk + e2[r] + 2e-5f * (fabsf(tk) + asl[r]);
     }
@@ -343,7 +354,7 @@ __global__ void __launch_bounds__(MW_WARPS * 32) knn_merge_band_warp_kernel(
         m += __popc(b);
     }
     if (lane == 0) {
-        lcount[r] = m;  // m <= T <= MW_MAX <= lcap
+        lcount[r] = m;  // m <= T <= CAPK <= lcap
         thr[r] = t_new;
         cnt[r] = 0;
     }
@@ -600,9 +611,19 @@ cudaError_t launch_knn_merge_band(int nrows, int k, const int32_t* krow, int cap
     const size_t smem = knn_merge_band_smem(lcap, cap);
     cudaError_t e = set_smem_attr((const void*)knn_merge_band_kernel, smem);
     if (e != cudaSuccess) return e;
-    if (lcap >= MW_MAX)
-        knn_merge_band_warp_kernel<<<(unsigned)ceil_div(nrows, MW_WARPS), MW_WARPS * 32, 0, s>>>(
+    if (k > 32 && lcap >= MW_MAX_L) {
+        constexpr size_t ws = merge_warp_smem<MW_MAX_L, MW_WARPS_L>();
+        e = set_smem_attr((const void*)knn_merge_band_warp_kernel<MW_MAX_L, MW_WARPS_L>, ws);
+        if (e != cudaSuccess) return e;
+        knn_merge_band_warp_kernel<MW_MAX_L, MW_WARPS_L><<<(unsigned)ceil_div(nrows, MW_WARPS_L), MW_WARPS_L * 32, ws, s>>>(
             nrows, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact);
+    } else if (lcap >= MW_MAX) {
+        constexpr size_t ws = merge_warp_smem<MW_MAX, MW_WARPS>();
+        e = set_smem_attr((const void*)knn_merge_band_warp_kernel<MW_MAX, MW_WARPS>, ws);
+        if (e != cudaSuccess) return e;
+        knn_merge_band_warp_kernel<MW_MAX, MW_WARPS><<<(unsigned)ceil_div(nrows, MW_WARPS), MW_WARPS * 32, ws, s>>>(
+            nrows, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact);
+    }
     knn_merge_band_kernel<<<(unsigned)nrows, KM_THREADS, smem, s>>>(k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl,
                                                                     list, lcount, thr, need_exact);
     return cudaGetLastError();
