@@ -630,6 +630,7 @@ int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_
         CK(sc.pcnt.reserve((size_t)chunk));
         CK(sc.plcount.reserve((size_t)chunk));
         CK(sc.pneed.reserve((size_t)chunk));
+        CK(sc.ptodo.reserve((size_t)chunk + 1));
         CK(sc.pcand_id.reserve((size_t)chunk * PROBE_CAP));
         CK(sc.pcand_s.reserve((size_t)chunk * PROBE_CAP));
         CK(sc.pband.reserve((size_t)chunk * lcap));
@@ -691,7 +692,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
                                       sc.pcand_s.p, h->d_err.p, s, b == 0));
                 CK(launch_knn_merge_band((int)nc, np_max, d_np + q0, PROBE_CAP, lcap, sc.pcnt.p, sc.pcand_id.p,
                                          sc.pcand_s.p, sc.pe2.p, sc.pasl.p, sc.pband.p, sc.plcount.p, sc.pthr.p,
-                                         sc.pneed.p, s));
+                                         sc.pneed.p, sc.ptodo.p, s));
                 launches += 2;
                 b = e;
             }
@@ -699,7 +700,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
             CK(mark(1, true));
             CK(launch_probe_final(qp, nc, h->o.dimension, h->d_coarse.p, h->nlist, d_np + q0, np_max, d_k + q0,
                                   h->d_live.p, h->o.fallback ? 1 : 0, lcap, sc.pband.p, sc.plcount.p, sc.pneed.p,
-                                  sc.D.p, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, sc.fbcount.p, s));
+                                  sc.D.p, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, sc.fbcount.p, sc.ptodo.p, s));
             CK(launch_probe_order(sc.probe_ids.p, nc, np_max, h->nlist, sc.order_scratch.p, sc.qorder.p, s));
             CK(mark(1, false));
             CK(mark(2, true));

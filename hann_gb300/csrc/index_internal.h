@@ -145,7 +145,7 @@ struct SearchScratch {
     DBuf<unsigned long long> fbcount;
     // screened probe (band lists per query)
     DBuf<float> pe2, pasl, pthr, pcand_s;
-    DBuf<int32_t> pcnt, pcand_id, plcount, pneed;
+    DBuf<int32_t> pcnt, pcand_id, plcount, pneed, ptodo;  // ptodo: rows left to the block kernels (+ count)
     DBuf<unsigned long long> pband;
     DBuf<int32_t> qorder, order_scratch;  // L2-friendly query order for scan and rerank
 };

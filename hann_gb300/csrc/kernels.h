@@ -125,7 +125,8 @@ cudaError_t launch_probe_final(const float* Q, int64_t nq, int dim, const float*
                                const int32_t* nprobe, int np_max, const int32_t* k, const int32_t* list_len,
                                int allow_fallback, int lcap, const unsigned long long* band, const int32_t* lcount,
                                const int32_t* need_exact, float* Drow, int32_t* probe_ids, float* probe_d,
-                               int32_t* fallback, unsigned long long* fallback_count, cudaStream_t s);
+                               int32_t* fallback, unsigned long long* fallback_count, int32_t* todo,
+                               cudaStream_t s);
 
 // out[0] = max_i sqrt(sqnorm[i]), out[1] = max_i resid[i].
 cudaError_t launch_norm_maxes(const float* sqnorm, const float* resid, int n, float* out, cudaStream_t s);
@@ -248,10 +249,12 @@ cudaError_t launch_gemm_filter(const void* a_bf16, int64_t nrows, const void* b_
                                int col_begin, int col_end, const float2* cterm, int cmode, const float* rthr, int cap,
                                int32_t* cnt, int32_t* cand_id, float* cand_s, int* err, cudaStream_t s,
                                bool first = false);
+// todo: nrows + 1 ints of scratch (the rows left to the block kernel and
+// their count).
 cudaError_t launch_knn_merge_band(int nrows, int k, const int32_t* krow, int cap, int lcap, int32_t* cnt,
                                   const int32_t* cand_id, const float* cand_s, const float* e2, const float* asl,
                                   unsigned long long* list, int32_t* lcount, float* thr, int32_t* need_exact,
-                                  cudaStream_t s);
+                                  int32_t* todo, cudaStream_t s);
 size_t knn_merge_band_smem(int lcap, int cap);
 cudaError_t launch_knn_final_band(int metric, int nrows, int k, int lcap, int dim, const float* queries,
                                   const float* base, const float* qnorm, const float* bnorm,

@@ -242,8 +242,8 @@ __global__ void __launch_bounds__(KM_THREADS) knn_merge_exact_kernel(
 // A list that would exceed lcap, or a candidate buffer that overflowed,
 // sends the query to the exact SIMT path (need_exact) and stops its screen.
 // krow (optional) gives a per-row k, capped at k.
-__global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
-    int k, const int32_t* __restrict__ krow, int cap, int lcap, int32_t* __restrict__ cnt,
+__device__ __forceinline__ void merge_band_row(
+    int64_t r, int k, const int32_t* __restrict__ krow, int cap, int lcap, int32_t* __restrict__ cnt,
     const int32_t* __restrict__ cand_id,
     const float* __restrict__ cand_s, const float* __restrict__ e2, const float* __restrict__ asl,
     unsigned long long* __restrict__ list, int32_t* __restrict__ lcount, float* __restrict__ thr,
@@ -253,7 +253,6 @@ __global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
     __shared__ unsigned long long s_and, s_or, s_prefix;
     __shared__ unsigned int s_rem;
     __shared__ int s_pos;
-    const int64_t r = blockIdx.x;
     const int c = cnt[r];
     if (c == 0) return;
     if (need_exact[r] || c > cap) {
@@ -300,6 +299,25 @@ __global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
     }
 }
 
+// Block merge of the rows in todo[0, *todo_count) (the rows the warp form
+// left), or of row blockIdx.x when todo is null.
+__global__ void __launch_bounds__(KM_THREADS) knn_merge_band_kernel(
+    int k, const int32_t* __restrict__ krow, int cap, int lcap, int32_t* __restrict__ cnt,
+    const int32_t* __restrict__ cand_id,
+    const float* __restrict__ cand_s, const float* __restrict__ e2, const float* __restrict__ asl,
+    unsigned long long* __restrict__ list, int32_t* __restrict__ lcount, float* __restrict__ thr,
+    int32_t* __restrict__ need_exact, const int32_t* __restrict__ todo, const int32_t* __restrict__ todo_count) {
+    if (!todo) {
+        merge_band_row(blockIdx.x, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact);
+        return;
+    }
+    const int n = *todo_count;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        merge_band_row(todo[i], k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact);
+        __syncthreads();
+    }
+}
+
 // Warp merge capacities: band list + candidates up to which one warp merges
 // a row. The small form (8 warps a block) serves the probe's bands; rows of
 // a k-NN with k > 32 carry about 8 k keys after a chunk, for the large form
@@ -323,7 +341,8 @@ __global__ void __launch_bounds__(WARPS * 32) knn_merge_band_warp_kernel(
     int nrows, int k, const int32_t* __restrict__ krow, int cap, int lcap, int32_t* __restrict__ cnt,
     const int32_t* __restrict__ cand_id, const float* __restrict__ cand_s, const float* __restrict__ e2,
     const float* __restrict__ asl, unsigned long long* __restrict__ list, int32_t* __restrict__ lcount,
-    float* __restrict__ thr, const int32_t* __restrict__ need_exact) {
+    float* __restrict__ thr, const int32_t* __restrict__ need_exact, int32_t* __restrict__ todo,
+    int32_t* __restrict__ todo_count) {
     extern __shared__ __align__(16) unsigned long long mw_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned int* hist = reinterpret_cast<unsigned int*>(mw_smem + WARPS * CAPK) + w * 256;
@@ -331,7 +350,12 @@ __global__ void __launch_bounds__(WARPS * 32) knn_merge_band_warp_kernel(
     if (r >= nrows) return;
     const int c = cnt[r];
     const int L = lcount[r];
-    if (c == 0 || need_exact[r] || c > cap || L + c > CAPK) return;
+    if (c == 0) return;
+    if (need_exact[r] || c > cap || L + c > CAPK) {
+        // left to the block kernel
+        if (lane == 0) todo[atomicAdd(todo_count, 1)] = (int32_t)r;
+        return;
+    }
     unsigned long long* keys = mw_smem + w * CAPK;
     const int kr = krow ? max(1, min(krow[r], k)) : k;
     for (int i = lane; i < L; i += 32) keys[i] = list[r * lcap + i];
@@ -606,26 +630,35 @@ size_t knn_merge_band_smem(int lcap, int cap) { return (size_t)(lcap + cap) * si
 cudaError_t launch_knn_merge_band(int nrows, int k, const int32_t* krow, int cap, int lcap, int32_t* cnt,
                                   const int32_t* cand_id, const float* cand_s, const float* e2, const float* asl,
                                   unsigned long long* list, int32_t* lcount, float* thr, int32_t* need_exact,
-                                  cudaStream_t s) {
+                                  int32_t* todo, cudaStream_t s) {
     if (nrows <= 0) return cudaSuccess;
     const size_t smem = knn_merge_band_smem(lcap, cap);
     cudaError_t e = set_smem_attr((const void*)knn_merge_band_kernel, smem);
     if (e != cudaSuccess) return e;
+    int32_t* todo_count = todo + nrows;
+    const bool warp_form = lcap >= MW_MAX;
+    if (warp_form) {
+        e = cudaMemsetAsync(todo_count, 0, sizeof(int32_t), s);
+        if (e != cudaSuccess) return e;
+    }
     if (k > 32 && lcap >= MW_MAX_L) {
         constexpr size_t ws = merge_warp_smem<MW_MAX_L, MW_WARPS_L>();
         e = set_smem_attr((const void*)knn_merge_band_warp_kernel<MW_MAX_L, MW_WARPS_L>, ws);
         if (e != cudaSuccess) return e;
         knn_merge_band_warp_kernel<MW_MAX_L, MW_WARPS_L><<<(unsigned)ceil_div(nrows, MW_WARPS_L), MW_WARPS_L * 32, ws, s>>>(
-            nrows, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact);
-    } else if (lcap >= MW_MAX) {
+            nrows, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact, todo, todo_count);
+    } else if (warp_form) {
         constexpr size_t ws = merge_warp_smem<MW_MAX, MW_WARPS>();
         e = set_smem_attr((const void*)knn_merge_band_warp_kernel<MW_MAX, MW_WARPS>, ws);
         if (e != cudaSuccess) return e;
         knn_merge_band_warp_kernel<MW_MAX, MW_WARPS><<<(unsigned)ceil_div(nrows, MW_WARPS), MW_WARPS * 32, ws, s>>>(
-            nrows, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact);
+            nrows, k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list, lcount, thr, need_exact, todo, todo_count);
     }
-    knn_merge_band_kernel<<<(unsigned)nrows, KM_THREADS, smem, s>>>(k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl,
-                                                                    list, lcount, thr, need_exact);
+    // the rows the warp form left: a grid of a few blocks per SM walks the list
+    const unsigned grid = warp_form ? (unsigned)std::min<int64_t>(nrows, 4 * 152) : (unsigned)nrows;
+    knn_merge_band_kernel<<<grid, KM_THREADS, smem, s>>>(k, krow, cap, lcap, cnt, cand_id, cand_s, e2, asl, list,
+                                                         lcount, thr, need_exact, warp_form ? todo : nullptr,
+                                                         todo_count);
     return cudaGetLastError();
 }
 

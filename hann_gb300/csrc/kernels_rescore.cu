@@ -132,14 +132,19 @@ __global__ void __launch_bounds__(PFW_WARPS * 32) probe_final_warp_kernel(
     const int32_t* __restrict__ nprobe, int np_max, const int32_t* __restrict__ kq,
     const int32_t* __restrict__ list_len, int allow_fb, int lcap, const unsigned long long* __restrict__ band,
     const int32_t* __restrict__ lcount, const int32_t* __restrict__ need_exact, int32_t* __restrict__ probe_ids,
-    float* __restrict__ probe_d, int32_t* __restrict__ fallback, unsigned long long* __restrict__ fb_count) {
+    float* __restrict__ probe_d, int32_t* __restrict__ fallback, unsigned long long* __restrict__ fb_count,
+    int32_t* __restrict__ todo, int32_t* __restrict__ todo_count) {
     __shared__ float qv_all[PFW_WARPS][QMAX];
     __shared__ unsigned long long keys_all[PFW_WARPS][PFW_CAP];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t q = (int64_t)blockIdx.x * PFW_WARPS + w;
     if (q >= nq) return;
     const int L = lcount[q];
-    if (need_exact[q] || L > PFW_CAP) return;
+    if (need_exact[q] || L > PFW_CAP) {
+        // left to probe_final_kernel
+        if (lane == 0) todo[atomicAdd(todo_count, 1)] = (int32_t)q;
+        return;
+    }
     float* qv = qv_all[w];
     unsigned long long* keys = keys_all[w];
     for (int e = lane; e < dim; e += 32) qv[e] = Q[q * dim + e];
@@ -182,8 +187,8 @@ __global__ void __launch_bounds__(PFW_WARPS * 32) probe_final_warp_kernel(
 // whole exact row into Drow (global scratch, nlist per query) and selects on
 // it, ties at the cut taken in list order. Also sets the fallback flag like
 // probe_select_band.
-__global__ void __launch_bounds__(PB_THREADS) probe_final_kernel(
-    const float* __restrict__ Q, int dim, const float* __restrict__ coarse, int nlist,
+__device__ __forceinline__ void probe_final_row(
+    int64_t q, const float* __restrict__ Q, int dim, const float* __restrict__ coarse, int nlist,
     const int32_t* __restrict__ nprobe, int np_max, const int32_t* __restrict__ kq,
     const int32_t* __restrict__ list_len, int allow_fb, int lcap, const unsigned long long* __restrict__ band,
     const int32_t* __restrict__ lcount, const int32_t* __restrict__ need_exact, float* __restrict__ Drow,
@@ -198,7 +203,6 @@ __global__ void __launch_bounds__(PB_THREADS) probe_final_kernel(
     __shared__ int s_pos, s_wsum[PB_THREADS / 32];
     __shared__ unsigned long long s_total;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int64_t q = blockIdx.x;
     if (!need_exact[q] && lcount[q] <= PFW_CAP) return;  // done by probe_final_warp_kernel
     const int np = min(nprobe[q], nlist);
     for (int e = tid; e < dim; e += PB_THREADS) qv[e] = Q[q * dim + e];
@@ -273,6 +277,23 @@ __global__ void __launch_bounds__(PB_THREADS) probe_final_kernel(
         const int fb = (allow_fb && s_total < (unsigned long long)kq[q]) ? 1 : 0;
         fallback[q] = fb;
         if (fb) atomicAdd(fb_count, 1ull);
+    }
+}
+
+// The queries probe_final_warp_kernel left, todo[0, *todo_count).
+__global__ void __launch_bounds__(PB_THREADS) probe_final_kernel(
+    const float* __restrict__ Q, int dim, const float* __restrict__ coarse, int nlist,
+    const int32_t* __restrict__ nprobe, int np_max, const int32_t* __restrict__ kq,
+    const int32_t* __restrict__ list_len, int allow_fb, int lcap, const unsigned long long* __restrict__ band,
+    const int32_t* __restrict__ lcount, const int32_t* __restrict__ need_exact, float* __restrict__ Drow,
+    int32_t* __restrict__ probe_ids, float* __restrict__ probe_d, int32_t* __restrict__ fallback,
+    unsigned long long* __restrict__ fb_count, const int32_t* __restrict__ todo,
+    const int32_t* __restrict__ todo_count) {
+    const int n = *todo_count;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        probe_final_row(todo[i], Q, dim, coarse, nlist, nprobe, np_max, kq, list_len, allow_fb, lcap, band, lcount,
+                        need_exact, Drow, probe_ids, probe_d, fallback, fb_count);
+        __syncthreads();
     }
 }
 
@@ -378,18 +399,22 @@ cudaError_t launch_probe_final(const float* Q, int64_t nq, int dim, const float*
                                const int32_t* nprobe, int np_max, const int32_t* k, const int32_t* list_len,
                                int allow_fallback, int lcap, const unsigned long long* band, const int32_t* lcount,
                                const int32_t* need_exact, float* Drow, int32_t* probe_ids, float* probe_d,
-                               int32_t* fallback, unsigned long long* fallback_count, cudaStream_t s) {
+                               int32_t* fallback, unsigned long long* fallback_count, int32_t* todo, cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
     if (np_max > PB_MAX || dim > QMAX || lcap < np_max) return cudaErrorInvalidValue;
     const size_t smem = probe_final_smem(lcap, np_max);
     cudaError_t e = cudaFuncSetAttribute(probe_final_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
+    int32_t* todo_count = todo + nq;
+    e = cudaMemsetAsync(todo_count, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return e;
     probe_final_warp_kernel<<<(unsigned)ceil_div(nq, PFW_WARPS), PFW_WARPS * 32, 0, s>>>(
         Q, nq, dim, coarse, nlist, nprobe, np_max, k, list_len, allow_fallback, lcap, band, lcount, need_exact,
-        probe_ids, probe_d, fallback, fallback_count);
-    probe_final_kernel<<<(unsigned)nq, PB_THREADS, smem, s>>>(Q, dim, coarse, nlist, nprobe, np_max, k, list_len,
-                                                              allow_fallback, lcap, band, lcount, need_exact, Drow,
-                                                              probe_ids, probe_d, fallback, fallback_count);
+        probe_ids, probe_d, fallback, fallback_count, todo, todo_count);
+    // the queries the warp form left: a grid of a few blocks per SM walks the list
+    probe_final_kernel<<<(unsigned)std::min<int64_t>(nq, 4 * 152), PB_THREADS, smem, s>>>(
+        Q, dim, coarse, nlist, nprobe, np_max, k, list_len, allow_fallback, lcap, band, lcount, need_exact, Drow,
+        probe_ids, probe_d, fallback, fallback_count, todo, todo_count);
     return cudaGetLastError();
 }
 

@@ -65,7 +65,7 @@ struct hann_knn {
     // per query block
     DBuf<__nv_bfloat16> q_bf;
     DBuf<float> qsq, qres, qnorm, e2, asl, thr_f, cand_v;
-    DBuf<int32_t> cnt, cand_id, lcount, need_exact, exact_list, redo, qlist2;
+    DBuf<int32_t> cnt, cand_id, lcount, need_exact, exact_list, redo, qlist2, todo;
     DBuf<unsigned long long> list, thr_k;
     DBuf<int> counters;               // [0] exact_count, [1] GEMM error, [2..] redo counts per chunk
     DBuf<float> q_in;
@@ -138,6 +138,7 @@ int reserve_block(hann_knn* h, int64_t qb, int k, int nchunks) {
     CK(h->thr_k.reserve(qb));
     CK(h->thr_f.reserve(qb));
     CK(h->need_exact.reserve(qb));
+    CK(h->todo.reserve(qb + 1));
     CK(h->exact_list.reserve(qb));
     CK(h->qlist2.reserve(qb));
     CK(h->redo.reserve((size_t)qb * nchunks));
@@ -235,7 +236,7 @@ int knn_screen(hann_knn* h, int metric, const float* q, int nrows, int k, int64_
                               h->cterm[cos].p, cos, h->thr_f.p, KNN_CAP, h->cnt.p, h->cand_id.p, h->cand_v.p,
                               h->counters.p + 1, s, c == 0));
         CK(launch_knn_merge_band(nrows, k, nullptr, KNN_CAP, lcap, h->cnt.p, h->cand_id.p, h->cand_v.p, h->e2.p, h->asl.p,
-                                 h->list.p, h->lcount.p, h->thr_f.p, h->need_exact.p, s));
+                                 h->list.p, h->lcount.p, h->thr_f.p, h->need_exact.p, h->todo.p, s));
     }
     h->stats.chunks += nch;
     CK(launch_knn_final_band(metric, nrows, k, lcap, h->dim, q, h->base.p, h->qnorm.p, h->bnorm.p, h->list.p,
