@@ -551,24 +551,61 @@ __global__ void order_count_kernel(const int32_t* __restrict__ probe_ids, int64_
 
 // Exclusive prefix of cnt[0..n) in place, one block.
 __global__ void order_scan_kernel(int32_t* __restrict__ cnt, int n) {
-    __shared__ int32_t part[1024];
-    const int t = threadIdx.x;
+    constexpr int PER_MAX = 32;
+    __shared__ int32_t wsum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const int per = (n + 1023) / 1024;
+    // thread t owns elements [t * per, (t + 1) * per); up to PER_MAX of them
+    // are loaded at once into registers (independent loads)
+    int v[PER_MAX];
     int sum = 0;
-    for (int i = t * per; i < min(n, (t + 1) * per); i++) sum += cnt[i];
-    part[t] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const int v = t >= o ? part[t - o] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+    if (per <= PER_MAX) {
+#pragma unroll
+        for (int j = 0; j < PER_MAX; j++) {
+            const int i = t * per + j;
+            v[j] = (j < per && i < n) ? cnt[i] : 0;
+            sum += v[j];
+        }
+    } else {
+        for (int i = t * per; i < min(n, (t + 1) * per); i++) sum += cnt[i];
     }
-    int run = part[t] - sum;
-    for (int i = t * per; i < min(n, (t + 1) * per); i++) {
-        const int c = cnt[i];
-        cnt[i] = run;
-        run += c;
+    // block exclusive scan of the per-thread sums: warp shuffles, then the
+    // warp totals by warp 0
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += x;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const int tot = wsum[lane];
+        int x = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        wsum[lane] = x - tot;
+    }
+    __syncthreads();
+    int run = incl - sum + wsum[w];
+    if (per <= PER_MAX) {
+#pragma unroll
+        for (int j = 0; j < PER_MAX; j++) {
+            const int i = t * per + j;
+            if (j < per && i < n) {
+                cnt[i] = run;
+                run += v[j];
+            }
+        }
+    } else {
+        for (int i = t * per; i < min(n, (t + 1) * per); i++) {
+            const int c = cnt[i];
+            cnt[i] = run;
+            run += c;
+        }
     }
 }
 
