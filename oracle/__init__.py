@@ -52,7 +52,7 @@ def build(force: bool = False) -> None:
     if force or not os.path.exists(LIB_PATH) or (
         os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "hann_oracle.c"))
     ):
-        subprocess.run(["make", "-s", "-C", HERE, os.path.join(HERE, "libhann_oracle.so")], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "lib"], check=True)
     subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, stdout=subprocess.DEVNULL)
 
 
