@@ -339,7 +339,11 @@ def main():
     ids_d = torch.empty(nq, args.k, dtype=torch.int64, device=dev)
     dist_d = torch.empty(nq, args.k, dtype=torch.float64, device=dev)
     nout_d = torch.empty(nq, dtype=torch.int32, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    # a stream of its own: the search is enqueued on it, and the events that
+    # time it are recorded on it (a null handle would send the work to the
+    # index's internal stream, which the events would not bracket)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.synchronize()
 
     def step():
         idx.SearchBatchDevice(q.data_ptr(), nq, args.k, choice, mode, ids_d.data_ptr(), dist_d.data_ptr(),
@@ -638,7 +642,8 @@ def knn_section(args, torch, dev):
     idx = hg.KNN(base.cpu().numpy())
     ids = torch.empty(nq, k, dtype=torch.int64, device=dev)
     dist = torch.empty(nq, k, dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)  # the k-NN runs and its timing events on one stream
+    torch.cuda.synchronize()
     nr = min(100, nq)
     b64 = base.double()
     q64 = q[:nr].double()

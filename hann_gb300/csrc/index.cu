@@ -1130,11 +1130,13 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     const int np = std::min<int>(nprobe, h->nlist);
     SearchScratch& sc = h->main;
-    std::vector<int32_t> kv(nq, k), nv(nq, np);
-    CK(upload(sc.k, kv.data(), kv.size(), s));
-    CK(upload(sc.np, nv.data(), nv.size(), s));
+    // k and nprobe filled on the device: the call enqueues everything on s
+    // and returns without waiting, so back-to-back calls keep the GPU busy
+    CK(sc.k.reserve((size_t)nq));
+    CK(sc.np.reserve((size_t)nq));
     CK(sc.fbcount.reserve(1));
-    CK(cudaStreamSynchronize(s));
+    CK(launch_fill_i32(sc.k.p, nq, k, s));
+    CK(launch_fill_i32(sc.np.p, nq, np, s));
     return run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
 }
 

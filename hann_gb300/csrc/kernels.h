@@ -271,6 +271,7 @@ cudaError_t launch_ref_sqnorm(const float* x, int64_t n, int dim, float* out, cu
 cudaError_t launch_knn_col_terms(const float* sqnorm, const float* resid, int64_t n, int cosine, float2* terms,
                                  unsigned int* maxes, cudaStream_t s);
 cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
+cudaError_t launch_fill_i32(int32_t* p, int64_t n, int32_t v, cudaStream_t s);
 // (sqnorm[i], -2): squared-Euclidean screen terms.
 cudaError_t launch_sq_terms(const float* sqnorm, int64_t n, float2* terms, cudaStream_t s);
 // Per-query band constants e2 (= 2 eps) and slack scale.

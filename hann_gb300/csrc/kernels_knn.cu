@@ -727,6 +727,10 @@ __global__ void fill_f32_kernel(float* __restrict__ p, int64_t n, float v) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = v;
 }
+__global__ void fill_i32_kernel(int32_t* __restrict__ p, int64_t n, int32_t v) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
 __global__ void sq_terms_kernel(const float* __restrict__ sqnorm, int64_t n, float2* __restrict__ terms) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) terms[i] = make_float2(sqnorm[i], -2.0f);
@@ -736,6 +740,12 @@ __global__ void sq_terms_kernel(const float* __restrict__ sqnorm, int64_t n, flo
 cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     fill_f32_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(p, n, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_i32(int32_t* p, int64_t n, int32_t v, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    fill_i32_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(p, n, v);
     return cudaGetLastError();
 }
 

@@ -119,7 +119,9 @@ int hann_pqivf_search_batch(hann_pqivf* h, const float* queries, int64_t nq, con
 
 /* Same as hann_pqivf_search_batch with every buffer in device memory and
  * the work enqueued on `stream` (a cudaStream_t, NULL = the handle's own);
- * k and nprobe are uniform. Returns once enqueued. */
+ * k and nprobe are uniform. Returns once enqueued, without waiting for the
+ * device. Calls share the handle's scratch: calls on different streams must
+ * be ordered by the caller. */
 int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k, int32_t nprobe,
                                    int32_t mode, int64_t* d_ids, double* d_distances, int32_t* d_n_out,
                                    void* stream);

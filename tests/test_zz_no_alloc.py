@@ -61,6 +61,7 @@ def test_noalloc_matches_device_search_two_calls(index, mode):
         got_ids = torch.full((nq, k), -7, dtype=torch.int64, device="cuda")
         got_d = torch.zeros((nq, k), dtype=torch.float64, device="cuda")
         got_n = torch.zeros(nq, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()  # the fills above ran on torch's stream
         idx.SearchBatchDevice(q.data_ptr(), nq, k, nprobe, mode, ref_ids.data_ptr(), ref_d.data_ptr(),
                               ref_n.data_ptr(), stream)
         rc = noalloc(idx.handle, _P(q.data_ptr()), nq, k, nprobe, mode, _P(got_ids.data_ptr()),
