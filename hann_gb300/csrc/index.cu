@@ -693,7 +693,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
                 CK(launch_knn_merge_band((int)nc, np_max, d_np + q0, PROBE_CAP, lcap, sc.pcnt.p, sc.pcand_id.p,
                                          sc.pcand_s.p, sc.pe2.p, sc.pasl.p, sc.pband.p, sc.plcount.p, sc.pthr.p,
                                          sc.pneed.p, sc.ptodo.p, s));
-                launches += 2;
+                launches += 3;  // the filter GEMM, the warp merge and the block merge
                 b = e;
             }
             CK(mark(0, false));
@@ -714,7 +714,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
                              d_dist + q0 * kmax, d_nout + q0, s));
             p.qorder = nullptr;
             CK(mark(3, false));
-            h->launches += launches + 6;
+            h->launches += launches + 7;  // + probe final (2), query order (3), scan, rerank
             continue;
         }
         CK(mark(0, true));
@@ -1137,6 +1137,7 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
     CK(sc.fbcount.reserve(1));
     CK(launch_fill_i32(sc.k.p, nq, k, s));
     CK(launch_fill_i32(sc.np.p, nq, np, s));
+    h->launches += 2;
     return run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
 }
 
