@@ -100,6 +100,8 @@ EXPORTED = (
     "hann_serve_submit_priority", "hann_serve_cancel", "hann_pqivf_set_candidate_clusters",
     "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot",
 )
+# Entry points of include/hann_gb300_diag.h.
+EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats")
 
 
 def load_library(path: str | None = None) -> ctypes.CDLL:
@@ -141,6 +143,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_arena_stats.argtypes = [_P, _P]
         L.hann_pqivf_save_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_load_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
@@ -511,6 +514,13 @@ class Index:
         data = r.read() if hasattr(r, "read") else bytes(r)
         ser = gob.decode_pqivf(data)
         self.import_state(gob_to_state(ser, self._opts))
+
+    def ArenaStats(self) -> dict:
+        """Row arena of the device layout (diagnostics)."""
+        out = np.zeros(5, dtype=np.int64)
+        self._check(self._L.hann_pqivf_arena_stats(self._h, _ptr(out)))
+        return dict(zip(("rows_allocated", "rows_packed", "hole_rows", "list_moves", "full_relayouts"),
+                        (int(v) for v in out)))
 
     def SaveSnapshot(self, path) -> None:
         """Write the binary snapshot (the gob stream's content as flat arrays;

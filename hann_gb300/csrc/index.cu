@@ -11,6 +11,7 @@
 // Rows of one inverted list are contiguous; every list starts on a multiple
 // of 32 rows and keeps spare capacity so Adds append in place.
 #include "index_internal.h"
+#include "hann_gb300_diag.h"
 
 static thread_local std::string g_new_error;
 
@@ -29,14 +30,20 @@ static int64_t list_capacity(int64_t len) { return round_up(len + len / 4 + 32, 
 // list; the host only renumbers the lists that held tombstones. The previous
 // arrays are kept as the next relayout's destination, so a relayout of an
 // index that does not grow allocates nothing.
+// Free rows kept at the end of the arena after a full relayout, for lists
+// that outgrow their capacity to move into (an eighth of the rows, at least
+// 4,096).
+static int64_t arena_slack(int64_t packed) { return round_up(std::max<int64_t>(packed / 8, 4096), 32); }
+
 static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_rows = true) {
     const int dim = h->o.dimension;
     std::vector<int64_t> start(h->nlist);
-    int64_t total = 0;
+    int64_t packed = 0;
     for (int l = 0; l < h->nlist; l++) {
-        start[l] = total;
-        total += round_up(caps[l], 32);
+        start[l] = packed;
+        packed += round_up(caps[l], 32);
     }
+    const int64_t total = packed + arena_slack(packed);
     if (total >= (int64_t)1 << 31) return h->fail(HANN_E_UNSUPPORTED, "more than 2^31 stored rows");
     CK(h->s_vectors.reserve((size_t)total * dim));
     CK(h->s_term.reserve((size_t)total));
@@ -46,14 +53,15 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
     // scan words: each list's region rounded up to whole groups of rows
     const bool sw = scan_skew_supported(h->o.num_subquantizers);
     std::vector<int64_t> swstart(h->nlist);
-    int64_t swtotal = 0;
+    int64_t swtotal = 0, swcap = 0;
     if (sw) {
         const int G = scan_group_rows(h->o.num_subquantizers);
         for (int l = 0; l < h->nlist; l++) {
             swstart[l] = swtotal;
             swtotal += round_up(round_up(caps[l], 32), G);
         }
-        CK(h->s_scanw.reserve((size_t)swtotal * scan_words_per_row(h->o.num_subquantizers)));
+        swcap = swtotal + round_up(arena_slack(packed), G);
+        CK(h->s_scanw.reserve((size_t)swcap * scan_words_per_row(h->o.num_subquantizers)));
     }
     if (move_rows && h->rows_cap > 0) {
         std::vector<int64_t> src(h->nlist);
@@ -94,12 +102,79 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
     h->h_cap.assign(h->nlist, 0);
     for (int l = 0; l < h->nlist; l++) h->h_cap[l] = round_up(caps[l], 32);
     h->rows_cap = total;
+    h->arena_end = packed;
+    h->hole_rows = 0;
+    h->sw_end = swtotal;
+    h->sw_cap = swcap;
+    h->full_relayouts++;
     CK(upload(h->d_start, h->h_start.data(), h->h_start.size(), h->stream));
     if (sw) {
         h->h_swstart = swstart;
         CK(upload(h->d_swstart, h->h_swstart.data(), h->h_swstart.size(), h->stream));
     }
     CK(cudaStreamSynchronize(h->stream));
+    return HANN_OK;
+}
+
+// Moves the given lists (all slots, tombstones too, in place order) to the
+// arena's free tail with the given capacities, leaving their old slots as
+// holes, and rebuilds their scan words there. Sets *done; does nothing when
+// the tail is too small or the holes would pass a quarter of the arena (the
+// caller then relayouts everything). The moved rows keep their positions in
+// their lists, so the host bookkeeping only changes the lists' starts.
+static int grow_lists(hann_pqivf* h, const std::vector<int>& lists, const std::vector<int64_t>& caps, bool* done) {
+    *done = false;
+    const int n = (int)lists.size();
+    if (n == 0 || h->rows_cap == 0) return HANN_OK;
+    const bool sw = scan_skew_supported(h->o.num_subquantizers);
+    const int G = scan_group_rows(h->o.num_subquantizers);
+    int64_t need = 0, need_sw = 0, freed = 0;
+    for (int i = 0; i < n; i++) {
+        need += round_up(caps[i], 32);
+        need_sw += round_up(round_up(caps[i], 32), G);
+        freed += h->h_cap[lists[i]];
+    }
+    if (h->arena_end + need > h->rows_cap || (sw && h->sw_end + need_sw > h->sw_cap)) return HANN_OK;
+    if ((h->hole_rows + freed) * 4 > h->rows_cap) return HANN_OK;
+    std::vector<int64_t> src(n), dst(n), swd(n);
+    std::vector<int32_t> len(n), cmp(n, 0);
+    int64_t at = h->arena_end, swat = h->sw_end;
+    for (int i = 0; i < n; i++) {
+        const int l = lists[i];
+        src[i] = h->h_start[l];
+        len[i] = (int32_t)h->list_ids[l].size();
+        dst[i] = at;
+        swd[i] = swat;
+        at += round_up(caps[i], 32);
+        swat += round_up(round_up(caps[i], 32), G);
+    }
+    MutationScratch& m = h->mut;
+    CK(upload(m.mv_src, src.data(), src.size(), h->stream));
+    CK(upload(m.mv_dst, dst.data(), dst.size(), h->stream));
+    CK(upload(m.mv_sw, swd.data(), swd.size(), h->stream));
+    CK(upload(m.mv_len, len.data(), len.size(), h->stream));
+    CK(upload(m.mv_cmp, cmp.data(), cmp.size(), h->stream));
+    // source and destination slots are disjoint parts of the same arrays
+    CK(launch_relayout_lists(n, m.mv_src.p, m.mv_len.p, m.mv_dst.p, m.mv_cmp.p, h->o.dimension, h->code_stride / 4,
+                             h->d_vectors.p, h->d_vectors.p, h->d_codes.p, h->d_codes.p, h->d_term.p, h->d_term.p,
+                             h->d_row_id.p, h->d_row_id.p, h->d_row_cluster.p, h->d_row_cluster.p, h->stream));
+    if (sw)
+        CK(launch_scan_words_lists(h->d_codes.p, h->code_stride, h->o.num_subquantizers, m.mv_dst.p, m.mv_len.p,
+                                   m.mv_sw.p, n, h->d_scanw.p, h->stream));
+    for (int i = 0; i < n; i++) {
+        const int l = lists[i];
+        h->h_start[l] = dst[i];
+        h->h_cap[l] = round_up(caps[i], 32);
+        if (sw) h->h_swstart[l] = swd[i];
+    }
+    h->arena_end = at;
+    h->sw_end = swat;
+    h->hole_rows += freed;
+    h->list_moves += n;
+    CK(upload(h->d_start, h->h_start.data(), h->h_start.size(), h->stream));
+    if (sw) CK(upload(h->d_swstart, h->h_swstart.data(), h->h_swstart.size(), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    *done = true;
     return HANN_OK;
 }
 
@@ -214,6 +289,7 @@ static int assign_rows(hann_pqivf* h, AssignScratch& sc, const float* x, int64_t
 // append -- or relayouts first when needed.
 int add_prepare(hann_pqivf* h, const int64_t* ids, const float* vecs, int64_t n) {
     MutationScratch& m = h->mut;
+    m.held = false;
     m.n = n;
     m.grow = false;
     if (n <= 0) return HANN_OK;
@@ -243,7 +319,23 @@ int add_commit(hann_pqivf* h, const int64_t* ids) {
     if (n <= 0) return HANN_OK;
     const int dim = h->o.dimension;
     if (m.grow) {
-        // one relayout that also drops every tombstone
+        // lists over capacity move to the arena's tail with twice their
+        // rows of room, when it has space
+        std::vector<int> gl;
+        std::vector<int64_t> gc;
+        for (int l = 0; l < h->nlist; l++) {
+            const int64_t need = (int64_t)h->list_ids[l].size() + m.add[l];
+            if (need <= h->h_cap[l]) continue;
+            gl.push_back(l);
+            gc.push_back(std::max<int64_t>(list_capacity(2 * (h->live_count[l] + m.add[l])), round_up(need, 32)));
+        }
+        bool moved = false;
+        int grc = grow_lists(h, gl, gc, &moved);
+        if (grc) return grc;
+        if (moved) m.grow = false;
+    }
+    if (m.grow) {
+        // otherwise one relayout of every list, which also drops every tombstone
         std::vector<int64_t> caps(h->nlist);
         // every list gets its headroom back; lists that overflowed double
         for (int l = 0; l < h->nlist; l++) {
@@ -293,6 +385,7 @@ static int assign_batch(hann_pqivf* h, const int64_t* ids, const float* vecs, in
 // see a row move. A relayout compacts the tombstones away once they exceed a
 // quarter of the slots.
 static int remove_rows(hann_pqivf* h, const std::vector<int64_t>& ids) {
+    h->mut.held = false;
     if (ids.empty()) return HANN_OK;
     std::vector<int64_t> rows;
     for (int64_t id : ids) {
@@ -421,6 +514,7 @@ static int kmeans_device(hann_pqivf* h, const float* x, int64_t ld, int off, int
 }
 
 static int train_impl(hann_pqivf* h, SeedSource seeds) {
+    h->mut.held = false;
     const int dim = h->o.dimension, M = h->o.num_subquantizers;
     // Consolidate every vector, clustered and pending, in ascending id order.
     std::vector<std::pair<int64_t, int64_t>> all;  // (id, source)
@@ -920,9 +1014,18 @@ int bulk_add_locked(hann_pqivf* h, const int64_t* ids, const float* vectors, int
             sid[i] = ids[order[i]];
             std::memcpy(&sv[(size_t)i * dim], vectors + order[i] * dim, sizeof(float) * dim);
         }
-        int rc = add_prepare(h, sid.data(), sv.data(), f);
-        if (rc) return rc;
-        if (h->mut.grow && !allow_relayout) {
+        // A call that stopped for a relayout left these same rows prepared
+        // (nothing else changes the index before the caller comes back).
+        MutationScratch& m = h->mut;
+        int rc = HANN_OK;
+        if (!(allow_relayout && m.held && m.held_ids == sid)) {
+            rc = add_prepare(h, sid.data(), sv.data(), f);
+            if (rc) return rc;
+        }
+        m.held = false;
+        if (m.grow && !allow_relayout) {
+            m.held = true;
+            m.held_ids = sid;
             if (needs_relayout) *needs_relayout = true;
             return HANN_OK;
         }
@@ -1141,6 +1244,18 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
     return run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
 }
 
+int hann_pqivf_arena_stats(void* hv, int64_t* out) {
+    hann_pqivf* h = static_cast<hann_pqivf*>(hv);
+    if (!h || !out) return HANN_E_INVALID;
+    std::shared_lock<std::shared_mutex> lk(h->mu);
+    out[0] = h->rows_cap;
+    out[1] = h->arena_end;
+    out[2] = h->hole_rows;
+    out[3] = h->list_moves;
+    out[4] = h->full_relayouts;
+    return HANN_OK;
+}
+
 int hann_pqivf_set_candidate_clusters(hann_pqivf* h, int32_t n) {
     if (!h) return HANN_E_INVALID;
     if (n <= 0) return h->fail(HANN_E_INVALID, "candidate clusters must be positive");
@@ -1301,6 +1416,7 @@ int import_locked(hann_pqivf* h, const hann_pqivf_layout* L, const float* coarse
                   const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
                   const int64_t* ids, const float* vectors, const int32_t* codes32, const uint8_t* codes8,
                   const uint8_t* has_codes, const int64_t* pending_ids, const float* pending_vectors) {
+    h->mut.held = false;
     // GobDecode's parameter checks (pqivf/index.go:1035-1045).
     if (L->dimension <= 0) return h->fail(HANN_E_INVALID, "serialized index has invalid dimension %d", L->dimension);
     if (L->num_subquantizers <= 0 || L->dimension % L->num_subquantizers != 0)

@@ -126,11 +126,15 @@ struct MutationScratch {
     DBuf<int32_t> asg;
     DBuf<uint8_t> codes;
     DBuf<int64_t> dst, ids, rows;
+    DBuf<int64_t> mv_src, mv_dst, mv_sw;  // list moves: old and new starts, new scan-word starts
+    DBuf<int32_t> mv_len, mv_cmp;
     AssignScratch asc;
     std::vector<int32_t> hasg;
     std::vector<int64_t> add;
     int64_t n = 0;
     bool grow = false;
+    bool held = false;               // prepared rows waiting for a relayout
+    std::vector<int64_t> held_ids;   // their ids
 };
 
 // Device scratch of one search stream: query staging, coarse scores, probe
@@ -175,7 +179,12 @@ struct hann_pqivf {
     std::vector<int64_t> cluster_counts;
     std::unordered_map<int64_t, int32_t> id_cluster;
     std::vector<int64_t> h_start, h_cap;
-    int64_t rows_cap = 0;
+    // Row arena: lists packed from 0 up to arena_end, then free slack up to
+    // rows_cap; a list that outgrows its capacity moves to the slack and
+    // leaves hole_rows behind until the next full relayout. Scan-word
+    // regions follow the same plan (sw_end, sw_cap).
+    int64_t rows_cap = 0, arena_end = 0, hole_rows = 0, sw_end = 0, sw_cap = 0;
+    int64_t list_moves = 0, full_relayouts = 0;
 
     DBuf<float> d_coarse, d_codebooks, d_vectors, d_term;
     DBuf<float> d_codebooks_t;  // [pqK][M][dsub], the scan's table-build layout

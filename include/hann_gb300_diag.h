@@ -21,6 +21,12 @@ extern "C" {
 int hann_gpu_bf16_scores(const float* a, int64_t n, const float* b, int32_t m, int32_t dim, float* scores,
                          int32_t* top_idx, float* top_val);
 
+/* The index's row arena: out[0] rows allocated, out[1] rows up to the end
+ * of the last list (the rest is free slack), out[2] rows left as holes by
+ * lists that moved, out[3] list moves and out[4] full relayouts since the
+ * handle was made. h is a hann_pqivf*. */
+int hann_pqivf_arena_stats(void* h, int64_t* out5);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,6 +26,7 @@ def test_every_declared_symbol_exported(built):
     missing = [n for n in sorted(decl) if not hasattr(L, n)]
     assert not missing, missing
     assert set(hg.EXPORTED) <= decl
+    assert set(hg.EXPORTED_DIAG) <= decl
 
 
 def test_library_is_in_tree(built):

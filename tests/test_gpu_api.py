@@ -184,6 +184,43 @@ def test_mutations_after_train_match_oracle():
     assert_same_results(*idx.SearchBatch(q, 10), *ora.search(q, 10, 4)[:3])
 
 
+def test_growing_lists_move_and_relayout():
+    """Chunks of vectors near one centroid overflow that list again and
+    again: it moves to the arena's free tail each time (its old slots become
+    holes) until the holes call for a full relayout. After every chunk, with
+    deletes between, the index answers like the oracle on its own state."""
+    rng = np.random.default_rng(17)
+    x = rng.normal(size=(3000, 16)).astype(np.float32)
+    idx = new_index(16, 32, 4, 16, 4, hg.WithCandidateClusters(6))
+    idx.BulkAddArrays(np.arange(3000), x)
+    idx.Train()
+    c0 = idx.export_state()["coarse"][5]
+    q = np.concatenate([c0 + 0.05 * rng.normal(size=(40, 16)),
+                        rng.normal(size=(40, 16))]).astype(np.float32)
+    next_id = 10_000
+    for rnd in range(12):
+        chunk = (c0 + 0.05 * rng.normal(size=(150 * (rnd + 1), 16))).astype(np.float32)
+        idx.BulkAddArrays(np.arange(next_id, next_id + len(chunk)), chunk)
+        next_id += len(chunk)
+        if rnd % 3 == 2:
+            idx.BulkDelete(list(range(next_id - 100, next_id)))
+        st = idx.export_state()
+        cl = np.repeat(np.arange(st["layout"]["nlist"]), st["list_len"])
+        assert np.array_equal(oracle.assign(st["vectors"], st["coarse"]), cl)
+        ora = state_to_oracle(st)
+        for mode in (0, 1):
+            g = idx.SearchBatch(q, 10, mode=mode)
+            if mode == 0:
+                assert_same_results(*g, *ora.search(q, 10, 6)[:3])
+            else:
+                assert (g[2] == 10).all()
+    assert idx.Stats().Count == 3000 + sum(150 * (r + 1) for r in range(12)) - 4 * 100
+    ar = idx.ArenaStats()
+    # the list moved into the slack, and at least once the holes (or the
+    # slack running out) called for a full relayout after training's
+    assert ar["list_moves"] >= 2 and ar["full_relayouts"] >= 2, ar
+
+
 def test_save_load_round_trip():
     rng = np.random.default_rng(6)
     x = rng.normal(size=(1000, 8)).astype(np.float32)
