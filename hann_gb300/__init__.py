@@ -98,7 +98,7 @@ EXPORTED = (
     "hann_gpu_distance_matrix", "hann_knn_new", "hann_knn_free", "hann_knn_last_error", "hann_knn_search",
     "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn", "hann_pqivf_set_plain_fp32",
     "hann_serve_submit_priority", "hann_serve_cancel", "hann_pqivf_set_candidate_clusters",
-    "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot",
+    "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot", "hann_pqivf_retrain",
 )
 # Entry points of include/hann_gb300_diag.h.
 EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats")
@@ -144,6 +144,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_arena_stats.argtypes = [_P, _P]
+        L.hann_pqivf_retrain.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_save_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_load_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
@@ -514,6 +515,11 @@ class Index:
         data = r.read() if hasattr(r, "read") else bytes(r)
         ser = gob.decode_pqivf(data)
         self.import_state(gob_to_state(ser, self._opts))
+
+    def Retrain(self, iters: int) -> None:
+        """Incremental re-Train: `iters` Lloyd iterations from the current
+        centroids and codebooks, then every vector reassigned and re-encoded."""
+        self._check(self._L.hann_pqivf_retrain(self._h, int(iters)))
 
     def ArenaStats(self) -> dict:
         """Row arena of the device layout (diagnostics)."""

@@ -435,6 +435,11 @@ struct SeedSource {
     const int64_t* reseed = nullptr;
     int64_t n_reseed = 0;
     int64_t reseed_used = 0;
+    // warm start (Retrain): k-means from the index's own centroids and
+    // codebooks (device arrays) for warm_iters iterations
+    const float* warm_coarse = nullptr;
+    const float* warm_codebooks = nullptr;
+    int warm_iters = 0;
 };
 
 static int64_t draw_reseed(hann_pqivf* h, SeedSource& src, int64_t n, bool& ok) {
@@ -456,14 +461,20 @@ static int64_t draw_reseed(hann_pqivf* h, SeedSource& src, int64_t n, bool& ok) 
 // clusters reseeded from `reseed` in cluster order.
 static int kmeans_device(hann_pqivf* h, const float* x, int64_t ld, int off, int64_t n, int dim, int k, int iters,
                          const std::vector<int64_t>& init, SeedSource& seeds, float* cent, int32_t* asg_buf,
-                         bool sub_mode, const float* sub_full, int M, int m, AssignScratch* sc) {
+                         bool sub_mode, const float* sub_full, int M, int m, AssignScratch* sc,
+                         const float* init_cent = nullptr) {
     // sub_mode: x is the full residual matrix [n][M*dim]; k-means runs on
     // columns [m*dim, (m+1)*dim) and cent is codebook m ([k][dim]).
+    // init_cent: start from these centroids instead of the init rows.
     DBuf<int64_t> dsrc;
     DBuf<double> sums;
     DBuf<int64_t> counts;
-    CK(upload(dsrc, init.data(), init.size(), h->stream));
-    CK(launch_gather_cols(x, ld, off, dsrc.p, nullptr, k, dim, cent, dim, h->stream));
+    if (init_cent) {
+        CK(cudaMemcpyAsync(cent, init_cent, sizeof(float) * (size_t)k * dim, cudaMemcpyDeviceToDevice, h->stream));
+    } else {
+        CK(upload(dsrc, init.data(), init.size(), h->stream));
+        CK(launch_gather_cols(x, ld, off, dsrc.p, nullptr, k, dim, cent, dim, h->stream));
+    }
     CK(sums.reserve((size_t)k * dim * (sub_mode ? M : 1)));
     CK(counts.reserve((size_t)k * (sub_mode ? M : 1)));
     std::vector<int64_t> hcounts(k);
@@ -552,8 +563,13 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
 
     // Coarse k-means (runKMeans(allVectors, coarseK, iters)).
     const int k = (int)std::min<int64_t>(h->o.coarse_k, n);
+    const bool warm = seeds.warm_coarse != nullptr;
+    if (warm && k != h->nlist)
+        return h->fail(HANN_E_STATE, "retrain needs the trained list count (%d); %lld vectors give %d", h->nlist,
+                       (long long)n, k);
     std::vector<int64_t> init;
-    if (seeds.coarse_init) {
+    if (warm) {
+    } else if (seeds.coarse_init) {
         init.assign(seeds.coarse_init, seeds.coarse_init + k);
         for (int64_t v : init)
             if (v < 0 || v >= n) return h->fail(HANN_E_INVALID, "coarse init index out of range");
@@ -565,8 +581,8 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     CK(C.reserve((size_t)k * dim));
     CK(asg.reserve((size_t)n));
     AssignScratch asc;
-    int rc = kmeans_device(h, X.p, dim, 0, n, dim, k, h->o.kmeans_iters, init, seeds, C.p, asg.p, false, nullptr, 0,
-                           0, &asc);
+    int rc = kmeans_device(h, X.p, dim, 0, n, dim, k, warm ? seeds.warm_iters : h->o.kmeans_iters, init, seeds, C.p,
+                           asg.p, false, nullptr, 0, 0, &asc, seeds.warm_coarse);
     if (rc) return rc;
     // Final assignment and inverted lists in ascending (cluster, id) order.
     rc = assign_rows(h, asc, X.p, n, dim, C.p, k, asg.p);
@@ -596,21 +612,26 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     CK(launch_residuals(X.p, dorder.p, dordc.p, n, dim, C.p, Rm.p, h->stream));
     const int kpq = (int)std::min<int64_t>(h->o.pq_k, n);
     const int ds = dim / M;
+    if (warm && kpq != h->pqk_eff)
+        return h->fail(HANN_E_STATE, "retrain needs the trained codebook size (%d); %lld vectors give %d", h->pqk_eff,
+                       (long long)n, kpq);
     DBuf<float> CB;
     CK(CB.reserve((size_t)M * kpq * ds));
     DBuf<int32_t> pqa;
     CK(pqa.reserve((size_t)n * M));
     for (int m = 0; m < M; m++) {
         std::vector<int64_t> pinit;
-        if (seeds.pq_init) {
+        if (warm) {
+        } else if (seeds.pq_init) {
             pinit.assign(seeds.pq_init + (int64_t)m * h->o.pq_k, seeds.pq_init + (int64_t)m * h->o.pq_k + kpq);
             for (int64_t v : pinit)
                 if (v < 0 || v >= n) return h->fail(HANN_E_INVALID, "subquantizer init index out of range");
         } else {
             pinit = h->rng.perm_prefix(n, kpq);
         }
-        rc = kmeans_device(h, Rm.p, dim, m * ds, n, ds, kpq, h->o.kmeans_iters, pinit, seeds,
-                           CB.p + (size_t)m * kpq * ds, pqa.p, true, Rm.p, M, m, nullptr);
+        rc = kmeans_device(h, Rm.p, dim, m * ds, n, ds, kpq, warm ? seeds.warm_iters : h->o.kmeans_iters, pinit,
+                           seeds, CB.p + (size_t)m * kpq * ds, pqa.p, true, Rm.p, M, m, nullptr,
+                           warm ? seeds.warm_codebooks + (size_t)m * kpq * ds : nullptr);
         if (rc) return rc;
     }
     Rm.reset();
@@ -1167,6 +1188,22 @@ int hann_pqivf_train_seeded(hann_pqivf* h, const int64_t* coarse_init, const int
 }
 
 int hann_pqivf_train(hann_pqivf* h) { return hann_pqivf_train_seeded(h, nullptr, nullptr, nullptr, 0); }
+
+int hann_pqivf_retrain(hann_pqivf* h, int32_t iters) {
+    if (!h) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> wl(h->wmu);
+    std::unique_lock<std::shared_mutex> lk(h->mu);
+    std::lock_guard<std::mutex> rl(h->run_mu);
+    cudaSetDevice(h->o.device);
+    if (iters < 0) return h->fail(HANN_E_INVALID, "retrain iterations must not be negative");
+    if (!h->trained || h->nlist == 0)
+        return h->fail(HANN_E_STATE, "PQIVF index is not trained. Call Train() before Retrain()");
+    SeedSource s;
+    s.warm_coarse = h->d_coarse.p;
+    s.warm_codebooks = h->d_codebooks.p;
+    s.warm_iters = iters;
+    return train_impl(h, s);
+}
 
 int hann_pqivf_search_batch(hann_pqivf* h, const float* queries, int64_t nq, const int32_t* k, const int32_t* nprobe,
                             int32_t kmax, int32_t mode, int64_t* ids, double* distances, int32_t* n_out) {

@@ -101,6 +101,15 @@ int hann_pqivf_train(hann_pqivf* h);
  * Any pointer may be NULL to draw from the handle's seeded generator. */
 int hann_pqivf_train_seeded(hann_pqivf* h, const int64_t* coarse_init, const int64_t* pq_init,
                             const int64_t* reseed, int64_t n_reseed);
+/* Incremental re-Train after many mutations (no counterpart: the
+ * reference's Train reseeds from scratch, pqivf/index.go:451-605, and keeps
+ * the centroids fixed between Train calls, 306-312). `iters` Lloyd
+ * iterations over every stored vector starting from the index's own
+ * centroids, then as many on the residuals starting from its own codebooks,
+ * then every vector reassigned and re-encoded, as Train does; 0 iterations
+ * only repacks the lists. Needs a trained index whose vector count still
+ * gives the same list and codebook sizes. */
+int hann_pqivf_retrain(hann_pqivf* h, int32_t iters);
 
 /* Index.Search (core/index.go:38; pqivf/index.go:850-949) for one query:
  * ids/distances (true Euclidean distance as float64) of up to k neighbours
