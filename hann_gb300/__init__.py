@@ -852,13 +852,19 @@ class Server:
             self._meta[t.value] = (0, 0)
         return t.value
 
-    def wait(self, ticket: int, timeout_ms: int = 60000):
+    def wait(self, ticket: int, timeout_ms: int = 60000, results: bool = True):
+        """Wait for a ticket: (ids, distances, counts, latency ms); with
+        results=False only the latency (the results are dropped uncopied)."""
         with self._meta_lock:
             nq, k = self._meta.pop(ticket)
+        lat = ctypes.c_double(0)
+        if not results:
+            self._check(self._L.hann_serve_wait(self._h, ticket, None, None, None, int(timeout_ms),
+                                                ctypes.byref(lat)))
+            return None, None, None, lat.value
         ids = np.zeros((nq, max(k, 1)), np.int64)
         dist = np.zeros((nq, max(k, 1)), np.float64)
         n = np.zeros(max(nq, 1), np.int32)
-        lat = ctypes.c_double(0)
         self._check(self._L.hann_serve_wait(self._h, ticket, _ptr(ids), _ptr(dist), _ptr(n), int(timeout_ms),
                                             ctypes.byref(lat)))
         return ids, dist, n[:nq], lat.value

@@ -147,3 +147,16 @@ def test_priority_and_cancel(index):
             srv.wait(t)
         with pytest.raises(hg.HannError):
             srv.cancel(123456789)
+
+
+def test_wait_without_results(index):
+    """A waiter that wants only the latency gets it without the copies; the
+    next request's results are unaffected."""
+    idx, x, rng = index
+    q = rng.normal(size=(5, 32)).astype(np.float32)
+    with hg.Server(idx, slots=2, max_batch_queries=64, max_k=10, max_nprobe=16) as srv:
+        ids, dist, n, lat = srv.wait(srv.submit(q, 7, 8), results=False)
+        assert ids is None and dist is None and n is None and lat > 0
+        ids, dist, n, _ = srv.wait(srv.submit(q, 7, 8))
+    want = idx.SearchBatch(q, 7, nprobe=8, mode=hg.MODE_EXACT_RERANK)
+    np.testing.assert_array_equal(ids, want[0])
