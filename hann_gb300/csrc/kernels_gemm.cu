@@ -552,12 +552,10 @@ cudaError_t launch_gemm(const __nv_bfloat16* a, int64_t nrows, const __nv_bfloat
     if (e != cudaSuccess) return e;
     e = make_map(&mb, b, ncols, kp, BN);
     if (e != cudaSuccess) return e;
-    static bool attr = false;
-    if (!attr) {
-        e = cudaFuncSetAttribute(dist_gemm_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // set on every launch: the attribute belongs to the current device's
+    // context, and launches may come from several threads and devices
+    e = cudaFuncSetAttribute(dist_gemm_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
     // Score matrices split the columns over CTAs so that small row counts
     // still fill the GPU (about four CTAs per SM in total).
     const int mtiles = (int)ceil_div(nrows, BM);

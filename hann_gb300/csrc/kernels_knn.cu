@@ -538,14 +538,10 @@ cudaError_t launch_filter_t(const float* q, const int32_t* qlist, int nrows, int
     if (nrows <= 0 || c_end <= c_begin) return cudaSuccess;
     if (dim <= KNN_SIMT_DMAX) {
         const size_t smem = (size_t)dim * (KF_TP + KF_TC) * sizeof(float);
-        static bool attr = false;
-        if (!attr) {
-            cudaError_t e = cudaFuncSetAttribute(knn_filter_kernel<METRIC, MATRIX>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)((size_t)KNN_SIMT_DMAX * (KF_TP + KF_TC) * sizeof(float)));
-            if (e != cudaSuccess) return e;
-            attr = true;
-        }
+        cudaError_t e = cudaFuncSetAttribute(knn_filter_kernel<METRIC, MATRIX>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)((size_t)KNN_SIMT_DMAX * (KF_TP + KF_TC) * sizeof(float)));
+        if (e != cudaSuccess) return e;
         const int64_t qtiles = ceil_div(nrows, KF_TP);
         const int64_t tiles = ceil_div(c_end - c_begin, KF_TC);
         // about four waves of one block per SM

@@ -375,13 +375,9 @@ cudaError_t launch_probe_select_band(float* S, const float* Q, const float* qn2,
     const int in_smem = row_bytes <= 160 * 1024 ? 1 : 0;
     const size_t dyn = in_smem ? row_bytes : 0;
     // static buffers (about 34 KiB) plus the row can pass the 48 KiB default
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(probe_select_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             160 * 1024);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    cudaError_t e = cudaFuncSetAttribute(probe_select_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         160 * 1024);
+    if (e != cudaSuccess) return e;
     probe_select_band_kernel<<<(unsigned)nq, PB_THREADS, dyn, s>>>(S, Q, qn2, qres, dim, kp, coarse, cmax, nlist,
                                                                   nprobe,
                                                                   np_max, k, list_len, allow_fallback, probe_ids,

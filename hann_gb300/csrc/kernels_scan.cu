@@ -37,7 +37,7 @@ constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr uint32_t KEY_INF = 0xff800000u;  // float_key(+inf)
-#define INF __int_as_float(0x7f800000)
+__device__ __forceinline__ float pos_inf() { return __int_as_float(0x7f800000); }
 constexpr int SCAN_FLAT_LISTS = 128;        // probe lists held for the balanced schedule
 
 // Keeps the `R` smallest keys of entries [0, count) (ties at the cut broken
@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             auto load_step = [&](uint4 (&sw)[MP / 8], float& term, int& tag) {
 #pragma unroll
                 for (int t = 0; t < MP / 8; t++) sw[t] = __ldg(csw + t * G);
-                term = crow < clen ? __ldg(cterm + crow) : INF;
+                term = crow < clen ? __ldg(cterm + crow) : pos_inf();
                 tag = (cl << 24) | crow;
                 cu++;
                 if (cu < cend) {
@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             };
             auto compute = [&](const uint4 (&sw)[MP / 8], float term, int tag) {
                 const int li = tag >> 24;
-                const uint32_t k = term < INF ? lookup(sw, s_lbase[li] + term) : KEY_INF;
+                const uint32_t k = term < pos_inf() ? lookup(sw, s_lbase[li] + term) : KEY_INF;
                 return k;
             };
             auto offer_tag = [&](uint32_t k, int tag) {

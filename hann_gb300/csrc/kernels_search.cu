@@ -611,13 +611,9 @@ cudaError_t launch_rerank(const ScanParams& p, const float* queries, int64_t nq,
     if (RP <= RW_MAX) {
         const size_t wsm = (size_t)(RR_THREADS / 32) * ((size_t)p.dim * sizeof(float) + (size_t)RP * 12);
         if (wsm <= 160 * 1024) {
-            static bool attr = false;
-            if (!attr) {
-                cudaError_t e = cudaFuncSetAttribute(rerank_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     160 * 1024);
-                if (e != cudaSuccess) return e;
-                attr = true;
-            }
+            cudaError_t e = cudaFuncSetAttribute(rerank_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 160 * 1024);
+            if (e != cudaSuccess) return e;
             rerank_warp_kernel<<<(unsigned)ceil_div(nq, RR_THREADS / 32), RR_THREADS, wsm, s>>>(
                 p, queries, nq, cand_row, cand_seq, R, RP, k, kmax, mode, ids, dist, nout);
             return cudaGetLastError();
