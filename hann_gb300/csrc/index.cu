@@ -1337,8 +1337,8 @@ int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_
         h->ev[st].clear();
         if (ms4) ms4[st] = tot;
     }
-    if (launches) *launches = h->launches;
-    h->launches = 0;
+    const int64_t nl = h->launches.exchange(0);
+    if (launches) *launches = nl;
     unsigned long long rows = 0;
     CK(cudaMemcpy(&rows, h->s_rows.p, sizeof(rows), cudaMemcpyDeviceToHost));
     CK(cudaMemset(h->s_rows.p, 0, sizeof(rows)));

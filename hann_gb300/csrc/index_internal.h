@@ -213,10 +213,11 @@ struct hann_pqivf {
     SearchScratch main;
     DBuf<unsigned long long> s_rows;
 
-    // stage profiling: pairs of events per stage
-    bool profile = false;
+    // stage profiling: pairs of events per stage (a diagnostic of the
+    // handle's own calls; not meant while a server drives the handle)
+    std::atomic<bool> profile{false};
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[4];
-    int64_t launches = 0;
+    std::atomic<int64_t> launches{0};  // kernels launched by searches (servers' threads included)
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];
