@@ -739,10 +739,11 @@ def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
     """The served stream: Poisson arrivals at `rate` requests/s, each a
     block of 1-512 queries (log-uniform), k uniform in [1, 100], nprobe
     log-uniform in [8, 256]; BulkAdd of 1,000-vector chunks and Deletes of
-    random ids, each at 1% of the request rate, applied between batches.
-    Queries are drawn from the first `nr` queries (which have ground truth).
-    Reports p50/p99 latency (submit to result), queries/s and recall@10 of
-    requests with k >= 10."""
+    random ids, each at 1% of the request rate, applied beside the running
+    batches. Queries are drawn from the first `nr` queries (which have ground
+    truth). Reports p50/p99 latency (submit to result, the server's clock),
+    queries/s, recall@10 over a sample of the requests with k >= 10, the
+    relayout holds and how late the submitter kept to its schedule."""
     import threading
     import queue as qmod
 
