@@ -595,6 +595,31 @@ def train_section(args, torch, dev):
                 log("snapshot", out["snapshot"])
             except Exception as e:  # pragma: no cover
                 out["snapshot"] = {"error": str(e)}
+            # the reference's own format: Save / Load through the gob stream
+            try:
+                import tempfile
+                with tempfile.TemporaryDirectory() as td:
+                    path = os.path.join(td, "index.gob")
+                    t = time.perf_counter()
+                    with open(path, "wb") as f:
+                        idx.Save(f)
+                    t_save = time.perf_counter() - t
+                    size = os.path.getsize(path)
+                    other = hg.New(dim)
+                    t = time.perf_counter()
+                    with open(path, "rb") as f:
+                        other.Load(f)
+                    torch.cuda.synchronize()
+                    t_load = time.perf_counter() - t
+                qs_ = x[:256].cpu().numpy()
+                same = all(np.array_equal(u, v) for u, v in zip(idx.SearchBatch(qs_, 10, nprobe=16, mode=1),
+                                                                 other.SearchBatch(qs_, 10, nprobe=16, mode=1)))
+                other.close()
+                out["gob"] = {"bytes": size, "save_s": round(t_save, 3), "load_s": round(t_load, 3),
+                              "same_results": bool(same)}
+                log("gob", out["gob"])
+            except Exception as e:  # pragma: no cover
+                out["gob"] = {"error": str(e)}
         if not plain and args.serve_seconds > 0:
             # the served stream on this 1M x 128 index as well
             try:

@@ -98,7 +98,9 @@ EXPORTED = (
     "hann_gpu_distance_matrix", "hann_knn_new", "hann_knn_free", "hann_knn_last_error", "hann_knn_search",
     "hann_knn_search_device", "hann_knn_get_stats", "hann_gpu_knn", "hann_pqivf_set_plain_fp32",
     "hann_serve_submit_priority", "hann_serve_cancel", "hann_pqivf_set_candidate_clusters",
-    "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot", "hann_pqivf_retrain",
+    "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot", "hann_pqivf_retrain", "hann_gob_encode",
+    "hann_gob_decode", "hann_gob_state_layout", "hann_gob_state_arrays", "hann_gob_state_free",
+    "hann_gob_last_error",
 )
 # Entry points of include/hann_gb300_diag.h.
 EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats")
@@ -147,6 +149,14 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_retrain.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_save_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_load_snapshot.argtypes = [_P, ctypes.c_char_p]
+        L.hann_gob_encode.argtypes = [ctypes.POINTER(_Layout)] + [_P] * 11 + [ctypes.c_int64, _P]
+        L.hann_gob_decode.argtypes = [_P, ctypes.c_int64, ctypes.POINTER(_P)]
+        L.hann_gob_state_layout.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(_Layout)]
+        L.hann_gob_state_arrays.argtypes = [_P] * 12
+        L.hann_gob_state_free.argtypes = [_P]
+        L.hann_gob_state_free.restype = None
+        L.hann_gob_last_error.argtypes = []
+        L.hann_gob_last_error.restype = ctypes.c_char_p
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
         L.hann_pqivf_list_lengths.argtypes = [_P, _P]
         L.hann_gpu_distance_matrix.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64,
@@ -508,13 +518,12 @@ class Index:
 
     def Save(self, w) -> None:
         """Write the reference's gob format (pqivf/index.go:1086-1093)."""
-        w.write(gob.encode_pqivf(state_to_gob(self.export_state())))
+        w.write(memoryview(gob_encode_state(self.export_state())))
 
     def Load(self, r) -> None:
         """Read the reference's gob format (pqivf/index.go:1095-1101)."""
         data = r.read() if hasattr(r, "read") else bytes(r)
-        ser = gob.decode_pqivf(data)
-        self.import_state(gob_to_state(ser, self._opts))
+        self.import_state(gob_decode_state(data, self._opts.candidate_clusters))
 
     def Retrain(self, iters: int) -> None:
         """Incremental re-Train: `iters` Lloyd iterations from the current
@@ -543,7 +552,60 @@ class Index:
 
 
 # ---------------------------------------------------------------------------
-# gob <-> array state
+# gob <-> array state. Save and Load use the native codec (csrc/gob.cu);
+# state_to_gob and gob_to_state pair the arrays with the pure-Python codec
+# in gob.py, which reads and writes the same bytes.
+
+
+def _gob_check(L, rc: int) -> None:
+    if rc != HANN_OK:
+        raise HannError(rc, L.hann_gob_last_error().decode())
+
+
+def gob_encode_state(st: dict) -> np.ndarray:
+    """The gob stream Save writes for export_state()'s arrays (GobEncode,
+    pqivf/index.go:992-1017, inside Save's encoder), as uint8."""
+    L = load_library()
+    lay = _Layout(**{f: int(st["layout"][f]) for f, _ in _Layout._fields_})
+    arrs = [np.ascontiguousarray(st["coarse"], np.float32), np.ascontiguousarray(st["codebooks"], np.float32),
+            np.ascontiguousarray(st["list_len"], np.int64), np.ascontiguousarray(st["list_key"], np.uint8),
+            np.ascontiguousarray(st["cluster_counts"], np.int64), np.ascontiguousarray(st["ids"], np.int64),
+            np.ascontiguousarray(st["vectors"], np.float32), np.ascontiguousarray(st["codes"], np.int32),
+            np.ascontiguousarray(st["pending_ids"], np.int64),
+            np.ascontiguousarray(st["pending_vectors"], np.float32)]
+    ptrs = [_ptr(a) for a in arrs]
+    n = ctypes.c_int64(0)
+    _gob_check(L, L.hann_gob_encode(ctypes.byref(lay), *ptrs, None, 0, ctypes.byref(n)))
+    out = np.empty(n.value, np.uint8)
+    _gob_check(L, L.hann_gob_encode(ctypes.byref(lay), *ptrs, _ptr(out), out.size, ctypes.byref(n)))
+    return out
+
+
+def gob_decode_state(data, default_candidate_clusters: int = 0) -> dict:
+    """Parse a gob stream and apply GobDecode's checks and defaults
+    (pqivf/index.go:1020-1084); the arrays import_state takes."""
+    L = load_library()
+    buf = np.frombuffer(data, np.uint8)
+    h = _P()
+    _gob_check(L, L.hann_gob_decode(_ptr(buf), buf.size, ctypes.byref(h)))
+    try:
+        lay = _Layout()
+        _gob_check(L, L.hann_gob_state_layout(h, int(default_candidate_clusters), ctypes.byref(lay)))
+        dim, M = lay.dimension, lay.num_subquantizers
+        nl, kq, nr, npd = lay.nlist, lay.pq_k_eff, lay.n_rows, lay.n_pending
+        st = {"layout": {f: getattr(lay, f) for f, _ in _Layout._fields_},
+              "coarse": np.zeros((nl, dim), np.float32), "codebooks": np.zeros((M, kq, dim // M), np.float32),
+              "list_len": np.zeros(nl, np.int64), "list_key": np.zeros(nl, np.uint8),
+              "cluster_counts": np.zeros(nl, np.int64), "ids": np.zeros(nr, np.int64),
+              "vectors": np.zeros((nr, dim), np.float32), "codes": np.zeros((nr, M), np.int32),
+              "has_codes": np.zeros(nr, np.uint8), "pending_ids": np.zeros(npd, np.int64),
+              "pending_vectors": np.zeros((npd, dim), np.float32)}
+        keys = ("coarse", "codebooks", "list_len", "list_key", "cluster_counts", "ids", "vectors", "codes",
+                "has_codes", "pending_ids", "pending_vectors")
+        _gob_check(L, L.hann_gob_state_arrays(h, *[_ptr(st[k]) for k in keys]))
+    finally:
+        L.hann_gob_state_free(h)
+    return st
 
 
 def state_to_gob(st: dict) -> dict:

@@ -263,6 +263,35 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* layout, const floa
                       const int64_t* ids, const float* vectors, const int32_t* codes, const uint8_t* has_codes,
                       const int64_t* pending_ids, const float* pending_vectors);
 
+/* ---- gob stream of Save/Load (pqivf/index.go:969-1101), host only -------
+ * Save is hann_pqivf_export + hann_gob_encode; Load is hann_gob_decode +
+ * hann_gob_state_layout + hann_gob_state_arrays + hann_pqivf_import. None of
+ * these calls touches the GPU. The gob bytes are those the reference's Save
+ * writes: the *pqivf.Index GobEncoder around a serializedPQIVF stream. */
+typedef struct hann_gob_state hann_gob_state;
+/* Encodes exported arrays (hann_pqivf_export's layout and arrays). With
+ * out == NULL only *out_len is set (the exact size); otherwise capacity
+ * must be at least that size. */
+int hann_gob_encode(const hann_pqivf_layout* layout, const float* coarse, const float* codebooks,
+                    const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
+                    const int64_t* ids, const float* vectors, const int32_t* codes, const int64_t* pending_ids,
+                    const float* pending_vectors, uint8_t* out, int64_t capacity, int64_t* out_len);
+/* Parses a gob stream (gob.Decoder.Decode of the *pqivf.Index value). */
+int hann_gob_decode(const uint8_t* data, int64_t len, hann_gob_state** out);
+/* GobDecode's checks and defaults (pqivf/index.go:1020-1084): the layout
+ * of the decoded index; default_candidate_clusters is the configured
+ * nprobe kept when the file carries none. */
+int hann_gob_state_layout(const hann_gob_state* st, int32_t default_candidate_clusters, hann_pqivf_layout* out);
+/* The decoded arrays, sized from the layout, as hann_pqivf_import takes
+ * them; has_codes[i] is 0 where entry i's codes are missing or out of
+ * range. */
+int hann_gob_state_arrays(const hann_gob_state* st, float* coarse, float* codebooks, int64_t* list_len,
+                          uint8_t* list_key, int64_t* cluster_counts, int64_t* ids, float* vectors, int32_t* codes,
+                          uint8_t* has_codes, int64_t* pending_ids, float* pending_vectors);
+void hann_gob_state_free(hann_gob_state* st);
+/* Message of the calling thread's last failed hann_gob_* call. */
+const char* hann_gob_last_error(void);
+
 /* Binary snapshot of the whole index (the content of Save/Load's gob
  * stream, pqivf/index.go:969-1101, as flat arrays with byte codes and a
  * checksum; layout in hann_gb300/csrc/snapshot.cu). Save lets searches run
