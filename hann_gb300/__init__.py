@@ -521,9 +521,24 @@ class Index:
         w.write(memoryview(gob_encode_state(self.export_state())))
 
     def Load(self, r) -> None:
-        """Read the reference's gob format (pqivf/index.go:1095-1101)."""
-        data = r.read() if hasattr(r, "read") else bytes(r)
-        self.import_state(gob_decode_state(data, self._opts.candidate_clusters))
+        """Read the reference's gob format (pqivf/index.go:1095-1101): the
+        stream from the reader's position to its end. A file on disk is
+        mapped rather than copied into memory."""
+        mapped = _map_rest(r)
+        if mapped is not None:
+            mm, off = mapped
+            try:
+                st = gob_decode_state(memoryview(mm)[off:], self._opts.candidate_clusters)
+                r.seek(0, os.SEEK_END)  # as read() would leave it
+            finally:
+                try:
+                    mm.close()
+                except BufferError:  # a traceback still holds a view: the map closes when that is freed
+                    pass
+        else:
+            data = r.read() if hasattr(r, "read") else bytes(r)
+            st = gob_decode_state(data, self._opts.candidate_clusters)
+        self.import_state(st)
 
     def Retrain(self, iters: int) -> None:
         """Incremental re-Train: `iters` Lloyd iterations from the current
@@ -555,6 +570,24 @@ class Index:
 # gob <-> array state. Save and Load use the native codec (csrc/gob.cu);
 # state_to_gob and gob_to_state pair the arrays with the pure-Python codec
 # in gob.py, which reads and writes the same bytes.
+
+
+def _map_rest(r):
+    """(read-only mmap of r's file, r's position) for a seekable file with
+    bytes after its position; None for anything else."""
+    import mmap
+
+    try:
+        fd, pos = r.fileno(), r.tell()
+        size = os.fstat(fd).st_size
+    except (AttributeError, OSError, ValueError, io.UnsupportedOperation):
+        return None
+    if pos >= size:
+        return None
+    try:
+        return mmap.mmap(fd, 0, access=mmap.ACCESS_READ), pos
+    except (OSError, ValueError):
+        return None
 
 
 def _gob_check(L, rc: int) -> None:

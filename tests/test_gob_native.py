@@ -215,3 +215,38 @@ def test_size_query_and_short_buffer():
     assert rc == hg.HANN_E_INVALID and n.value == full.size
     assert b"needed" in L.hann_gob_last_error()
     assert not out.any()  # nothing written
+
+
+def test_mapped_file_reads_from_position(tmp_path):
+    """Load maps a file on disk and decodes from the reader's position to
+    the end, as read() would; a bad stream in a mapped file still raises."""
+    st = random_state(np.random.default_rng(5))
+    blob = hg.gob_encode_state(st).tobytes()
+    p = tmp_path / "index.gob"
+    p.write_bytes(b"HEADER" + blob)
+    with open(p, "rb") as f:
+        f.read(6)
+        mm, off = hg._map_rest(f)
+        try:
+            got = hg.gob_decode_state(memoryview(mm)[off:])
+        finally:
+            mm.close()
+    want = hg.gob_decode_state(blob)
+    for k in KEYS:
+        np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+    # nothing after the position, a pipe-like reader, an in-memory stream
+    with open(p, "rb") as f:
+        f.seek(0, 2)
+        assert hg._map_rest(f) is None
+    import io
+    assert hg._map_rest(io.BytesIO(blob)) is None
+    bad = tmp_path / "bad.gob"
+    bad.write_bytes(blob[: len(blob) // 3])
+    with open(bad, "rb") as f:
+        mm, off = hg._map_rest(f)
+        with pytest.raises(hg.HannError):
+            hg.gob_decode_state(memoryview(mm)[off:])
+        try:
+            mm.close()
+        except BufferError:
+            pass

@@ -119,3 +119,23 @@ def test_snapshot_write_failure(tmp_path):
     os.mkdir(d)
     with pytest.raises(hg.HannError):
         idx.SaveSnapshot(d)  # a directory cannot be opened for writing
+
+
+def test_gob_file_round_trip(tmp_path):
+    """Save to a file and Load it back (the file is mapped, not read into
+    memory): the same index, the same bytes as an in-memory stream."""
+    idx, rng = trained_index(7)
+    path = tmp_path / "index.gob"
+    with open(path, "wb") as f:
+        idx.Save(f)
+    mem = io.BytesIO()
+    idx.Save(mem)
+    assert path.read_bytes() == mem.getvalue()
+    other = hg.New(3)
+    with open(path, "rb") as f:
+        other.Load(f)
+        assert f.read() == b""  # left at the end, as read() would
+    same_state(idx, other)
+    q = rng.normal(size=(32, 24)).astype(np.float32)
+    for u, v in zip(idx.SearchBatch(q, 9, mode=1), other.SearchBatch(q, 9, mode=1)):
+        np.testing.assert_array_equal(u, v)
