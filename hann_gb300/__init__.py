@@ -100,7 +100,7 @@ EXPORTED = (
     "hann_serve_submit_priority", "hann_serve_cancel", "hann_pqivf_set_candidate_clusters",
     "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot", "hann_pqivf_retrain", "hann_gob_encode",
     "hann_gob_decode", "hann_gob_state_layout", "hann_gob_state_arrays", "hann_gob_state_free",
-    "hann_gob_last_error",
+    "hann_gob_last_error", "hann_gob_encode_payload",
 )
 # Entry points of include/hann_gb300_diag.h.
 EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats")
@@ -150,6 +150,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_save_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_load_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_gob_encode.argtypes = [ctypes.POINTER(_Layout)] + [_P] * 11 + [ctypes.c_int64, _P]
+        L.hann_gob_encode_payload.argtypes = L.hann_gob_encode.argtypes
         L.hann_gob_decode.argtypes = [_P, ctypes.c_int64, ctypes.POINTER(_P)]
         L.hann_gob_state_layout.argtypes = [_P, ctypes.c_int32, ctypes.POINTER(_Layout)]
         L.hann_gob_state_arrays.argtypes = [_P] * 12
@@ -520,6 +521,16 @@ class Index:
         """Write the reference's gob format (pqivf/index.go:1086-1093)."""
         w.write(memoryview(gob_encode_state(self.export_state())))
 
+    def GobEncode(self) -> bytes:
+        """The serializedPQIVF gob stream (pqivf/index.go:992-1017)."""
+        return gob_encode_state(self.export_state(), wrapped=False).tobytes()
+
+    def GobDecode(self, data) -> None:
+        """Replace the index with a gob stream's content, GobDecode's checks
+        and defaults included (pqivf/index.go:1020-1084). Either GobEncode's
+        bytes or Save's stream."""
+        self.import_state(gob_decode_state(data, self._opts.candidate_clusters))
+
     def Load(self, r) -> None:
         """Read the reference's gob format (pqivf/index.go:1095-1101): the
         stream from the reader's position to its end. A file on disk is
@@ -595,10 +606,12 @@ def _gob_check(L, rc: int) -> None:
         raise HannError(rc, L.hann_gob_last_error().decode())
 
 
-def gob_encode_state(st: dict) -> np.ndarray:
+def gob_encode_state(st: dict, wrapped: bool = True) -> np.ndarray:
     """The gob stream Save writes for export_state()'s arrays (GobEncode,
-    pqivf/index.go:992-1017, inside Save's encoder), as uint8."""
+    pqivf/index.go:992-1017, inside Save's encoder), as uint8; with
+    wrapped=False, GobEncode's bytes alone."""
     L = load_library()
+    enc = L.hann_gob_encode if wrapped else L.hann_gob_encode_payload
     lay = _Layout(**{f: int(st["layout"][f]) for f, _ in _Layout._fields_})
     arrs = [np.ascontiguousarray(st["coarse"], np.float32), np.ascontiguousarray(st["codebooks"], np.float32),
             np.ascontiguousarray(st["list_len"], np.int64), np.ascontiguousarray(st["list_key"], np.uint8),
@@ -608,9 +621,9 @@ def gob_encode_state(st: dict) -> np.ndarray:
             np.ascontiguousarray(st["pending_vectors"], np.float32)]
     ptrs = [_ptr(a) for a in arrs]
     n = ctypes.c_int64(0)
-    _gob_check(L, L.hann_gob_encode(ctypes.byref(lay), *ptrs, None, 0, ctypes.byref(n)))
+    _gob_check(L, enc(ctypes.byref(lay), *ptrs, None, 0, ctypes.byref(n)))
     out = np.empty(n.value, np.uint8)
-    _gob_check(L, L.hann_gob_encode(ctypes.byref(lay), *ptrs, _ptr(out), out.size, ctypes.byref(n)))
+    _gob_check(L, enc(ctypes.byref(lay), *ptrs, _ptr(out), out.size, ctypes.byref(n)))
     return out
 
 

@@ -799,10 +799,16 @@ extern "C" {
 
 const char* hann_gob_last_error(void) { return g_gob_error.c_str(); }
 
-int hann_gob_encode(const hann_pqivf_layout* L, const float* coarse, const float* codebooks, const int64_t* list_len,
-                    const uint8_t* list_key, const int64_t* cluster_counts, const int64_t* ids, const float* vectors,
-                    const int32_t* codes, const int64_t* pending_ids, const float* pending_vectors, uint8_t* out,
-                    int64_t capacity, int64_t* out_len) {
+}  // extern "C"
+
+namespace {
+
+// wrap: the stream Save writes (the *pqivf.Index GobEncoder around the
+// payload); otherwise the payload alone, GobEncode's bytes.
+int encode_impl(const hann_pqivf_layout* L, const float* coarse, const float* codebooks, const int64_t* list_len,
+                const uint8_t* list_key, const int64_t* cluster_counts, const int64_t* ids, const float* vectors,
+                const int32_t* codes, const int64_t* pending_ids, const float* pending_vectors, uint8_t* out,
+                int64_t capacity, int64_t* out_len, bool wrap) {
     if (!L || !out_len) return fail(HANN_E_INVALID, "null layout or length");
     const int64_t dim = L->dimension, M = L->num_subquantizers, nl = L->nlist, kq = L->pq_k_eff;
     if (dim <= 0 || M <= 0 || dim % M != 0 || nl < 0 || kq < 0 || L->n_rows < 0 || L->n_pending < 0)
@@ -941,6 +947,7 @@ int hann_gob_encode(const hann_pqivf_layout* L, const float* coarse, const float
         put_int(outer, FIRST_USER_ID);
         outer.uint(0);  // singleton prefix
         outer.uint(inner_len);
+        if (!wrap) outer.b.clear();
         const size_t total = outer.b.size() + inner_len;
         *out_len = (int64_t)total;
         if (!out) return HANN_OK;  // size query
@@ -988,6 +995,27 @@ int hann_gob_encode(const hann_pqivf_layout* L, const float* coarse, const float
         return fail(HANN_E_NOMEM, "could not start encoder threads");
     }
     return HANN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hann_gob_encode(const hann_pqivf_layout* L, const float* coarse, const float* codebooks, const int64_t* list_len,
+                    const uint8_t* list_key, const int64_t* cluster_counts, const int64_t* ids, const float* vectors,
+                    const int32_t* codes, const int64_t* pending_ids, const float* pending_vectors, uint8_t* out,
+                    int64_t capacity, int64_t* out_len) {
+    return encode_impl(L, coarse, codebooks, list_len, list_key, cluster_counts, ids, vectors, codes, pending_ids,
+                       pending_vectors, out, capacity, out_len, true);
+}
+
+int hann_gob_encode_payload(const hann_pqivf_layout* L, const float* coarse, const float* codebooks,
+                            const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
+                            const int64_t* ids, const float* vectors, const int32_t* codes,
+                            const int64_t* pending_ids, const float* pending_vectors, uint8_t* out, int64_t capacity,
+                            int64_t* out_len) {
+    return encode_impl(L, coarse, codebooks, list_len, list_key, cluster_counts, ids, vectors, codes, pending_ids,
+                       pending_vectors, out, capacity, out_len, false);
 }
 
 int hann_gob_decode(const uint8_t* data, int64_t len, hann_gob_state** out) {

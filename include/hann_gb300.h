@@ -276,7 +276,16 @@ int hann_gob_encode(const hann_pqivf_layout* layout, const float* coarse, const 
                     const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
                     const int64_t* ids, const float* vectors, const int32_t* codes, const int64_t* pending_ids,
                     const float* pending_vectors, uint8_t* out, int64_t capacity, int64_t* out_len);
-/* Parses a gob stream (gob.Decoder.Decode of the *pqivf.Index value). */
+/* GobEncode's bytes (pqivf/index.go:992-1017): the serializedPQIVF stream
+ * alone, without Save's GobEncoder wrapper. Same size query and capacity
+ * rules as hann_gob_encode. */
+int hann_gob_encode_payload(const hann_pqivf_layout* layout, const float* coarse, const float* codebooks,
+                            const int64_t* list_len, const uint8_t* list_key, const int64_t* cluster_counts,
+                            const int64_t* ids, const float* vectors, const int32_t* codes,
+                            const int64_t* pending_ids, const float* pending_vectors, uint8_t* out, int64_t capacity,
+                            int64_t* out_len);
+/* Parses a gob stream: Save's (the *pqivf.Index GobEncoder value) or
+ * GobEncode's (a struct value, its fields matched by name). */
 int hann_gob_decode(const uint8_t* data, int64_t len, hann_gob_state** out);
 /* GobDecode's checks and defaults (pqivf/index.go:1020-1084): the layout
  * of the decoded index; default_candidate_clusters is the configured

@@ -4,6 +4,7 @@ from __future__ import annotations
 import numpy as np
 
 import oracle
+from hann_gb300 import gob
 
 # Distance tolerance of the parity bar: 1e-5 relative.
 REL = 1e-5
@@ -69,3 +70,21 @@ def gaussian_mixture(rng, n, dim, centers, sigma, center_scale=1.0):
     lab = rng.integers(0, centers, n)
     x = c[lab] + sigma * rng.normal(size=(n, dim))
     return x.astype(np.float32), c.astype(np.float32)
+
+
+def flat_struct_stream(fields):
+    """A gob stream holding one struct of int fields, as gob.NewEncoder
+    writes an anonymous struct value (the reference's tests build old and
+    future formats this way: fields are matched by name)."""
+    enc = gob._Encoder()
+    tid = enc.define_struct("", [(name, gob.T_INT) for name, _ in fields])
+    v = bytearray()
+    last = -1
+    for i, (_, val) in enumerate(fields):
+        if val:
+            gob._put_uint(v, i - last)
+            last = i
+            gob._put_int(v, val)
+    gob._put_uint(v, 0)
+    enc.value(tid, bytes(v))
+    return bytes(enc.out)

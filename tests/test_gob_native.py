@@ -9,6 +9,7 @@ import pytest
 
 import hann_gb300 as hg
 from hann_gb300 import gob
+from tests.helpers import flat_struct_stream
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "index_v1.gob")
 KEYS = ("coarse", "codebooks", "list_len", "list_key", "cluster_counts", "ids", "vectors", "codes", "has_codes",
@@ -250,3 +251,54 @@ def test_mapped_file_reads_from_position(tmp_path):
             mm.close()
         except BufferError:
             pass
+
+
+def test_gob_decode_errors():
+    """TestPQIVF_GobDecodeErrors (pqivf/index_test.go:741-764)."""
+    with pytest.raises(hg.HannError):
+        hg.gob_decode_state(b"not a gob stream")
+    with pytest.raises(hg.HannError, match="format version"):
+        hg.gob_decode_state(flat_struct_stream([("FormatVersion", 999)]))
+
+
+def test_gob_decode_legacy_fields():
+    """TestPQIVF_GobDecodeLegacyPendingVectors (pqivf/index_test.go:771-795):
+    a struct with only the five parameters decodes to an empty, untrained
+    index."""
+    st = hg.gob_decode_state(flat_struct_stream([("Dimension", 4), ("CoarseK", 2), ("NumSubquantizers", 2),
+                                                 ("PqK", 4), ("KMeansIters", 5)]))
+    lay = st["layout"]
+    assert (lay["dimension"], lay["coarse_k"], lay["num_subquantizers"], lay["pq_k"], lay["kmeans_iters"]) == \
+        (4, 2, 2, 4, 5)
+    assert (lay["nlist"], lay["n_rows"], lay["n_pending"], lay["trained"], lay["candidate_clusters"]) == \
+        (0, 0, 0, 0, 3)
+
+
+@pytest.mark.parametrize("fields", [
+    [("Dimension", 0)],
+    [("Dimension", 6), ("NumSubquantizers", 0)],
+    [("Dimension", 6), ("NumSubquantizers", 4)],
+    [("Dimension", 6), ("NumSubquantizers", 2), ("CoarseK", 0)],
+])
+def test_gob_decode_rejects_invalid_parameters(fields):
+    """TestPQIVF_GobDecodeRejectsInvalidParameters (pqivf/index_test.go:
+    944-980)."""
+    with pytest.raises(hg.HannError):
+        hg.gob_decode_state(flat_struct_stream(fields))
+
+
+def test_payload_is_the_wrapped_streams_content():
+    """GobEncode's bytes (pqivf/index.go:992-1017) are the serializedPQIVF
+    stream that Save's GobEncoder value carries."""
+    st = random_state(np.random.default_rng(12))
+    wrapped = hg.gob_encode_state(st).tobytes()
+    payload = hg.gob_encode_state(st, wrapped=False).tobytes()
+    assert wrapped.endswith(payload)
+    ((name, inner),) = gob.decode_stream(wrapped)
+    assert name == "*pqivf.Index" and inner == payload
+    ((name, ser),) = gob.decode_stream(payload)
+    assert name == "serializedPQIVF" and ser["Dimension"] == 12
+    a, b = hg.gob_decode_state(payload), hg.gob_decode_state(wrapped)
+    assert a["layout"] == b["layout"]
+    for k in KEYS:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)

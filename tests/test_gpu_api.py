@@ -270,3 +270,31 @@ def test_search_batch_uneven_k_and_nprobe():
     for i in (0, 17, 63):
         gi = idx.SearchBatch(q[i:i + 1], int(k[i]), nprobe=int(npb[i]))
         assert np.array_equal(gi[0][0, :gi[2][0]], g[0][i, :g[2][i]])
+
+
+def test_gob_encode_decode_methods():
+    """GobEncode / GobDecode on the index (pqivf/index.go:992-1084), and a
+    struct holding only the five parameters decodes to an empty index that
+    takes an Add (pqivf/index_test.go:771-795)."""
+    from tests.helpers import flat_struct_stream
+
+    rng = np.random.default_rng(9)
+    x = rng.normal(size=(800, 8)).astype(np.float32)
+    idx = new_index(8, 8, 2, 16, 5)
+    idx.BulkAddArrays(np.arange(800), x)
+    idx.Train()
+    data = idx.GobEncode()
+    other = hg.New(8)
+    other.GobDecode(data)
+    a, b = idx.export_state(), other.export_state()
+    assert a["layout"] == b["layout"]
+    for key in ("coarse", "codebooks", "list_len", "ids", "vectors", "codes"):
+        assert np.array_equal(a[key], b[key]), key
+    legacy = hg.New(4)
+    legacy.GobDecode(flat_struct_stream([("Dimension", 4), ("CoarseK", 2), ("NumSubquantizers", 2), ("PqK", 4),
+                                         ("KMeansIters", 5)]))
+    legacy.Add(1, [1, 2, 3, 4])
+    assert legacy.Stats().Count == 1
+    with pytest.raises(hg.HannError):
+        legacy.GobDecode(b"not a gob stream")
+    assert legacy.Stats().Count == 1  # a failed decode changes nothing
