@@ -34,6 +34,7 @@ HANN_E_STATE = -4
 HANN_E_CUDA = -5
 HANN_E_NOMEM = -6
 HANN_E_UNSUPPORTED = -7
+HANN_E_CHANGED = -8
 
 MODE_PARITY = 0
 MODE_EXACT_RERANK = 1
@@ -139,7 +140,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                                                      ctypes.c_int32, _P, _P, _P, _P]
         L.hann_pqivf_stats.argtypes = [_P, ctypes.POINTER(_Stats)]
         L.hann_pqivf_export_layout.argtypes = [_P, ctypes.POINTER(_Layout)]
-        L.hann_pqivf_export.argtypes = [_P] + [_P] * 10
+        L.hann_pqivf_export.argtypes = [_P, ctypes.POINTER(_Layout)] + [_P] * 10
         L.hann_pqivf_import.argtypes = [_P, ctypes.POINTER(_Layout)] + [_P] * 11
         L.hann_gpu_distance_batch.argtypes = [ctypes.c_int32, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
@@ -159,7 +160,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_gob_last_error.argtypes = []
         L.hann_gob_last_error.restype = ctypes.c_char_p
         L.hann_pqivf_stage_times.argtypes = [_P, _P, _P, _P]
-        L.hann_pqivf_list_lengths.argtypes = [_P, _P]
+        L.hann_pqivf_list_lengths.argtypes = [_P, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
         L.hann_gpu_distance_matrix.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64,
                                                ctypes.c_int32, _P]
         L.hann_knn_new.argtypes = [_P, ctypes.c_int64, ctypes.c_int32]
@@ -467,9 +468,14 @@ class Index:
         return ms, int(n.value), int(rows.value)
 
     def ListLengths(self) -> np.ndarray:
-        out = np.zeros(max(self.DeviceStats()["nlist"], 1), dtype=np.int64)
-        self._check(self._L.hann_pqivf_list_lengths(self._h, _ptr(out)))
-        return out[:self.DeviceStats()["nlist"]]
+        n = ctypes.c_int32(self.DeviceStats()["nlist"])
+        for _ in range(100):
+            out = np.zeros(max(n.value, 1), dtype=np.int64)
+            rc = self._L.hann_pqivf_list_lengths(self._h, _ptr(out), out.size, ctypes.byref(n))
+            if rc != HANN_E_CHANGED:  # else a Train changed the list count: size again
+                break
+        self._check(rc)
+        return out[:n.value]
 
     def Stats(self) -> IndexStats:
         s = self._stats_raw()
@@ -481,24 +487,29 @@ class Index:
 
     # -- persistence ---------------------------------------------------------
     def export_state(self) -> dict:
-        """The index state as arrays (the GobEncode payload, pqivf/index.go:992-1017)."""
-        lay = _Layout()
-        self._check(self._L.hann_pqivf_export_layout(self._h, ctypes.byref(lay)))
-        dim, M = lay.dimension, lay.num_subquantizers
-        nl, kq, nr, npd = lay.nlist, lay.pq_k_eff, lay.n_rows, lay.n_pending
-        coarse = np.zeros((nl, dim), np.float32)
-        cbs = np.zeros((M, kq, dim // M), np.float32)
-        llen = np.zeros(nl, np.int64)
-        lkey = np.zeros(nl, np.uint8)
-        counts = np.zeros(nl, np.int64)
-        ids = np.zeros(nr, np.int64)
-        vecs = np.zeros((nr, dim), np.float32)
-        codes = np.zeros((nr, M), np.int32)
-        pids = np.zeros(npd, np.int64)
-        pvecs = np.zeros((npd, dim), np.float32)
-        self._check(self._L.hann_pqivf_export(self._h, _ptr(coarse), _ptr(cbs), _ptr(llen), _ptr(lkey),
-                                              _ptr(counts), _ptr(ids), _ptr(vecs), _ptr(codes), _ptr(pids),
-                                              _ptr(pvecs)))
+        """The index state as arrays (the GobEncode payload, pqivf/index.go:992-1017),
+        one consistent state even while other threads mutate the index."""
+        for _ in range(10_000):
+            lay = _Layout()
+            self._check(self._L.hann_pqivf_export_layout(self._h, ctypes.byref(lay)))
+            dim, M = lay.dimension, lay.num_subquantizers
+            nl, kq, nr, npd = lay.nlist, lay.pq_k_eff, lay.n_rows, lay.n_pending
+            coarse = np.empty((nl, dim), np.float32)
+            cbs = np.empty((M, kq, dim // M), np.float32)
+            llen = np.empty(nl, np.int64)
+            lkey = np.empty(nl, np.uint8)
+            counts = np.empty(nl, np.int64)
+            ids = np.empty(nr, np.int64)
+            vecs = np.empty((nr, dim), np.float32)
+            codes = np.empty((nr, M), np.int32)
+            pids = np.empty(npd, np.int64)
+            pvecs = np.empty((npd, dim), np.float32)
+            rc = self._L.hann_pqivf_export(self._h, ctypes.byref(lay), _ptr(coarse), _ptr(cbs), _ptr(llen),
+                                           _ptr(lkey), _ptr(counts), _ptr(ids), _ptr(vecs), _ptr(codes), _ptr(pids),
+                                           _ptr(pvecs))
+            if rc != HANN_E_CHANGED:  # else a mutation resized the index after the layout was read
+                break
+        self._check(rc)
         return {"layout": {f: getattr(lay, f) for f, _ in _Layout._fields_}, "coarse": coarse, "codebooks": cbs,
                 "list_len": llen, "list_key": lkey, "cluster_counts": counts, "ids": ids, "vectors": vecs,
                 "codes": codes, "pending_ids": pids, "pending_vectors": pvecs}

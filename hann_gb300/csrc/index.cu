@@ -13,7 +13,10 @@
 #include "index_internal.h"
 #include "hann_gb300_diag.h"
 
-static thread_local std::string g_new_error;
+std::string& hann_thread_error() {
+    static thread_local std::string e;
+    return e;
+}
 
 
 // Capacity for a list that must hold `len` rows.
@@ -912,7 +915,7 @@ void hann_pqivf_options_init(hann_pqivf_options* o, int32_t dimension) {
 int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out) {
     char buf[256];
     auto bad = [&](int code) {
-        g_new_error = buf;
+        hann_thread_error() = buf;
         return code;
     };
     if (!opts || !out) {
@@ -982,7 +985,7 @@ void hann_pqivf_free(hann_pqivf* h) {
     delete h;
 }
 
-const char* hann_pqivf_last_error(const hann_pqivf* h) { return h ? h->err.c_str() : g_new_error.c_str(); }
+const char* hann_pqivf_last_error(const hann_pqivf*) { return hann_thread_error().c_str(); }
 
 int hann_pqivf_bulk_add(hann_pqivf* h, const int64_t* ids, const float* vectors, int64_t n) {
     if (!h) return HANN_E_INVALID;
@@ -1346,9 +1349,12 @@ int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_
     return HANN_OK;
 }
 
-int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out) {
-    if (!h || !out) return HANN_E_INVALID;
+int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out, int32_t capacity, int32_t* n_out) {
+    if (!h || !n_out || (capacity > 0 && !out)) return HANN_E_INVALID;
     std::shared_lock<std::shared_mutex> lk(h->mu);
+    *n_out = h->nlist;
+    if (h->nlist > capacity)
+        return h->fail(HANN_E_CHANGED, "the index has %d lists, the buffer holds %d", h->nlist, (int)capacity);
     for (int l = 0; l < h->nlist; l++) out[l] = h->live_count[l];
     return HANN_OK;
 }
@@ -1365,9 +1371,10 @@ int hann_pqivf_stats(hann_pqivf* h, hann_pqivf_index_stats* out) {
     return HANN_OK;
 }
 
-int hann_pqivf_export_layout(hann_pqivf* h, hann_pqivf_layout* out) {
-    if (!h || !out) return HANN_E_INVALID;
-    std::shared_lock<std::shared_mutex> lk(h->mu);
+}  // extern "C"
+
+// The handle's layout; the caller holds h->mu.
+static void layout_locked(const hann_pqivf* h, hann_pqivf_layout* out) {
     out->dimension = h->o.dimension;
     out->coarse_k = h->o.coarse_k;
     out->num_subquantizers = h->o.num_subquantizers;
@@ -1380,16 +1387,32 @@ int hann_pqivf_export_layout(hann_pqivf* h, hann_pqivf_layout* out) {
     out->pq_k_eff = h->pqk_eff;
     out->n_rows = h->total_rows();
     out->n_pending = (int64_t)h->pending.size();
+}
+
+extern "C" {
+
+int hann_pqivf_export_layout(hann_pqivf* h, hann_pqivf_layout* out) {
+    if (!h || !out) return HANN_E_INVALID;
+    std::shared_lock<std::shared_mutex> lk(h->mu);
+    layout_locked(h, out);
     return HANN_OK;
 }
 
-int hann_pqivf_export(hann_pqivf* h, float* coarse, float* codebooks, int64_t* list_len, uint8_t* list_key,
-                      int64_t* cluster_counts, int64_t* ids, float* vectors, int32_t* codes, int64_t* pending_ids,
-                      float* pending_vectors) {
-    if (!h) return HANN_E_INVALID;
+int hann_pqivf_export(hann_pqivf* h, const hann_pqivf_layout* layout, float* coarse, float* codebooks,
+                      int64_t* list_len, uint8_t* list_key, int64_t* cluster_counts, int64_t* ids, float* vectors,
+                      int32_t* codes, int64_t* pending_ids, float* pending_vectors) {
+    if (!h || !layout) return HANN_E_INVALID;
     std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
+    // The arrays were sized from `layout`; a mutation since then would make
+    // the copies below overrun them.
+    hann_pqivf_layout now;
+    layout_locked(h, &now);
+    if (now.dimension != layout->dimension || now.num_subquantizers != layout->num_subquantizers ||
+        now.nlist != layout->nlist || now.pq_k_eff != layout->pq_k_eff || now.n_rows != layout->n_rows ||
+        now.n_pending != layout->n_pending)
+        return h->fail(HANN_E_CHANGED, "the index changed since its layout was read; read the layout again");
     cudaSetDevice(h->o.device);
     const int dim = h->o.dimension, M = h->o.num_subquantizers;
     if (h->nlist > 0) {

@@ -154,6 +154,11 @@ struct SearchScratch {
     DBuf<int32_t> qorder, order_scratch;  // L2-friendly query order for scan and rerank
 };
 
+// Message of the calling thread's last failed call on any handle. Kept per
+// thread (as errno is) so that concurrent callers of one handle each read
+// their own failure, and no thread rewrites a string another one reads.
+std::string& hann_thread_error();
+
 struct hann_pqivf {
     hann_pqivf_options o{};
     int dsub = 0, code_stride = 0;
@@ -161,7 +166,6 @@ struct hann_pqivf {
     std::mutex wmu;         // every writer; taken before mu
     std::mutex run_mu;
     MutationScratch mut;
-    std::string err;
     cudaStream_t stream = nullptr;
     Rng rng;
     bool trained = false;
@@ -225,7 +229,7 @@ struct hann_pqivf {
         va_start(ap, fmt);
         vsnprintf(buf, sizeof(buf), fmt, ap);
         va_end(ap);
-        err = buf;
+        hann_thread_error() = buf;
         return code;
     }
     int cuda_fail(cudaError_t e, const char* what) {

@@ -51,6 +51,9 @@ __global__ void knn_fill_kernel(int64_t nq, int k, int64_t n, int64_t* __restric
 
 using namespace hann;
 
+// Message of the calling thread's last failed hann_knn_* call.
+static thread_local std::string t_knn_error;
+
 struct hann_knn {
     int64_t n = 0;
     int dim = 0, kp = 0;
@@ -74,15 +77,14 @@ struct hann_knn {
 
     cudaStream_t stream = nullptr;
     std::mutex mu;
-    std::string err;
     hann_knn_stats stats{};
 
     int fail(int code, const char* msg) {
-        err = msg;
+        t_knn_error = msg;
         return code;
     }
     int cuda_fail(cudaError_t e, const char* what) {
-        err = std::string(what) + ": " + cudaGetErrorString(e);
+        t_knn_error = std::string(what) + ": " + cudaGetErrorString(e);
         return HANN_E_CUDA;
     }
 };
@@ -322,7 +324,7 @@ void hann_knn_free(hann_knn* h) {
     delete h;
 }
 
-const char* hann_knn_last_error(const hann_knn* h) { return h ? h->err.c_str() : "null handle"; }
+const char* hann_knn_last_error(const hann_knn*) { return t_knn_error.c_str(); }
 
 int hann_knn_search(hann_knn* h, int32_t metric, const float* queries, int64_t nq, int32_t k, int32_t method,
                     int64_t* ids, double* dist) {

@@ -71,6 +71,14 @@ struct Slot {
 
 }  // namespace
 
+// Message of the calling thread's last failed hann_serve_* call.
+static thread_local std::string t_serve_error;
+
+static int serve_fail(int rc, const char* msg) {
+    t_serve_error = msg;
+    return rc;
+}
+
 struct hann_server {
     hann_pqivf* h = nullptr;
     hann_serve_options o{};
@@ -83,7 +91,6 @@ struct hann_server {
     uint64_t next_ticket = 1;
     bool stop = false;
     std::thread thr;
-    std::string err;
     // statistics
     std::vector<double> lat_ms;
     int64_t queries_done = 0, requests_done = 0, batches = 0, mutations = 0;
@@ -245,7 +252,7 @@ void mutator(hann_server* s) {
             s->cv_work.notify_one();
         }
         s->mqueue.pop_front();
-        if (rc) r->error = h->err;
+        if (rc) r->error = hann_thread_error();
         r->status = rc;
         r->t_done = Clock::now();
         s->mutations++;
@@ -336,7 +343,7 @@ void scheduler(hann_server* s) {
                 if (!s->read_lock.owns_lock()) s->read_lock = std::shared_lock<std::shared_mutex>(h->mu);
                 const int rc = launch_batch(s, sl, take);
                 if (rc) {
-                    fail_requests(s, take, rc, h->err);
+                    fail_requests(s, take, rc, hann_thread_error());
                     sl.reqs.clear();
                     sl.busy = false;
                     s->cv_done.notify_all();
@@ -451,7 +458,7 @@ int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server*
 
 static int submit(hann_server* s, std::shared_ptr<Request> r, uint64_t* ticket) {
     std::lock_guard<std::mutex> lk(s->mu);
-    if (s->stop) return HANN_E_STATE;
+    if (s->stop) return serve_fail(HANN_E_STATE, "the server is stopping");
     r->ticket = s->next_ticket++;
     r->t_submit = Clock::now();
     if (!s->any) {
@@ -467,8 +474,8 @@ static int submit(hann_server* s, std::shared_ptr<Request> r, uint64_t* ticket) 
 }
 
 int hann_serve_submit(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe, uint64_t* ticket) {
-    if (!s || !queries || nq <= 0) return HANN_E_INVALID;
-    if (k <= 0 || k > s->o.max_k) return HANN_E_INVALID;
+    if (!s || !queries || nq <= 0) return serve_fail(HANN_E_INVALID, "invalid arguments: no queries");
+    if (k <= 0 || k > s->o.max_k) return serve_fail(HANN_E_INVALID, "k must be in [1, the server's max_k]");
     if (nprobe <= 0) nprobe = s->h->o.candidate_clusters;
     if (nprobe > s->o.max_nprobe) nprobe = s->o.max_nprobe;
     auto r = std::make_shared<Request>();
@@ -482,8 +489,8 @@ int hann_serve_submit(hann_server* s, const float* queries, int32_t nq, int32_t 
 
 int hann_serve_submit_priority(hann_server* s, const float* queries, int32_t nq, int32_t k, int32_t nprobe,
                                int32_t priority, uint64_t* ticket) {
-    if (!s || !queries || nq <= 0) return HANN_E_INVALID;
-    if (k <= 0 || k > s->o.max_k) return HANN_E_INVALID;
+    if (!s || !queries || nq <= 0) return serve_fail(HANN_E_INVALID, "invalid arguments: no queries");
+    if (k <= 0 || k > s->o.max_k) return serve_fail(HANN_E_INVALID, "k must be in [1, the server's max_k]");
     if (nprobe <= 0) nprobe = s->h->o.candidate_clusters;
     if (nprobe > s->o.max_nprobe) nprobe = s->o.max_nprobe;
     auto r = std::make_shared<Request>();
@@ -500,7 +507,7 @@ int hann_serve_cancel(hann_server* s, uint64_t ticket) {
     if (!s) return HANN_E_INVALID;
     std::lock_guard<std::mutex> lk(s->mu);
     auto it = s->tickets.find(ticket);
-    if (it == s->tickets.end()) return HANN_E_NOT_FOUND;
+    if (it == s->tickets.end()) return serve_fail(HANN_E_NOT_FOUND, "unknown ticket");
     auto r = it->second;
     for (auto* qq : {&s->queue_hi, &s->queue}) {
         for (auto q = qq->begin(); q != qq->end(); ++q) {
@@ -514,12 +521,11 @@ int hann_serve_cancel(hann_server* s, uint64_t ticket) {
             return HANN_OK;
         }
     }
-    s->err = "request already started or finished";
-    return HANN_E_STATE;
+    return serve_fail(HANN_E_STATE, "request already started or finished");
 }
 
 int hann_serve_submit_add(hann_server* s, const int64_t* ids, const float* vectors, int64_t n, uint64_t* ticket) {
-    if (!s || n < 0 || (n > 0 && (!ids || !vectors))) return HANN_E_INVALID;
+    if (!s || n < 0 || (n > 0 && (!ids || !vectors))) return serve_fail(HANN_E_INVALID, "invalid arguments");
     auto r = std::make_shared<Request>();
     r->kind = 1;
     r->ids.assign(ids, ids + n);
@@ -528,7 +534,7 @@ int hann_serve_submit_add(hann_server* s, const int64_t* ids, const float* vecto
 }
 
 int hann_serve_submit_delete(hann_server* s, const int64_t* ids, int64_t n, uint64_t* ticket) {
-    if (!s || n < 0 || (n > 0 && !ids)) return HANN_E_INVALID;
+    if (!s || n < 0 || (n > 0 && !ids)) return serve_fail(HANN_E_INVALID, "invalid arguments");
     auto r = std::make_shared<Request>();
     r->kind = 2;
     r->ids.assign(ids, ids + n);
@@ -540,18 +546,17 @@ int hann_serve_wait(hann_server* s, uint64_t ticket, int64_t* ids, double* dista
     if (!s) return HANN_E_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->tickets.find(ticket);
-    if (it == s->tickets.end()) return HANN_E_NOT_FOUND;
+    if (it == s->tickets.end()) return serve_fail(HANN_E_NOT_FOUND, "unknown ticket");
     auto r = it->second;
     const auto deadline = Clock::now() + std::chrono::milliseconds(timeout_ms < 0 ? 1000000000 : timeout_ms);
     while (r->status == 1) {
         if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && r->status == 1) {
-            s->err = "timed out waiting for the request";
-            return HANN_E_STATE;
+            return serve_fail(HANN_E_STATE, "timed out waiting for the request");
         }
     }
     s->tickets.erase(it);
     if (r->status < 0) {
-        s->err = r->error;
+        t_serve_error = r->error;
         return r->status;
     }
     if (r->kind == 0) {
@@ -589,7 +594,7 @@ int hann_serve_stats(hann_server* s, hann_serve_statistics* out) {
     return HANN_OK;
 }
 
-const char* hann_serve_last_error(const hann_server* s) { return s ? s->err.c_str() : ""; }
+const char* hann_serve_last_error(const hann_server*) { return t_serve_error.c_str(); }
 
 int hann_serve_stop(hann_server* s) {
     if (!s) return HANN_E_INVALID;

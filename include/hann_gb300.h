@@ -32,6 +32,7 @@ extern "C" {
 #define HANN_E_CUDA -5        /* CUDA runtime failure */
 #define HANN_E_NOMEM -6       /* device or host allocation failed */
 #define HANN_E_UNSUPPORTED -7 /* valid for the reference, outside this build's limits */
+#define HANN_E_CHANGED -8     /* the index changed between a size query and the call sized from it: query again */
 
 typedef struct hann_pqivf hann_pqivf;
 
@@ -71,8 +72,10 @@ typedef struct {
 /* pqivf.New (pqivf/index.go:106-146). Validation errors as the reference. */
 int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out);
 void hann_pqivf_free(hann_pqivf* h);
-/* Message of the last failure on this handle (or of the last failed
- * hann_pqivf_new on this thread when h is NULL). */
+/* Message of the calling thread's last failed hann_pqivf_* call, on any
+ * handle (h may be NULL, e.g. after a failed hann_pqivf_new). Kept per
+ * thread, as errno is, so that threads sharing a handle each read their own
+ * failure; valid until this thread's next failing call. */
 const char* hann_pqivf_last_error(const hann_pqivf* h);
 
 /* Index.Add (core/index.go:25; pqivf/index.go:212-237). */
@@ -151,8 +154,9 @@ int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on);
  * the rows scanned, then clears them. */
 int hann_pqivf_set_profiling(hann_pqivf* h, int32_t on);
 int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_t* rows_scanned);
-/* Current length of every inverted list (nlist entries). */
-int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out);
+/* Current length of every inverted list: *n_out = nlist, and out[0..nlist)
+ * when nlist <= capacity, else HANN_E_CHANGED (a Train changed nlist). */
+int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out, int32_t capacity, int32_t* n_out);
 
 /* Allocation-free variant of hann_pqivf_search_batch_device. It has no
  * counterpart in the reference. It is for callers that cannot allocate
@@ -231,6 +235,8 @@ int hann_serve_submit_delete(hann_server* s, const int64_t* ids, int64_t n, uint
 int hann_serve_wait(hann_server* s, uint64_t ticket, int64_t* ids, double* distances, int32_t* n_out,
                     int32_t timeout_ms, double* latency_ms);
 int hann_serve_stats(hann_server* s, hann_serve_statistics* out);
+/* Message of the calling thread's last failed hann_serve_* call (per
+ * thread, as hann_pqivf_last_error). */
 const char* hann_serve_last_error(const hann_server* s);
 /* Finishes the queued work, then releases the server. */
 int hann_serve_stop(hann_server* s);
@@ -247,15 +253,18 @@ typedef struct {
 } hann_pqivf_layout;
 
 int hann_pqivf_export_layout(hann_pqivf* h, hann_pqivf_layout* out);
-/* Arrays sized from the layout: coarse [nlist*dim], codebooks
- * [M*pq_k_eff*(dim/M)], list_len [nlist], list_key [nlist] (1 when the
- * reference's list map holds the cluster), cluster_counts [nlist], ids
- * [n_rows] (list by list, in storage order), vectors [n_rows*dim], codes
- * [n_rows*M] (int32), pending_ids [n_pending], pending_vectors
- * [n_pending*dim]. */
-int hann_pqivf_export(hann_pqivf* h, float* coarse, float* codebooks, int64_t* list_len, uint8_t* list_key,
-                      int64_t* cluster_counts, int64_t* ids, float* vectors, int32_t* codes, int64_t* pending_ids,
-                      float* pending_vectors);
+/* Arrays sized from `layout` (what hann_pqivf_export_layout returned):
+ * coarse [nlist*dim], codebooks [M*pq_k_eff*(dim/M)], list_len [nlist],
+ * list_key [nlist] (1 when the reference's list map holds the cluster),
+ * cluster_counts [nlist], ids [n_rows] (list by list, in storage order),
+ * vectors [n_rows*dim], codes [n_rows*M] (int32), pending_ids [n_pending],
+ * pending_vectors [n_pending*dim]. The arrays are one consistent state
+ * (GobEncode holds the read lock the same way, pqivf/index.go:992-1017);
+ * when a mutation changed those sizes after the layout was read, nothing is
+ * written and HANN_E_CHANGED is returned: read the layout again. */
+int hann_pqivf_export(hann_pqivf* h, const hann_pqivf_layout* layout, float* coarse, float* codebooks,
+                      int64_t* list_len, uint8_t* list_key, int64_t* cluster_counts, int64_t* ids, float* vectors,
+                      int32_t* codes, int64_t* pending_ids, float* pending_vectors);
 /* Replaces the handle's state (GobDecode, pqivf/index.go:1020-1084). Codes
  * of an entry with has_codes[i] == 0 are recomputed on the device. */
 int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* layout, const float* coarse, const float* codebooks,
@@ -357,6 +366,8 @@ typedef struct hann_knn_stats {
 /* Copies the flat base [n][dim] (host) to the device. NULL on failure. */
 hann_knn* hann_knn_new(const float* base, int64_t n, int32_t dim);
 void hann_knn_free(hann_knn* h);
+/* Message of the calling thread's last failed hann_knn_* call, also after
+ * a hann_knn_new that returned NULL (per thread, as hann_pqivf_last_error). */
 const char* hann_knn_last_error(const hann_knn* h);
 /* Host buffers: queries [nq][dim], ids [nq][k], dist [nq][k]. */
 int hann_knn_search(hann_knn* h, int32_t metric, const float* queries, int64_t nq, int32_t k, int32_t method,
