@@ -436,14 +436,16 @@ namespace {
 enum EntryRole { R_SKIP, R_ID, R_VEC, R_CODES, R_CLUSTER };
 
 // Ids below 9 are gob's basic types and interface; a stream numbers its own
-// types from a first user id (64 in Go's encoder, 65 in the Python codec).
+// types from a first user id (64 in Go's encoder, 65 in the Python codec),
+// one id per type it sends, so ids stay small: a larger one is malformed.
 constexpr int FIRST_DEFINABLE_ID = 9;
+constexpr int MAX_TYPE_ID = 1 << 16;
 
 struct Dec {
     std::vector<WireType> types;
     std::vector<uint8_t> known;
     void define(int tid, WireType wt) {
-        if (tid < FIRST_DEFINABLE_ID || tid > (1 << 20)) throw Err();
+        if (tid < FIRST_DEFINABLE_ID || tid > MAX_TYPE_ID) throw Err();
         if ((size_t)tid >= types.size()) {
             types.resize(tid + 1);
             known.resize(tid + 1, 0);
@@ -780,7 +782,7 @@ template <typename F> void each_value(const uint8_t* data, size_t len, Dec& dec,
         In m(r.take(n), (size_t)n);
         const int64_t tid = m.sint();
         if (tid < 0) {
-            if (tid < -(int64_t)(1 << 20)) throw Err();
+            if (tid < -(int64_t)MAX_TYPE_ID) throw Err();
             dec.define((int)-tid, decode_wiretype(m));
             continue;
         }

@@ -302,3 +302,17 @@ def test_payload_is_the_wrapped_streams_content():
     assert a["layout"] == b["layout"]
     for k in KEYS:
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_out_of_range_type_ids_rejected():
+    """A type definition with an id far beyond any stream's own numbering,
+    or a value of an undefined type, is malformed."""
+    for tid in (-(1 << 17), -(1 << 30), 1 << 17, 3, 70):
+        msg = bytearray()
+        gob._put_int(msg, tid)
+        msg += b"\x01\x02\x03"
+        data = bytearray()
+        gob._put_uint(data, len(msg))
+        data += msg
+        with pytest.raises(hg.HannError):
+            hg.gob_decode_state(bytes(data))
