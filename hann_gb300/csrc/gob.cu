@@ -423,7 +423,8 @@ struct hann_gob_state {
     // Rows of all lists, stream order. Left uninitialised where an entry is
     // malformed; such an index is rejected before the rows are read.
     Buf<int64_t> ids;
-    Buf<float> vecs;       // rows x dimension
+    Buf<float> vecs;       // rows x dimension, when vecs_stored
+    bool vecs_stored = false;
     Buf<int64_t> ncodes;   // codes per row
     Buf<int32_t> codes;    // row after row; -1 for a value outside int32
     std::vector<int64_t> pending_ids;
@@ -515,19 +516,25 @@ struct Dec {
         }
         return n;
     }
-    // Appends the rows of a [][]float32 to out, each of length want (a row
-    // of another length sets bad and leaves zeros); returns the row count.
+    // Appends the rows of a [][]float32 to out when each has length want; a
+    // row of another length sets bad (the index is then rejected) and is not
+    // stored. Storage grows only by floats the stream holds, so a small
+    // malformed stream cannot make a large allocation. Returns the row count.
     int64_t float_rows(In& r, int tid, int64_t want, std::vector<float>& out, bool& bad) {
         const WireType& wt = type(tid);
         if (wt.kind != 1 && wt.kind != 2) throw Err();
         float_slice(wt.elem);
         const uint64_t n = r.count();
-        const size_t w = (size_t)std::max<int64_t>(want, 0);
-        const size_t base = out.size();
-        out.resize(base + (size_t)n * w, 0.0f);
         for (uint64_t j = 0; j < n; j++) {
-            const uint64_t got = floats_into(r, out.data() + base + j * w, want > 0 ? want : -1);
-            if ((int64_t)got != want) bad = true;
+            const uint64_t k = r.count();
+            if (want > 0 && (int64_t)k == want) {
+                const size_t base = out.size();
+                out.resize(base + (size_t)k);
+                for (uint64_t i = 0; i < k; i++) out[base + i] = r.flt();
+            } else {
+                for (uint64_t i = 0; i < k; i++) r.skip_uint();
+                bad = true;
+            }
         }
         return (int64_t)n;
     }
@@ -610,8 +617,8 @@ struct Dec {
                 case R_ID: st.ids[row] = integer(r, ft); break;
                 case R_CLUSTER: (void)integer(r, ft); break;
                 case R_VEC: {
-                    const uint64_t got = floats_into(r, dim > 0 ? st.vecs.data() + row * dim : nullptr,
-                                                     dim > 0 ? dim : -1);
+                    const uint64_t got = floats_into(r, st.vecs_stored ? st.vecs.data() + row * dim : nullptr,
+                                                     st.vecs_stored ? dim : -1);
                     have_vec = true;
                     if ((int64_t)got != dim && g.bad_row < 0) {
                         g.bad_row = row;
@@ -665,11 +672,14 @@ struct Dec {
             st.segs.push_back(g);
         }
         const size_t end = r.i;
-        const int64_t dim = st.dimension;
+        // Vectors get rows x dim floats only when the stream is long enough to
+        // hold them all at full length; when it is not, some entry's vector is
+        // short (the index is rejected) and none is stored.
+        st.vecs_stored = st.dimension > 0 && rows > 0 && (uint64_t)rows <= r.n / (uint64_t)st.dimension;
         st.ids.alloc((size_t)rows);
         st.ncodes.alloc((size_t)rows);
         st.codes.alloc((size_t)ncodes);
-        st.vecs.alloc(dim > 0 ? (size_t)rows * (size_t)dim : 0);
+        st.vecs.alloc(st.vecs_stored ? (size_t)rows * (size_t)st.dimension : 0);
         std::atomic<int> failed{0};
         parallel_for((int64_t)st.segs.size(), [&](int64_t s) {
             if (failed.load(std::memory_order_relaxed)) return;
@@ -760,11 +770,15 @@ struct Dec {
                 const uint64_t n = r.count();
                 for (uint64_t j = 0; j < n; j++) {
                     st.pending_ids.push_back(integer(r, mt.key));
-                    const size_t base = st.pending.size();
-                    if (dim > 0) st.pending.resize(base + (size_t)dim, 0.0f);
-                    const uint64_t got =
-                        floats_into(r, dim > 0 ? st.pending.data() + base : nullptr, dim > 0 ? dim : -1);
-                    if ((int64_t)got != dim && st.bad_pending < 0) st.bad_pending = st.pending_ids.back();
+                    const uint64_t k = r.count();
+                    if (dim > 0 && (int64_t)k == dim) {  // stored only at full length (see float_rows)
+                        const size_t base = st.pending.size();
+                        st.pending.resize(base + (size_t)k);
+                        for (uint64_t i = 0; i < k; i++) st.pending[base + i] = r.flt();
+                    } else {
+                        for (uint64_t i = 0; i < k; i++) r.skip_uint();
+                        if (st.bad_pending < 0) st.bad_pending = st.pending_ids.back();
+                    }
                 }
             } else {
                 skip(r, ft);

@@ -316,3 +316,21 @@ def test_out_of_range_type_ids_rejected():
         data += msg
         with pytest.raises(hg.HannError):
             hg.gob_decode_state(bytes(data))
+
+
+def test_huge_dimension_rejected_without_large_allocation():
+    """A small stream claiming a huge dimension is refused; nothing is sized
+    from the claimed dimension before the stream shows the floats."""
+    import resource
+    import time
+
+    before = resource.getrusage(resource.RUSAGE_SELF).ru_maxrss
+    for dim in (10**9, 2**40):
+        for ser in (_ser(Dimension=dim),
+                    {"Dimension": dim, "CoarseK": 2, "NumSubquantizers": 1, "PqK": 2, "KMeansIters": 1,
+                     "PendingVectors": {i: [1.0, 2.0] for i in range(2000)}}):
+            t = time.time()
+            with pytest.raises(hg.HannError):
+                hg.gob_decode_state(gob.encode_pqivf(ser))
+            assert time.time() - t < 5
+    assert resource.getrusage(resource.RUSAGE_SELF).ru_maxrss - before < 512 * 1024  # KiB: under 512 MiB
