@@ -22,7 +22,7 @@ import pytest
 import hann_gb300 as hg
 from tests.helpers import gaussian_mixture
 
-DEADLINE_S = 60.0
+DEADLINE_S = 30.0
 
 
 def new_index(dim, coarse_k, m, pqk, iters, *more):

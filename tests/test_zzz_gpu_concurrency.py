@@ -17,7 +17,7 @@ from tests import concurrency_scenarios as cs
 pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CHILD_TIMEOUT_S = 600
+CHILD_TIMEOUT_S = 300
 
 
 @pytest.fixture(scope="module")
