@@ -507,7 +507,7 @@ def main():
             "plain_one_query_per_call_qps": plain_qps,
             "plain_fp32_gpu_qps": plain_fp32_qps, "plain_fp32_same_ids": plain_same,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": scan_traffic(args), "kernel": "scan_skew_kernel",
+                         "frac": achieved / peak, "traffic": scan_traffic(args, choice), "kernel": "scan_skew_kernel",
                          "bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
             "cpu_baseline": cb,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -747,14 +747,16 @@ def knn_section(args, torch, dev):
     return out
 
 
-def scan_traffic(args):
+def scan_traffic(args, nprobe):
     """DRAM bytes (read + write) of one scan launch on this workload, from the
-    1-pass ncu capture kept in profiles/ (ncu cannot run inside the bench)."""
+    1-pass ncu capture kept in profiles/ (ncu cannot run inside the bench);
+    None when the capture was of another workload."""
     path = os.path.join(HERE, "profiles", "scan_skew_kernel_10Mx96_dram.json")
-    if not os.path.exists(path) or (args.n, args.dim, args.nlist, args.nq) != (10_000_000, 96, 16384, 10_000):
-        return None
     try:
         rec = json.load(open(path))
+        if (rec["n"], rec["dim"], rec["nlist"], rec["M"], rec["nq"], rec["nprobe"], rec["k"]) != \
+                (args.n, args.dim, args.nlist, args.m, args.nq, nprobe, args.k):
+            return None
         return float(rec["dram_bytes_read_per_launch"]) + float(rec["dram_bytes_write_per_launch"])
     except Exception:
         return None
@@ -883,7 +885,8 @@ def workload_config(args, nprobe, mode, rec):
         "n": args.n, "dim": args.dim, "nlist": args.nlist, "M": args.m, "pq_k": args.pqk, "nq": args.nq,
         "k": args.k, "nprobe": nprobe, "mode": "exact_rerank" if mode == 1 else "parity",
         "recall_by_nprobe": {f"{a}/{'exact' if b == 1 else 'pq'}": round(v, 4) for (a, b), v in rec.items()},
-        "l2": "inputs larger than L2 (240 MB codes + 3.84 GB raw vectors), no flush",
+        "l2": f"inputs larger than L2 ({args.n * (2 * args.m) / 1e6:.0f} MB of scan words + "
+              f"{args.n * args.dim * 4 / 1e9:.2f} GB raw vectors), no flush",
     }
 
 

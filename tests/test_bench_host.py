@@ -1,0 +1,82 @@
+"""Host-side pieces of bench.py that the JSON line depends on, on CPU:
+recall, the clocks record (median SM clock under load, throttle reasons),
+the DRAM-traffic record tied to its exact workload, the workload config and
+the default step counts."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def args_for(**over):
+    old = sys.argv
+    sys.argv = ["bench.py"]
+    try:
+        a = bench.parse()
+    finally:
+        sys.argv = old
+    for k, v in over.items():
+        setattr(a, k, v)
+    return a
+
+
+def test_defaults_meet_the_timing_rules():
+    a = args_for()
+    assert a.gpus == 1 and a.warmup >= 3 and a.steps >= 1
+    assert (a.n, a.dim, a.nlist, a.m, a.pqk, a.nq, a.k) == (10_000_000, 96, 16384, 24, 256, 10_000, 10)
+
+
+def test_recall_at():
+    gt = np.array([[1, 2, 3], [4, 5, 6]])
+    ids = np.array([[3, 2, 9, 1], [7, 8, 9, 4]])  # only the first k ids count
+    assert bench.recall_at(ids, gt) == (2 / 3 + 0 / 3) / 2
+
+
+class _FakeProc:
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+
+def test_clock_record():
+    c = bench.ClockSampler(0)
+    c.proc = _FakeProc()
+    c.lines = [
+        "0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 2055, 2070, 1350.0, 0x4, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 1390.2, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "garbage line",
+        "0, [N/A], 2070, 10, 0x0, Not Active, Not Active, Not Active, Not Active",
+    ]
+    r = c.stop()
+    assert r["sm_mhz"] == 2070 and r["sm_max_mhz"] == 2070 and r["samples"] == 3
+    assert r["reasons"] == ["sw_power_cap"]
+    c.lines.append("0, 1200, 2070, 700, 0x8, Active, Not Active, Active, Not Active")
+    assert bench.ClockSampler.stop(c)["reasons"] == ["hw_slowdown", "sw_power_cap", "sw_thermal_slowdown"]
+    none = bench.ClockSampler(0)
+    assert none.stop()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_traffic_record_only_for_its_workload():
+    a = args_for()
+    t = bench.scan_traffic(a, 32)
+    assert t is not None and 6e9 < t < 2e10  # the captured launch's DRAM read + write bytes
+    assert bench.scan_traffic(a, 128) is None  # another nprobe: another launch
+    assert bench.scan_traffic(args_for(n=4_000_000), 32) is None
+    assert bench.scan_traffic(args_for(m=16), 32) is None
+
+
+def test_workload_config():
+    a = args_for()
+    cfg = bench.workload_config(a, 32, 1, {(32, 1): 0.98, (32, 0): 0.6})
+    assert cfg["nprobe"] == 32 and cfg["mode"] == "exact_rerank"
+    assert cfg["recall_by_nprobe"] == {"32/exact": 0.98, "32/pq": 0.6}
+    assert "480 MB of scan words" in cfg["l2"] and "3.84 GB raw vectors" in cfg["l2"]
+    assert "model" not in cfg
