@@ -41,6 +41,8 @@ MODE_EXACT_RERANK = 1
 
 METRIC_SQEUCLID, METRIC_EUCLID, METRIC_MANHATTAN, METRIC_COSINE = 0, 1, 2, 3
 
+HANN_TUNE_LADDER_MAX = 14
+
 
 class HannError(Exception):
     def __init__(self, code: int, message: str):
@@ -146,6 +148,9 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_tune_candidate_clusters.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
+                                                         _P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.c_int32,
+                                                         _P, _P, _P, _P]
         L.hann_pqivf_arena_stats.argtypes = [_P, _P]
         L.hann_pqivf_retrain.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_save_snapshot.argtypes = [_P, ctypes.c_char_p]
@@ -421,35 +426,29 @@ class Index:
                               ground_truth=None, apply: bool = True):
         """The smallest nprobe of `ladder` whose recall@k on `queries` reaches
         `target_recall` against exact k-NN over the stored vectors (computed on
-        the GPU by the batched exact k-NN unless ground_truth ids are given).
-        Returns (nprobe, {nprobe: recall}); with apply, the index's default
-        nprobe becomes the chosen value. When no value reaches the target the
-        largest is chosen."""
+        the GPU by the batched exact k-NN unless ground_truth ids are given),
+        through hann_pqivf_tune_candidate_clusters. Returns (nprobe, {nprobe:
+        recall}); with apply, the index's default nprobe becomes the chosen
+        value. When no value reaches the target the largest tried is chosen."""
         q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self._dim)
-        if ground_truth is None:
-            st = self.export_state()
-            flat = np.ascontiguousarray(st["vectors"], dtype=np.float32)
-            rows, _ = knn(q, flat, k, "squared_euclidean")
-            ground_truth = np.where(rows >= 0, np.asarray(st["ids"])[np.maximum(rows, 0)], -1)
-        gt = np.asarray(ground_truth)
-        nlist = self.DeviceStats()["nlist"]
-        if ladder is None:
-            ladder = [p for p in (1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096) if p <= nlist]
-            if not ladder or ladder[-1] != min(nlist, 4096):
-                ladder.append(min(nlist, 4096))
-        rec = {}
-        chosen = ladder[-1]
-        for p in ladder:
-            ids, _, n = self.SearchBatch(q, k, nprobe=p, mode=mode)
-            hits = sum(len(set(ids[i, :n[i]].tolist()) & set(gt[i][gt[i] >= 0].tolist())) for i in range(len(q)))
-            tot = int((gt >= 0).sum())
-            rec[p] = hits / tot if tot else 1.0
-            if rec[p] >= target_recall:
-                chosen = p
-                break
-        if apply:
-            self.SetCandidateClusters(chosen)
-        return chosen, rec
+        nq = q.shape[0]
+        k = int(k)
+        lad = None if ladder is None else np.ascontiguousarray(ladder, dtype=np.int32)
+        cap = HANN_TUNE_LADDER_MAX if lad is None else max(1, lad.size)
+        gt = None
+        if ground_truth is not None:
+            gt = np.full((nq, k), -1, dtype=np.int64)
+            g = np.asarray(ground_truth, dtype=np.int64).reshape(nq, -1)
+            gt[:, :min(k, g.shape[1])] = g[:, :k]
+        chosen = ctypes.c_int32(0)
+        ntried = ctypes.c_int32(0)
+        tried = np.zeros(cap, dtype=np.int32)
+        rec = np.zeros(cap, dtype=np.float64)
+        self._check(self._L.hann_pqivf_tune_candidate_clusters(
+            self._h, _ptr(q), nq, k, float(target_recall), _ptr(lad) if lad is not None else None,
+            0 if lad is None else int(lad.size), int(mode), _ptr(gt) if gt is not None else None,
+            1 if apply else 0, ctypes.byref(chosen), _ptr(tried), _ptr(rec), ctypes.byref(ntried)))
+        return int(chosen.value), {int(tried[i]): float(rec[i]) for i in range(ntried.value)}
 
     def SetPlainFP32(self, on: bool) -> None:
         """Switch the FP32 SIMT-only mode (same results, no tensor cores)."""

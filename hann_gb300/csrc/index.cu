@@ -760,7 +760,8 @@ int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_
 
 int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k,
                       const int32_t* d_np, int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist,
-                      int32_t* d_nout, cudaStream_t s) {
+                      int32_t* d_nout, cudaStream_t s, unsigned long long* fb_counter) {
+    unsigned long long* fbc = fb_counter ? fb_counter : sc.fbcount.p;
     const int R = rerank_depth(h, kmax, mode);
     if (R > 480) return h->fail(HANN_E_UNSUPPORTED, "k (%d) above this build's limit of 448", kmax);
     np_max = std::min(np_max, h->nlist);
@@ -818,7 +819,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
             CK(mark(1, true));
             CK(launch_probe_final(qp, nc, h->o.dimension, h->d_coarse.p, h->nlist, d_np + q0, np_max, d_k + q0,
                                   h->d_live.p, h->o.fallback ? 1 : 0, lcap, sc.pband.p, sc.plcount.p, sc.pneed.p,
-                                  sc.D.p, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, sc.fbcount.p, sc.ptodo.p, s));
+                                  sc.D.p, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, fbc, sc.ptodo.p, s));
             CK(launch_probe_order(sc.probe_ids.p, nc, np_max, h->nlist, sc.order_scratch.p, sc.qorder.p, s));
             CK(mark(1, false));
             CK(mark(2, true));
@@ -849,11 +850,10 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
             CK(launch_probe_select_band(sc.D.p, qp, sc.qn2.p, sc.qres.p, nc, h->o.dimension, h->kp, h->d_coarse.p,
                                         h->d_cmax.p,
                                         h->nlist, d_np + q0, np_max, d_k + q0, h->d_live.p, h->o.fallback ? 1 : 0,
-                                        sc.probe_ids.p, sc.probe_d.p, sc.fb.p, sc.fbcount.p, s));
+                                        sc.probe_ids.p, sc.probe_d.p, sc.fb.p, fbc, s));
         } else {
             CK(launch_probe_select(sc.D.p, nc, h->nlist, d_np + q0, np_max, d_k + q0, h->d_live.p,
-                                   h->o.fallback ? 1 : 0, sc.probe_ids.p, sc.probe_d.p, sc.fb.p,
-                                   sc.fbcount.p, s));
+                                   h->o.fallback ? 1 : 0, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, fbc, s));
         }
         CK(mark(1, false));
         CK(mark(2, true));
@@ -966,6 +966,9 @@ int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out) {
     if (e == cudaSuccess) e = h->main.fbcount.reserve(1);
     if (e == cudaSuccess) e = h->s_rows.reserve(1);
     if (e == cudaSuccess) e = cudaMemset(h->s_rows.p, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = h->d_fb_dev.reserve(1);
+    if (e == cudaSuccess) e = cudaMemset(h->d_fb_dev.p, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->dev_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         snprintf(buf, sizeof(buf), "CUDA initialisation failed: %s", cudaGetErrorString(e));
         delete h;
@@ -978,6 +981,8 @@ int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out) {
 void hann_pqivf_free(hann_pqivf* h) {
     if (!h) return;
     cudaSetDevice(h->o.device);
+    wait_device_searches(h);
+    if (h->dev_ev) cudaEventDestroy(h->dev_ev);
     if (h->stream) {
         cudaStreamSynchronize(h->stream);
         cudaStreamDestroy(h->stream);
@@ -993,6 +998,7 @@ int hann_pqivf_bulk_add(hann_pqivf* h, const int64_t* ids, const float* vectors,
     std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     return bulk_add_locked(h, ids, vectors, n);
 }
 
@@ -1093,6 +1099,7 @@ int hann_pqivf_delete(hann_pqivf* h, int64_t id) {
     std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     return delete_ids(h, {id}, true);
 }
 
@@ -1102,6 +1109,7 @@ int hann_pqivf_bulk_delete(hann_pqivf* h, const int64_t* ids, int64_t n) {
     std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     return bulk_delete_locked(h, ids, n);
 }
 
@@ -1131,6 +1139,7 @@ int hann_pqivf_bulk_update(hann_pqivf* h, const int64_t* ids, const float* vecto
     std::lock_guard<std::mutex> wl(h->wmu);
     std::unique_lock<std::shared_mutex> lk(h->mu);
     cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     const int dim = h->o.dimension;
     std::vector<int64_t> order(n);
     std::iota(order.begin(), order.end(), 0);
@@ -1182,6 +1191,7 @@ int hann_pqivf_train_seeded(hann_pqivf* h, const int64_t* coarse_init, const int
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     SeedSource s;
     s.coarse_init = coarse_init;
     s.pq_init = pq_init;
@@ -1198,6 +1208,7 @@ int hann_pqivf_retrain(hann_pqivf* h, int32_t iters) {
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     if (iters < 0) return h->fail(HANN_E_INVALID, "retrain iterations must not be negative");
     if (!h->trained || h->nlist == 0)
         return h->fail(HANN_E_STATE, "PQIVF index is not trained. Call Train() before Retrain()");
@@ -1281,7 +1292,11 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
     CK(launch_fill_i32(sc.k.p, nq, k, s));
     CK(launch_fill_i32(sc.np.p, nq, np, s));
     h->launches += 2;
-    return run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s);
+    rc = run_search(h, sc, d_queries, nq, sc.k.p, sc.np.p, np, k, mode, d_ids, d_distances, d_n_out, s,
+                    h->d_fb_dev.p);
+    if (rc) return rc;
+    CK(note_device_search(h, s));
+    return HANN_OK;
 }
 
 int hann_pqivf_arena_stats(void* hv, int64_t* out) {
@@ -1309,6 +1324,8 @@ int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on) {
     if (!h) return HANN_E_INVALID;
     std::unique_lock<std::mutex> w(h->wmu);
     std::unique_lock<std::shared_mutex> g(h->mu);
+    cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     h->o.plain_fp32 = on ? 1 : 0;
     if (!h->trained) return HANN_OK;
     return prepare_coarse(h);
@@ -1362,12 +1379,122 @@ int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out, int32_t capacity, int32
 int hann_pqivf_stats(hann_pqivf* h, hann_pqivf_index_stats* out) {
     if (!h || !out) return HANN_E_INVALID;
     std::shared_lock<std::shared_mutex> lk(h->mu);
+    // Fallbacks of device-buffer searches are counted on the device: wait for
+    // those enqueued so far, then add the device count.
+    unsigned long long dev_fb = 0;
+    {
+        std::lock_guard<std::mutex> rl(h->run_mu);
+        cudaSetDevice(h->o.device);
+        CK(wait_device_searches(h));
+        CK(cudaMemcpyAsync(&dev_fb, h->d_fb_dev.p, sizeof(dev_fb), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
     out->count = (int64_t)h->pending.size() + h->total_rows();
     out->dimension = h->o.dimension;
-    out->fallback_searches = h->fallback_searches.load();
+    out->fallback_searches = h->fallback_searches.load() + (int64_t)dev_fb;
     out->trained = h->trained ? 1 : 0;
     out->nlist = h->nlist;
     out->rows_capacity = h->rows_cap;
+    return HANN_OK;
+}
+
+int hann_pqivf_tune_candidate_clusters(hann_pqivf* h, const float* queries, int64_t nq, int32_t k,
+                                       double target_recall, const int32_t* ladder, int32_t n_ladder, int32_t mode,
+                                       const int64_t* ground_truth, int32_t apply, int32_t* chosen,
+                                       int32_t* tried_out, double* recall_out, int32_t* n_tried) {
+    if (!h) return HANN_E_INVALID;
+    if (nq <= 0 || !queries || !chosen) return h->fail(HANN_E_INVALID, "invalid arguments");
+    if (k <= 0) return h->fail(HANN_E_INVALID, "k must be positive");
+    if (mode != 0 && mode != 1) return h->fail(HANN_E_INVALID, "mode must be 0 or 1");
+    if (ladder && n_ladder <= 0) return h->fail(HANN_E_INVALID, "empty nprobe ladder");
+    const int dim = h->o.dimension;
+    int nlist = 0;
+    std::vector<int64_t> gt;
+    {
+        std::shared_lock<std::shared_mutex> lk(h->mu);
+        int rc = check_searchable(h);
+        if (rc) return rc;
+        nlist = h->nlist;
+        if (ground_truth) {
+            gt.assign(ground_truth, ground_truth + nq * k);
+        } else {
+            // Exact k-NN over the stored (live) vectors on the device: gather
+            // them into one flat base, then the batched k-NN's tensor-core
+            // screen with exact rescoring.
+            std::lock_guard<std::mutex> rl(h->run_mu);
+            cudaSetDevice(h->o.device);
+            std::vector<int64_t> rows, ids;
+            for (int l = 0; l < h->nlist; l++)
+                for (size_t j = 0; j < h->list_ids[l].size(); j++)
+                    if (h->list_alive[l][j]) {
+                        rows.push_back(h->h_start[l] + (int64_t)j);
+                        ids.push_back(h->list_ids[l][j]);
+                    }
+            const int64_t n = (int64_t)rows.size();
+            DBuf<int64_t> d_rows;
+            DBuf<float> base;
+            CK(upload(d_rows, rows.data(), rows.size(), h->stream));
+            CK(base.reserve((size_t)n * dim));
+            CK(launch_copy_words(h->d_vectors.p, d_rows.p, base.p, nullptr, n, dim, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            hann_knn* kh = knn_new_from_device(base.p, n, dim, h->stream);
+            if (!kh) return h->fail(HANN_E_CUDA, "could not build the exact k-NN of the stored vectors");
+            std::vector<int64_t> r((size_t)nq * k);
+            std::vector<double> d((size_t)nq * k);
+            rc = hann_knn_search(kh, HANN_METRIC_SQEUCLID, queries, nq, k, HANN_KNN_AUTO, r.data(), d.data());
+            std::string msg = rc ? std::string(hann_knn_last_error(kh)) : std::string();
+            hann_knn_free(kh);
+            if (rc) return h->fail(rc, "exact k-NN for the recall target: %s", msg.c_str());
+            gt.resize(r.size());
+            for (size_t i = 0; i < r.size(); i++) gt[i] = r[i] >= 0 ? ids[(size_t)r[i]] : -1;
+        }
+    }
+    std::vector<int32_t> lad;
+    if (ladder) {
+        lad.assign(ladder, ladder + n_ladder);
+    } else {
+        for (int p = 1; p <= 4096; p *= 2)
+            if (p <= nlist) lad.push_back(p);
+        if (lad.empty() || lad.back() != std::min(nlist, 4096)) lad.push_back(std::min(nlist, 4096));
+    }
+    for (int32_t p : lad)
+        if (p <= 0) return h->fail(HANN_E_INVALID, "nprobe must be positive");
+    int64_t tot = 0;
+    for (int64_t v : gt) tot += v >= 0;
+    std::vector<int32_t> kk((size_t)nq, k), npv((size_t)nq);
+    std::vector<int64_t> ids((size_t)nq * k);
+    std::vector<double> dist((size_t)nq * k);
+    std::vector<int32_t> nout((size_t)nq);
+    int32_t pick = lad.back(), ntried = 0;
+    for (size_t li = 0; li < lad.size(); li++) {
+        std::fill(npv.begin(), npv.end(), lad[li]);
+        int rc = hann_pqivf_search_batch(h, queries, nq, kk.data(), npv.data(), k, mode, ids.data(), dist.data(),
+                                         nout.data());
+        if (rc) return rc;
+        int64_t hits = 0;
+        for (int64_t i = 0; i < nq; i++) {
+            const int64_t* g = gt.data() + i * k;
+            for (int j = 0; j < nout[(size_t)i]; j++) {
+                const int64_t id = ids[(size_t)(i * k + j)];
+                for (int t = 0; t < k; t++)
+                    if (g[t] >= 0 && g[t] == id) {
+                        hits++;
+                        break;
+                    }
+            }
+        }
+        const double rec = tot ? (double)hits / (double)tot : 1.0;
+        if (tried_out) tried_out[ntried] = lad[li];
+        if (recall_out) recall_out[ntried] = rec;
+        ntried++;
+        if (rec >= target_recall) {
+            pick = lad[li];
+            break;
+        }
+    }
+    *chosen = pick;
+    if (n_tried) *n_tried = ntried;
+    if (apply) return hann_pqivf_set_candidate_clusters(h, pick);
     return HANN_OK;
 }
 
@@ -1462,6 +1589,7 @@ int hann_pqivf_import(hann_pqivf* h, const hann_pqivf_layout* L, const float* co
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
     return import_locked(h, L, coarse, codebooks, list_len, list_key, cluster_counts, ids, vectors, codes, nullptr,
                          has_codes, pending_ids, pending_vectors);
 }
@@ -1655,10 +1783,8 @@ cudaError_t noalloc_arena(int dev, unsigned char** out) {
     return cudaSuccess;
 }
 
-__global__ void noalloc_fill_kernel(int32_t* a, int32_t va, int32_t* b, int32_t vb, int64_t n,
-                                    unsigned long long* counter) {
+__global__ void noalloc_fill_kernel(int32_t* a, int32_t va, int32_t* b, int32_t vb, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) *counter = 0ull;
     if (i < n) {
         a[i] = va;
         b[i] = vb;
@@ -1686,6 +1812,15 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     const int R = rerank_depth(h, k, mode);
     if (R > 480) return h->fail(HANN_E_UNSUPPORTED, "k (%d) above this build's limit of 448", k);
     if (np > 4096) return h->fail(HANN_E_UNSUPPORTED, "more than 4096 probed lists per query");
+    // Every query needs at least 4 * nlist bytes of the arena (its row of
+    // coarse distances): a larger batch is refused before the sizes below are
+    // multiplied out, so a huge nq cannot wrap them past the check.
+    const int64_t nq_cap = (int64_t)(NOALLOC_ARENA_BYTES / (sizeof(float) * (size_t)std::max(1, h->nlist)));
+    if (nq > nq_cap)
+        return h->fail(HANN_E_UNSUPPORTED,
+                       "allocation-free search of %lld queries cannot fit its fixed %zu-byte arena (at most %lld "
+                       "queries at nlist %d); split the batch",
+                       (long long)nq, NOALLOC_ARENA_BYTES, (long long)nq_cap, h->nlist);
     // Scratch layout inside the arena, every region 256-byte aligned.
     const size_t b_D = align256((size_t)nq * h->nlist * sizeof(float));
     const size_t b_pid = align256((size_t)nq * np * sizeof(int32_t));
@@ -1694,7 +1829,7 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     const size_t b_cr = align256((size_t)nq * R * sizeof(int32_t));
     const size_t b_cd = align256((size_t)nq * R * sizeof(float));
     const size_t b_cs = align256((size_t)nq * R * sizeof(uint32_t));
-    const size_t need = b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd + b_cs + 256;
+    const size_t need = b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd + b_cs;
     if (need > NOALLOC_ARENA_BYTES)
         return h->fail(HANN_E_UNSUPPORTED,
                        "allocation-free search of %lld queries needs %zu bytes of scratch, above its fixed %zu-byte "
@@ -1712,21 +1847,23 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     int32_t* crow = reinterpret_cast<int32_t*>(base + b_D + b_pid + b_pd + 3 * b_q32);
     float* cd = reinterpret_cast<float*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr);
     uint32_t* cs = reinterpret_cast<uint32_t*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd);
-    unsigned long long* fbc =
-        reinterpret_cast<unsigned long long*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd + b_cs);
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     // The arena keeps the previous call's contents: the per-query k and
-    // nprobe and the fallback counter are written first; every other region
-    // is fully written by the kernel that produces it before it is read.
-    noalloc_fill_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(dk, k, dnp, np, nq, fbc);
+    // nprobe are written first; every other region is fully written by the
+    // kernel that produces it before it is read. Fallbacks are counted in the
+    // handle's device counter (allocated with the handle), which Stats reads.
+    noalloc_fill_kernel<<<(unsigned)((nq + 255) / 256), 256, 0, s>>>(dk, k, dnp, np, nq);
     CK(cudaGetLastError());
     ScanParams p = h->scan_params();
     p.kq = dk;
     p.mode = mode;
     p.rerank_fixed = h->o.rerank;
     CK(launch_dist_matrix(d_queries, nq, h->o.dimension, h->d_coarse.p, h->nlist, D, s));
-    CK(launch_probe_select(D, nq, h->nlist, dnp, np, dk, h->d_live.p, h->o.fallback ? 1 : 0, pid, pd, fb, fbc, s));
+    CK(launch_probe_select(D, nq, h->nlist, dnp, np, dk, h->d_live.p, h->o.fallback ? 1 : 0, pid, pd, fb,
+                           h->d_fb_dev.p, s));
     CK(launch_scan(p, d_queries, nq, pid, pd, dnp, np, fb, R, crow, cd, cs, nullptr, s));
     CK(launch_rerank(p, d_queries, nq, crow, cs, R, dk, k, mode, d_ids, d_distances, d_n_out, s));
+    h->launches += 5;  // fill, distance matrix, probe select, scan, rerank
+    CK(note_device_search(h, s));
     return HANN_OK;
 }

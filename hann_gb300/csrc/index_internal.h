@@ -216,6 +216,16 @@ struct hann_pqivf {
     // search scratch of the handle's own stream
     SearchScratch main;
     DBuf<unsigned long long> s_rows;
+    // Device-buffer searches (hann_pqivf_search_batch_device and its
+    // allocation-free variant) return before their kernels run, on the
+    // caller's stream. dev_ev is recorded after the last one's kernels; every
+    // mutation waits for it before it touches a device array, so a relayout
+    // cannot move rows under a scan still reading them. d_fb_dev counts their
+    // brute-force fallbacks on the device; Stats adds it once the searches
+    // behind dev_ev are done.
+    cudaEvent_t dev_ev = nullptr;
+    bool dev_pending = false;
+    DBuf<unsigned long long> d_fb_dev;
 
     // stage profiling: pairs of events per stage (a diagnostic of the
     // handle's own calls; not meant while a server drives the handle)
@@ -276,6 +286,25 @@ struct hann_pqivf {
         if (_e != cudaSuccess) return h->cuda_fail(_e, #expr); \
     } while (0)
 
+// Marks the end of a device-buffer search enqueued on stream s (shared lock
+// and run_mu held).
+inline cudaError_t note_device_search(hann_pqivf* h, cudaStream_t s) {
+    cudaError_t e = cudaEventRecord(h->dev_ev, s);
+    if (e == cudaSuccess) h->dev_pending = true;
+    return e;
+}
+
+// Waits until every device-buffer search enqueued so far has finished. Called
+// by mutations (exclusive lock held, so no new search is enqueued meanwhile)
+// before they write or move device arrays: those searches run on callers'
+// streams, which neither the handle's stream nor a synchronous copy orders.
+inline cudaError_t wait_device_searches(hann_pqivf* h) {
+    if (!h->dev_pending) return cudaSuccess;
+    cudaError_t e = cudaEventSynchronize(h->dev_ev);
+    if (e == cudaSuccess) h->dev_pending = false;
+    return e;
+}
+
 template <typename T>
 inline cudaError_t upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s) {
     cudaError_t e = b.reserve(n);
@@ -288,7 +317,8 @@ inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
 // Search pipeline of index.cu, usable from any stream with its own scratch.
 int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, const int32_t* d_k, const int32_t* d_np,
-               int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist, int32_t* d_nout, cudaStream_t s);
+               int np_max, int kmax, int mode, int64_t* d_ids, double* d_dist, int32_t* d_nout, cudaStream_t s,
+               unsigned long long* fb_counter = nullptr);
 int check_searchable(hann_pqivf* h);
 int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_max, int kmax, int mode);
 int rerank_depth(const hann_pqivf* h, int kmax, int mode);
@@ -302,6 +332,8 @@ int bulk_delete_locked(hann_pqivf* h, const int64_t* ids, int64_t n, bool allow_
 int add_prepare(hann_pqivf* h, const int64_t* ids, const float* vecs, int64_t n);
 int add_commit(hann_pqivf* h, const int64_t* ids);
 bool compaction_due(const hann_pqivf* h, int64_t extra);
+// k-NN handle (knn.cu) over n rows of dim floats already on the device.
+struct hann_knn* knn_new_from_device(const float* d_base, int64_t n, int32_t dim, cudaStream_t s);
 // Replaces the handle's state (every lock held); codes as ints (codes32) or
 // bytes (codes8), M per row.
 int import_locked(hann_pqivf* h, const hann_pqivf_layout* L, const float* coarse, const float* codebooks,

@@ -317,6 +317,32 @@ hann_knn* hann_knn_new(const float* base, int64_t n, int32_t dim) {
     return h;
 }
 
+}  // extern "C"
+
+// A k-NN handle over a base already in device memory (copied, device to
+// device, on stream s): the recall tuner's ground truth over an index's
+// stored vectors.
+hann_knn* knn_new_from_device(const float* d_base, int64_t n, int32_t dim, cudaStream_t s) {
+    if (n < 0 || dim < 0 || n >= ((int64_t)1 << 31)) return nullptr;
+    hann_knn* h = new (std::nothrow) hann_knn();
+    if (!h) return nullptr;
+    h->n = n;
+    h->dim = dim;
+    h->kp = gemm_kpad(dim > 0 ? dim : 1);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        h->base.reserve((size_t)n * dim) != cudaSuccess ||
+        (n * dim > 0 && (cudaMemcpyAsync(h->base.p, d_base, sizeof(float) * n * dim, cudaMemcpyDeviceToDevice, s) !=
+                             cudaSuccess ||
+                         cudaStreamSynchronize(s) != cudaSuccess))) {
+        if (h->stream) cudaStreamDestroy(h->stream);
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+
+extern "C" {
+
 void hann_knn_free(hann_knn* h) {
     if (!h) return;
     cudaStreamSynchronize(h->stream);

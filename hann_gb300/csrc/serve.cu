@@ -235,7 +235,8 @@ void mutator(hann_server* s) {
             {
                 std::lock_guard<std::mutex> wl(h->wmu);
                 std::unique_lock<std::shared_mutex> xl(h->mu);
-                rc = apply(true, nullptr);
+                const cudaError_t we = wait_device_searches(h);
+                rc = we == cudaSuccess ? apply(true, nullptr) : h->cuda_fail(we, "waiting for device searches");
             }
             t3 = Clock::now();
             relaid = true;

@@ -318,6 +318,10 @@ int hann_pqivf_load_snapshot(hann_pqivf* h, const char* path) {
     std::unique_lock<std::shared_mutex> lk(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
     cudaSetDevice(h->o.device);
+    {
+        cudaError_t e = wait_device_searches(h);
+        if (e != cudaSuccess) return h->cuda_fail(e, "waiting for device searches");
+    }
     h->o.seed = hd.seed;
     h->rng.seed(hd.seed);
     h->o.rerank = hd.rerank;

@@ -133,7 +133,9 @@ int hann_pqivf_search_batch(hann_pqivf* h, const float* queries, int64_t nq, con
  * the work enqueued on `stream` (a cudaStream_t, NULL = the handle's own);
  * k and nprobe are uniform. Returns once enqueued, without waiting for the
  * device. Calls share the handle's scratch: calls on different streams must
- * be ordered by the caller. */
+ * be ordered by the caller. A mutation of the handle waits for the searches
+ * enqueued before it; brute-force fallbacks are counted on the device and
+ * appear in hann_pqivf_stats (which waits for those searches). */
 int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k, int32_t nprobe,
                                    int32_t mode, int64_t* d_ids, double* d_distances, int32_t* d_n_out,
                                    void* stream);
@@ -141,6 +143,24 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
 /* Sets the default nprobe (WithCandidateClusters, pqivf/index.go:86-94) of a
  * live index, e.g. to the value a recall-target tuning picked. */
 int hann_pqivf_set_candidate_clusters(hann_pqivf* h, int32_t n);
+
+/* nprobe from a recall target: the caller side of Search, where the
+ * reference's callers pick WithCandidateClusters by hand
+ * (example/run_datasets.go:115-120, pqivf/index.go:86-94). Tries the nprobe
+ * values of `ladder` (n_ladder entries, ascending; NULL = 1, 2, 4, ... up to
+ * min(nlist, 4096), at most HANN_TUNE_LADDER_MAX values) in order, searching
+ * the nq queries with k and mode, and stops at the first whose recall@k
+ * reaches target_recall; *chosen = that nprobe, or the last one tried when
+ * none does. Recall is measured against ground_truth ids [nq][k] (-1 = no
+ * neighbour), or, when NULL, against an exact k-NN of the stored vectors
+ * computed on the GPU. tried_out / recall_out (may be NULL; room for every
+ * ladder entry) receive each nprobe tried and its recall, *n_tried their
+ * count. With apply != 0 the index's default nprobe becomes *chosen. */
+#define HANN_TUNE_LADDER_MAX 14
+int hann_pqivf_tune_candidate_clusters(hann_pqivf* h, const float* queries, int64_t nq, int32_t k,
+                                       double target_recall, const int32_t* ladder, int32_t n_ladder, int32_t mode,
+                                       const int64_t* ground_truth, int32_t apply, int32_t* chosen,
+                                       int32_t* tried_out, double* recall_out, int32_t* n_tried);
 
 /* Switches the plain-FP32 mode of hann_pqivf_options at run time (no
  * reference counterpart; results do not change). */
@@ -168,11 +188,14 @@ int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out, int32_t capacity, int32
  * loads this library holds until the process exits; a batch whose scratch
  * (about nq * (4 * nlist + 8 * nprobe + 12 * rerank depth + 12) bytes) does
  * not fit is rejected with HANN_E_UNSUPPORTED and a message that says so.
+ * The coarse distances dominate: every query needs a full row of them, so
+ * the number of queries per call is small when the index has many lists
+ * (about 250 queries at 16,384 lists, about 65,000 at 64 lists).
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * Every call shares the array, so calls whose work overlaps on the GPU
- * (different streams, threads or handles) race; serialise them. Like the
- * call it mirrors, it does not update FallbackSearches. */
+ * (different streams, threads or handles) race; serialise them. Fallbacks
+ * are counted as for hann_pqivf_search_batch_device. */
 int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k,
                                            int32_t nprobe, int32_t mode, int64_t* d_ids, double* d_distances,
                                            int32_t* d_n_out, void* stream);

@@ -53,7 +53,8 @@ def build(force: bool = False) -> None:
         os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "hann_oracle.c"))
     ):
         subprocess.run(["make", "-s", "-C", HERE, "lib"], check=True)
-    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True, stdout=subprocess.DEVNULL)
+    ref = os.environ.get("HANN_REFERENCE_TREE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref], check=True, stdout=subprocess.DEVNULL)
 
 
 def lib():
@@ -82,6 +83,10 @@ def lib():
             L.hann_oracle_search_batch.argtypes = [
                 ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _f32p, _f32p, _i64p, _i64p, _f32p,
                 _i32p, _u8p, _i32p, _f32p, ctypes.c_int64, _i32p, _i32p, ctypes.c_int, ctypes.c_int,
+                _i64p, _f64p, _i32p, _i32p, ctypes.c_int]
+            L.hann_oracle_search_batch_rerank.argtypes = [
+                ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _f32p, _f32p, _i64p, _i64p, _f32p,
+                _i32p, _u8p, _i32p, _f32p, ctypes.c_int64, _i32p, _i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                 _i64p, _f64p, _i32p, _i32p, ctypes.c_int]
             L.hann_oracle_probe.argtypes = [ctypes.c_int, ctypes.c_int, _f32p, _f32p, ctypes.c_int, _i32p]
             L.hann_oracle_knn.argtypes = [ctypes.c_int, _f32p, ctypes.c_int64, _f32p, ctypes.c_int64, ctypes.c_int,
@@ -268,8 +273,11 @@ class OracleIndex:
     def count(self) -> int:
         return int(self.ids.size)
 
-    def search(self, queries, k, nprobe, nthreads: int = 1):
-        """Independent Search calls (pqivf/index.go:850-949).
+    def search(self, queries, k, nprobe, nthreads: int = 1, rerank: int = 0):
+        """Independent Search calls (pqivf/index.go:850-949). With rerank > 0,
+        the `rerank` best candidates by PQ distance are reordered by the exact
+        distance to their stored vectors (the GPU's exact-rerank mode on the
+        CPU; the reference itself has no such mode).
 
         Returns (ids[nq][kmax], dist[nq][kmax], n[nq], fallback[nq])."""
         q = _f32(queries).reshape(-1, self.dim)
@@ -288,12 +296,12 @@ class OracleIndex:
         ecl = self.entry_cluster if self.entry_cluster.size else np.zeros(1, np.int32)
         idsin = self.ids if self.ids.size else np.zeros(1, np.int64)
         if nq:
-            lib().hann_oracle_search_batch(
+            lib().hann_oracle_search_batch_rerank(
                 self.dim, self.M, self.pqK, self.nlist, _p(self.coarse, _f32p), _p(self.codebooks, _f32p),
                 _p(self.list_off, _i64p), _p(idsin, _i64p), _p(vecs, _f32p), _p(codes, _i32p),
                 _p(has, _u8p), _p(ecl, _i32p), _p(q, _f32p), nq, _p(kk, _i32p), _p(npr, _i32p),
-                int(self.fallback), kmax, _p(ids, _i64p), _p(dist, _f64p), _p(nout, _i32p), _p(fb, _i32p),
-                nthreads)
+                int(self.fallback), int(rerank), kmax, _p(ids, _i64p), _p(dist, _f64p), _p(nout, _i32p),
+                _p(fb, _i32p), nthreads)
         return ids, dist, nout, fb
 
     def probe(self, query, nprobe):

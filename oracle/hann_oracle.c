@@ -433,8 +433,12 @@ static double entry_rank(const oracle_index* ix, const float* q, int64_t pos, fl
     return (double)sqeuclid(q, ix->vectors + (size_t)pos * dim, dim);
 }
 
-/* Returns the result count, or -1 on an allocation failure. */
-static int search_one(const oracle_index* ix, const float* q, int k, int nprobe, int fallback,
+/* Returns the result count, or -1 on an allocation failure. With rerank > 0
+ * the candidates are cut to the `rerank` best by the reference's PQ distance
+ * and reordered by the exact FP32 distance to their stored vectors (the
+ * GPU's exact-rerank mode, restated on the CPU; the reference has no such
+ * mode). */
+static int search_one(const oracle_index* ix, const float* q, int k, int nprobe, int fallback, int rerank,
                       int64_t* ids_out, double* dist_out, int* used_fallback,
                       int32_t* probe_out /* nullable, [nprobe] */) {
     int dim = ix->dim, nlist = ix->nlist;
@@ -468,6 +472,11 @@ static int search_one(const oracle_index* ix, const float* q, int k, int nprobe,
         }
     }
     qsort(cs, nc, sizeof(struct cand), cmp_cand);
+    if (rerank > 0) {
+        if (nc > rerank) nc = rerank;
+        for (int64_t i = 0; i < nc; i++) cs[i].d = (double)sqeuclid(q, ix->vectors + (size_t)cs[i].pos * dim, dim);
+        qsort(cs, nc, sizeof(struct cand), cmp_cand);
+    }
     int kk = k < nc ? k : (int)nc;
     for (int i = 0; i < kk; i++) {
         ids_out[i] = ix->ids[cs[i].pos];
@@ -479,7 +488,7 @@ static int search_one(const oracle_index* ix, const float* q, int k, int nprobe,
 }
 
 struct search_ctx {
-    const oracle_index* ix; const float* q; const int32_t* k; const int32_t* nprobe; int fallback;
+    const oracle_index* ix; const float* q; const int32_t* k; const int32_t* nprobe; int fallback; int rerank;
     int kmax; int64_t* ids; double* dist; int32_t* nout; int32_t* fb;
 };
 static void search_range(void* p, int64_t b, int64_t e) {
@@ -487,10 +496,18 @@ static void search_range(void* p, int64_t b, int64_t e) {
     for (int64_t i = b; i < e; i++) {
         int ufb = 0;
         c->nout[i] = search_one(c->ix, c->q + (size_t)i * c->ix->dim, c->k[i], c->nprobe[i], c->fallback,
-                                c->ids + (size_t)i * c->kmax, c->dist + (size_t)i * c->kmax, &ufb, NULL);
+                                c->rerank, c->ids + (size_t)i * c->kmax, c->dist + (size_t)i * c->kmax, &ufb,
+                                NULL);
         if (c->fb) c->fb[i] = ufb;
     }
 }
+
+void hann_oracle_search_batch_rerank(int dim, int M, int pqK, int nlist, const float* coarse, const float* codebooks,
+                                     const int64_t* list_off, const int64_t* ids, const float* vectors,
+                                     const int32_t* codes, const uint8_t* has_codes, const int32_t* entry_cluster,
+                                     const float* queries, int64_t nq, const int32_t* k, const int32_t* nprobe,
+                                     int fallback, int rerank, int kmax, int64_t* ids_out, double* dist_out,
+                                     int32_t* n_out, int32_t* fallback_out, int nthreads);
 
 /* Batch of independent Search calls, fanned out over nthreads like the
  * reference's query pool (example/run_datasets.go:84-120). Output rows have
@@ -501,9 +518,22 @@ void hann_oracle_search_batch(int dim, int M, int pqK, int nlist, const float* c
                               const float* queries, int64_t nq, const int32_t* k, const int32_t* nprobe,
                               int fallback, int kmax, int64_t* ids_out, double* dist_out, int32_t* n_out,
                               int32_t* fallback_out, int nthreads) {
+    hann_oracle_search_batch_rerank(dim, M, pqK, nlist, coarse, codebooks, list_off, ids, vectors, codes, has_codes,
+                                    entry_cluster, queries, nq, k, nprobe, fallback, 0, kmax, ids_out, dist_out,
+                                    n_out, fallback_out, nthreads);
+}
+
+/* The same with the exact rerank of search_one (rerank 0 = the reference's
+ * Search). */
+void hann_oracle_search_batch_rerank(int dim, int M, int pqK, int nlist, const float* coarse, const float* codebooks,
+                                     const int64_t* list_off, const int64_t* ids, const float* vectors,
+                                     const int32_t* codes, const uint8_t* has_codes, const int32_t* entry_cluster,
+                                     const float* queries, int64_t nq, const int32_t* k, const int32_t* nprobe,
+                                     int fallback, int rerank, int kmax, int64_t* ids_out, double* dist_out,
+                                     int32_t* n_out, int32_t* fallback_out, int nthreads) {
     oracle_index ix = {dim, M, pqK, nlist, coarse, codebooks, list_off, ids, vectors, codes, has_codes,
                        entry_cluster};
-    struct search_ctx c = {&ix, queries, k, nprobe, fallback, kmax, ids_out, dist_out, n_out, fallback_out};
+    struct search_ctx c = {&ix, queries, k, nprobe, fallback, rerank, kmax, ids_out, dist_out, n_out, fallback_out};
     parallel_for(nq, nthreads, search_range, &c);
 }
 

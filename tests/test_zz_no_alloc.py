@@ -7,6 +7,8 @@ with a device-memory budget fixed at start-up). Its scratch is one fixed
 16 MiB device array inside the library. These tests call it through the C
 ABI and check it against hann_pqivf_search_batch_device, the entry point it
 mirrors, on two calls in a row (the array keeps the previous call's contents),
+on a batch that fills the array to within one query of its end, on queries
+that take the brute-force fallback (counted in Stats like the mirrored call's),
 and check that an oversized batch is refused with an error instead of running.
 This file is collected last so a failure here leaves every other test run.
 """
@@ -89,3 +91,92 @@ def test_noalloc_rejects_oversized_batch(index):
                  _P(n.data_ptr()), _P(0))
     assert rc == hg.HANN_E_UNSUPPORTED
     assert b"arena" in L.hann_pqivf_last_error(idx.handle)
+
+
+ARENA = 16 << 20
+
+
+def _scratch_bytes(nq, nlist, nprobe, R):
+    """The entry point's scratch layout: every region rounded to 256 bytes."""
+    a = lambda b: (b + 255) // 256 * 256  # noqa: E731
+    return a(nq * nlist * 4) + 2 * a(nq * nprobe * 4) + 3 * a(nq * 4) + 3 * a(nq * R * 4)
+
+
+def _compare(idx, L, noalloc, q, k, nprobe, mode, stream, torch):
+    nq = q.shape[0]
+    outs = []
+    for use_noalloc in (False, True):
+        ids = torch.full((nq, k), -7, dtype=torch.int64, device="cuda")
+        d = torch.zeros((nq, k), dtype=torch.float64, device="cuda")
+        n = torch.zeros(nq, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        if use_noalloc:
+            rc = noalloc(idx.handle, _P(q.data_ptr()), nq, k, nprobe, mode, _P(ids.data_ptr()), _P(d.data_ptr()),
+                         _P(n.data_ptr()), _P(stream))
+            assert rc == 0, L.hann_pqivf_last_error(idx.handle)
+        else:
+            idx.SearchBatchDevice(q.data_ptr(), nq, k, nprobe, mode, ids.data_ptr(), d.data_ptr(), n.data_ptr(),
+                                  stream)
+        torch.cuda.synchronize()
+        outs.append((ids.cpu().numpy(), d.cpu().numpy(), n.cpu().numpy()))
+    assert_same_results(*outs[1], *outs[0])
+    return outs
+
+
+def test_noalloc_batch_filling_the_arena(index):
+    """The largest batch whose scratch fits: the last region ends within one
+    query's share of the array's end."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    idx, rng = index
+    L, noalloc = _noalloc_fn()
+    k, nprobe, nlist, R = 10, 6, 64, 64  # R: rerank depth of k 10 (k + 32, rounded up to 32)
+    nq = ARENA // (4 * nlist)
+    while _scratch_bytes(nq, nlist, nprobe, R) > ARENA:
+        nq -= 1
+    assert ARENA - _scratch_bytes(nq, nlist, nprobe, R) < _scratch_bytes(1, nlist, nprobe, R) + 8 * 256
+    q = torch.from_numpy(rng.normal(size=(nq, 32)).astype(np.float32)).cuda()
+    _compare(idx, L, noalloc, q, k, nprobe, 0, torch.cuda.current_stream().cuda_stream, torch)
+    # one query more no longer fits and is refused
+    q1 = torch.zeros((nq + 1, 32), dtype=torch.float32, device="cuda")
+    ids = torch.empty((nq + 1, k), dtype=torch.int64, device="cuda")
+    d = torch.empty((nq + 1, k), dtype=torch.float64, device="cuda")
+    n = torch.empty(nq + 1, dtype=torch.int32, device="cuda")
+    rc = noalloc(idx.handle, _P(q1.data_ptr()), nq + 1, k, nprobe, 0, _P(ids.data_ptr()), _P(d.data_ptr()),
+                 _P(n.data_ptr()), _P(0))
+    assert rc == hg.HANN_E_UNSUPPORTED
+
+
+def test_noalloc_fallback_queries(gpu):
+    """Lists emptied by deletions: queries whose probed list holds fewer than
+    k rows scan every list (the brute-force fallback), with the same results
+    and the same FallbackSearches count as the mirrored call."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    rng = np.random.default_rng(77)
+    x = rng.normal(size=(6000, 16)).astype(np.float32)
+    idx = hg.New(16, hg.WithCoarseK(64), hg.WithNumSubquantizers(4), hg.WithPQK(16), hg.WithKMeansIters(4))
+    idx.BulkAddArrays(np.arange(len(x)), x)
+    idx.Train()
+    st = idx.export_state()
+    lens = np.asarray(st["list_len"])
+    starts = np.concatenate([[0], np.cumsum(lens)[:-1]])
+    # empty every other list
+    dead = np.concatenate([st["ids"][starts[c]:starts[c] + lens[c]] for c in range(0, len(lens), 2)])
+    idx.BulkDelete(dead.tolist())
+    L, noalloc = _noalloc_fn()
+    k = 120
+    q = torch.from_numpy(rng.normal(size=(200, 16)).astype(np.float32)).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    f0 = idx.Stats().FallbackSearches
+    outs = _compare(idx, L, noalloc, q, k, 1, 0, stream, torch)
+    f1 = idx.Stats().FallbackSearches
+    assert (outs[1][2] == k).all()  # every query found k rows: the fallback ran
+    assert f1 > f0 and (f1 - f0) % 2 == 0  # the same count from each entry point
+    outs2 = _compare(idx, L, noalloc, q, k, 1, 0, stream, torch)
+    assert (f1 - f0) == (idx.Stats().FallbackSearches - f1)
+    for a, b in zip(outs[1], outs2[1]):
+        np.testing.assert_array_equal(a, b)
+    idx.close()
