@@ -74,6 +74,16 @@ def parse():
     ap.add_argument("--train-bench", type=int, default=1,
                     help="run the training section (1M x 128, coarse 4096, 16 x 256 PQ, 25 iterations)")
     ap.add_argument("--train-only", action="store_true", help="run only the training section")
+    ap.add_argument("--export-index", type=str, default="",
+                    help="build the search index, write its state and the queries to this directory, exit "
+                         "(the reference arm runs this in a child process so that its own process maps no "
+                         "library of this repository)")
+    ap.add_argument("--cpu-step-seconds", type=float, default=1.0,
+                    help="reference arm: CPU seconds per step (each step a sample of the queries)")
+    ap.add_argument("--config1", type=int, default=1,
+                    help="run the plain 20k x 128 PQIVF section (train + search, GPU and CPU oracle)")
+    ap.add_argument("--train-oracle-iters", type=int, default=2,
+                    help="k-means iterations of the oracle's inertia check on the 1M x 128 training shape")
     ap.add_argument("--knn-variants", type=str,
                     default="squared_euclidean/tensor,cosine/tensor,manhattan/exact,squared_euclidean/exact,"
                             "cosine/exact")
@@ -251,39 +261,221 @@ def build_index(args, x, torch):
     return idx, xh, t2 - t1
 
 
-def cpu_baseline(args, idx, q_host, nprobe, mode_rows):
-    """The oracle (C restatement of the reference's Search) timed on the host
-    cores on a bounded sample of the same queries."""
+def compare_results(g_ids, g_d, g_n, o_ids, o_d, o_n, rel=1e-5):
+    """Parity of two result sets under the bar of the tests: counts equal,
+    distances within `rel` relative, ids equal except inside ties (an id
+    may differ only where the two distances it competes at lie within rel).
+    Returns counts of the queries that break each part."""
+    g_n = np.asarray(g_n)
+    o_n = np.asarray(o_n)
+    count_mismatch = int((g_n != o_n).sum())
+    id_bad = 0
+    max_rel = 0.0
+    for i in range(len(g_n)):
+        c = int(min(g_n[i], o_n[i]))
+        gd = np.asarray(g_d[i][:c], np.float64)
+        od = np.asarray(o_d[i][:c], np.float64)
+        if c:
+            max_rel = max(max_rel, float(np.max(np.abs(gd - od) / np.maximum(np.abs(od), 1e-12))))
+        gi, oi = list(g_ids[i][:c]), list(o_ids[i][:c])
+        for j in range(c):
+            if gi[j] == oi[j]:
+                continue
+            if gi[j] in oi:
+                jj = oi.index(gi[j])
+                ok = abs(od[jj] - od[j]) <= rel * max(abs(od[j]), 1e-12) + 1e-12
+            else:
+                ok = abs(gd[j] - od[c - 1]) <= rel * max(abs(od[c - 1]), 1e-12) + 1e-12
+            if not ok:
+                id_bad += 1
+                break
+    return {"queries": int(len(g_n)), "count_mismatches": count_mismatch,
+            "id_mismatches_outside_ties": id_bad, "max_rel_dist_err": max_rel}
+
+
+def oracle_index_from_state(st):
+    import oracle
+
+    lay = st["layout"]
+    return oracle.OracleIndex.from_csr(lay["dimension"], lay["num_subquantizers"], lay["pq_k_eff"], st["coarse"],
+                                       st["codebooks"], st["list_len"], st["ids"], st["vectors"], st["codes"])
+
+
+def rerank_depth(k, mode):
+    """Candidates the GPU reranks per query (the library's automatic depth):
+    k + 32 in parity mode, max(4k, 64) in exact-rerank mode, rounded up to 32."""
+    r = k + 32 if mode == 0 else max(4 * k, 64)
+    return (r + 31) // 32 * 32
+
+
+def cpu_legs(args, idx, q_host, nprobe, gpu_parity, gpu_exact):
+    """The oracle over every query of the step, on all host cores: the
+    reference's Search (parity mode: reconstructed-vector PQ distances) and
+    the same search with the GPU's exact rerank of the best candidates.
+    Each is timed, and the GPU's results for the same queries are compared
+    with it. Returns (cpu_baseline, parity)."""
     import oracle
 
     oracle.build()
-    st = idx.export_state()
-    lay = st["layout"]
-    ix = oracle.OracleIndex.from_csr(lay["dimension"], lay["num_subquantizers"], lay["pq_k_eff"], st["coarse"],
-                                     st["codebooks"], st["list_len"], st["ids"], st["vectors"], st["codes"])
-    del st
+    oracle.set_tier(oracle.TIER_NEON)
+    ix = oracle_index_from_state(idx.export_state())
     cores = os.cpu_count() or 1
-    probe_n = min(64, q_host.shape[0])
+    nq = q_host.shape[0]
     t0 = time.perf_counter()
-    ix.search(q_host[:probe_n], args.k, nprobe, nthreads=cores)
-    dt = time.perf_counter() - t0
-    per_q = dt / probe_n
-    n = int(min(q_host.shape[0], max(probe_n, args.cpu_seconds / max(per_q, 1e-9))))
+    o_par = ix.search(q_host, args.k, nprobe, nthreads=cores)
+    t_par = time.perf_counter() - t0
+    R = rerank_depth(args.k, 1)
     t0 = time.perf_counter()
-    ix.search(q_host[:n], args.k, nprobe, nthreads=cores)
-    dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": "queries/s", "cores": cores, "kind": "port",
-            "sample": f"{n} of {q_host.shape[0]} queries, nprobe {nprobe}, k {args.k}, parity (reconstructed-"
-                      f"vector) distances, {cores} threads, {dt:.1f} s"}
+    o_ex = ix.search(q_host, args.k, nprobe, nthreads=cores, rerank=R)
+    t_ex = time.perf_counter() - t0
+    parity = {"reference_pq_distances": compare_results(*gpu_parity, *o_par[:3]),
+              "exact_rerank": compare_results(*gpu_exact, *o_ex[:3]),
+              "what": f"GPU results of all {nq} queries of the step (nprobe {nprobe}, k {args.k}) against the "
+                      "oracle's on the same exported index: counts, ids outside 1e-5-relative ties, "
+                      "largest relative distance error"}
+    cb = {"value": nq / t_ex, "unit": "queries/s", "cores": cores, "kind": "port",
+          "sample": f"all {nq} queries of the step, nprobe {nprobe}, k {args.k}, the reference's Search "
+                    f"restated in C (NEON summation order) + exact FP32 rerank of the best {R} candidates "
+                    f"(the GPU arm's mode), {cores} threads, {t_ex:.1f} s",
+          "parity_mode_queries_per_s": nq / t_par,
+          "parity_mode_sample": f"all {nq} queries, the reference's Search alone (PQ distances), {t_par:.1f} s"}
+    return cb, parity
+
+
+def export_index(args):
+    """Child process of the reference arm: builds the 10M x 96 index on the
+    GPU (the CPU cannot train it in minutes), picks nprobe from recall as the
+    GPU arm does, and writes the index state, the queries and the ground
+    truth as .npy files to args.export_index."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    import __graft_entry__ as ge
+
+    ge.build()
+    x, q = make_data(args, torch, dev)
+    idx, _, _ = build_index(args, x, torch)
+    q_host = q.cpu().numpy()
+    nr = min(args.recall_queries, args.nq)
+    gt = ground_truth(torch, x, q[:nr], args.k)
+    del x
+    choice, rec = pick_nprobe(args, idx, q_host, gt, nr)
+    st = idx.export_state()
+    out = args.export_index
+    lay = st["layout"]
+    for key in ("coarse", "codebooks", "list_len", "ids", "vectors"):
+        np.save(os.path.join(out, key + ".npy"), np.ascontiguousarray(st[key]))
+    np.save(os.path.join(out, "codes.npy"), np.ascontiguousarray(st["codes"], dtype=np.uint8))
+    np.save(os.path.join(out, "queries.npy"), q_host)
+    np.save(os.path.join(out, "gt.npy"), gt)
+    meta = {"dim": lay["dimension"], "M": lay["num_subquantizers"], "pq_k": lay["pq_k_eff"], "choice": choice,
+            "recall_gpu": {f"{a}/{'exact' if b == 1 else 'pq'}": v for (a, b), v in rec.items()}}
+    json.dump(meta, open(os.path.join(out, "meta.json"), "w"))
+    idx.close()
+    return 0
+
+
+def pick_nprobe(args, idx, q_host, gt, nr):
+    """Recall@10 at each nprobe in both modes; the first nprobe whose
+    exact-rerank recall reaches the target (else the largest)."""
+    probes = [int(p) for p in args.nprobe.split(",")]
+    rec = {}
+    for npb in probes:
+        for mode in (1, 0):
+            ids, _, _ = idx.SearchBatch(q_host[:nr], args.k, nprobe=npb, mode=mode)
+            rec[(npb, mode)] = recall_at(ids, gt)
+    log("recall", {f"nprobe{a}_mode{b}": round(v, 4) for (a, b), v in rec.items()})
+    choice = next((p for p in probes if rec[(p, 1)] >= args.target_recall), probes[-1])
+    return choice, rec
+
+
+def reference_arm(args):
+    """The reference's CPU path on the host cores: the oracle's restatement
+    of pqivf Search (C, NEON summation order) over the same index, timed in
+    steps of a bounded query sample. The index is built by a child process
+    (--export-index) and read back from files, so this process loads no
+    library of this repository."""
+    import shutil
+    import tempfile
+
+    import oracle
+
+    oracle.build()
+    oracle.set_tier(oracle.TIER_NEON)
+    td = tempfile.mkdtemp(prefix="hann_ref_")
+    try:
+        cmd = [sys.executable, os.path.abspath(__file__), "--export-index", td] + [
+            a for a in sys.argv[1:] if not a.startswith("--impl") and a != "reference"]
+        env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+        t0 = time.perf_counter()
+        subprocess.run(cmd, check=True, env=env, stdout=subprocess.DEVNULL)
+        build_s = time.perf_counter() - t0
+        meta = json.load(open(os.path.join(td, "meta.json")))
+        ld = lambda name: np.load(os.path.join(td, name + ".npy"))  # noqa: E731
+        ix = oracle.OracleIndex.from_csr(meta["dim"], meta["M"], meta["pq_k"], ld("coarse"), ld("codebooks"),
+                                         ld("list_len"), ld("ids"), ld("vectors"), ld("codes"))
+        q_host = ld("queries")
+        gt = ld("gt")
+    finally:
+        shutil.rmtree(td, ignore_errors=True)
+    choice = int(meta["choice"])
+    cores = os.cpu_count() or 1
+    R = rerank_depth(args.k, 1)
+    nq = q_host.shape[0]
+    # calibrate the step: about cpu_step_seconds of CPU work
+    t0 = time.perf_counter()
+    ix.search(q_host[:256], args.k, choice, nthreads=cores, rerank=R)
+    per_q = (time.perf_counter() - t0) / 256
+    S = int(max(256, min(nq, args.cpu_step_seconds / max(per_q, 1e-9))))
+    pos = 0
+
+    def step():
+        nonlocal pos
+        rows = (np.arange(S) + pos) % nq
+        pos = (pos + S) % nq
+        t = time.perf_counter()
+        ix.search(q_host[rows], args.k, choice, nthreads=cores, rerank=R)
+        return time.perf_counter() - t
+
+    for _ in range(args.warmup):
+        step()
+    times = [step() for _ in range(args.steps)]
+    qps = S * len(times) / sum(times)
+    nr = gt.shape[0]
+    ids_ex, _, _, _ = ix.search(q_host[:nr], args.k, choice, nthreads=cores, rerank=R)
+    t0 = time.perf_counter()
+    ids_par, _, _, _ = ix.search(q_host[:nr], args.k, choice, nthreads=cores)
+    par_qps = nr / (time.perf_counter() - t0)
+    rec = {"exact_rerank": recall_at(ids_ex, gt), "reference_pq_distances": recall_at(ids_par, gt)}
+    sample = (f"{S} queries per step of the {nq}-query workload (rotating), nprobe {choice}, k {args.k}: "
+              f"the reference's Search restated in C (NEON summation order) with the GPU arm's exact FP32 rerank "
+              f"of the best {R} candidates, {cores} threads; ms_per_step is scaled to {nq} queries")
+    line = {"impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * nq / qps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(args, choice, 1),
+            "recall_at_10": rec,
+            "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port", "sample": sample},
+            "parity_mode_queries_per_s": par_qps,
+            "parity_mode_sample": f"first {nr} queries, the reference's Search alone (PQ distances)",
+            "index_build": f"trained on the GPU by a child process ({build_s:.0f} s incl. data and ground truth), "
+                           "read back from files; only Search is timed",
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
 
 
 def main():
     args = parse()
+    if args.export_index:
+        return export_index(args)
     import torch
 
     ws, rank, local = dist_setup(args)
-    if args.impl == "reference" and rank != 0:
-        return 0
+    if args.impl == "reference":
+        # rank 0 alone runs the CPU arm; the index comes from a child process
+        return reference_arm(args) if rank == 0 else 0
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     import __graft_entry__ as ge
@@ -306,33 +498,8 @@ def main():
     torch.cuda.empty_cache()
 
     # recall at each nprobe, exact-rerank mode and parity mode
-    probes = [int(p) for p in args.nprobe.split(",")]
-    rec = {}
-    for npb in probes:
-        for mode in (1, 0):
-            ids, _, _ = idx.SearchBatch(q_host[:nr], args.k, nprobe=npb, mode=mode)
-            rec[(npb, mode)] = recall_at(ids, gt)
-    log("recall", {f"nprobe{a}_mode{b}": round(v, 4) for (a, b), v in rec.items()})
-    choice = None
-    for npb in probes:
-        if rec[(npb, 1)] >= args.target_recall:
-            choice = npb
-            break
-    if choice is None:
-        choice = probes[-1]
+    choice, rec = pick_nprobe(args, idx, q_host, gt, nr)
     mode = 1
-
-    if args.impl == "reference":
-        cb = cpu_baseline(args, idx, q_host, choice, None)
-        # steps: repeat bounded samples
-        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "queries/s", "n_gpus": ws,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * 1.0 / cb["value"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": workload_config(args, choice, mode, rec),
-                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
-                                            "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return 0
 
     # ------------------------------------------------------------------ timed
     nq = args.nq
@@ -443,9 +610,31 @@ def main():
         idx.SearchBatch(q_host[i:i + 1], args.k, nprobe=choice, mode=mode)
     plain_qps = nplain / (time.perf_counter() - t0)
 
+    # the other nprobe values of the workload, timed the same way
+    by_nprobe = {}
+    for npb in [int(p) for p in args.nprobe.split(",")]:
+        def step_np():
+            idx.SearchBatchDevice(q.data_ptr(), nq, args.k, npb, mode, ids_d.data_ptr(), dist_d.data_ptr(),
+                                  nout_d.data_ptr(), stream.cuda_stream)
+        for _ in range(args.warmup):
+            step_np()
+        torch.cuda.synchronize()
+        n0 = torch.cuda.Event(enable_timing=True)
+        n1 = torch.cuda.Event(enable_timing=True)
+        n0.record(stream)
+        for _ in range(args.steps):
+            step_np()
+        n1.record(stream)
+        torch.cuda.synchronize()
+        ms_np = n0.elapsed_time(n1) / args.steps
+        by_nprobe[str(npb)] = {"queries_per_s": nq / (ms_np / 1e3), "ms_per_step": ms_np,
+                               "recall_at_10_exact_rerank": rec[(npb, 1)],
+                               "recall_at_10_reference_pq_distances": rec[(npb, 0)]}
+    log("by nprobe", by_nprobe)
+
     # roofline of the scan kernel: algorithmic bytes = rows scanned (counted
-    # by the kernel) x (M code bytes + the 4-byte per-row term)
-    code_bytes = args.m + 4
+    # by the kernel, per (query, list)) x M code bytes
+    code_bytes = args.m
     per_search = max(1, min(nq, (1 << 28) // args.nlist))
     scan_launches = args.steps * -(-nq // per_search)
     scan_ms = stage_ms[2] / scan_launches
@@ -488,20 +677,36 @@ def main():
             knn = {"error": str(e)}
 
     cb = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            cb = cpu_baseline(args, idx, q_host, choice, None)
+            gpu_par = idx.SearchBatch(q_host, args.k, nprobe=choice, mode=0)
+            gpu_ex = idx.SearchBatch(q_host, args.k, nprobe=choice, mode=1)
+            cb, parity = cpu_legs(args, idx, q_host, choice, gpu_par, gpu_ex)
+            log("cpu baseline", cb)
+            log("parity", parity)
         except Exception as e:  # pragma: no cover
             log("cpu baseline failed:", e)
             cb = {"value": None, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port", "sample": str(e)}
+
+    config1 = None
+    if args.config1 and rank == 0:
+        try:
+            config1 = config1_section(args, torch, dev)
+        except Exception as e:  # pragma: no cover
+            log("config1 section failed:", e)
+            config1 = {"error": str(e)}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(args, choice, mode, rec),
+            "config": workload_config(args, choice, mode),
             "recall_at_10": rec[(choice, mode)],
+            "recall_by_nprobe": {f"{a}/{'exact' if b == 1 else 'pq'}": round(v, 4) for (a, b), v in rec.items()},
+            "by_nprobe": by_nprobe,
+            "parity": parity,
             "stage_ms_per_step": [round(v / args.steps, 4) for v in stage_ms],
             "train_s": round(train_s, 2),
             "plain_one_query_per_call_qps": plain_qps,
@@ -516,6 +721,7 @@ def main():
             "served_stream": served,
             "knn": knn,
             "train": train,
+            "config1": config1,
         }
         if served and "p50_ms" in served[0]:
             line["p50_ms"] = served[0]["p50_ms"]
@@ -527,6 +733,81 @@ def main():
 
         dist.destroy_process_group()
     return 0
+
+
+def config1_section(args, torch, dev):
+    """Plain PQIVF, the reference's CPU-sized case: 20,000 x 128 float32 from
+    a Gaussian mixture of 64 centres (N(0,1), sigma 0.3); coarse 64, 8 x 256
+    PQ, 10 k-means iterations from one seeded init given to both sides; 1,000
+    queries from the same mixture, top-10, default nprobe 3. GPU and oracle
+    each train and search; reported: train seconds, batched queries/s, one-
+    query-per-call p50/p99, recall@10 against FP64 brute force, coarse
+    inertia of both trainings (FP64) and the GPU search against the oracle
+    on the GPU-trained index."""
+    import hann_gb300 as hg
+    import oracle
+
+    oracle.build()
+    oracle.set_tier(oracle.TIER_NEON)
+    rng = np.random.default_rng(args.seed + 101)
+    n, dim, nc, nqq, k = 20_000, 128, 64, 1000, 10
+    cent = rng.normal(size=(nc, dim))
+    x = (cent[rng.integers(0, nc, n)] + 0.3 * rng.normal(size=(n, dim))).astype(np.float32)
+    qs = (cent[rng.integers(0, nc, nqq)] + 0.3 * rng.normal(size=(nqq, dim))).astype(np.float32)
+    ids = np.arange(n, dtype=np.int64)
+    cinit = rng.permutation(n)[:64]
+    pinit = np.stack([rng.permutation(n)[:256] for _ in range(8)])
+    reseed = rng.integers(0, n, 10000)
+    cores = os.cpu_count() or 1
+    gt, _ = oracle.brute_force_knn_fp64(qs, x, k, "euclidean", base_ids=ids)
+    out = {"workload": f"{n} x {dim} Gaussian mixture (64 centres, sigma 0.3); coarse 64; 8 x 256 PQ; 10 "
+                       f"k-means iterations from one seeded init; {nqq} queries; k {k}; nprobe 3"}
+    idx = hg.New(dim, hg.WithCoarseK(64), hg.WithNumSubquantizers(8), hg.WithPQK(256), hg.WithKMeansIters(10))
+    idx.BulkAddArrays(ids, x)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    idx.TrainSeeded(cinit, pinit, reseed)
+    torch.cuda.synchronize()
+    g_train = time.perf_counter() - t
+    idx.SearchBatch(qs, k, mode=0)
+    t = time.perf_counter()
+    g_ids, g_d, g_n = idx.SearchBatch(qs, k, mode=0)
+    g_batch = nqq / (time.perf_counter() - t)
+    lat = []
+    for i in range(nqq):
+        t = time.perf_counter()
+        idx.Search(qs[i], k)
+        lat.append(time.perf_counter() - t)
+    t = time.perf_counter()
+    ora, info = oracle.train(ids, x, 64, 8, 256, 10, cinit, pinit, reseed, nthreads=cores)
+    c_train = time.perf_counter() - t
+    t = time.perf_counter()
+    o_res = ora.search(qs, k, 3, nthreads=cores)
+    c_batch = nqq / (time.perf_counter() - t)
+    clat = []
+    for i in range(nqq):
+        t = time.perf_counter()
+        ora.search(qs[i:i + 1], k, 3, nthreads=1)
+        clat.append(time.perf_counter() - t)
+    st = idx.export_state()
+    g_asg = oracle.assign(x, st["coarse"], cores)
+    gi = oracle.inertia_fp64(x, st["coarse"], g_asg)
+    oi = oracle.inertia_fp64(x, ora.coarse, info["assign"])
+    on_gpu_index = oracle_index_from_state(st).search(qs, k, 3, nthreads=cores)
+    out["gpu"] = {"train_s": round(g_train, 4), "queries_per_s_batched": g_batch,
+                  "p50_ms_one_query_per_call": 1e3 * float(np.percentile(lat, 50)),
+                  "p99_ms_one_query_per_call": 1e3 * float(np.percentile(lat, 99)),
+                  "recall_at_10_vs_fp64": recall_at(g_ids, gt), "coarse_inertia_fp64": gi}
+    out["cpu_oracle"] = {"train_s": round(c_train, 3), "cores": cores, "queries_per_s_batched": c_batch,
+                         "p50_ms_one_query_per_call": 1e3 * float(np.percentile(clat, 50)),
+                         "p99_ms_one_query_per_call": 1e3 * float(np.percentile(clat, 99)),
+                         "recall_at_10_vs_fp64": recall_at(o_res[0], gt), "coarse_inertia_fp64": oi,
+                         "kind": "port (the reference's Train and Search restated in C, NEON order)"}
+    out["inertia_rel_diff"] = abs(gi - oi) / oi
+    out["search_parity_on_gpu_index"] = compare_results(g_ids, g_d, g_n, *on_gpu_index[:3])
+    idx.close()
+    log("config1", out)
+    return out
 
 
 def train_section(args, torch, dev):
@@ -636,7 +917,60 @@ def train_section(args, torch, dev):
     a, b = states["tensor_core"], states["plain_fp32"]
     out["identical_index"] = bool(all(np.array_equal(a[key], b[key]) for key in ("coarse", "list_len", "ids",
                                                                                 "codes")))
+    if args.train_oracle_iters > 0 and not args.no_cpu_baseline:
+        try:
+            out["oracle_check"] = train_oracle_check(args, torch, dev, x, xh, k)
+            log("train oracle check", out["oracle_check"])
+        except Exception as e:  # pragma: no cover
+            out["oracle_check"] = {"error": str(e)}
     return out
+
+
+def train_oracle_check(args, torch, dev, x, xh, k):
+    """Coarse k-means on the 1M x 128, k 4,096 shape from one seeded init,
+    on the GPU (Train with that init) and in the oracle (runKMeans restated
+    in C, all host cores), for args.train_oracle_iters iterations (fewer than
+    the workload's 25: each oracle iteration is ~5e11 multiply-adds on the
+    CPU). Reports both inertias (FP64, every point to its nearest centroid)
+    and the CPU's seconds per iteration."""
+    import hann_gb300 as hg
+    import oracle
+
+    oracle.build()
+    oracle.set_tier(oracle.TIER_NEON)
+    n, dim = xh.shape
+    T = args.train_oracle_iters
+    rng = np.random.default_rng(args.seed + 13)
+    cinit = rng.permutation(n)[:k]
+    pinit = np.stack([rng.permutation(n)[:256] for _ in range(16)])
+    reseed = rng.integers(0, n, 100000)
+    idx = hg.New(dim, hg.WithCoarseK(k), hg.WithNumSubquantizers(16), hg.WithPQK(256), hg.WithKMeansIters(T))
+    idx.BulkAddArrays(np.arange(n, dtype=np.int64), xh)
+    idx.TrainSeeded(cinit, pinit, reseed)
+    g_cent = idx.export_state()["coarse"]
+    idx.close()
+    cores = os.cpu_count() or 1
+    t = time.perf_counter()
+    o_cent, _ = oracle.kmeans(xh, k, T, cinit, reseed, nthreads=cores)
+    c_s = time.perf_counter() - t
+
+    def inertia(cent):
+        c = torch.from_numpy(np.ascontiguousarray(cent)).to(dev)
+        cn = (c * c).sum(1)
+        tot = 0.0
+        for s0 in range(0, n, 1 << 16):
+            xb = x[s0:s0 + (1 << 16)]
+            a = torch.argmin(cn[None, :] - 2.0 * xb @ c.T, dim=1)
+            d = xb.double() - c[a].double()
+            tot += float((d * d).sum().item())
+        return tot
+
+    torch.backends.cuda.matmul.allow_tf32 = False
+    gi, oi = inertia(g_cent), inertia(o_cent)
+    return {"iterations": T, "gpu_inertia_fp64": gi, "oracle_inertia_fp64": oi, "rel_diff": abs(gi - oi) / oi,
+            "cpu_s_per_iteration": c_s / T, "cores": cores,
+            "what": "coarse k-means from the same seeded init and reseed stream, GPU Train vs the oracle's "
+                    "runKMeans restatement; CPU seconds per iteration are the oracle's (assignment dominates)"}
 
 
 def knn_histogram_data(torch, dev, n, dim, seed):
@@ -876,7 +1210,7 @@ def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
             "max_batch_probes": args.serve_batch_probes}
 
 
-def workload_config(args, nprobe, mode, rec):
+def workload_config(args, nprobe, mode):
     return {
         "workload": f"pqivf-search {args.n // 1_000_000}M x {args.dim} unit-norm Gaussian mixture "
                     f"({args.centers} centers, sigma {args.sigma}); coarse {args.nlist}; "
@@ -884,8 +1218,8 @@ def workload_config(args, nprobe, mode, rec):
                     f"{'exact FP32 rerank of raw vectors' if mode == 1 else 'reference PQ distances'}",
         "n": args.n, "dim": args.dim, "nlist": args.nlist, "M": args.m, "pq_k": args.pqk, "nq": args.nq,
         "k": args.k, "nprobe": nprobe, "mode": "exact_rerank" if mode == 1 else "parity",
-        "recall_by_nprobe": {f"{a}/{'exact' if b == 1 else 'pq'}": round(v, 4) for (a, b), v in rec.items()},
-        "l2": f"inputs larger than L2 ({args.n * (2 * args.m) / 1e6:.0f} MB of scan words + "
+        "l2": f"inputs larger than L2 ({args.n * args.m / 1e6:.0f} MB of codes, {args.n * 2 * args.m / 1e6:.0f} MB "
+              f"of scan words + "
               f"{args.n * args.dim * 4 / 1e9:.2f} GB raw vectors), no flush",
     }
 

@@ -228,7 +228,45 @@ void hann_oracle_cosine_parts(const float* a, const float* b, size_t n, int tier
     cosine_parts(a, b, n, tier, &out3[0], &out3[1], &out3[2]);
 }
 
+/* The NEON tier of sum_squared_diff (4 lanes, 4 accumulators, fused
+ * multiply-add; core/simd_kernels.inc.h:64-102 with simd_kernels_neon.inc.h)
+ * written with one small array per accumulator so that the compiler can keep
+ * each in a vector register: the same operations in the same order as the
+ * generic path of hann_oracle_sqeuclid_tier, only faster, for the timed CPU
+ * baseline and the large parity checks. */
+static float sqeuclid_neon(const float* a, const float* b, size_t n) {
+    float c0[4] = {0, 0, 0, 0}, c1[4] = {0, 0, 0, 0}, c2[4] = {0, 0, 0, 0}, c3[4] = {0, 0, 0, 0};
+    size_t i = 0;
+    const size_t lim4 = n - (n % 16);
+    for (; i < lim4; i += 16) {
+        for (int l = 0; l < 4; l++) {
+            const float d0 = a[i + l] - b[i + l], d1 = a[i + 4 + l] - b[i + 4 + l];
+            const float d2 = a[i + 8 + l] - b[i + 8 + l], d3 = a[i + 12 + l] - b[i + 12 + l];
+            c0[l] = fmaf(d0, d0, c0[l]);
+            c1[l] = fmaf(d1, d1, c1[l]);
+            c2[l] = fmaf(d2, d2, c2[l]);
+            c3[l] = fmaf(d3, d3, c3[l]);
+        }
+    }
+    const size_t lim = n - (n % 4);
+    for (; i < lim; i += 4)
+        for (int l = 0; l < 4; l++) {
+            const float d = a[i + l] - b[i + l];
+            c0[l] = fmaf(d, d, c0[l]);
+        }
+    float v[4];
+    for (int l = 0; l < 4; l++) v[l] = (c0[l] + c1[l]) + (c2[l] + c3[l]);
+    float sum = (v[0] + v[1]) + (v[2] + v[3]);
+    for (; i < n; i++) {
+        const float d = a[i] - b[i];
+        const float p = d * d;
+        sum = sum + p;
+    }
+    return sum;
+}
+
 static inline float sqeuclid(const float* a, const float* b, size_t n) {
+    if (g_tier == TIER_NEON) return sqeuclid_neon(a, b, n);
     return hann_oracle_sqeuclid_tier(a, b, n, g_tier);
 }
 
@@ -240,8 +278,8 @@ void hann_oracle_batch(int metric, const float* q, const float* flat, size_t dim
         const float* x = flat + i * dim;
         float r;
         switch (metric) {
-        case 0: r = hann_oracle_sqeuclid_tier(q, x, dim, g_tier); break;
-        case 1: r = sqrtf(hann_oracle_sqeuclid_tier(q, x, dim, g_tier)); break;
+        case 0: r = sqeuclid(q, x, dim); break;
+        case 1: r = sqrtf(sqeuclid(q, x, dim)); break;
         case 2: r = hann_oracle_manhattan_tier(q, x, dim, g_tier); break;
         default: r = hann_oracle_cosine_tier(q, x, dim, g_tier); break;
         }

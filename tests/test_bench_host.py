@@ -74,9 +74,35 @@ def test_traffic_record_only_for_its_workload():
 
 
 def test_workload_config():
+    """The config names the workload from the arguments alone, so both arms
+    (and every rank) report the same one."""
     a = args_for()
-    cfg = bench.workload_config(a, 32, 1, {(32, 1): 0.98, (32, 0): 0.6})
+    cfg = bench.workload_config(a, 32, 1)
     assert cfg["nprobe"] == 32 and cfg["mode"] == "exact_rerank"
-    assert cfg["recall_by_nprobe"] == {"32/exact": 0.98, "32/pq": 0.6}
     assert "480 MB of scan words" in cfg["l2"] and "3.84 GB raw vectors" in cfg["l2"]
     assert "model" not in cfg
+    assert bench.workload_config(a, 32, 1) == cfg
+
+
+def test_compare_results_counts_only_real_mismatches():
+    o_ids = np.array([[1, 2, 3], [4, 5, 6]])
+    o_d = np.array([[0.1, 0.2, 0.3], [0.1, 0.2, 0.3]])
+    o_n = np.array([3, 3])
+    # a swap inside a tie of the reference distance is not a mismatch
+    g_ids = np.array([[1, 3, 2], [4, 5, 6]])
+    g_d = np.array([[0.1, 0.2, 0.2], [0.1, 0.2, 0.3]])
+    o_d2 = np.array([[0.1, 0.2, 0.2], [0.1, 0.2, 0.3]])
+    r = bench.compare_results(g_ids, g_d, o_n, o_ids, o_d2, o_n)
+    assert r["id_mismatches_outside_ties"] == 0 and r["count_mismatches"] == 0 and r["max_rel_dist_err"] == 0
+    # a different id at a different distance is one
+    g_ids = np.array([[1, 2, 9], [4, 5, 6]])
+    g_d = np.array([[0.1, 0.2, 0.25], [0.1, 0.2, 0.3]])
+    r = bench.compare_results(g_ids, g_d, o_n, o_ids, o_d, o_n)
+    assert r["id_mismatches_outside_ties"] == 1 and r["max_rel_dist_err"] > 0.1
+    r = bench.compare_results(o_ids, o_d, np.array([3, 2]), o_ids, o_d, o_n)
+    assert r["count_mismatches"] == 1
+
+
+def test_rerank_depth_matches_the_library():
+    assert bench.rerank_depth(10, 0) == 64 and bench.rerank_depth(10, 1) == 64
+    assert bench.rerank_depth(100, 1) == 416 and bench.rerank_depth(1, 0) == 64

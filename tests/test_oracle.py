@@ -162,3 +162,40 @@ def test_search_semantics_small():
     # brute-force fallback: k above the probed candidates
     r_ids, r_d, r_n, fb = ix.search(x[:3], 299, 1)
     assert fb.all() and (r_n == 299).all()
+
+
+def test_neon_fast_path_equals_generic_tier():
+    """The vectorisable NEON-order squared distance the oracle's search and
+    k-means use equals the generic lane-by-lane restatement bit for bit."""
+    oracle.set_tier(oracle.TIER_NEON)
+    rng = np.random.default_rng(1)
+    for n in (1, 3, 4, 15, 16, 17, 31, 32, 96, 128, 129, 784):
+        a = (rng.normal(size=(300, n)) * rng.choice([1e-3, 1, 1e3], size=(300, 1))).astype(np.float32)
+        b = rng.normal(size=n).astype(np.float32)
+        generic = np.array([oracle.sqeuclid(a[i], b, tier=oracle.TIER_NEON) for i in range(300)], np.float32)
+        assert np.array_equal(generic.astype(np.float64), oracle.batch(oracle.METRIC_SQEUCLID, b, a)), n
+
+
+def test_exact_rerank_search_mode():
+    """rerank=R keeps the R best candidates by PQ distance and orders them by
+    the exact distance to their stored vectors: with R covering every
+    candidate of the probed lists the result is the exact k-NN over those
+    lists."""
+    oracle.set_tier(oracle.TIER_NEON)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((400, 8)).astype(np.float32)
+    ids = np.arange(400)
+    ix, _ = oracle.train(ids, x, 4, 2, 8, 4, rng.permutation(400)[:4], [rng.permutation(400)[:8] for _ in range(2)],
+                         reseed_idx=rng.integers(0, 400, 100))
+    q = rng.standard_normal((20, 8)).astype(np.float32)
+    r_ids, r_d, r_n, _ = ix.search(q, 5, 2, rerank=400)
+    for i in range(len(q)):
+        probed = oracle.OracleIndex.probe(ix, q[i], 2)
+        rows = np.concatenate([np.arange(ix.list_off[c], ix.list_off[c + 1]) for c in probed])
+        d = np.array([oracle.sqeuclid(q[i], ix.vectors[r]) for r in rows], np.float64)
+        order = np.argsort(d, kind="stable")[:5]
+        assert np.array_equal(r_ids[i, :5], ix.ids[rows[order]])
+        np.testing.assert_allclose(r_d[i, :5], np.sqrt(d[order]), rtol=1e-12)
+    # rerank of fewer candidates than k still returns the candidates it kept
+    r_ids, r_d, r_n, _ = ix.search(q, 5, 2, rerank=3)
+    assert (r_n == 3).all()
