@@ -106,7 +106,8 @@ EXPORTED = (
     "hann_gob_last_error", "hann_gob_encode_payload",
 )
 # Entry points of include/hann_gb300_diag.h.
-EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats")
+EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats", "hann_pqivf_rows_decoded",
+                 "hann_pqivf_scan_options")
 
 
 def load_library(path: str | None = None) -> ctypes.CDLL:
@@ -152,6 +153,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
                                                          _P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.c_int32,
                                                          _P, _P, _P, _P]
         L.hann_pqivf_arena_stats.argtypes = [_P, _P]
+        L.hann_pqivf_rows_decoded.argtypes = [_P, _P]
+        L.hann_pqivf_scan_options.argtypes = [_P, _P, _P]
         L.hann_pqivf_retrain.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_save_snapshot.argtypes = [_P, ctypes.c_char_p]
         L.hann_pqivf_load_snapshot.argtypes = [_P, ctypes.c_char_p]
@@ -572,6 +575,28 @@ class Index:
         self._check(self._L.hann_pqivf_arena_stats(self._h, _ptr(out)))
         return dict(zip(("rows_allocated", "rows_packed", "hole_rows", "list_moves", "full_relayouts"),
                         (int(v) for v in out)))
+
+    SCAN_OPTION_KEYS = ("list_major", "min_queries", "first_chunk", "chunk_growth", "rows_per_item", "ctas_per_sm")
+
+    def ScanOptions(self, **set_) -> dict:
+        """The list scan's choices (diagnostics; results do not depend on
+        them): list_major (the tensor-core list-major scan, else the table
+        scan), min_queries, first_chunk, chunk_growth, rows_per_item,
+        ctas_per_sm. Keyword arguments replace the named ones."""
+        cur = np.zeros(6, dtype=np.int32)
+        self._check(self._L.hann_pqivf_scan_options(self._h, None, _ptr(cur)))
+        if set_:
+            for key, val in set_.items():
+                cur[self.SCAN_OPTION_KEYS.index(key)] = int(val)
+            self._check(self._L.hann_pqivf_scan_options(self._h, _ptr(cur), None))
+        return dict(zip(self.SCAN_OPTION_KEYS, (int(v) for v in cur)))
+
+    def RowsDecoded(self) -> int:
+        """Rows the list-major scan decoded while profiling was on, as of the
+        last StageTimes call."""
+        out = np.zeros(1, dtype=np.int64)
+        self._check(self._L.hann_pqivf_rows_decoded(self._h, _ptr(out)))
+        return int(out[0])
 
     def SaveSnapshot(self, path) -> None:
         """Write the binary snapshot (the gob stream's content as flat arrays;

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhann_gb300.so")
-SOURCES = ["kernels_train.cu", "kernels_search.cu", "kernels_scan.cu", "kernels_exact.cu", "kernels_gemm.cu", "kernels_rescore.cu", "kernels_knn.cu", "index.cu", "serve.cu", "knn.cu", "snapshot.cu", "gob.cu"]
+SOURCES = ["kernels_train.cu", "kernels_search.cu", "kernels_scan.cu", "kernels_exact.cu", "kernels_gemm.cu", "kernels_rescore.cu", "kernels_knn.cu", "kernels_lms.cu", "index.cu", "serve.cu", "knn.cu", "snapshot.cu", "gob.cu"]
 HEADERS = ["common.cuh", "kernels.h", "index_internal.h", "select.cuh", "tile_dist.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")

@@ -10,6 +10,8 @@
 //   row_id [rows] i64, row_cluster [rows] i32
 // Rows of one inverted list are contiguous; every list starts on a multiple
 // of 32 rows and keeps spare capacity so Adds append in place.
+#include <cuda_fp16.h>
+
 #include "index_internal.h"
 #include "hann_gb300_diag.h"
 
@@ -183,10 +185,13 @@ static int grow_lists(hann_pqivf* h, const std::vector<int>& lists, const std::v
 
 static int upload_lens(hann_pqivf* h) {
     std::vector<int32_t> len(h->nlist), live(h->nlist);
+    int64_t mx = 0;
     for (int l = 0; l < h->nlist; l++) {
         len[l] = (int32_t)h->list_ids[l].size();
         live[l] = (int32_t)h->live_count[l];
+        mx = std::max<int64_t>(mx, len[l]);
     }
+    h->max_list_slots = mx;
     CK(upload(h->d_len, len.data(), len.size(), h->stream));
     CK(upload(h->d_live, live.data(), live.size(), h->stream));
     if (h->scanw_dirty && h->rows_cap > 0) {
@@ -198,9 +203,69 @@ static int upload_lens(hann_pqivf* h) {
     return HANN_OK;
 }
 
+// FP16 codebooks for the list-major scan and the constants of its error
+// bound: over every residual r the codebooks can reconstruct, max ||r|| and
+// max ||r - r~|| (r~ the FP16 rounding) are at most the square roots of the
+// sums over subquantizers of the largest codeword norm and rounding error;
+// |term| = | ||r||^2 + 2 <c, r> | <= rmax^2 + 2 max||c|| rmax.
+static int prepare_lms(hann_pqivf* h) {
+    const int M = h->o.num_subquantizers, dim = h->o.dimension;
+    h->lms_ok = !h->o.plain_fp32 && h->nlist > 0 && h->pqk_eff > 0 && lms_supported(dim, M, h->pqk_eff);
+    if (!h->lms_ok) return HANN_OK;
+    const size_t ncb = (size_t)M * h->pqk_eff * h->dsub;
+    std::vector<uint16_t> cb16(ncb);
+    double r2 = 0.0, d2 = 0.0;
+    for (int m = 0; m < M; m++) {
+        double mx = 0.0, md = 0.0;
+        for (int j = 0; j < h->pqk_eff; j++) {
+            double n2 = 0.0, e2 = 0.0;
+            for (int e = 0; e < h->dsub; e++) {
+                const size_t i = ((size_t)m * h->pqk_eff + j) * h->dsub + e;
+                const float v = h->h_codebooks[i];
+                const __half hv = __float2half_rn(v);
+                cb16[i] = __half_as_ushort(hv);
+                const double d = (double)v - (double)__half2float(hv);
+                n2 += (double)v * v;
+                e2 += d * d;
+            }
+            mx = std::max(mx, n2);
+            md = std::max(md, e2);
+        }
+        r2 += mx;
+        d2 += md;
+    }
+    double cmax = 0.0;
+    for (int l = 0; l < h->nlist; l++) {
+        double n2 = 0.0;
+        for (int e = 0; e < dim; e++) {
+            const double v = h->h_coarse[(size_t)l * dim + e];
+            n2 += v * v;
+        }
+        cmax = std::max(cmax, n2);
+    }
+    const double rmax = std::sqrt(r2) * 1.0001, rd = std::sqrt(d2) * 1.0001;
+    cmax = std::sqrt(cmax) * 1.0001;
+    h->lms_bound.rmax = (float)rmax;
+    h->lms_bound.rd = (float)rd;
+    h->lms_bound.tmax = (float)((rmax * rmax + 2.0 * cmax * rmax) * 1.0001);
+    h->lms_bound.kpad = (dim + 15) / 16 * 16;
+    if (!std::isfinite(h->lms_bound.tmax) || rmax > 6.0e4) {
+        // FP16 cannot hold these codewords: the table scan serves every batch
+        h->lms_ok = false;
+        return HANN_OK;
+    }
+    CK(upload(h->d_cb16, cb16.data(), cb16.size(), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HANN_OK;
+}
+
 // BF16 centroids, their FP32 squared norms and the largest norm, for the
 // tensor-core preselection (dimensions up to 128).
 static int prepare_coarse(hann_pqivf* h) {
+    {
+        const int rc = prepare_lms(h);
+        if (rc) return rc;
+    }
     if (h->nlist > 0 && h->pqk_eff > 0) {
         const size_t ncb = (size_t)h->o.num_subquantizers * h->pqk_eff * h->dsub;
         CK(h->d_codebooks_t.reserve(ncb));
@@ -723,6 +788,9 @@ constexpr int PROBE_FIRST = 256;        // first centroid chunk at least (every 
 // Every scratch buffer run_search needs for nq queries (in chunks of at most
 // 2^28 / nlist), reserved up front; a server calls it once per slot at start
 // so no batch ever reaches the allocator.
+bool lms_use(const hann_pqivf* h, int64_t nq, int np_max);
+int reserve_lms_scratch(hann_pqivf* h, SearchScratch& sc, int64_t chunk, int np_max);
+
 int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_max, int kmax, int mode) {
     const int R = rerank_depth(h, kmax, mode);
     np_max = std::min(np_max, h->nlist);
@@ -755,6 +823,149 @@ int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_
         CK(sc.qorder.reserve((size_t)chunk));
         CK(sc.order_scratch.reserve((size_t)h->nlist));
     }
+    if (lms_use(h, chunk, np_max)) return reserve_lms_scratch(h, sc, chunk, np_max);
+    return HANN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The list-major scan (kernels_lms.cu) of one chunk of queries whose probe
+// lists are in sc.probe_ids / probe_d / fb: work queue, chunked scan with
+// band merges, candidates for the rerank; queries it cannot serve exactly
+// are listed in sc.lredo (count at lredo[nc]) for the table scan.
+
+static int sm_count(int dev) {
+    static int cached[64] = {};
+    if (dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        cached[dev] = v;
+    }
+    return cached[dev];
+}
+
+static LmsChunks lms_chunks(const LmsConfig& cfg, int np_max) {
+    LmsChunks ch{};
+    ch.n = 0;
+    ch.bound[0] = 0;
+    int b = std::min(np_max, std::max(1, cfg.first));
+    while (true) {
+        ch.bound[++ch.n] = b;
+        if (b >= np_max) break;
+        if (ch.n == LMS_MAX_CHUNKS - 1) {
+            ch.bound[++ch.n] = np_max;
+            break;
+        }
+        b = std::min<int64_t>(np_max, (int64_t)b * std::max(2, cfg.growth));
+    }
+    return ch;
+}
+
+static int lms_cap(const hann_pqivf* h) {
+    const int64_t first = std::max<int64_t>(1, h->lms.first) * h->max_list_slots;
+    return (int)std::min<int64_t>(8192, std::max<int64_t>(2048, round_up(first, 256)));
+}
+constexpr int LMS_LCAP = 2048;  // band list per query: the large warp form of the band merge
+
+// Whether a batch takes the list-major scan: on the index's state and the
+// batch size only, never on the other queries' k or nprobe, so that a
+// query's result does not depend on its batch. (Every rerank depth this
+// build accepts, at most 480, fits the band list.)
+bool lms_use(const hann_pqivf* h, int64_t nq, int np_max) {
+    return h->lms_ok && h->lms.enabled && nq >= h->lms.min_queries && np_max >= 1;
+}
+static_assert(LMS_LCAP / 2 >= 480, "band lists must hold the largest rerank depth");
+
+static int lms_item_cap(const hann_pqivf* h, int64_t nq, int np_max, const LmsChunks& ch) {
+    int wmax = 0;
+    for (int c = 0; c < ch.n; c++) wmax = std::max(wmax, ch.bound[c + 1] - ch.bound[c]);
+    const int64_t pairs = nq * (int64_t)wmax;
+    const int64_t groups = pairs / LMS_NQ + std::min<int64_t>(h->nlist, pairs);
+    const int64_t ranges = h->max_list_slots / std::max(1, h->lms.rows_max) + 1;
+    return (int)std::min<int64_t>(INT32_MAX / 2, groups * ranges + 1);
+}
+
+int reserve_lms_scratch(hann_pqivf* h, SearchScratch& sc, int64_t chunk, int np_max) {
+    const LmsChunks ch = lms_chunks(h->lms, np_max);
+    const int cap = lms_cap(h);
+    const int icap = lms_item_cap(h, chunk, np_max, ch);
+    CK(sc.q16.reserve((size_t)chunk * 128));
+    CK(sc.le2.reserve((size_t)chunk));
+    CK(sc.lasl.reserve((size_t)chunk));
+    CK(sc.lthr.reserve((size_t)chunk));
+    CK(sc.lcnt.reserve((size_t)chunk));
+    CK(sc.llcount.reserve((size_t)chunk));
+    CK(sc.lneed.reserve((size_t)chunk));
+    CK(sc.lbandk.reserve((size_t)chunk));
+    CK(sc.ltodo.reserve((size_t)chunk + 1));
+    CK(sc.lredo.reserve((size_t)chunk + 1));
+    CK(sc.lcand_id.reserve((size_t)chunk * cap));
+    CK(sc.lcand_s.reserve((size_t)chunk * cap));
+    CK(sc.lband.reserve((size_t)chunk * LMS_LCAP));
+    CK(sc.lcounts.reserve((size_t)ch.n * h->nlist));
+    CK(sc.lcursor.reserve((size_t)ch.n * h->nlist));
+    CK(sc.ltotal.reserve(2));
+    CK(sc.lpair_q.reserve((size_t)chunk * np_max));
+    CK(sc.lpair_base.reserve((size_t)chunk * np_max));
+    CK(sc.lpair_off.reserve((size_t)chunk * np_max));
+    CK(sc.litems.reserve((size_t)ch.n * icap));
+    CK(sc.ln_items.reserve((size_t)ch.n));
+    CK(sc.litem_counter.reserve(1));
+    CK(sc.lstats.reserve(2));
+    return HANN_OK;
+}
+
+static int run_lms(hann_pqivf* h, SearchScratch& sc, const float* qp, int64_t nc, const int32_t* d_k,
+                   const int32_t* d_np, int np_max, int kmax, int mode, int R, cudaStream_t s) {
+    const LmsChunks ch = lms_chunks(h->lms, np_max);
+    const int cap = lms_cap(h);
+    const int icap = lms_item_cap(h, nc, np_max, ch);
+    const int M = h->o.num_subquantizers;
+    CK(launch_lms_prep(qp, nc, h->o.dimension, sc.probe_ids.p, sc.probe_d.p, d_np, np_max, sc.fb.p, h->d_len.p,
+                       ch.bound[1], h->lms_bound, mode, d_k, h->o.rerank, sc.lbandk.p, sc.q16.p, sc.le2.p, sc.lasl.p,
+                       sc.lcnt.p, sc.llcount.p, sc.lthr.p, sc.lneed.p, s));
+    CK(launch_lms_queue(sc.probe_ids.p, sc.probe_d.p, d_np, nc, np_max, sc.fb.p, ch, h->nlist, h->d_len.p,
+                        h->lms.rows_max, icap, sc.lcounts.p, sc.lcursor.p, sc.ltotal.p, sc.litems.p, sc.ln_items.p,
+                        sc.lpair_q.p, sc.lpair_base.p, sc.lpair_off.p, s));
+    LmsParams lp{};
+    lp.codes = h->d_codes.p;
+    lp.code_stride = h->code_stride;
+    lp.term = h->d_term.p;
+    lp.list_start = h->d_start.p;
+    lp.cb16 = h->d_cb16.p;
+    lp.M = M;
+    lp.dsub = h->dsub;
+    lp.pqK = h->pqk_eff;
+    lp.dim = h->o.dimension;
+    lp.q16 = sc.q16.p;
+    lp.item_counter = sc.litem_counter.p;
+    lp.item_cap = icap;
+    lp.pair_q = sc.lpair_q.p;
+    lp.pair_base = sc.lpair_base.p;
+    lp.pair_off = sc.lpair_off.p;
+    lp.thr = sc.lthr.p;
+    lp.cnt = sc.lcnt.p;
+    lp.cand_id = sc.lcand_id.p;
+    lp.cand_s = sc.lcand_s.p;
+    lp.cap = cap;
+    lp.stats = h->profile ? h->s_rows.p : nullptr;
+    lp.err = h->d_err.p;
+    const int grid = sm_count(h->o.device) * std::max(1, h->lms.ctas_per_sm);
+    const int bandk_max = mode == 0 ? kmax : R;
+    for (int c = 0; c < ch.n; c++) {
+        lp.items = sc.litems.p + (int64_t)c * icap;
+        lp.n_items = sc.ln_items.p + c;
+        lp.dense = c == 0 ? 1 : 0;
+        CK(launch_lms_scan(lp, grid, s));
+        // k >= 33 selects the band merge's large warp form (2,048 keys a row)
+        CK(launch_knn_merge_band((int)nc, std::max(bandk_max, 64), sc.lbandk.p, cap, LMS_LCAP, sc.lcnt.p,
+                                 sc.lcand_id.p, sc.lcand_s.p, sc.le2.p, sc.lasl.p, sc.lband.p, sc.llcount.p,
+                                 sc.lthr.p, sc.lneed.p, sc.ltodo.p, s));
+    }
+    CK(launch_lms_finish(nc, mode, R, LMS_LCAP, d_k, h->o.rerank, sc.lband.p, sc.llcount.p, sc.lneed.p,
+                         sc.probe_ids.p, d_np, np_max, h->d_row_cluster.p, sc.ltotal.p + 1, sc.cand_row.p,
+                         sc.cand_seq.p, sc.lredo.p, s));
+    h->launches += 8 + 5 * ch.n;
     return HANN_OK;
 }
 
@@ -789,6 +1000,46 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
     // full score matrix.
     const bool screened = h->tc && h->nlist >= SCREEN_MIN_LISTS;
     const int lcap = std::max(1024, 2 * np_max);
+    const bool lms = lms_use(h, chunk, np_max);
+    // The list scan and the rerank of queries [q0, q0 + nc) whose probe lists
+    // are ready: the list-major tensor-core scan, then the table scan for the
+    // queries it leaves (brute-force fallbacks and overflowing bands); or the
+    // table scan alone (qorder: the L2-friendly block order).
+    auto scan_rerank = [&](int64_t q0, int64_t nc, const float* qp, const int32_t* qorder) -> int {
+        p.kq = d_k + q0;
+        if (lms && nc >= h->lms.min_queries) {
+            CK(mark(2, true));
+            const int lrc = run_lms(h, sc, qp, nc, d_k + q0, d_np + q0, np_max, kmax, mode, R, s);
+            if (lrc) return lrc;
+            CK(mark(2, false));
+            CK(mark(3, true));
+            p.qorder = nullptr;
+            CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+                             d_dist + q0 * kmax, d_nout + q0, s));
+            ScanParams pr = p;
+            pr.qorder = sc.lredo.p;
+            pr.qcount = sc.lredo.p + nc;
+            CK(launch_scan(pr, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R, sc.cand_row.p,
+                           sc.cand_d.p, sc.cand_seq.p, nullptr, s));
+            CK(launch_rerank(pr, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+                             d_dist + q0 * kmax, d_nout + q0, s));
+            CK(mark(3, false));
+            h->launches += 3;
+            return HANN_OK;
+        }
+        CK(mark(2, true));
+        p.qorder = qorder;
+        CK(launch_scan(p, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R, sc.cand_row.p,
+                       sc.cand_d.p, sc.cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
+        CK(mark(2, false));
+        CK(mark(3, true));
+        CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+                         d_dist + q0 * kmax, d_nout + q0, s));
+        p.qorder = nullptr;
+        CK(mark(3, false));
+        h->launches += 2;
+        return HANN_OK;
+    };
     for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
         const int64_t nc = std::min(chunk, nq - q0);
         const float* qp = d_q + q0 * h->o.dimension;
@@ -822,18 +1073,9 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
                                   sc.D.p, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, fbc, sc.ptodo.p, s));
             CK(launch_probe_order(sc.probe_ids.p, nc, np_max, h->nlist, sc.order_scratch.p, sc.qorder.p, s));
             CK(mark(1, false));
-            CK(mark(2, true));
-            p.kq = d_k + q0;
-            p.qorder = sc.qorder.p;
-            CK(launch_scan(p, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R,
-                           sc.cand_row.p, sc.cand_d.p, sc.cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
-            CK(mark(2, false));
-            CK(mark(3, true));
-            CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
-                             d_dist + q0 * kmax, d_nout + q0, s));
-            p.qorder = nullptr;
-            CK(mark(3, false));
-            h->launches += launches + 7;  // + probe final (2), query order (3), scan, rerank
+            const int rc = scan_rerank(q0, nc, qp, sc.qorder.p);
+            if (rc) return rc;
+            h->launches += launches + 5;  // + probe final (2), query order (3)
             continue;
         }
         CK(mark(0, true));
@@ -856,16 +1098,9 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
                                    h->o.fallback ? 1 : 0, sc.probe_ids.p, sc.probe_d.p, sc.fb.p, fbc, s));
         }
         CK(mark(1, false));
-        CK(mark(2, true));
-        p.kq = d_k + q0;
-        CK(launch_scan(p, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R,
-                       sc.cand_row.p, sc.cand_d.p, sc.cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
-        CK(mark(2, false));
-        CK(mark(3, true));
-        CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
-                         d_dist + q0 * kmax, d_nout + q0, s));
-        CK(mark(3, false));
-        h->launches += h->tc ? 5 : 4;
+        const int rc = scan_rerank(q0, nc, qp, nullptr);
+        if (rc) return rc;
+        h->launches += h->tc ? 3 : 2;
     }
     return HANN_OK;
 }
@@ -964,8 +1199,8 @@ int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out) {
     cudaError_t e = cudaSetDevice(o.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = h->main.fbcount.reserve(1);
-    if (e == cudaSuccess) e = h->s_rows.reserve(1);
-    if (e == cudaSuccess) e = cudaMemset(h->s_rows.p, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = h->s_rows.reserve(2);
+    if (e == cudaSuccess) e = cudaMemset(h->s_rows.p, 0, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = h->d_fb_dev.reserve(1);
     if (e == cudaSuccess) e = cudaMemset(h->d_fb_dev.p, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->dev_ev, cudaEventDisableTiming);
@@ -1359,10 +1594,46 @@ int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_
     }
     const int64_t nl = h->launches.exchange(0);
     if (launches) *launches = nl;
-    unsigned long long rows = 0;
-    CK(cudaMemcpy(&rows, h->s_rows.p, sizeof(rows), cudaMemcpyDeviceToHost));
+    unsigned long long rows[2] = {0, 0};
+    CK(cudaMemcpy(rows, h->s_rows.p, sizeof(rows), cudaMemcpyDeviceToHost));
     CK(cudaMemset(h->s_rows.p, 0, sizeof(rows)));
-    if (rows_scanned) *rows_scanned = (int64_t)rows;
+    if (rows_scanned) *rows_scanned = (int64_t)rows[0];
+    h->rows_decoded = (int64_t)rows[1];
+    return HANN_OK;
+}
+
+int hann_pqivf_rows_decoded(void* hv, int64_t* out) {
+    hann_pqivf* h = static_cast<hann_pqivf*>(hv);
+    if (!h || !out) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> rl(h->run_mu);
+    *out = h->rows_decoded;
+    return HANN_OK;
+}
+
+int hann_pqivf_scan_options(void* hv, const int32_t* set6, int32_t* get6) {
+    hann_pqivf* h = static_cast<hann_pqivf*>(hv);
+    if (!h) return HANN_E_INVALID;
+    std::unique_lock<std::mutex> w(h->wmu);
+    std::unique_lock<std::shared_mutex> g(h->mu);
+    std::lock_guard<std::mutex> rl(h->run_mu);
+    if (set6) {
+        if (set6[1] < 1 || set6[2] < 1 || set6[3] < 2 || set6[4] < 1 || set6[5] < 1 || set6[5] > 2)
+            return h->fail(HANN_E_INVALID, "invalid list-scan options");
+        h->lms.enabled = set6[0] ? 1 : 0;
+        h->lms.min_queries = set6[1];
+        h->lms.first = set6[2];
+        h->lms.growth = set6[3];
+        h->lms.rows_max = set6[4];
+        h->lms.ctas_per_sm = set6[5];
+    }
+    if (get6) {
+        get6[0] = h->lms.enabled;
+        get6[1] = h->lms.min_queries;
+        get6[2] = h->lms.first;
+        get6[3] = h->lms.growth;
+        get6[4] = h->lms.rows_max;
+        get6[5] = h->lms.ctas_per_sm;
+    }
     return HANN_OK;
 }
 

@@ -152,6 +152,29 @@ struct SearchScratch {
     DBuf<int32_t> pcnt, pcand_id, plcount, pneed, ptodo;  // ptodo: rows left to the block kernels (+ count)
     DBuf<unsigned long long> pband;
     DBuf<int32_t> qorder, order_scratch;  // L2-friendly query order for scan and rerank
+    // list-major tensor-core scan (kernels_lms.cu)
+    DBuf<uint16_t> q16;
+    DBuf<float> le2, lasl, lthr, lcand_s, lpair_base;
+    DBuf<int32_t> lcnt, lcand_id, llcount, lneed, ltodo, lredo, lbandk, lcounts, lcursor, ltotal, lpair_q,
+        lpair_off, ln_items, litem_counter;
+    DBuf<unsigned long long> lband, lstats;
+    DBuf<LmsItem> litems;
+};
+
+// The list-major scan's choices: chunks of probe ranks, rows per work item,
+// blocks per SM, and the smallest batch worth it. Defaults until the
+// autotuner (hann_pqivf_autotune) measures better ones for the index.
+struct LmsConfig {
+    int enabled = 1;       // 0: every batch takes the table scan
+    // Smaller batches take the table scan. 1 by default: in exact-rerank
+    // mode the two scans may pass different candidates to the rerank (FP16
+    // against FP32 screening at the rerank depth), so a query's result would
+    // depend on the size of the batch it runs in.
+    int min_queries = 1;
+    int first = 1;         // probe ranks in the first chunk (written densely)
+    int growth = 8;        // each later chunk ends at growth x the previous end
+    int rows_max = 1024;   // rows of one list per work item
+    int ctas_per_sm = 2;
 };
 
 // Message of the calling thread's last failed call on any handle. Kept per
@@ -213,6 +236,15 @@ struct hann_pqivf {
     DBuf<uint8_t> s_codes;
     DBuf<uint16_t> s_scanw;
 
+    // list-major tensor-core scan: FP16 codebooks [M][pqK][dsub], the error
+    // bound's constants, the longest list (slots) and the scan's choices
+    DBuf<uint16_t> d_cb16;
+    LmsBound lms_bound{};
+    bool lms_ok = false;
+    int64_t max_list_slots = 0;
+    LmsConfig lms;
+    int64_t rows_decoded = 0;  // rows the list-major scan decoded, as of the last hann_pqivf_stage_times
+
     // search scratch of the handle's own stream
     SearchScratch main;
     DBuf<unsigned long long> s_rows;
@@ -267,6 +299,7 @@ struct hann_pqivf {
         p.codes = d_codes.p;
         p.scanw = scan_skew_supported(o.num_subquantizers) ? d_scanw.p : nullptr;
         p.qorder = nullptr;
+        p.qcount = nullptr;
         p.sw_start = d_swstart.p;
         p.term = d_term.p;
         p.row_cluster = d_row_cluster.p;

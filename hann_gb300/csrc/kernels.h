@@ -149,6 +149,7 @@ struct ScanParams {
     const int64_t* row_id;    // [rows]
     const int32_t* kq;        // [nq] per-query k (sets each query's rerank depth)
     const int32_t* qorder;    // optional: block b works on query qorder[b] (L2-friendly order)
+    const int32_t* qcount;    // optional with qorder: blocks at or past *qcount have no query
     int mode, rerank_fixed;
 };
 
@@ -214,6 +215,81 @@ cudaError_t launch_relayout_lists(int nlist, const int64_t* src_start, const int
                                   const float* vin, float* vout, const void* cin, void* cout, const float* tin,
                                   float* tout, const int64_t* rin, int64_t* rout, const int32_t* clin, int32_t* clout,
                                   cudaStream_t s);
+
+// ---- list-major batched scan on the tensor cores (kernels_lms.cu) --------------
+
+constexpr int LMS_NQ = 64;        // queries per work item (the MMA's largest N here)
+constexpr int LMS_MAX_CHUNKS = 8;  // probe-rank chunks of one search
+
+// One work item: rows [row_begin, row_begin + n_rows) of list `list` against
+// the n_pairs queries whose pairs start at pair_begin in the pair arrays.
+struct LmsItem {
+    int32_t list, pair_begin, n_pairs, row_begin, n_rows, pad0, pad1, pad2;
+};
+
+// Probe-rank chunks: chunk c holds ranks [bound[c], bound[c + 1]), the last
+// one up to each query's nprobe.
+struct LmsChunks {
+    int n;
+    int bound[LMS_MAX_CHUNKS + 1];
+};
+
+// Index-wide constants of the FP16 error bound: max ||r|| and max ||r - r~||
+// over every reconstructable residual (from the codebooks), max |term|, the
+// padded K of the dot products.
+struct LmsBound {
+    float rmax, rd, tmax;
+    int kpad;
+};
+
+struct LmsParams {
+    const uint8_t* codes;
+    int code_stride;
+    const float* term;
+    const int64_t* list_start;
+    const void* cb16;  // __half [M][pqK][dsub]
+    int M, dsub, pqK, dim;
+    const void* q16;   // __half [nq][128]
+    const LmsItem* items;
+    const int32_t* n_items;
+    int32_t* item_counter;
+    int item_cap;       // items of one chunk's region
+    const int32_t* pair_q;
+    const float* pair_base;
+    const int32_t* pair_off;
+    const float* thr;
+    int32_t* cnt;
+    int32_t* cand_id;
+    float* cand_s;
+    int cap, dense;
+    unsigned long long* stats;  // optional: [0] (query, row) pairs scored, [1] rows decoded
+    int* err;
+};
+
+bool lms_supported(int dim, int M, int pqK);
+int lms_smem_bytes();
+cudaError_t launch_lms_prep(const float* Q, int64_t nq, int dim, const int32_t* probe_ids, const float* probe_d,
+                            const int32_t* nprobe, int np_max, const int32_t* fallback, const int32_t* list_len,
+                            int first_w, const LmsBound& bd, int mode, const int32_t* kq, int rfixed, int32_t* bandk,
+                            void* q16, float* e2, float* asl, int32_t* cnt, int32_t* lcount, float* thr, int32_t* need,
+                            cudaStream_t s);
+// Work queue of every chunk: counts [n * nlist], cursor [n * nlist],
+// totals [2] ([1]: set when a chunk's items overflow item_cap, which sends
+// every query to the table scan), items [n * item_cap], n_items [n], pair
+// arrays [nq * np_max].
+cudaError_t launch_lms_queue(const int32_t* probe_ids, const float* probe_d, const int32_t* nprobe, int64_t nq,
+                             int np_max, const int32_t* fallback, const LmsChunks& ch, int nlist,
+                             const int32_t* list_len, int rows_max, int item_cap, int32_t* counts, int32_t* cursor,
+                             int32_t* totals, LmsItem* items, int32_t* n_items, int32_t* pair_q, float* pair_base,
+                             int32_t* pair_off, cudaStream_t s);
+cudaError_t launch_lms_scan(const LmsParams& p, int grid, cudaStream_t s);
+// Band lists to rerank candidates; queries for the table scan to redo
+// (count at redo[nq]).
+cudaError_t launch_lms_finish(int64_t nq, int mode, int R, int lcap, const int32_t* kq, int rfixed,
+                              const unsigned long long* list, const int32_t* lcount, const int32_t* need,
+                              const int32_t* probe_ids, const int32_t* nprobe, int np_max, const int32_t* row_cluster,
+                              const int32_t* overflow, int32_t* cand_row, uint32_t* cand_seq, int32_t* redo,
+                              cudaStream_t s);
 
 // ---- batched exact k-NN over a flat base (kernels_knn.cu) ------------------------
 

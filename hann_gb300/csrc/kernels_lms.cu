@@ -202,8 +202,8 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
     uint64_t* t_full = bars + 8;   // [2]
     uint64_t* t_empty = bars + 10; // [2]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 12);
-    int* s_item = reinterpret_cast<int*>(bars + 13);
-    volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 14);
+    int* s_item = reinterpret_cast<int*>(bars + 13);  // [0..1] claimed items, [2..3] stage-wait results
+    volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 15);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Every operand byte starts at zero: the K padding past the dimension and
@@ -239,18 +239,26 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
     const int ksteps = (p.dim + 15) >> 4;
 
     if (warp < 4) {
-        // ---------------- producers: claim items, load queries, decode tiles
+        // ---------------- producers: claim items, load queries, decode tiles.
+        // Thread 0 of the four warps makes every decision that can end the
+        // loop (which item, whether a wait ran out) and publishes it before a
+        // named barrier of the 128 threads, so all of them take the same
+        // path and meet at every barrier.
         const int pt = threadIdx.x;  // 0..127: the tile row this thread decodes
+        const int n_items = min(*p.n_items, p.item_cap);
         int item_seq = 0, tile_seq = 0;
         while (true) {
-            if (pt == 0) *s_item = atomicAdd(p.item_counter, 1);
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            const int idx = *s_item;
-            asm volatile("bar.sync 1, 128;" ::: "memory");
             const int b = item_seq & 1;
-            if (item_seq >= 2 && !mbar_wait(&b_empty[b], ((item_seq >> 1) - 1) & 1, p.err, s_abort)) break;
-            if (*s_abort) break;
-            const bool last = idx >= *p.n_items;
+            if (pt == 0) {
+                int idx = atomicAdd(p.item_counter, 1);
+                bool ok = *s_abort == 0;
+                if (ok && item_seq >= 2) ok = mbar_wait(&b_empty[b], ((item_seq >> 1) - 1) & 1, p.err, s_abort);
+                s_item[item_seq & 1] = ok ? idx : -1;
+            }
+            asm volatile("bar.sync 1, 128;" ::: "memory");
+            const int idx = s_item[item_seq & 1];
+            if (idx < 0) break;  // a wait ran out
+            const bool last = idx >= n_items;
             LmsItem it;
             if (!last) it = p.items[idx];
             if (pt == 0) {
@@ -277,7 +285,8 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
                     uint4 v = make_uint4(0, 0, 0, 0);
                     if (j < it.n_pairs) {
                         const int32_t q = p.pair_q[(int64_t)it.pair_begin + j];
-                        v = __ldg(reinterpret_cast<const uint4*>(p.q16 + (int64_t)q * 128) + c);
+                        v = __ldg(reinterpret_cast<const uint4*>(static_cast<const __half*>(p.q16) + (int64_t)q * 128) +
+                                  c);
                     }
                     const int kb = c >> 3, cc = c & 7;
                     *reinterpret_cast<uint4*>(bt + kb * NQ * 128 + j * 128 + ((cc ^ (j & 7)) << 4)) = v;
@@ -292,15 +301,20 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
             bool ok = true;
             for (int t = 0; t < ntiles; t++, tile_seq++) {
                 const int s = tile_seq % A_STAGES;
-                if (tile_seq >= A_STAGES &&
-                    !mbar_wait(&a_empty[s], ((tile_seq / A_STAGES) - 1) & 1, p.err, s_abort)) {
-                    ok = false;
-                    break;
+                if (tile_seq >= A_STAGES) {
+                    if (pt == 0)
+                        s_item[2 + (tile_seq & 1)] =
+                            mbar_wait(&a_empty[s], ((tile_seq / A_STAGES) - 1) & 1, p.err, s_abort) ? 1 : 0;
+                    asm volatile("bar.sync 1, 128;" ::: "memory");
+                    if (s_item[2 + (tile_seq & 1)] == 0) {
+                        ok = false;
+                        break;
+                    }
                 }
                 const int lr = t * TM + pt;
                 if (lr < it.n_rows)
                     decode_row<DSUB>(sA + s * A_STAGE_BYTES, pt, p.codes + (row0 + lr) * p.code_stride, p.M, p.dsub,
-                                     p.pqK, p.cb16);
+                                     p.pqK, static_cast<const __half*>(p.cb16));
                 fence_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&a_full[s]);
@@ -465,13 +479,14 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
 __global__ void lms_prep_kernel(const float* __restrict__ Q, int64_t nq, int dim, const int32_t* __restrict__ probe_ids,
                                 const float* __restrict__ probe_d, const int32_t* __restrict__ nprobe, int np_max,
                                 const int32_t* __restrict__ fallback, const int32_t* __restrict__ list_len, int first_w,
-                                LmsBound bd, int mode, __half* __restrict__ q16, float* __restrict__ e2,
+                                LmsBound bd, int mode, const int32_t* __restrict__ kq, int rfixed,
+                                int32_t* __restrict__ bandk, __half* __restrict__ q16, float* __restrict__ e2,
                                 float* __restrict__ asl, int32_t* __restrict__ cnt, int32_t* __restrict__ lcount,
                                 float* __restrict__ thr, int32_t* __restrict__ need) {
     const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (q >= nq) return;
-    float s = 0.0f, e = 0.0f;
+    float s = 0.0f, e = 0.0f, amax = 0.0f;
     for (int j = lane; j < 128; j += 32) {
         const float v = j < dim ? Q[q * dim + j] : 0.0f;
         const __half h = __float2half_rn(v);
@@ -479,11 +494,13 @@ __global__ void lms_prep_kernel(const float* __restrict__ Q, int64_t nq, int dim
         const float d = v - __half2float(h);
         s = fmaf(v, v, s);
         e = fmaf(d, d, e);
+        amax = fmaxf(amax, fabsf(v));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         s += __shfl_xor_sync(0xffffffffu, s, o);
         e += __shfl_xor_sync(0xffffffffu, e, o);
+        amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     }
     const int np = min(nprobe[q], np_max);
     int c0 = 0;
@@ -506,10 +523,15 @@ __global__ void lms_prep_kernel(const float* __restrict__ Q, int64_t nq, int dim
             e2[q] = 0.0f;
             asl[q] = 0.0f;
         }
-        const bool fb = fallback[q] != 0;
+        // a component FP16 cannot hold (or a non-finite one) sends the query
+        // to the table scan, as does the brute-force fallback
+        const bool fb = fallback[q] != 0 || !(amax <= 6.0e4f) || !(s < 3.0e38f);
         need[q] = fb ? 1 : 0;
         lcount[q] = 0;
         thr[q] = __int_as_float(0x7f800000);
+        // the band keeps the query's k best (parity: every row the reference's
+        // top k can be) or its rerank depth (exact rerank)
+        bandk[q] = mode == 0 ? kq[q] : rerank_depth_for(kq[q], mode, rfixed);
         cnt[q] = fb ? 0 : c0;
     }
 }
@@ -574,7 +596,7 @@ __global__ void lms_scan_counts_kernel(int32_t* __restrict__ v, int n, int32_t* 
 __global__ void lms_items_kernel(const int32_t* __restrict__ offsets, const int32_t* __restrict__ total, int nch,
                                  int nlist, const int32_t* __restrict__ list_len, int rows_max, int item_cap,
                                  LmsItem* __restrict__ items, int32_t* __restrict__ n_items,
-                                 int32_t* __restrict__ cursor, int* __restrict__ err) {
+                                 int32_t* __restrict__ cursor, int32_t* __restrict__ overflow) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (int64_t)nch * nlist) return;
     const int c = (int)(e / nlist), l = (int)(e - (int64_t)c * nlist);
@@ -586,7 +608,7 @@ __global__ void lms_items_kernel(const int32_t* __restrict__ offsets, const int3
     const int gq = (n + NQ - 1) / NQ, gr = (len + rows_max - 1) / rows_max;
     const int base = atomicAdd(&n_items[c], gq * gr);
     if (base + gq * gr > item_cap) {
-        atomicExch(err, 2);
+        atomicExch(overflow, 1);
         return;
     }
     LmsItem* out = items + (int64_t)c * item_cap + base;
@@ -638,8 +660,9 @@ __global__ void lms_finish_kernel(int64_t nq, int mode, int R, int lcap, const i
                                   const unsigned long long* __restrict__ list, const int32_t* __restrict__ lcount,
                                   const int32_t* __restrict__ need, const int32_t* __restrict__ probe_ids,
                                   const int32_t* __restrict__ nprobe, int np_max,
-                                  const int32_t* __restrict__ row_cluster, int32_t* __restrict__ cand_row,
-                                  uint32_t* __restrict__ cand_seq, int32_t* __restrict__ redo) {
+                                  const int32_t* __restrict__ row_cluster, const int32_t* __restrict__ overflow,
+                                  int32_t* __restrict__ cand_row, uint32_t* __restrict__ cand_seq,
+                                  int32_t* __restrict__ redo) {
     extern __shared__ __align__(16) unsigned long long fk[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
@@ -648,7 +671,7 @@ __global__ void lms_finish_kernel(int64_t nq, int mode, int R, int lcap, const i
     unsigned int* hist = reinterpret_cast<unsigned int*>(fk + (int64_t)(blockDim.x >> 5) * (lcap + 64)) + w * 256;
     const int L = lcount[q];
     const int Rq = min(R, rerank_depth_for(kq[q], mode, rfixed));
-    bool flag = need[q] != 0 || (mode == 0 && L > R);
+    const bool flag = need[q] != 0 || (mode == 0 && L > R) || *overflow != 0;
     if (flag) {
         if (lane == 0) redo[atomicAdd(&redo[nq], 1)] = (int32_t)q;
         for (int i = lane; i < R; i += 32) {
@@ -705,11 +728,12 @@ bool lms_supported(int dim, int M, int pqK) {
 
 cudaError_t launch_lms_prep(const float* Q, int64_t nq, int dim, const int32_t* probe_ids, const float* probe_d,
                             const int32_t* nprobe, int np_max, const int32_t* fallback, const int32_t* list_len,
-                            int first_w, const LmsBound& bd, int mode, void* q16, float* e2, float* asl, int32_t* cnt,
-                            int32_t* lcount, float* thr, int32_t* need, cudaStream_t s) {
+                            int first_w, const LmsBound& bd, int mode, const int32_t* kq, int rfixed, int32_t* bandk,
+                            void* q16, float* e2, float* asl, int32_t* cnt, int32_t* lcount, float* thr, int32_t* need,
+                            cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
     lms_prep_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(Q, nq, dim, probe_ids, probe_d, nprobe, np_max, fallback,
-                                                              list_len, first_w, bd, mode,
+                                                              list_len, first_w, bd, mode, kq, rfixed, bandk,
                                                               static_cast<__half*>(q16), e2, asl, cnt, lcount, thr,
                                                               need);
     return cudaGetLastError();
@@ -719,10 +743,11 @@ cudaError_t launch_lms_queue(const int32_t* probe_ids, const float* probe_d, con
                              int np_max, const int32_t* fallback, const LmsChunks& ch, int nlist,
                              const int32_t* list_len, int rows_max, int item_cap, int32_t* counts, int32_t* cursor,
                              int32_t* totals, LmsItem* items, int32_t* n_items, int32_t* pair_q, float* pair_base,
-                             int32_t* pair_off, int* err, cudaStream_t s) {
+                             int32_t* pair_off, cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
     const int64_t ncl = (int64_t)ch.n * nlist;
     cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * ncl, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(totals, 0, 2 * sizeof(int32_t), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(n_items, 0, sizeof(int32_t) * ch.n, s);
     if (e != cudaSuccess) return e;
     const int64_t np = nq * np_max;
@@ -730,7 +755,7 @@ cudaError_t launch_lms_queue(const int32_t* probe_ids, const float* probe_d, con
                                                                  counts);
     lms_scan_counts_kernel<<<1, 1024, 0, s>>>(counts, (int)ncl, totals);
     lms_items_kernel<<<(unsigned)ceil_div(ncl, 256), 256, 0, s>>>(counts, totals, ch.n, nlist, list_len, rows_max,
-                                                                  item_cap, items, n_items, cursor, err);
+                                                                  item_cap, items, n_items, cursor, totals + 1);
     lms_scatter_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, s>>>(probe_ids, probe_d, nprobe, nq, np_max, fallback,
                                                                    ch, nlist, list_len, cursor, pair_q, pair_base,
                                                                    pair_off);
@@ -760,7 +785,8 @@ size_t lms_finish_smem(int lcap) { return 8 * ((size_t)(lcap + 64) * 8 + 256 * 4
 cudaError_t launch_lms_finish(int64_t nq, int mode, int R, int lcap, const int32_t* kq, int rfixed,
                               const unsigned long long* list, const int32_t* lcount, const int32_t* need,
                               const int32_t* probe_ids, const int32_t* nprobe, int np_max, const int32_t* row_cluster,
-                              int32_t* cand_row, uint32_t* cand_seq, int32_t* redo, cudaStream_t s) {
+                              const int32_t* overflow, int32_t* cand_row, uint32_t* cand_seq, int32_t* redo,
+                              cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(redo + nq, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return e;
@@ -768,8 +794,8 @@ cudaError_t launch_lms_finish(int64_t nq, int mode, int R, int lcap, const int32
     e = cudaFuncSetAttribute(lms_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     lms_finish_kernel<<<(unsigned)ceil_div(nq, 8), 256, smem, s>>>(nq, mode, R, lcap, kq, rfixed, list, lcount, need,
-                                                                  probe_ids, nprobe, np_max, row_cluster, cand_row,
-                                                                  cand_seq, redo);
+                                                                  probe_ids, nprobe, np_max, row_cluster, overflow,
+                                                                  cand_row, cand_seq, redo);
     return cudaGetLastError();
 }
 

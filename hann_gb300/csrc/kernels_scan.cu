@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
     const int copies = 32 / M;
     const int G = 32;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (p.qcount && (int)blockIdx.x >= *p.qcount) return;
     const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const float* qv = Q + q * p.dim;
     if (tid == 0) {

@@ -293,6 +293,7 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(ScanParams p, const fl
     __shared__ uint32_t s_tau;
     __shared__ int s_wcount[SC_WARPS];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (p.qcount && (int)blockIdx.x >= *p.qcount) return;
     const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const float* qv = Q + q * p.dim;
     if (tid == 0) s_tau = float_key(F_INF);
@@ -499,6 +500,7 @@ __global__ void __launch_bounds__(RR_THREADS) rerank_warp_kernel(ScanParams p, c
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t qi = (int64_t)blockIdx.x * (RR_THREADS / 32) + w;
     if (qi >= nq) return;
+    if (p.qcount && qi >= *p.qcount) return;
     const int64_t q = p.qorder ? p.qorder[qi] : qi;
     float* qv = reinterpret_cast<float*>(smraw) + (int64_t)w * (p.dim + 3 * RP);
     float* cd = qv + p.dim;
@@ -559,6 +561,7 @@ __global__ void __launch_bounds__(RR_THREADS) rerank_kernel(ScanParams p, const 
     uint32_t* cs = reinterpret_cast<uint32_t*>(cd + RP);
     int32_t* cr = reinterpret_cast<int32_t*>(cs + RP);
     __shared__ int s_valid;
+    if (p.qcount && (int)blockIdx.x >= *p.qcount) return;
     const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const int tid = threadIdx.x;
     if (tid == 0) s_valid = 0;

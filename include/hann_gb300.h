@@ -195,7 +195,11 @@ int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out, int32_t capacity, int32
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * Every call shares the array, so calls whose work overlaps on the GPU
  * (different streams, threads or handles) race; serialise them. Fallbacks
- * are counted as for hann_pqivf_search_batch_device. */
+ * are counted as for hann_pqivf_search_batch_device. It scans the lists with
+ * the table scan: in exact-rerank mode (1) its results are those of
+ * hann_pqivf_search_batch_device with the list-major scan switched off,
+ * which may differ from the list-major scan's where a row competes at the
+ * rerank depth; in mode 0 both give the reference's results. */
 int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float* d_queries, int64_t nq, int32_t k,
                                            int32_t nprobe, int32_t mode, int64_t* d_ids, double* d_distances,
                                            int32_t* d_n_out, void* stream);

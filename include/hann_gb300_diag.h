@@ -27,6 +27,19 @@ int hann_gpu_bf16_scores(const float* a, int64_t n, const float* b, int32_t m, i
  * handle was made. h is a hann_pqivf*. */
 int hann_pqivf_arena_stats(void* h, int64_t* out5);
 
+/* Rows the list-major scan decoded (each list's rows once per work item),
+ * counted while profiling was on, as of the last hann_pqivf_stage_times
+ * (whose rows_scanned counts the scored (query, row) pairs). */
+int hann_pqivf_rows_decoded(void* h, int64_t* out);
+
+/* The list scan's choices. set6 (may be NULL) replaces them, get6 (may be
+ * NULL) receives them: [0] list-major tensor-core scan on (1) or the table
+ * scan for every batch (0); [1] smallest batch that takes the list-major
+ * scan; [2] probe ranks in its first chunk; [3] growth of the later chunks'
+ * ends; [4] rows of a list per work item; [5] blocks per SM (1 or 2). Results
+ * do not depend on them. */
+int hann_pqivf_scan_options(void* h, const int32_t* set6, int32_t* get6);
+
 #ifdef __cplusplus
 }
 #endif

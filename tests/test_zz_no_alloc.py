@@ -64,8 +64,19 @@ def test_noalloc_matches_device_search_two_calls(index, mode):
         got_d = torch.zeros((nq, k), dtype=torch.float64, device="cuda")
         got_n = torch.zeros(nq, dtype=torch.int32, device="cuda")
         torch.cuda.synchronize()  # the fills above ran on torch's stream
-        idx.SearchBatchDevice(q.data_ptr(), nq, k, nprobe, mode, ref_ids.data_ptr(), ref_d.data_ptr(),
-                              ref_n.data_ptr(), stream)
+        # The allocation-free call runs the table scan. With the exact rerank
+        # the list-major scan may hand different candidates to the rerank at
+        # the rerank depth, so that mode is compared with the device entry
+        # point running the table scan too; the reference's PQ distances
+        # (mode 0) agree whichever scan runs.
+        if mode == 1:
+            idx.ScanOptions(list_major=0)
+        try:
+            idx.SearchBatchDevice(q.data_ptr(), nq, k, nprobe, mode, ref_ids.data_ptr(), ref_d.data_ptr(),
+                                  ref_n.data_ptr(), stream)
+            torch.cuda.synchronize()
+        finally:
+            idx.ScanOptions(list_major=1)
         rc = noalloc(idx.handle, _P(q.data_ptr()), nq, k, nprobe, mode, _P(got_ids.data_ptr()),
                      _P(got_d.data_ptr()), _P(got_n.data_ptr()), _P(stream))
         assert rc == 0, L.hann_pqivf_last_error(idx.handle)
