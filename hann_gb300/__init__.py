@@ -103,7 +103,8 @@ EXPORTED = (
     "hann_serve_submit_priority", "hann_serve_cancel", "hann_pqivf_set_candidate_clusters",
     "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot", "hann_pqivf_retrain", "hann_gob_encode",
     "hann_gob_decode", "hann_gob_state_layout", "hann_gob_state_arrays", "hann_gob_state_free",
-    "hann_gob_last_error", "hann_gob_encode_payload",
+    "hann_gob_last_error", "hann_gob_encode_payload", "hann_pqivf_tune_candidate_clusters",
+    "hann_pqivf_autotune_scan",
 )
 # Entry points of include/hann_gb300_diag.h.
 EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats", "hann_pqivf_rows_decoded",
@@ -149,6 +150,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_autotune_scan.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P, _P, _P]
         L.hann_pqivf_tune_candidate_clusters.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
                                                          _P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.c_int32,
                                                          _P, _P, _P, _P]
@@ -576,14 +578,33 @@ class Index:
         return dict(zip(("rows_allocated", "rows_packed", "hole_rows", "list_moves", "full_relayouts"),
                         (int(v) for v in out)))
 
-    SCAN_OPTION_KEYS = ("list_major", "min_queries", "first_chunk", "chunk_growth", "rows_per_item", "ctas_per_sm")
+    TUNE_NPROBES = (8, 16, 32, 64, 128, 256)
+
+    def AutotuneScan(self, queries, k: int = 10, mode: int = 1) -> dict:
+        """Times the table scan and forms of the list-major scan on these
+        queries at nprobe 8..256 and keeps the fastest routing (see
+        hann_pqivf_autotune_scan). Returns the chosen options and the
+        measured milliseconds per nprobe of both scans."""
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self._dim)
+        chosen = np.zeros(8, dtype=np.int32)
+        tab = np.zeros(6, dtype=np.float64)
+        lm = np.zeros(6, dtype=np.float64)
+        self._check(self._L.hann_pqivf_autotune_scan(self._h, _ptr(q), q.shape[0], int(k), int(mode), _ptr(chosen),
+                                                     _ptr(tab), _ptr(lm)))
+        return {"options": dict(zip(self.SCAN_OPTION_KEYS, (int(v) for v in chosen))),
+                "ms_table_scan": {p: float(t) for p, t in zip(self.TUNE_NPROBES, tab) if t >= 0},
+                "ms_list_major": {p: float(t) for p, t in zip(self.TUNE_NPROBES, lm) if t >= 0}}
+
+    SCAN_OPTION_KEYS = ("list_major", "min_queries", "first_chunk", "chunk_growth", "rows_per_item", "ctas_per_sm",
+                        "seed_threshold", "min_nprobe")
 
     def ScanOptions(self, **set_) -> dict:
         """The list scan's choices (diagnostics; results do not depend on
         them): list_major (the tensor-core list-major scan, else the table
         scan), min_queries, first_chunk, chunk_growth, rows_per_item,
-        ctas_per_sm. Keyword arguments replace the named ones."""
-        cur = np.zeros(6, dtype=np.int32)
+        ctas_per_sm, seed_threshold, min_nprobe. Keyword arguments replace
+        the named ones."""
+        cur = np.zeros(8, dtype=np.int32)
         self._check(self._L.hann_pqivf_scan_options(self._h, None, _ptr(cur)))
         if set_:
             for key, val in set_.items():

@@ -862,8 +862,10 @@ static LmsChunks lms_chunks(const LmsConfig& cfg, int np_max) {
 }
 
 static int lms_cap(const hann_pqivf* h) {
-    const int64_t first = std::max<int64_t>(1, h->lms.first) * h->max_list_slots;
-    return (int)std::min<int64_t>(8192, std::max<int64_t>(2048, round_up(first, 256)));
+    // the dense first chunk holds every row of its lists; otherwise the
+    // threshold keeps the appends far below one list's length
+    const int64_t first = h->lms.seed ? h->max_list_slots : std::max<int64_t>(1, h->lms.first) * h->max_list_slots;
+    return (int)std::min<int64_t>(8192, std::max<int64_t>(h->lms.seed ? 4096 : 2048, round_up(first, 256)));
 }
 constexpr int LMS_LCAP = 2048;  // band list per query: the large warp form of the band merge
 
@@ -872,7 +874,7 @@ constexpr int LMS_LCAP = 2048;  // band list per query: the large warp form of t
 // query's result does not depend on its batch. (Every rerank depth this
 // build accepts, at most 480, fits the band list.)
 bool lms_use(const hann_pqivf* h, int64_t nq, int np_max) {
-    return h->lms_ok && h->lms.enabled && nq >= h->lms.min_queries && np_max >= 1;
+    return h->lms_ok && h->lms.enabled && nq >= h->lms.min_queries && np_max >= std::max(1, h->lms.min_nprobe);
 }
 static_assert(LMS_LCAP / 2 >= 480, "band lists must hold the largest rerank depth");
 
@@ -891,6 +893,9 @@ int reserve_lms_scratch(hann_pqivf* h, SearchScratch& sc, int64_t chunk, int np_
     const int icap = lms_item_cap(h, chunk, np_max, ch);
     CK(sc.q16.reserve((size_t)chunk * 128));
     CK(sc.le2.reserve((size_t)chunk));
+    CK(sc.leps.reserve((size_t)chunk));
+    CK(sc.lones.reserve((size_t)chunk));
+    CK(sc.lzeros.reserve((size_t)chunk));
     CK(sc.lasl.reserve((size_t)chunk));
     CK(sc.lthr.reserve((size_t)chunk));
     CK(sc.lcnt.reserve((size_t)chunk));
@@ -921,11 +926,27 @@ static int run_lms(hann_pqivf* h, SearchScratch& sc, const float* qp, int64_t nc
     const int cap = lms_cap(h);
     const int icap = lms_item_cap(h, nc, np_max, ch);
     const int M = h->o.num_subquantizers;
+    const bool seed = h->lms.seed != 0;
     CK(launch_lms_prep(qp, nc, h->o.dimension, sc.probe_ids.p, sc.probe_d.p, d_np, np_max, sc.fb.p, h->d_len.p,
-                       ch.bound[1], h->lms_bound, mode, d_k, h->o.rerank, sc.lbandk.p, sc.q16.p, sc.le2.p, sc.lasl.p,
-                       sc.lcnt.p, sc.llcount.p, sc.lthr.p, sc.lneed.p, s));
-    CK(launch_lms_queue(sc.probe_ids.p, sc.probe_d.p, d_np, nc, np_max, sc.fb.p, ch, h->nlist, h->d_len.p,
-                        h->lms.rows_max, icap, sc.lcounts.p, sc.lcursor.p, sc.ltotal.p, sc.litems.p, sc.ln_items.p,
+                       seed ? 0 : ch.bound[1], h->lms.min_nprobe, h->lms_bound, mode, d_k, h->o.rerank, sc.lbandk.p,
+                       sc.leps.p, sc.q16.p,
+                       sc.le2.p, sc.lasl.p, sc.lcnt.p, sc.llcount.p, sc.lthr.p, sc.lneed.p, s));
+    if (seed) {
+        // the table scan of each query's nearest list (no brute-force
+        // fallback: those queries go to the table scan anyway) sets the
+        // first thresholds
+        ScanParams ps = h->scan_params();
+        ps.mode = mode;
+        ps.kq = d_k;
+        CK(launch_fill_i32(sc.lones.p, nc, 1, s));
+        CK(cudaMemsetAsync(sc.lzeros.p, 0, sizeof(int32_t) * (size_t)nc, s));
+        CK(launch_scan(ps, qp, nc, sc.probe_ids.p, sc.probe_d.p, sc.lones.p, np_max, sc.lzeros.p, R, sc.cand_row.p,
+                       sc.cand_d.p, sc.cand_seq.p, nullptr, s));
+        CK(launch_lms_seed(nc, R, sc.cand_d.p, sc.lbandk.p, sc.leps.p, sc.le2.p, sc.lasl.p, sc.lthr.p, s));
+        h->launches += 3;
+    }
+    CK(launch_lms_queue(sc.probe_ids.p, sc.probe_d.p, d_np, nc, np_max, sc.lneed.p, ch, h->nlist, h->d_len.p,
+                        h->d_start.p, h->lms.rows_max, icap, sc.lcounts.p, sc.lcursor.p, sc.ltotal.p, sc.litems.p, sc.ln_items.p,
                         sc.lpair_q.p, sc.lpair_base.p, sc.lpair_off.p, s));
     LmsParams lp{};
     lp.codes = h->d_codes.p;
@@ -955,7 +976,7 @@ static int run_lms(hann_pqivf* h, SearchScratch& sc, const float* qp, int64_t nc
     for (int c = 0; c < ch.n; c++) {
         lp.items = sc.litems.p + (int64_t)c * icap;
         lp.n_items = sc.ln_items.p + c;
-        lp.dense = c == 0 ? 1 : 0;
+        lp.dense = !seed && c == 0 ? 1 : 0;
         CK(launch_lms_scan(lp, grid, s));
         // k >= 33 selects the band merge's large warp form (2,048 keys a row)
         CK(launch_knn_merge_band((int)nc, std::max(bandk_max, 64), sc.lbandk.p, cap, LMS_LCAP, sc.lcnt.p,
@@ -1602,6 +1623,127 @@ int hann_pqivf_stage_times(hann_pqivf* h, double* ms4, int64_t* launches, int64_
     return HANN_OK;
 }
 
+int hann_pqivf_autotune_scan(hann_pqivf* h, const float* queries, int64_t nq, int32_t k, int32_t mode,
+                             int32_t* chosen8, double* ms_table, double* ms_list) {
+    if (!h) return HANN_E_INVALID;
+    if (nq <= 0 || !queries) return h->fail(HANN_E_INVALID, "invalid arguments");
+    if (k <= 0) return h->fail(HANN_E_INVALID, "k must be positive");
+    if (mode != 0 && mode != 1) return h->fail(HANN_E_INVALID, "mode must be 0 or 1");
+    std::lock_guard<std::mutex> wl(h->wmu);
+    std::unique_lock<std::shared_mutex> lk(h->mu);
+    std::lock_guard<std::mutex> rl(h->run_mu);
+    cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
+    int rc = check_searchable(h);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    DBuf<float> dq;
+    DBuf<int32_t> dk, dnp, dn;
+    DBuf<int64_t> di;
+    DBuf<double> dd;
+    CK(upload(dq, queries, (size_t)nq * h->o.dimension, s));
+    CK(dk.reserve((size_t)nq));
+    CK(dnp.reserve((size_t)nq));
+    CK(dn.reserve((size_t)nq));
+    CK(di.reserve((size_t)nq * k));
+    CK(dd.reserve((size_t)nq * k));
+    CK(launch_fill_i32(dk.p, nq, k, s));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const LmsConfig saved = h->lms;
+    // the median of three timed runs after a warm one, in ms
+    auto time_search = [&](int np) -> double {
+        if (launch_fill_i32(dnp.p, nq, np, s) != cudaSuccess) return -1.0;
+        float best[3] = {0, 0, 0};
+        for (int r = 0; r < 4; r++) {
+            if (cudaEventRecord(e0, s) != cudaSuccess) return -1.0;
+            if (run_search(h, h->main, dq.p, nq, dk.p, dnp.p, np, k, mode, di.p, dd.p, dn.p, s) != HANN_OK)
+                return -1.0;
+            if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) return -1.0;
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r > 0) best[r - 1] = ms;
+        }
+        std::sort(best, best + 3);
+        return best[1];
+    };
+    // list-major candidates: chunk growth and the rows of a list per work item
+    // (the list-split threshold); the first chunk takes each query's nearest list
+    const int grid[][3] = {{1, 32, 512}, {1, 8, 512}, {1, 32, 1024}, {1, 8, 256}};
+    const int ngrid = (int)(sizeof(grid) / sizeof(grid[0]));
+    const int ladder[] = {8, 16, 32, 64, 128, 256};
+    const int nl = (int)(sizeof(ladder) / sizeof(ladder[0]));
+    double tab[6], lm[6][4];
+    int used = 0;
+    bool fail = false;
+    for (int i = 0; i < nl && !fail; i++) {
+        const int np = std::min(ladder[i], h->nlist);
+        if (i > 0 && np == std::min(ladder[i - 1], h->nlist)) break;
+        used = i + 1;
+        h->lms = saved;
+        h->lms.enabled = 0;
+        tab[i] = time_search(np);
+        for (int g = 0; g < ngrid; g++) {
+            h->lms = saved;
+            h->lms.enabled = h->lms_ok ? 1 : 0;
+            h->lms.min_nprobe = 1;
+            h->lms.min_queries = 1;
+            h->lms.seed = 0;
+            h->lms.first = grid[g][0];
+            h->lms.growth = grid[g][1];
+            h->lms.rows_max = grid[g][2];
+            lm[i][g] = h->lms_ok ? time_search(np) : 1e30;
+        }
+        fail = tab[i] < 0.0;
+        for (int g = 0; g < ngrid; g++) fail |= lm[i][g] < 0.0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->lms = saved;
+    if (fail) return h->fail(HANN_E_CUDA, "a tuning search failed");
+    // the list-major form with the smallest total over the ladder, then the
+    // crossover: the smallest ladder value from which it is faster at every
+    // larger value
+    int bg = 0;
+    double bsum = 1e300;
+    for (int g = 0; g < ngrid; g++) {
+        double sum = 0.0;
+        for (int i = 0; i < used; i++) sum += lm[i][g];
+        if (sum < bsum) {
+            bsum = sum;
+            bg = g;
+        }
+    }
+    int cross = h->nlist + 1;  // never
+    for (int i = used - 1; i >= 0; i--) {
+        if (lm[i][bg] < tab[i]) cross = std::min(ladder[i], h->nlist);
+        else break;
+    }
+    h->lms.enabled = h->lms_ok ? 1 : 0;
+    h->lms.min_queries = 1;
+    h->lms.seed = 0;
+    h->lms.first = grid[bg][0];
+    h->lms.growth = grid[bg][1];
+    h->lms.rows_max = grid[bg][2];
+    h->lms.min_nprobe = cross;
+    if (chosen8) {
+        chosen8[0] = h->lms.enabled;
+        chosen8[1] = h->lms.min_queries;
+        chosen8[2] = h->lms.first;
+        chosen8[3] = h->lms.growth;
+        chosen8[4] = h->lms.rows_max;
+        chosen8[5] = h->lms.ctas_per_sm;
+        chosen8[6] = h->lms.seed;
+        chosen8[7] = h->lms.min_nprobe;
+    }
+    for (int i = 0; i < nl; i++) {
+        if (ms_table) ms_table[i] = i < used ? tab[i] : -1.0;
+        if (ms_list) ms_list[i] = i < used ? lm[i][bg] : -1.0;
+    }
+    return HANN_OK;
+}
+
 int hann_pqivf_rows_decoded(void* hv, int64_t* out) {
     hann_pqivf* h = static_cast<hann_pqivf*>(hv);
     if (!h || !out) return HANN_E_INVALID;
@@ -1610,29 +1752,35 @@ int hann_pqivf_rows_decoded(void* hv, int64_t* out) {
     return HANN_OK;
 }
 
-int hann_pqivf_scan_options(void* hv, const int32_t* set6, int32_t* get6) {
+int hann_pqivf_scan_options(void* hv, const int32_t* set8, int32_t* get8) {
     hann_pqivf* h = static_cast<hann_pqivf*>(hv);
     if (!h) return HANN_E_INVALID;
     std::unique_lock<std::mutex> w(h->wmu);
     std::unique_lock<std::shared_mutex> g(h->mu);
     std::lock_guard<std::mutex> rl(h->run_mu);
-    if (set6) {
-        if (set6[1] < 1 || set6[2] < 1 || set6[3] < 2 || set6[4] < 1 || set6[5] < 1 || set6[5] > 2)
+    if (set8) {
+        const int32_t* set7 = set8;
+        if (set7[1] < 1 || set7[2] < 1 || set7[3] < 2 || set7[4] < 1 || set7[5] < 1 || set7[5] > 2 || set8[7] < 1)
             return h->fail(HANN_E_INVALID, "invalid list-scan options");
-        h->lms.enabled = set6[0] ? 1 : 0;
-        h->lms.min_queries = set6[1];
-        h->lms.first = set6[2];
-        h->lms.growth = set6[3];
-        h->lms.rows_max = set6[4];
-        h->lms.ctas_per_sm = set6[5];
+        h->lms.min_nprobe = set8[7];
+        h->lms.enabled = set7[0] ? 1 : 0;
+        h->lms.min_queries = set7[1];
+        h->lms.first = set7[2];
+        h->lms.growth = set7[3];
+        h->lms.rows_max = set7[4];
+        h->lms.ctas_per_sm = set7[5];
+        h->lms.seed = set7[6] ? 1 : 0;
     }
-    if (get6) {
-        get6[0] = h->lms.enabled;
-        get6[1] = h->lms.min_queries;
-        get6[2] = h->lms.first;
-        get6[3] = h->lms.growth;
-        get6[4] = h->lms.rows_max;
-        get6[5] = h->lms.ctas_per_sm;
+    if (get8) {
+        int32_t* get7 = get8;
+        get8[7] = h->lms.min_nprobe;
+        get7[0] = h->lms.enabled;
+        get7[1] = h->lms.min_queries;
+        get7[2] = h->lms.first;
+        get7[3] = h->lms.growth;
+        get7[4] = h->lms.rows_max;
+        get7[5] = h->lms.ctas_per_sm;
+        get7[6] = h->lms.seed;
     }
     return HANN_OK;
 }

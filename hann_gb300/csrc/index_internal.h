@@ -154,7 +154,8 @@ struct SearchScratch {
     DBuf<int32_t> qorder, order_scratch;  // L2-friendly query order for scan and rerank
     // list-major tensor-core scan (kernels_lms.cu)
     DBuf<uint16_t> q16;
-    DBuf<float> le2, lasl, lthr, lcand_s, lpair_base;
+    DBuf<float> le2, lasl, lthr, lcand_s, lpair_base, leps;
+    DBuf<int32_t> lones, lzeros;  // per-query nprobe 1 and no fallback: the seeding table scan
     DBuf<int32_t> lcnt, lcand_id, llcount, lneed, ltodo, lredo, lbandk, lcounts, lcursor, ltotal, lpair_q,
         lpair_off, ln_items, litem_counter;
     DBuf<unsigned long long> lband, lstats;
@@ -171,10 +172,17 @@ struct LmsConfig {
     // against FP32 screening at the rerank depth), so a query's result would
     // depend on the size of the batch it runs in.
     int min_queries = 1;
-    int first = 1;         // probe ranks in the first chunk (written densely)
-    int growth = 8;        // each later chunk ends at growth x the previous end
-    int rows_max = 1024;   // rows of one list per work item
-    int ctas_per_sm = 2;
+    // 1: each query's first threshold comes from a table scan of its nearest
+    // list and every chunk appends below it; 0: the first chunk writes every
+    // score of its lists (densely, no threshold yet)
+    int seed = 0;
+    int first = 1;         // probe ranks in the first chunk
+    int growth = 32;       // each later chunk ends at growth x the previous end
+    int rows_max = 512;    // rows of one list per work item (the list-split threshold)
+    // Queries probing fewer lists take the table scan: below about this many
+    // probes per query the table scan is faster (the autotuner measures it).
+    int min_nprobe = 64;
+    int ctas_per_sm = 1;   // persistent blocks per SM (one fits: the codebooks sit in shared memory)
 };
 
 // Message of the calling thread's last failed call on any handle. Kept per

@@ -224,7 +224,8 @@ constexpr int LMS_MAX_CHUNKS = 8;  // probe-rank chunks of one search
 // One work item: rows [row_begin, row_begin + n_rows) of list `list` against
 // the n_pairs queries whose pairs start at pair_begin in the pair arrays.
 struct LmsItem {
-    int32_t list, pair_begin, n_pairs, row_begin, n_rows, pad0, pad1, pad2;
+    int32_t list, pair_begin, n_pairs, row_begin, n_rows, pad;
+    int64_t row0;  // global row of row_begin
 };
 
 // Probe-rank chunks: chunk c holds ranks [bound[c], bound[c + 1]), the last
@@ -270,16 +271,22 @@ bool lms_supported(int dim, int M, int pqK);
 int lms_smem_bytes();
 cudaError_t launch_lms_prep(const float* Q, int64_t nq, int dim, const int32_t* probe_ids, const float* probe_d,
                             const int32_t* nprobe, int np_max, const int32_t* fallback, const int32_t* list_len,
-                            int first_w, const LmsBound& bd, int mode, const int32_t* kq, int rfixed, int32_t* bandk,
-                            void* q16, float* e2, float* asl, int32_t* cnt, int32_t* lcount, float* thr, int32_t* need,
-                            cudaStream_t s);
-// Work queue of every chunk: counts [n * nlist], cursor [n * nlist],
+                            int first_w, int min_nprobe, const LmsBound& bd, int mode, const int32_t* kq, int rfixed,
+                            int32_t* bandk, float* eps, void* q16, float* e2, float* asl, int32_t* cnt,
+                            int32_t* lcount, float* thr, int32_t* need, cudaStream_t s);
+// First thresholds from a table scan of each query's nearest list (its R
+// best scores in cand_d [nq][R]).
+cudaError_t launch_lms_seed(int64_t nq, int R, const float* cand_d, const int32_t* bandk, const float* eps,
+                            const float* e2, const float* asl, float* thr, cudaStream_t s);
+// Work queue of every chunk (queries flagged in `skip` -- the prep's
+// table-scan flags -- take no part): counts [n * nlist], cursor [n * nlist],
 // totals [2] ([1]: set when a chunk's items overflow item_cap, which sends
 // every query to the table scan), items [n * item_cap], n_items [n], pair
 // arrays [nq * np_max].
 cudaError_t launch_lms_queue(const int32_t* probe_ids, const float* probe_d, const int32_t* nprobe, int64_t nq,
                              int np_max, const int32_t* fallback, const LmsChunks& ch, int nlist,
-                             const int32_t* list_len, int rows_max, int item_cap, int32_t* counts, int32_t* cursor,
+                             const int32_t* list_len, const int64_t* list_start, int rows_max, int item_cap,
+                             int32_t* counts, int32_t* cursor,
                              int32_t* totals, LmsItem* items, int32_t* n_items, int32_t* pair_q, float* pair_base,
                              int32_t* pair_off, cudaStream_t s);
 cudaError_t launch_lms_scan(const LmsParams& p, int grid, cudaStream_t s);

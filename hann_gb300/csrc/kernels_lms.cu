@@ -37,16 +37,29 @@
 // rerank rescores the band in the reference's FP32 order. Queries whose band
 // or buffers overflow go to the table scan (kernels_scan.cu) instead.
 //
-// Block layout (288 threads): warps 0-3 claim items, load the item's queries
-// (B) and decode the row tiles (A) into two shared-memory stages; warp 4
-// allocates tensor memory and issues the MMAs (two accumulator buffers of 64
-// columns, so the epilogue of one tile overlaps the next tile's MMA); warps
-// 5-8 drain the accumulators, one TMEM lane quarter each. Every mbarrier
-// wait is bounded: past the limit the kernel records an error, the roles
-// leave their loops, and the tensor memory is still released.
+// Block layout (320 threads, one block per SM): warp 9 claims items and
+// writes each item's metadata and column information into a ring of eight
+// slots and its queries (B) into one of two shared-memory buffers, so it runs
+// up to a few items ahead; warps 0-3 decode the row tiles (A) into three or
+// four shared-memory stages (as many as the FP16 codebooks leave room for)
+// from the codebooks held in shared memory, each thread one row, the next
+// tile's code words loaded while the current one decodes; warp 4 allocates
+// all 512 tensor-memory columns and issues the MMAs into eight accumulator
+// buffers of 64 columns, so the epilogue trails the MMAs by up to eight
+// tiles; warps 5-8 drain the accumulators, one TMEM lane quarter each.
+// Every mbarrier wait is bounded: past the limit the kernel records an
+// error, the roles leave their loops, and the tensor memory is still
+// released.
+//
+// Routing. The decode makes this scan pay off only where a list is shared
+// by many of the batch's queries, i.e. at large nprobe; queries probing
+// fewer lists than the index's min_nprobe take the table scan in the same
+// batch. The choice depends on the query alone, never on the batch, so a
+// query's exact-rerank result does not change with the batch it is in.
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -55,13 +68,14 @@
 namespace hann {
 namespace {
 
-constexpr int LMS_THREADS = 288;
+constexpr int LMS_THREADS = 320;
 constexpr int TM = 128;            // rows per tile (MMA M)
 constexpr int NQ = LMS_NQ;         // queries per item (largest MMA N)
-constexpr int A_STAGES = 2;
+constexpr int A_STAGES_MAX = 4;
 constexpr int A_STAGE_BYTES = 2 * TM * 128;  // two 64-element K blocks, 128-byte rows
 constexpr int B_BUF_BYTES = 2 * NQ * 128;
-constexpr int TMEM_COLS = 2 * NQ;  // two accumulator buffers
+constexpr int T_BUFS = 8;            // accumulator buffers in tensor memory
+constexpr int TMEM_COLS = T_BUFS * NQ;  // all 512 columns: one block per SM
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
 
 struct ColInfo {
@@ -71,8 +85,21 @@ struct ColInfo {
     int32_t off;   // first-chunk position of the list in the query's candidate buffer
 };
 
-constexpr int SMEM_BYTES = 1024 + A_STAGES * A_STAGE_BYTES + 2 * B_BUF_BYTES + 2 * NQ * (int)sizeof(ColInfo) +
-                           2 * (int)sizeof(LmsItem) + 256;
+// Fixed part of the shared memory (operand stages, column information,
+// metadata, barriers, the epilogue warps' scratch); the FP16 codebooks
+// follow it (at most 128 x 256 halves = 64 KiB), so one block runs per SM.
+constexpr int CB_SMEM_MAX = 128 * 256 * 2;
+__host__ __device__ constexpr int cb_smem_bytes(int dim, int pqK) { return (dim * pqK * 2 + 15) / 16 * 16; }
+constexpr int M_RING = 8;       // items whose metadata and columns are staged at once
+constexpr int BAR_BYTES = 384;  // the mbarriers, the TMEM address and the abort flag
+__host__ __device__ constexpr int smem_fixed(int stages) {
+    return 1024 + stages * A_STAGE_BYTES + 2 * B_BUF_BYTES + M_RING * NQ * (int)sizeof(ColInfo) +
+           M_RING * (int)sizeof(LmsItem) + BAR_BYTES + 4 * 128 * 4;
+}
+// A stages: four while they fit beside the codebooks in 227 KiB, else three.
+__host__ __device__ constexpr int a_stages(int dim, int pqK) {
+    return smem_fixed(4) + cb_smem_bytes(dim, pqK) <= 227 * 1024 ? 4 : 3;
+}
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -159,51 +186,164 @@ __device__ __forceinline__ uint32_t sw_off(int row, int e, int rows) {
     return (uint32_t)(kb * rows * 128 + row * 128 + ((((byte >> 4) ^ (row & 7)) << 4) | (byte & 15)));
 }
 
+// A row's code bytes as 32-bit words (code_stride is a multiple of 4): the
+// decoders load the next tile's words while they decode the current one.
+constexpr int CW_MAX = 8;  // words a row may carry for the fast decode (M <= 32)
+__device__ __forceinline__ void load_codes(const uint8_t* __restrict__ code, int nw, uint32_t (&cw)[CW_MAX]) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(code);
+#pragma unroll
+    for (int i = 0; i < CW_MAX; i++) cw[i] = i < nw ? __ldg(w + i) : 0u;
+}
+
 // Writes the FP16 residual of one row into its A-tile row: dsub elements per
-// subquantizer, looked up in the FP16 codebooks [M][pqK][dsub].
+// subquantizer, looked up in the FP16 codebooks [M][pqK][dsub] held in
+// shared memory. The fast forms (dsub 4 or 8, M <= 32) take the row's code
+// words from registers and issue every lookup of a group of eight before
+// its stores.
 template <int DSUB>
-__device__ __forceinline__ void decode_row(unsigned char* tile, int prow, const uint8_t* __restrict__ code, int M,
-                                           int dsub, int pqK, const __half* __restrict__ cb16) {
-    if constexpr (DSUB == 4) {
-        // 8-byte codeword pieces; four elements stay inside one 16-byte chunk
-        const uint2* cb = reinterpret_cast<const uint2*>(cb16);
-        for (int m = 0; m < M; m++) {
-            const uint2 v = __ldg(cb + (int64_t)m * pqK + code[m]);
-            *reinterpret_cast<uint2*>(tile + sw_off(prow, 4 * m, TM)) = v;
-        }
-    } else if constexpr (DSUB == 8) {
-        const uint4* cb = reinterpret_cast<const uint4*>(cb16);
-        for (int m = 0; m < M; m++) {
-            const uint4 v = __ldg(cb + (int64_t)m * pqK + code[m]);
-            *reinterpret_cast<uint4*>(tile + sw_off(prow, 8 * m, TM)) = v;
+__device__ __forceinline__ void decode_row(unsigned char* tile, int prow, const uint32_t (&cw)[CW_MAX],
+                                           const uint8_t* __restrict__ code, int M, int dsub, int pqK,
+                                           const __half* cbs) {
+    if constexpr (DSUB == 4 || DSUB == 8) {
+        using V = typename std::conditional<DSUB == 4, uint2, uint4>::type;
+        const V* cb = reinterpret_cast<const V*>(cbs);
+#pragma unroll
+        for (int g = 0; g < 4 * CW_MAX; g += 8) {
+            if (g < M) {
+                V v[8];
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    const uint32_t byte = (cw[g / 4 + e / 4] >> (8 * (e & 3))) & 0xffu;
+                    if (g + e < M) v[e] = cb[(g + e) * pqK + (int)byte];
+                }
+                if constexpr (DSUB == 4) {
+                    // two subquantizers per 16-byte store: a warp's 32 rows then
+                    // fill 32 distinct banks per wavefront (the swizzle spreads
+                    // rows r and r + 1 .. r + 7 over the eight chunk positions)
+#pragma unroll
+                    for (int e = 0; e < 8; e += 2) {
+                        if (g + e + 1 < M)
+                            *reinterpret_cast<uint4*>(tile + sw_off(prow, 4 * (g + e), TM)) =
+                                make_uint4(v[e].x, v[e].y, v[e + 1].x, v[e + 1].y);
+                        else if (g + e < M)
+                            *reinterpret_cast<uint2*>(tile + sw_off(prow, 4 * (g + e), TM)) = v[e];
+                    }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; e++)
+                        if (g + e < M) *reinterpret_cast<V*>(tile + sw_off(prow, DSUB * (g + e), TM)) = v[e];
+                }
+            }
         }
     } else {
         for (int m = 0; m < M; m++) {
-            const __half* w = cb16 + ((int64_t)m * pqK + code[m]) * dsub;
+            const __half* w = cbs + ((int64_t)m * pqK + code[m]) * dsub;
             for (int e = 0; e < dsub; e++)
                 *reinterpret_cast<__half*>(tile + sw_off(prow, m * dsub + e, TM)) = w[e];
         }
     }
 }
 
+// One accumulator row (this thread's list row against the item's columns)
+// to candidates. NP, the item's column count rounded up to 16, makes every
+// loop fully unrolled and branch-free, so the column information is read in
+// groups of eight loads in flight rather than one latency per column.
+//   dense (the first chunk): every score at the row's fixed position in its
+//     query's buffer, no atomics;
+//   otherwise: a pass mask of the scores at or below each query's threshold;
+//     when a lane of the warp passes anything, one ballot per column into the
+//     warp's scratch (wbal[0..64)), every column's slots reserved at once
+//     (lane l for columns l and l + 32, both atomics in flight; wbal[64..128)
+//     receives the first slots), then the passing rows written.
+template <int NP>
+__device__ __forceinline__ void epi_tile(const LmsParams& p, const ColInfo* ci, float (&acc)[NQ], int n_pairs,
+                                         bool valid, int64_t grow, float term, int row_pos, uint32_t* wbal) {
+    const int lane = threadIdx.x & 31;
+    if (p.dense) {
+#pragma unroll
+        for (int g = 0; g < NP; g += 8) {
+            ColInfo c[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) c[u] = ci[g + u];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int pos = c[u].off + row_pos;
+                if (valid && g + u < n_pairs && pos < p.cap) {
+                    const int64_t o = (int64_t)c[u].q * p.cap + pos;
+                    p.cand_id[o] = (int32_t)grow;
+                    p.cand_s[o] = __fmaf_rn(-2.0f, acc[g + u], c[u].base + term);
+                }
+            }
+        }
+        return;
+    }
+    uint64_t mask = 0;
+#pragma unroll
+    for (int g = 0; g < NP; g += 8) {
+        ColInfo c[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) c[u] = ci[g + u];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const float sv = __fmaf_rn(-2.0f, acc[g + u], c[u].base + term);
+            acc[g + u] = sv;
+            const bool pass = valid && g + u < n_pairs && sv <= c[u].tau;
+            mask |= (uint64_t)(pass ? 1u : 0u) << (g + u);
+        }
+    }
+    if (!__any_sync(0xffffffffu, mask != 0ull)) return;
+    int32_t* wbase = reinterpret_cast<int32_t*>(wbal + 64);
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+        const unsigned bal = __ballot_sync(0xffffffffu, ((mask >> j) & 1ull) != 0ull);
+        if (lane == 0) wbal[j] = bal;
+    }
+    __syncwarp();
+    const uint32_t b0 = lane < n_pairs ? wbal[lane] : 0u;
+    const uint32_t b1 = lane + 32 < n_pairs ? wbal[lane + 32] : 0u;
+    int r0 = 0, r1 = 0;
+    if (b0) r0 = atomicAdd(p.cnt + ci[lane].q, __popc(b0));
+    if (b1) r1 = atomicAdd(p.cnt + ci[lane + 32].q, __popc(b1));
+    if (lane < n_pairs) wbase[lane] = r0;
+    if (lane + 32 < n_pairs) wbase[lane + 32] = r1;
+    __syncwarp();
+    const unsigned ltm = (1u << lane) - 1u;
+#pragma unroll
+    for (int j = 0; j < NP; j++) {
+        if ((mask >> j) & 1ull) {
+            const int pos = wbase[j] + __popc(wbal[j] & ltm);
+            if (pos < p.cap) {
+                const int64_t o = (int64_t)ci[j].q * p.cap + pos;
+                p.cand_id[o] = (int32_t)grow;
+                p.cand_s[o] = acc[j];
+            }
+        }
+    }
+    __syncwarp();
+}
+
 template <int DSUB>
-__global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
+__global__ void __launch_bounds__(LMS_THREADS, 1) lms_scan_kernel(LmsParams p) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int A_STAGES = a_stages(p.dim, p.pqK);
     unsigned char* sA = base;
     unsigned char* sB = sA + A_STAGES * A_STAGE_BYTES;
-    ColInfo* cols = reinterpret_cast<ColInfo*>(sB + 2 * B_BUF_BYTES);   // [2][NQ]
-    LmsItem* meta = reinterpret_cast<LmsItem*>(cols + 2 * NQ);          // [2]
-    uint64_t* bars = reinterpret_cast<uint64_t*>(meta + 2);
-    uint64_t* a_full = bars;       // [A_STAGES]
-    uint64_t* a_empty = bars + 2;  // [A_STAGES]
-    uint64_t* b_full = bars + 4;   // [2]
-    uint64_t* b_empty = bars + 6;  // [2]
-    uint64_t* t_full = bars + 8;   // [2]
-    uint64_t* t_empty = bars + 10; // [2]
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 12);
-    int* s_item = reinterpret_cast<int*>(bars + 13);  // [0..1] claimed items, [2..3] stage-wait results
-    volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 15);
+    ColInfo* cols = reinterpret_cast<ColInfo*>(sB + 2 * B_BUF_BYTES);  // [M_RING][NQ]
+    LmsItem* meta = reinterpret_cast<LmsItem*>(cols + M_RING * NQ);    // [M_RING]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(meta + M_RING);
+    uint64_t* a_full = bars;                    // [A_STAGES_MAX] tile decoded
+    uint64_t* a_empty = a_full + A_STAGES_MAX;  // [A_STAGES_MAX] tile consumed by the MMAs
+    uint64_t* m_full = a_empty + A_STAGES_MAX;  // [M_RING] item metadata and columns staged
+    uint64_t* m_empty = m_full + M_RING;        // [M_RING] ... read by every role
+    uint64_t* b_full = m_empty + M_RING;        // [2] item queries staged
+    uint64_t* b_empty = b_full + 2;             // [2] ... consumed by the MMAs
+    uint64_t* t_full = b_empty + 2;             // [T_BUFS] accumulator ready
+    uint64_t* t_empty = t_full + T_BUFS;        // [T_BUFS] accumulator drained
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(t_empty + T_BUFS);
+    volatile int* s_abort = reinterpret_cast<volatile int*>(t_empty + T_BUFS) + 2;
+    uint32_t* escr = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(bars) + BAR_BYTES);  // [4][128]
+    __half* cbs = reinterpret_cast<__half*>(escr + 4 * 128);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Every operand byte starts at zero: the K padding past the dimension and
@@ -211,14 +351,25 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
     // values, which the epilogue then ignores.
     for (int i = threadIdx.x; i < (A_STAGES * A_STAGE_BYTES + 2 * B_BUF_BYTES) / 16; i += LMS_THREADS)
         reinterpret_cast<uint4*>(sA)[i] = make_uint4(0, 0, 0, 0);
+    {
+        const int ncb = p.M * p.pqK * p.dsub;
+        const unsigned short* src = static_cast<const unsigned short*>(p.cb16);
+        for (int i = threadIdx.x; i < ncb; i += LMS_THREADS) reinterpret_cast<unsigned short*>(cbs)[i] = src[i];
+    }
     if (threadIdx.x == 0) {
-        for (int s = 0; s < A_STAGES; s++) {
-            mbar_init(&a_full[s], 4);
-            mbar_init(&a_empty[s], 1);
+        for (int s = 0; s < A_STAGES_MAX; s++) {
+            mbar_init(&a_full[s], 4);   // the four decoder warps
+            mbar_init(&a_empty[s], 1);  // the MMA commit
+        }
+        for (int m = 0; m < M_RING; m++) {
+            mbar_init(&m_full[m], 1);   // the loader warp
+            mbar_init(&m_empty[m], 9);  // four decoder warps, the MMA thread, four epilogue warps
         }
         for (int b = 0; b < 2; b++) {
-            mbar_init(&b_full[b], 4);
-            mbar_init(&b_empty[b], 5);  // the MMA commit + the four epilogue warps
+            mbar_init(&b_full[b], 1);   // the loader warp
+            mbar_init(&b_empty[b], 1);  // the MMA commit
+        }
+        for (int b = 0; b < T_BUFS; b++) {
             mbar_init(&t_full[b], 1);
             mbar_init(&t_empty[b], 4);
         }
@@ -239,85 +390,66 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
     const int ksteps = (p.dim + 15) >> 4;
 
     if (warp < 4) {
-        // ---------------- producers: claim items, load queries, decode tiles.
-        // Thread 0 of the four warps makes every decision that can end the
-        // loop (which item, whether a wait ran out) and publishes it before a
-        // named barrier of the 128 threads, so all of them take the same
-        // path and meet at every barrier.
+        // ---------------- decoders: the item's row tiles into the A stages,
+        // one row per thread, the next tile's code words loaded ahead
         const int pt = threadIdx.x;  // 0..127: the tile row this thread decodes
-        const int n_items = min(*p.n_items, p.item_cap);
+        const int nw = p.code_stride >> 2;
+        const bool fast = (DSUB == 4 || DSUB == 8) && nw <= CW_MAX;
         int item_seq = 0, tile_seq = 0;
+        uint32_t cw[CW_MAX], cn[CW_MAX];
+#pragma unroll
+        for (int i = 0; i < CW_MAX; i++) cw[i] = cn[i] = 0u;
+        bool pre = false;  // cw already holds this item's first code words
         while (true) {
-            const int b = item_seq & 1;
-            if (pt == 0) {
-                int idx = atomicAdd(p.item_counter, 1);
-                bool ok = *s_abort == 0;
-                if (ok && item_seq >= 2) ok = mbar_wait(&b_empty[b], ((item_seq >> 1) - 1) & 1, p.err, s_abort);
-                s_item[item_seq & 1] = ok ? idx : -1;
-            }
-            asm volatile("bar.sync 1, 128;" ::: "memory");
-            const int idx = s_item[item_seq & 1];
-            if (idx < 0) break;  // a wait ran out
-            const bool last = idx >= n_items;
-            LmsItem it;
-            if (!last) it = p.items[idx];
-            if (pt == 0) {
-                if (last) meta[b].n_rows = -1;
-                else meta[b] = it;
-            }
-            if (!last) {
-                ColInfo* ci = cols + b * NQ;
-                if (pt < it.n_pairs) {
-                    const int64_t pr = (int64_t)it.pair_begin + pt;
-                    const int32_t q = p.pair_q[pr];
-                    ColInfo c;
-                    c.q = q;
-                    c.base = p.pair_base[pr];
-                    c.tau = p.dense ? __int_as_float(0x7f800000) : p.thr[q];
-                    c.off = p.dense ? p.pair_off[pr] : 0;
-                    ci[pt] = c;
-                }
-                // the item's queries into B: row j = query j, 16 chunks of 16 bytes
-                const int npad = (it.n_pairs + 15) & ~15;
-                unsigned char* bt = sB + b * B_BUF_BYTES;
-                for (int e = pt; e < npad * 16; e += 128) {
-                    const int j = e >> 4, c = e & 15;
-                    uint4 v = make_uint4(0, 0, 0, 0);
-                    if (j < it.n_pairs) {
-                        const int32_t q = p.pair_q[(int64_t)it.pair_begin + j];
-                        v = __ldg(reinterpret_cast<const uint4*>(static_cast<const __half*>(p.q16) + (int64_t)q * 128) +
-                                  c);
-                    }
-                    const int kb = c >> 3, cc = c & 7;
-                    *reinterpret_cast<uint4*>(bt + kb * NQ * 128 + j * 128 + ((cc ^ (j & 7)) << 4)) = v;
-                }
-            }
-            fence_async_smem();
+            const int m = item_seq % M_RING;
+            if (!__all_sync(0xffffffffu, mbar_wait(&m_full[m], (item_seq / M_RING) & 1, p.err, s_abort))) break;
+            const LmsItem it = meta[m];
             __syncwarp();
-            if (lane == 0) mbar_arrive(&b_full[b]);
-            if (last) break;
+            if (lane == 0) mbar_arrive(&m_empty[m]);  // the item lives in registers from here
+            if (it.n_rows < 0) break;
             const int ntiles = (it.n_rows + TM - 1) / TM;
-            const int64_t row0 = p.list_start[it.list] + it.row_begin;
+            const uint8_t* rows = p.codes + it.row0 * p.code_stride;
+            if (fast && !pre && pt < it.n_rows) load_codes(rows + (int64_t)pt * p.code_stride, nw, cw);
+            pre = false;
             bool ok = true;
             for (int t = 0; t < ntiles; t++, tile_seq++) {
                 const int s = tile_seq % A_STAGES;
-                if (tile_seq >= A_STAGES) {
-                    if (pt == 0)
-                        s_item[2 + (tile_seq & 1)] =
-                            mbar_wait(&a_empty[s], ((tile_seq / A_STAGES) - 1) & 1, p.err, s_abort) ? 1 : 0;
-                    asm volatile("bar.sync 1, 128;" ::: "memory");
-                    if (s_item[2 + (tile_seq & 1)] == 0) {
-                        ok = false;
-                        break;
-                    }
+                if (tile_seq >= A_STAGES &&
+                    !__all_sync(0xffffffffu, mbar_wait(&a_empty[s], ((tile_seq / A_STAGES) - 1) & 1, p.err, s_abort))) {
+                    ok = false;
+                    break;
                 }
                 const int lr = t * TM + pt;
+                const int ln = lr + TM;
+                if (fast) {
+                    if (t + 1 < ntiles) {
+                        if (ln < it.n_rows) load_codes(rows + (int64_t)ln * p.code_stride, nw, cn);
+                    } else {
+                        // last tile: the next item's first rows, when the
+                        // loader has staged its metadata already
+                        const int mn = (item_seq + 1) % M_RING;
+                        uint32_t rdy = lane == 0 ? (mbar_try(&m_full[mn], ((item_seq + 1) / M_RING) & 1) ? 1u : 0u) : 0u;
+                        rdy = __shfl_sync(0xffffffffu, rdy, 0);
+                        if (rdy) {
+                            const LmsItem nx = meta[mn];
+                            if (nx.n_rows > 0) {
+                                if (pt < nx.n_rows)
+                                    load_codes(p.codes + (nx.row0 + pt) * p.code_stride, nw, cn);
+                                pre = true;
+                            }
+                        }
+                    }
+                }
                 if (lr < it.n_rows)
-                    decode_row<DSUB>(sA + s * A_STAGE_BYTES, pt, p.codes + (row0 + lr) * p.code_stride, p.M, p.dsub,
-                                     p.pqK, static_cast<const __half*>(p.cb16));
+                    decode_row<DSUB>(sA + s * A_STAGE_BYTES, pt, cw, rows + (int64_t)lr * p.code_stride, p.M, p.dsub,
+                                     p.pqK, cbs);
                 fence_async_smem();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&a_full[s]);
+                if (fast) {
+#pragma unroll
+                    for (int i = 0; i < CW_MAX; i++) cw[i] = cn[i];
+                }
             }
             if (!ok) break;
             if (p.stats && pt == 0) {
@@ -326,27 +458,105 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
             }
             item_seq++;
         }
+    } else if (warp == 9) {
+        // ---------------- loader: claims items and stages their metadata and
+        // column information (a ring of M_RING items, so the decoders run
+        // ahead of the epilogue) and their queries (B, two buffers). An item
+        // is claimed and its pair data loaded before any wait, and the
+        // queries move with cp.async, all in flight at once.
+        const int n_items = min(*p.n_items, p.item_cap);
+        int item_seq = 0;
+        while (true) {
+            const int m = item_seq % M_RING, b = item_seq & 1;
+            int idx = 0;
+            if (lane == 0) idx = atomicAdd(p.item_counter, 1);
+            idx = __shfl_sync(0xffffffffu, idx, 0);
+            const bool last = idx >= n_items;
+            LmsItem it;
+            it.n_pairs = 0;
+            ColInfo ca{0, 0.0f, 0.0f, 0}, cb{0, 0.0f, 0.0f, 0};
+            if (!last) {
+                it = p.items[idx];
+                if (lane < it.n_pairs) {
+                    const int64_t pr = (int64_t)it.pair_begin + lane;
+                    ca.q = p.pair_q[pr];
+                    ca.base = p.pair_base[pr];
+                    ca.off = p.dense ? p.pair_off[pr] : 0;
+                }
+                if (lane + 32 < it.n_pairs) {
+                    const int64_t pr = (int64_t)it.pair_begin + lane + 32;
+                    cb.q = p.pair_q[pr];
+                    cb.base = p.pair_base[pr];
+                    cb.off = p.dense ? p.pair_off[pr] : 0;
+                }
+                ca.tau = p.dense || lane >= it.n_pairs ? __int_as_float(0x7f800000) : p.thr[ca.q];
+                cb.tau = p.dense || lane + 32 >= it.n_pairs ? __int_as_float(0x7f800000) : p.thr[cb.q];
+            }
+            if (item_seq >= M_RING &&
+                !__all_sync(0xffffffffu, mbar_wait(&m_empty[m], ((item_seq / M_RING) - 1) & 1, p.err, s_abort)))
+                break;
+            if (lane == 0) {
+                if (last) meta[m].n_rows = -1;
+                else meta[m] = it;
+            }
+            if (!last) {
+                ColInfo* ci = cols + m * NQ;
+                if (lane < it.n_pairs) ci[lane] = ca;
+                if (lane + 32 < it.n_pairs) ci[lane + 32] = cb;
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&m_full[m]);
+            if (last) break;
+            if (item_seq >= 2 &&
+                !__all_sync(0xffffffffu, mbar_wait(&b_empty[b], ((item_seq >> 1) - 1) & 1, p.err, s_abort)))
+                break;
+            // the item's queries into B: row j = query j, 16 chunks of 16
+            // bytes; rows past n_pairs keep earlier (finite) contents
+            const int npad = (it.n_pairs + 15) & ~15;
+            const uint32_t bt = su32(sB + b * B_BUF_BYTES);
+            const __half* q16 = static_cast<const __half*>(p.q16);
+            for (int i = 0; i < npad / 2; i++) {
+                const int e = i * 32 + lane, j = e >> 4, c = e & 15;
+                const int32_t va = __shfl_sync(0xffffffffu, ca.q, j & 31);
+                const int32_t vb = __shfl_sync(0xffffffffu, cb.q, j & 31);
+                if (j < it.n_pairs) {
+                    const int32_t q = j < 32 ? va : vb;
+                    const uint32_t dst = bt + (uint32_t)((c >> 3) * NQ * 128 + j * 128 + (((c & 7) ^ (j & 7)) << 4));
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst),
+                                 "l"(q16 + (int64_t)q * 128 + c * 8)
+                                 : "memory");
+                }
+            }
+            asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&b_full[b]);
+            item_seq++;
+        }
     } else if (warp == 4) {
         // ---------------- MMA issue (one thread)
         if (lane == 0) {
             int item_seq = 0, tile_seq = 0;
             while (true) {
-                const int b = item_seq & 1;
-                if (!mbar_wait(&b_full[b], (item_seq >> 1) & 1, p.err, s_abort)) break;
-                const LmsItem it = meta[b];
+                const int m = item_seq % M_RING, b = item_seq & 1;
+                if (!mbar_wait(&m_full[m], (item_seq / M_RING) & 1, p.err, s_abort)) break;
+                const LmsItem it = meta[m];
+                mbar_arrive(&m_empty[m]);
                 if (it.n_rows < 0) break;
+                if (!mbar_wait(&b_full[b], (item_seq >> 1) & 1, p.err, s_abort)) break;
                 const int npad = (it.n_pairs + 15) & ~15;
                 const uint32_t idesc = idesc_f16(npad);
                 const int ntiles = (it.n_rows + TM - 1) / TM;
                 const uint32_t b_base = su32(sB + b * B_BUF_BYTES);
                 bool ok = true;
                 for (int t = 0; t < ntiles; t++, tile_seq++) {
-                    const int s = tile_seq % A_STAGES, tb = tile_seq & 1;
+                    const int s = tile_seq % A_STAGES, tb = tile_seq % T_BUFS;
                     if (!mbar_wait(&a_full[s], (tile_seq / A_STAGES) & 1, p.err, s_abort)) {
                         ok = false;
                         break;
                     }
-                    if (tile_seq >= 2 && !mbar_wait(&t_empty[tb], ((tile_seq >> 1) - 1) & 1, p.err, s_abort)) {
+                    if (tile_seq >= T_BUFS &&
+                        !mbar_wait(&t_empty[tb], ((tile_seq / T_BUFS) - 1) & 1, p.err, s_abort)) {
                         ok = false;
                         break;
                     }
@@ -373,20 +583,25 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
         // ---------------- epilogue: one TMEM lane quarter per warp
         const int quarter = warp & 3;
         const int prow = quarter * 32 + lane;
-        const unsigned ltm = (1u << lane) - 1u;
         int item_seq = 0, tile_seq = 0;
         while (true) {
-            const int b = item_seq & 1;
-            if (!__all_sync(0xffffffffu, mbar_wait(&b_full[b], (item_seq >> 1) & 1, p.err, s_abort))) break;
-            const LmsItem it = meta[b];
+            const int m = item_seq % M_RING;
+            if (!__all_sync(0xffffffffu, mbar_wait(&m_full[m], (item_seq / M_RING) & 1, p.err, s_abort))) break;
+            const LmsItem it = meta[m];
             if (it.n_rows < 0) break;
-            const ColInfo* ci = cols + b * NQ;
+            const ColInfo* ci = cols + m * NQ;
             const int ntiles = (it.n_rows + TM - 1) / TM;
-            const int64_t row0 = p.list_start[it.list] + it.row_begin;
+            const int64_t row0 = it.row0;
             bool ok = true;
             for (int t = 0; t < ntiles; t++, tile_seq++) {
-                const int tb = tile_seq & 1;
-                if (!__all_sync(0xffffffffu, mbar_wait(&t_full[tb], (tile_seq >> 1) & 1, p.err, s_abort))) {
+                const int tb = tile_seq % T_BUFS;
+                // the row's term is loaded before the wait, so its latency
+                // overlaps the MMA
+                const int lr = t * TM + prow;
+                const bool valid = lr < it.n_rows;
+                const int64_t grow = row0 + lr;
+                const float term = valid ? __ldg(p.term + grow) : __int_as_float(0x7f800000);
+                if (!__all_sync(0xffffffffu, mbar_wait(&t_full[tb], (tile_seq / T_BUFS) & 1, p.err, s_abort))) {
                     ok = false;
                     break;
                 }
@@ -398,66 +613,15 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&t_empty[tb]);
-                const int lr = t * TM + prow;
-                const bool valid = lr < it.n_rows;
-                const int64_t grow = row0 + lr;
-                const float term = valid ? __ldg(p.term + grow) : __int_as_float(0x7f800000);
-                if (p.dense) {
-                    // every score at the row's fixed position in the query's buffer
-#pragma unroll
-                    for (int j = 0; j < NQ; j++) {
-                        if (j < it.n_pairs && valid) {
-                            const ColInfo c = ci[j];
-                            const int pos = c.off + it.row_begin + lr;
-                            if (pos < p.cap) {
-                                const int64_t o = (int64_t)c.q * p.cap + pos;
-                                p.cand_id[o] = (int32_t)grow;
-                                p.cand_s[o] = __fmaf_rn(-2.0f, acc[j], c.base + term);
-                            }
-                        }
-                    }
-                } else {
-                    // pass masks first: most tiles of later chunks pass nothing
-                    uint32_t m0 = 0, m1 = 0;
-#pragma unroll
-                    for (int j = 0; j < NQ; j++) {
-                        if (j < it.n_pairs) {
-                            const ColInfo c = ci[j];
-                            const float s = __fmaf_rn(-2.0f, acc[j], c.base + term);
-                            acc[j] = s;
-                            if (valid && s <= c.tau) {
-                                if (j < 32) m0 |= 1u << j;
-                                else m1 |= 1u << (j - 32);
-                            }
-                        }
-                    }
-                    if (__any_sync(0xffffffffu, (m0 | m1) != 0u)) {
-#pragma unroll
-                        for (int j = 0; j < NQ; j++) {
-                            if (j < it.n_pairs) {
-                                const bool pass = ((j < 32 ? m0 >> j : m1 >> (j - 32)) & 1u) != 0u;
-                                const unsigned bal = __ballot_sync(0xffffffffu, pass);
-                                if (bal) {
-                                    const int32_t q = ci[j].q;
-                                    int pos0 = 0;
-                                    if (lane == __ffs(bal) - 1) pos0 = atomicAdd(p.cnt + q, __popc(bal));
-                                    pos0 = __shfl_sync(0xffffffffu, pos0, __ffs(bal) - 1);
-                                    if (pass) {
-                                        const int pos = pos0 + __popc(bal & ltm);
-                                        if (pos < p.cap) {
-                                            const int64_t o = (int64_t)q * p.cap + pos;
-                                            p.cand_id[o] = (int32_t)grow;
-                                            p.cand_s[o] = acc[j];
-                                        }
-                                    }
-                                }
-                            }
-                        }
-                    }
-                }
+                const int np16 = (it.n_pairs + 15) >> 4;
+                uint32_t* wbal = escr + (warp - 5) * 128;
+                if (np16 <= 1) epi_tile<16>(p, ci, acc, it.n_pairs, valid, grow, term, it.row_begin + lr, wbal);
+                else if (np16 == 2) epi_tile<32>(p, ci, acc, it.n_pairs, valid, grow, term, it.row_begin + lr, wbal);
+                else if (np16 == 3) epi_tile<48>(p, ci, acc, it.n_pairs, valid, grow, term, it.row_begin + lr, wbal);
+                else epi_tile<64>(p, ci, acc, it.n_pairs, valid, grow, term, it.row_begin + lr, wbal);
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(&b_empty[b]);
+            if (lane == 0) mbar_arrive(&m_empty[m]);
             if (!ok) break;
             item_seq++;
         }
@@ -479,8 +643,9 @@ __global__ void __launch_bounds__(LMS_THREADS, 2) lms_scan_kernel(LmsParams p) {
 __global__ void lms_prep_kernel(const float* __restrict__ Q, int64_t nq, int dim, const int32_t* __restrict__ probe_ids,
                                 const float* __restrict__ probe_d, const int32_t* __restrict__ nprobe, int np_max,
                                 const int32_t* __restrict__ fallback, const int32_t* __restrict__ list_len, int first_w,
-                                LmsBound bd, int mode, const int32_t* __restrict__ kq, int rfixed,
-                                int32_t* __restrict__ bandk, __half* __restrict__ q16, float* __restrict__ e2,
+                                int min_nprobe, LmsBound bd, int mode, const int32_t* __restrict__ kq, int rfixed,
+                                int32_t* __restrict__ bandk, float* __restrict__ eps_out, __half* __restrict__ q16,
+                                float* __restrict__ e2,
                                 float* __restrict__ asl, int32_t* __restrict__ cnt, int32_t* __restrict__ lcount,
                                 float* __restrict__ thr, int32_t* __restrict__ need) {
     const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -515,6 +680,7 @@ __global__ void lms_prep_kernel(const float* __restrict__ Q, int64_t nq, int dim
         const float eps = 2.0f * (qn * bd.rd + qd * bd.rmax + qd * bd.rd) +
                           2.0f * (float)bd.kpad * u22 * (qn + qd) * (bd.rmax + bd.rd);
         const float bmax = np > 0 ? probe_d[q * np_max + np - 1] : 0.0f;
+        eps_out[q] = eps;
         if (mode == 0) {
             e2[q] = 2.0f * eps;
             asl[q] = bmax + bd.tmax + 2.0f * qn * bd.rmax;
@@ -525,7 +691,9 @@ __global__ void lms_prep_kernel(const float* __restrict__ Q, int64_t nq, int dim
         }
         // a component FP16 cannot hold (or a non-finite one) sends the query
         // to the table scan, as does the brute-force fallback
-        const bool fb = fallback[q] != 0 || !(amax <= 6.0e4f) || !(s < 3.0e38f);
+        // so does a query probing fewer lists than min_nprobe (the table scan
+        // is faster there; the choice depends on the query alone)
+        const bool fb = fallback[q] != 0 || !(amax <= 6.0e4f) || !(s < 3.0e38f) || np < min_nprobe;
         need[q] = fb ? 1 : 0;
         lcount[q] = 0;
         thr[q] = __int_as_float(0x7f800000);
@@ -594,7 +762,8 @@ __global__ void lms_scan_counts_kernel(int32_t* __restrict__ v, int n, int32_t* 
 // region by an atomic counter. cursor receives a copy of the offsets (the
 // scatter's fill pointers).
 __global__ void lms_items_kernel(const int32_t* __restrict__ offsets, const int32_t* __restrict__ total, int nch,
-                                 int nlist, const int32_t* __restrict__ list_len, int rows_max, int item_cap,
+                                 int nlist, const int32_t* __restrict__ list_len,
+                                 const int64_t* __restrict__ list_start, int rows_max, int item_cap,
                                  LmsItem* __restrict__ items, int32_t* __restrict__ n_items,
                                  int32_t* __restrict__ cursor, int32_t* __restrict__ overflow) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -620,7 +789,8 @@ __global__ void lms_items_kernel(const int32_t* __restrict__ offsets, const int3
             it.n_pairs = min(NQ, n - a * NQ);
             it.row_begin = r * rows_max;
             it.n_rows = min(rows_max, len - r * rows_max);
-            it.pad0 = it.pad1 = it.pad2 = 0;
+            it.pad = 0;
+            it.row0 = list_start[l] + (int64_t)it.row_begin;
             out[a * gr + r] = it;
         }
 }
@@ -720,7 +890,44 @@ __global__ void lms_finish_kernel(int64_t nq, int mode, int R, int lcap, const i
 
 }  // namespace
 
-int lms_smem_bytes() { return SMEM_BYTES; }
+// The first threshold of every query from the table scan of its nearest list
+// (cand_d [nq][R]: the best scores, +inf past the count; their largest is at
+// or above the R-th best of that list). Every row the final band can hold
+// has a screened score at or below
+//   the band's k-th best + e2 + slack <= (that largest + eps) + e2 + slack,
+// eps covering the FP16 screen against the table's FP32 scores, so the
+// threshold below drops none of them. Queries whose nearest list holds fewer
+// rows than their band start at +inf.
+__global__ void lms_seed_kernel(int64_t nq, int R, const float* __restrict__ cand_d, const int32_t* __restrict__ bandk,
+                                const float* __restrict__ eps, const float* __restrict__ e2,
+                                const float* __restrict__ asl, float* __restrict__ thr) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    int cnt = 0;
+    float mx = -__int_as_float(0x7f800000);
+    for (int i = 0; i < R; i++) {
+        const float d = cand_d[q * R + i];
+        if (d < __int_as_float(0x7f800000)) {
+            cnt++;
+            mx = fmaxf(mx, d);
+        }
+    }
+    float t = __int_as_float(0x7f800000);
+    if (cnt >= bandk[q] && cnt > 0) {
+        const float a = fabsf(mx) + asl[q];
+        t = mx + eps[q] + e2[q] + 2e-5f * a + 1e-6f * fabsf(mx);
+    }
+    thr[q] = t;
+}
+
+cudaError_t launch_lms_seed(int64_t nq, int R, const float* cand_d, const int32_t* bandk, const float* eps,
+                            const float* e2, const float* asl, float* thr, cudaStream_t s) {
+    if (nq <= 0) return cudaSuccess;
+    lms_seed_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(nq, R, cand_d, bandk, eps, e2, asl, thr);
+    return cudaGetLastError();
+}
+
+int lms_smem_bytes() { return smem_fixed(3) + CB_SMEM_MAX; }
 
 bool lms_supported(int dim, int M, int pqK) {
     return dim > 0 && dim <= 128 && M > 0 && dim % M == 0 && pqK >= 1 && pqK <= 256;
@@ -728,12 +935,13 @@ bool lms_supported(int dim, int M, int pqK) {
 
 cudaError_t launch_lms_prep(const float* Q, int64_t nq, int dim, const int32_t* probe_ids, const float* probe_d,
                             const int32_t* nprobe, int np_max, const int32_t* fallback, const int32_t* list_len,
-                            int first_w, const LmsBound& bd, int mode, const int32_t* kq, int rfixed, int32_t* bandk,
-                            void* q16, float* e2, float* asl, int32_t* cnt, int32_t* lcount, float* thr, int32_t* need,
-                            cudaStream_t s) {
+                            int first_w, int min_nprobe, const LmsBound& bd, int mode, const int32_t* kq, int rfixed,
+                            int32_t* bandk, float* eps, void* q16, float* e2, float* asl, int32_t* cnt,
+                            int32_t* lcount, float* thr, int32_t* need, cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
     lms_prep_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(Q, nq, dim, probe_ids, probe_d, nprobe, np_max, fallback,
-                                                              list_len, first_w, bd, mode, kq, rfixed, bandk,
+                                                              list_len, first_w, min_nprobe, bd, mode, kq, rfixed, bandk,
+                                                              eps,
                                                               static_cast<__half*>(q16), e2, asl, cnt, lcount, thr,
                                                               need);
     return cudaGetLastError();
@@ -741,7 +949,8 @@ cudaError_t launch_lms_prep(const float* Q, int64_t nq, int dim, const int32_t* 
 
 cudaError_t launch_lms_queue(const int32_t* probe_ids, const float* probe_d, const int32_t* nprobe, int64_t nq,
                              int np_max, const int32_t* fallback, const LmsChunks& ch, int nlist,
-                             const int32_t* list_len, int rows_max, int item_cap, int32_t* counts, int32_t* cursor,
+                             const int32_t* list_len, const int64_t* list_start, int rows_max, int item_cap,
+                             int32_t* counts, int32_t* cursor,
                              int32_t* totals, LmsItem* items, int32_t* n_items, int32_t* pair_q, float* pair_base,
                              int32_t* pair_off, cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
@@ -754,8 +963,9 @@ cudaError_t launch_lms_queue(const int32_t* probe_ids, const float* probe_d, con
     lms_count_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, s>>>(probe_ids, nprobe, nq, np_max, fallback, ch, nlist,
                                                                  counts);
     lms_scan_counts_kernel<<<1, 1024, 0, s>>>(counts, (int)ncl, totals);
-    lms_items_kernel<<<(unsigned)ceil_div(ncl, 256), 256, 0, s>>>(counts, totals, ch.n, nlist, list_len, rows_max,
-                                                                  item_cap, items, n_items, cursor, totals + 1);
+    lms_items_kernel<<<(unsigned)ceil_div(ncl, 256), 256, 0, s>>>(counts, totals, ch.n, nlist, list_len, list_start,
+                                                                  rows_max, item_cap, items, n_items, cursor,
+                                                                  totals + 1);
     lms_scatter_kernel<<<(unsigned)ceil_div(np, 256), 256, 0, s>>>(probe_ids, probe_d, nprobe, nq, np_max, fallback,
                                                                    ch, nlist, list_len, cursor, pair_q, pair_base,
                                                                    pair_off);
@@ -769,13 +979,15 @@ cudaError_t launch_lms_scan(const LmsParams& p, int grid, cudaStream_t s) {
     case 8: fn = (const void*)lms_scan_kernel<8>; break;
     default: fn = (const void*)lms_scan_kernel<0>; break;
     }
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    const int smem = smem_fixed(a_stages(p.dim, p.pqK)) + cb_smem_bytes(p.dim, p.pqK);
+    if (cb_smem_bytes(p.dim, p.pqK) > CB_SMEM_MAX) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(p.item_counter, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return e;
     LmsParams pp = p;
     void* args[] = {(void*)&pp};
-    e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(LMS_THREADS), args, SMEM_BYTES, s);
+    e = cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(LMS_THREADS), args, smem, s);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }

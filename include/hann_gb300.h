@@ -140,6 +140,22 @@ int hann_pqivf_search_batch_device(hann_pqivf* h, const float* d_queries, int64_
                                    int32_t mode, int64_t* d_ids, double* d_distances, int32_t* d_n_out,
                                    void* stream);
 
+/* Autotuner of the list scan (no reference counterpart: the reference scans
+ * each query's candidates one by one, pqivf/index.go:905-936). Times the
+ * table scan and a few forms of the list-major tensor-core scan (chunking
+ * of the probe ranks, rows of a list per work item) on the nq host queries
+ * with k and mode, at nprobe 8, 16, 32, 64, 128 and 256 (capped at nlist),
+ * keeps the fastest list-major form and routes every later query probing at
+ * least the crossover nprobe (the smallest from which that form wins at
+ * every larger value) to it, the others to the table scan. chosen8 (may be
+ * NULL) receives the options in the layout of hann_pqivf_scan_options;
+ * ms_table / ms_list (may be NULL, 6 entries) the measured milliseconds of
+ * the table scan and of the chosen form per nprobe (-1 where not run). In
+ * mode 0 results do not depend on the choice; in mode 1 a query's result
+ * depends only on the query and the tuned state. */
+int hann_pqivf_autotune_scan(hann_pqivf* h, const float* queries, int64_t nq, int32_t k, int32_t mode,
+                             int32_t* chosen8, double* ms_table, double* ms_list);
+
 /* Sets the default nprobe (WithCandidateClusters, pqivf/index.go:86-94) of a
  * live index, e.g. to the value a recall-target tuning picked. */
 int hann_pqivf_set_candidate_clusters(hann_pqivf* h, int32_t n);

@@ -32,13 +32,16 @@ int hann_pqivf_arena_stats(void* h, int64_t* out5);
  * (whose rows_scanned counts the scored (query, row) pairs). */
 int hann_pqivf_rows_decoded(void* h, int64_t* out);
 
-/* The list scan's choices. set6 (may be NULL) replaces them, get6 (may be
+/* The list scan's choices. set8 (may be NULL) replaces them, get8 (may be
  * NULL) receives them: [0] list-major tensor-core scan on (1) or the table
  * scan for every batch (0); [1] smallest batch that takes the list-major
  * scan; [2] probe ranks in its first chunk; [3] growth of the later chunks'
- * ends; [4] rows of a list per work item; [5] blocks per SM (1 or 2). Results
- * do not depend on them. */
-int hann_pqivf_scan_options(void* h, const int32_t* set6, int32_t* get6);
+ * ends; [4] rows of a list per work item; [5] blocks per SM (1 or 2); [6]
+ * first thresholds from a table scan of each query's nearest list (1) or a
+ * first chunk that keeps every score (0); [7] fewest probed lists of a
+ * query that takes the list-major scan (the others take the table scan).
+ * In mode 0 results do not depend on them. */
+int hann_pqivf_scan_options(void* h, const int32_t* set8, int32_t* get8);
 
 #ifdef __cplusplus
 }

@@ -35,6 +35,7 @@ def unit_index(seed, n=30000, dim=96, centers=200, nlist=128, M=24, pqk=256, ite
     idx = hg.New(dim, hg.WithCoarseK(nlist), hg.WithNumSubquantizers(M), hg.WithPQK(pqk), hg.WithKMeansIters(iters))
     idx.BulkAddArrays(np.arange(n, dtype=np.int64), x)
     idx.Train()
+    idx.ScanOptions(min_nprobe=1)  # every query through the list-major scan
     return idx, x, q
 
 
@@ -45,10 +46,10 @@ def bench_like():
     idx.close()
 
 
-def test_default_options_take_the_list_major_scan(bench_like):
+def test_list_major_scan_runs(bench_like):
     idx, _, q = bench_like
     opts = idx.ScanOptions()
-    assert opts["list_major"] == 1
+    assert opts["list_major"] == 1 and opts["min_nprobe"] == 1
     idx.SetProfiling(True)
     idx.StageTimes()
     idx.SearchBatch(q[:200], 10, nprobe=8)
@@ -70,6 +71,9 @@ def test_parity_against_oracle(bench_like, nprobe, k):
     dict(first_chunk=1, chunk_growth=2, rows_per_item=128, ctas_per_sm=1),
     dict(first_chunk=2, chunk_growth=4, rows_per_item=256, ctas_per_sm=2),
     dict(first_chunk=1, chunk_growth=64, rows_per_item=4096, ctas_per_sm=2),
+    dict(seed_threshold=0, first_chunk=1, chunk_growth=8),
+    dict(seed_threshold=1, first_chunk=4, chunk_growth=4),
+    dict(min_nprobe=16),
 ])
 def test_options_do_not_change_results(bench_like, opts):
     idx, _, q = bench_like
@@ -144,6 +148,7 @@ def test_shapes(dim, M):
     try:
         idx.BulkAddArrays(np.arange(len(x), dtype=np.int64), x)
         idx.Train()
+        idx.ScanOptions(min_nprobe=1)
         ora = state_to_oracle(idx.export_state())
         g = idx.SearchBatch(q, 10, nprobe=6)
         o = ora.search(q, 10, 6, nthreads=NT)
@@ -164,3 +169,41 @@ def test_uneven_k_and_nprobe(bench_like):
     for i in range(0, len(q), 7):
         o = ora.search(q[i:i + 1], int(k[i]), int(npb[i]), nthreads=1)
         assert_same_results(ids[i:i + 1, :k[i]], dist[i:i + 1, :k[i]], n[i:i + 1], *o[:3])
+
+
+def test_routing_by_nprobe(bench_like):
+    """Queries probing fewer lists than min_nprobe take the table scan, the
+    others the list-major scan, in one batch: every result is the
+    reference's."""
+    idx, _, q = bench_like
+    before = idx.ScanOptions()
+    try:
+        idx.ScanOptions(min_nprobe=20)
+        rng = np.random.default_rng(12)
+        npb = rng.integers(1, 60, len(q)).astype(np.int32)
+        ora = state_to_oracle(idx.export_state())
+        ids, dist, n = idx.SearchBatch(q, 10, nprobe=npb)
+        for i in range(0, len(q), 5):
+            o = ora.search(q[i:i + 1], 10, int(npb[i]), nthreads=1)
+            assert_same_results(ids[i:i + 1], dist[i:i + 1], n[i:i + 1], *o[:3])
+    finally:
+        idx.ScanOptions(**before)
+
+
+def test_autotune_scan(bench_like):
+    """The autotuner measures both scans on a sample, keeps one routing, and
+    searches afterwards still give the reference's results."""
+    idx, _, q = bench_like
+    before = idx.ScanOptions()
+    try:
+        r = idx.AutotuneScan(q[:400], 10, mode=1)
+        opts = r["options"]
+        assert opts == idx.ScanOptions()
+        assert opts["min_nprobe"] in (8, 16, 32, 64, 128, 129)
+        assert set(r["ms_table_scan"]) == {8, 16, 32, 64, 128} == set(r["ms_list_major"])
+        assert all(v > 0 for v in r["ms_table_scan"].values())
+        ora = state_to_oracle(idx.export_state())
+        for nprobe in (8, 128):
+            assert_same_results(*idx.SearchBatch(q, 10, nprobe=nprobe), *ora.search(q, 10, nprobe, nthreads=NT)[:3])
+    finally:
+        idx.ScanOptions(**before)
