@@ -55,8 +55,8 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
     CK(h->s_row_id.reserve((size_t)total));
     CK(h->s_row_cluster.reserve((size_t)total));
     CK(h->s_codes.reserve((size_t)total * h->code_stride));
-    // scan words: each list's region rounded up to whole groups of rows
-    const bool sw = scan_skew_supported(h->o.num_subquantizers);
+    // scan codes: each list's region rounded up to whole groups of rows
+    const bool sw = scan_adc_supported(h->o.num_subquantizers);
     std::vector<int64_t> swstart(h->nlist);
     int64_t swtotal = 0, swcap = 0;
     if (sw) {
@@ -66,7 +66,7 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
             swtotal += round_up(round_up(caps[l], 32), G);
         }
         swcap = swtotal + round_up(arena_slack(packed), G);
-        CK(h->s_scanw.reserve((size_t)swcap * scan_words_per_row(h->o.num_subquantizers)));
+        CK(h->s_scanc.reserve((size_t)swcap * scan_codes_per_row(h->o.num_subquantizers)));
     }
     if (move_rows && h->rows_cap > 0) {
         std::vector<int64_t> src(h->nlist);
@@ -101,8 +101,8 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
     h->d_row_id.swap(h->s_row_id);
     h->d_row_cluster.swap(h->s_row_cluster);
     h->d_codes.swap(h->s_codes);
-    if (sw) h->d_scanw.swap(h->s_scanw);
-    h->scanw_dirty = true;  // rebuilt by upload_lens, which every caller runs next
+    if (sw) h->d_scanc.swap(h->s_scanc);
+    h->scanc_dirty = true;  // rebuilt by upload_lens, which every caller runs next
     h->h_start = start;
     h->h_cap.assign(h->nlist, 0);
     for (int l = 0; l < h->nlist; l++) h->h_cap[l] = round_up(caps[l], 32);
@@ -123,7 +123,7 @@ static int relayout(hann_pqivf* h, const std::vector<int64_t>& caps, bool move_r
 
 // Moves the given lists (all slots, tombstones too, in place order) to the
 // arena's free tail with the given capacities, leaving their old slots as
-// holes, and rebuilds their scan words there. Sets *done; does nothing when
+// holes, and rebuilds their scan codes there. Sets *done; does nothing when
 // the tail is too small or the holes would pass a quarter of the arena (the
 // caller then relayouts everything). The moved rows keep their positions in
 // their lists, so the host bookkeeping only changes the lists' starts.
@@ -131,7 +131,7 @@ static int grow_lists(hann_pqivf* h, const std::vector<int>& lists, const std::v
     *done = false;
     const int n = (int)lists.size();
     if (n == 0 || h->rows_cap == 0) return HANN_OK;
-    const bool sw = scan_skew_supported(h->o.num_subquantizers);
+    const bool sw = scan_adc_supported(h->o.num_subquantizers);
     const int G = scan_group_rows(h->o.num_subquantizers);
     int64_t need = 0, need_sw = 0, freed = 0;
     for (int i = 0; i < n; i++) {
@@ -164,8 +164,8 @@ static int grow_lists(hann_pqivf* h, const std::vector<int>& lists, const std::v
                              h->d_vectors.p, h->d_vectors.p, h->d_codes.p, h->d_codes.p, h->d_term.p, h->d_term.p,
                              h->d_row_id.p, h->d_row_id.p, h->d_row_cluster.p, h->d_row_cluster.p, h->stream));
     if (sw)
-        CK(launch_scan_words_lists(h->d_codes.p, h->code_stride, h->o.num_subquantizers, m.mv_dst.p, m.mv_len.p,
-                                   m.mv_sw.p, n, h->d_scanw.p, h->stream));
+        CK(launch_scan_codes_lists(h->d_codes.p, h->code_stride, h->o.num_subquantizers, m.mv_dst.p, m.mv_len.p,
+                                   m.mv_sw.p, n, h->d_scanc.p, h->stream));
     for (int i = 0; i < n; i++) {
         const int l = lists[i];
         h->h_start[l] = dst[i];
@@ -194,10 +194,10 @@ static int upload_lens(hann_pqivf* h) {
     h->max_list_slots = mx;
     CK(upload(h->d_len, len.data(), len.size(), h->stream));
     CK(upload(h->d_live, live.data(), live.size(), h->stream));
-    if (h->scanw_dirty && h->rows_cap > 0) {
-        CK(launch_scan_words_lists(h->d_codes.p, h->code_stride, h->o.num_subquantizers, h->d_start.p, h->d_len.p,
-                                   h->d_swstart.p, h->nlist, h->d_scanw.p, h->stream));
-        h->scanw_dirty = false;
+    if (h->scanc_dirty && h->rows_cap > 0) {
+        CK(launch_scan_codes_lists(h->d_codes.p, h->code_stride, h->o.num_subquantizers, h->d_start.p, h->d_len.p,
+                                   h->d_swstart.p, h->nlist, h->d_scanc.p, h->stream));
+        h->scanc_dirty = false;
     }
     CK(cudaStreamSynchronize(h->stream));
     return HANN_OK;
@@ -259,11 +259,67 @@ static int prepare_lms(hann_pqivf* h) {
     return HANN_OK;
 }
 
+// Centred codebooks for the FP16 lookup tables (kernels_scan.cu): each
+// codeword minus its subquantizer's mean, in the table-build layout
+// [pqK][M][dsub]; the means; each subquantizer's largest centred codeword
+// norm (rounded up); and the bounds max ||r|| <= sqrt(sum_m max_j
+// ||c_mj||^2) and |term| <= rmax^2 + 2 max ||c|| rmax that size the screen's
+// allowance for FP32 roundings.
+static int prepare_adc(hann_pqivf* h) {
+    const int M = h->o.num_subquantizers, K = h->pqk_eff, ds = h->dsub, dim = h->o.dimension;
+    if (!scan_adc_supported(M) || K <= 0 || h->nlist <= 0) return HANN_OK;
+    std::vector<float> cbc((size_t)K * M * ds), mu((size_t)dim, 0.0f), rm(M);
+    double r2 = 0.0;
+    for (int m = 0; m < M; m++) {
+        const float* cb = h->h_codebooks.data() + (size_t)m * K * ds;
+        for (int e = 0; e < ds; e++) {
+            double a = 0.0;
+            for (int j = 0; j < K; j++) a += cb[(size_t)j * ds + e];
+            mu[(size_t)m * ds + e] = (float)(a / K);
+        }
+        double cmx = 0.0, mx = 0.0;
+        for (int j = 0; j < K; j++) {
+            double n2 = 0.0, c2 = 0.0;
+            for (int e = 0; e < ds; e++) {
+                const float v = cb[(size_t)j * ds + e];
+                const float c = v - mu[(size_t)m * ds + e];
+                cbc[((size_t)j * M + m) * ds + e] = c;
+                n2 += (double)v * v;
+                c2 += (double)c * c;
+            }
+            mx = std::max(mx, n2);
+            cmx = std::max(cmx, c2);
+        }
+        rm[m] = (float)(std::sqrt(cmx) * 1.0001);
+        r2 += mx;
+    }
+    double cmax = 0.0;
+    for (int l = 0; l < h->nlist; l++) {
+        double n2 = 0.0;
+        for (int e = 0; e < dim; e++) {
+            const double v = h->h_coarse[(size_t)l * dim + e];
+            n2 += v * v;
+        }
+        cmax = std::max(cmax, n2);
+    }
+    const double rfull = std::sqrt(r2) * 1.0001;
+    cmax = std::sqrt(cmax) * 1.0001;
+    h->adc_rfull = (float)rfull;
+    h->adc_tbound = (float)((rfull * rfull + 2.0 * cmax * rfull) * 1.0001);
+    CK(upload(h->d_adc_cb, cbc.data(), cbc.size(), h->stream));
+    CK(upload(h->d_adc_mu, mu.data(), mu.size(), h->stream));
+    CK(upload(h->d_adc_rm, rm.data(), rm.size(), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return HANN_OK;
+}
+
 // BF16 centroids, their FP32 squared norms and the largest norm, for the
 // tensor-core preselection (dimensions up to 128).
 static int prepare_coarse(hann_pqivf* h) {
     {
-        const int rc = prepare_lms(h);
+        int rc = prepare_lms(h);
+        if (rc) return rc;
+        rc = prepare_adc(h);
         if (rc) return rc;
     }
     if (h->nlist > 0 && h->pqk_eff > 0) {
@@ -432,8 +488,8 @@ int add_commit(hann_pqivf* h, const int64_t* ids) {
     CK(launch_copy_words(m.codes.p, nullptr, h->d_codes.p, m.dst.p, n, h->code_stride / 4, h->stream));
     CK(launch_copy_words(m.ids.p, nullptr, h->d_row_id.p, m.dst.p, n, 2, h->stream));
     CK(launch_copy_words(m.asg.p, nullptr, h->d_row_cluster.p, m.dst.p, n, 1, h->stream));
-    CK(launch_scan_words_rows(h->d_codes.p, h->code_stride, h->o.num_subquantizers, h->d_start.p, h->d_swstart.p,
-                              m.dst.p, m.asg.p, n, h->d_scanw.p, h->stream));
+    CK(launch_scan_codes_rows(h->d_codes.p, h->code_stride, h->o.num_subquantizers, h->d_start.p, h->d_swstart.p,
+                              m.dst.p, m.asg.p, n, h->d_scanc.p, h->stream));
     // the term last: a row becomes selectable only once it is complete
     CK(launch_copy_words(m.term.p, nullptr, h->d_term.p, m.dst.p, n, 1, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -808,6 +864,9 @@ int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_
     CK(sc.cand_d.reserve((size_t)chunk * R));
     CK(sc.cand_seq.reserve((size_t)chunk * R));
     CK(sc.fbcount.reserve(1));
+    CK(sc.scut.reserve((size_t)chunk));
+    CK(sc.seps.reserve((size_t)chunk));
+    CK(sc.credo.reserve((size_t)chunk + 1));
     if (h->tc && h->nlist >= SCREEN_MIN_LISTS) {
         const int lcap = std::max(1024, 2 * np_max);
         CK(sc.pe2.reserve((size_t)chunk));
@@ -938,6 +997,7 @@ static int run_lms(hann_pqivf* h, SearchScratch& sc, const float* qp, int64_t nc
         ScanParams ps = h->scan_params();
         ps.mode = mode;
         ps.kq = d_k;
+        ps.adc16 = 0;  // the thresholds must bound exact distances: FP32 tables
         CK(launch_fill_i32(sc.lones.p, nc, 1, s));
         CK(cudaMemsetAsync(sc.lzeros.p, 0, sizeof(int32_t) * (size_t)nc, s));
         CK(launch_scan(ps, qp, nc, sc.probe_ids.p, sc.probe_d.p, sc.lones.p, np_max, sc.lzeros.p, R, sc.cand_row.p,
@@ -1026,39 +1086,59 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
     // are ready: the list-major tensor-core scan, then the table scan for the
     // queries it leaves (brute-force fallbacks and overflowing bands); or the
     // table scan alone (qorder: the L2-friendly block order).
+    // Parity mode with FP16 tables: the rerank proves each query's top k
+    // from the scan's cut and lists the queries it cannot prove, which are
+    // scanned and reranked again with FP32 tables.
+    const bool check = mode == 0 && p.adc16 && p.scanc && scan_adc_supported(h->o.num_subquantizers);
     auto scan_rerank = [&](int64_t q0, int64_t nc, const float* qp, const int32_t* qorder) -> int {
         p.kq = d_k + q0;
+        ScanParams pt = p;  // the table scan: every query, or those the list-major scan leaves
+        pt.qorder = qorder;
+        pt.qcount = nullptr;
+        unsigned long long* rows = h->profile ? h->s_rows.p : nullptr;
+        CK(mark(2, true));
         if (lms && nc >= h->lms.min_queries) {
-            CK(mark(2, true));
             const int lrc = run_lms(h, sc, qp, nc, d_k + q0, d_np + q0, np_max, kmax, mode, R, s);
             if (lrc) return lrc;
             CK(mark(2, false));
             CK(mark(3, true));
-            p.qorder = nullptr;
-            CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+            ScanParams pl = p;
+            pl.qorder = nullptr;
+            CK(launch_rerank(pl, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
                              d_dist + q0 * kmax, d_nout + q0, s));
-            ScanParams pr = p;
-            pr.qorder = sc.lredo.p;
-            pr.qcount = sc.lredo.p + nc;
-            CK(launch_scan(pr, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R, sc.cand_row.p,
-                           sc.cand_d.p, sc.cand_seq.p, nullptr, s));
-            CK(launch_rerank(pr, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
-                             d_dist + q0 * kmax, d_nout + q0, s));
-            CK(mark(3, false));
-            h->launches += 3;
-            return HANN_OK;
+            pt.qorder = sc.lredo.p;
+            pt.qcount = sc.lredo.p + nc;
+            rows = nullptr;
+            h->launches += 1;
         }
-        CK(mark(2, true));
-        p.qorder = qorder;
-        CK(launch_scan(p, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R, sc.cand_row.p,
-                       sc.cand_d.p, sc.cand_seq.p, h->profile ? h->s_rows.p : nullptr, s));
-        CK(mark(2, false));
-        CK(mark(3, true));
-        CK(launch_rerank(p, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+        if (check) {
+            pt.scan_cut = sc.scut.p;
+            pt.scan_eps = sc.seps.p;
+            pt.redo = sc.credo.p;
+            pt.redo_count = sc.credo.p + nc;
+            CK(cudaMemsetAsync(sc.credo.p + nc, 0, sizeof(int32_t), s));
+        }
+        CK(launch_scan(pt, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R, sc.cand_row.p,
+                       sc.cand_d.p, sc.cand_seq.p, rows, s));
+        if (!pt.qcount) {
+            CK(mark(2, false));
+            CK(mark(3, true));
+        }
+        CK(launch_rerank(pt, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
                          d_dist + q0 * kmax, d_nout + q0, s));
-        p.qorder = nullptr;
-        CK(mark(3, false));
         h->launches += 2;
+        if (check) {
+            ScanParams pf = p;
+            pf.adc16 = 0;
+            pf.qorder = sc.credo.p;
+            pf.qcount = sc.credo.p + nc;
+            CK(launch_scan(pf, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R, sc.cand_row.p,
+                           sc.cand_d.p, sc.cand_seq.p, nullptr, s));
+            CK(launch_rerank(pf, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
+                             d_dist + q0 * kmax, d_nout + q0, s));
+            h->launches += 2;
+        }
+        CK(mark(3, false));
         return HANN_OK;
     };
     for (int64_t q0 = 0; q0 < nq; q0 += chunk) {
@@ -1224,6 +1304,8 @@ int hann_pqivf_new(const hann_pqivf_options* opts, hann_pqivf** out) {
     if (e == cudaSuccess) e = cudaMemset(h->s_rows.p, 0, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = h->d_fb_dev.reserve(1);
     if (e == cudaSuccess) e = cudaMemset(h->d_fb_dev.p, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = h->d_adc_redo.reserve(1);
+    if (e == cudaSuccess) e = cudaMemset(h->d_adc_redo.p, 0, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->dev_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         snprintf(buf, sizeof(buf), "CUDA initialisation failed: %s", cudaGetErrorString(e));
@@ -1576,6 +1658,16 @@ int hann_pqivf_set_candidate_clusters(hann_pqivf* h, int32_t n) {
     return HANN_OK;
 }
 
+int hann_pqivf_set_adc_fp16(hann_pqivf* h, int32_t on) {
+    if (!h) return HANN_E_INVALID;
+    std::unique_lock<std::mutex> w(h->wmu);
+    std::unique_lock<std::shared_mutex> g(h->mu);
+    cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
+    h->adc16 = on ? 1 : 0;
+    return HANN_OK;
+}
+
 int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on) {
     if (!h) return HANN_E_INVALID;
     std::unique_lock<std::mutex> w(h->wmu);
@@ -1749,6 +1841,20 @@ int hann_pqivf_rows_decoded(void* hv, int64_t* out) {
     if (!h || !out) return HANN_E_INVALID;
     std::lock_guard<std::mutex> rl(h->run_mu);
     *out = h->rows_decoded;
+    return HANN_OK;
+}
+
+int hann_pqivf_adc_redos(void* hv, int64_t* out) {
+    hann_pqivf* h = static_cast<hann_pqivf*>(hv);
+    if (!h || !out) return HANN_E_INVALID;
+    std::unique_lock<std::mutex> w(h->wmu);
+    std::unique_lock<std::shared_mutex> g(h->mu);
+    cudaSetDevice(h->o.device);
+    CK(wait_device_searches(h));
+    unsigned long long v = 0;
+    CK(cudaMemcpyAsync(&v, h->d_adc_redo.p, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    *out = (int64_t)v;
     return HANN_OK;
 }
 
@@ -2248,7 +2354,8 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     const size_t b_cr = align256((size_t)nq * R * sizeof(int32_t));
     const size_t b_cd = align256((size_t)nq * R * sizeof(float));
     const size_t b_cs = align256((size_t)nq * R * sizeof(uint32_t));
-    const size_t need = b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd + b_cs;
+    const size_t b_redo = align256((size_t)(nq + 1) * sizeof(int32_t));
+    const size_t need = b_D + b_pid + b_pd + 5 * b_q32 + b_cr + b_cd + b_cs + b_redo;
     if (need > NOALLOC_ARENA_BYTES)
         return h->fail(HANN_E_UNSUPPORTED,
                        "allocation-free search of %lld queries needs %zu bytes of scratch, above its fixed %zu-byte "
@@ -2266,6 +2373,10 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     int32_t* crow = reinterpret_cast<int32_t*>(base + b_D + b_pid + b_pd + 3 * b_q32);
     float* cd = reinterpret_cast<float*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr);
     uint32_t* cs = reinterpret_cast<uint32_t*>(base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd);
+    unsigned char* tail = base + b_D + b_pid + b_pd + 3 * b_q32 + b_cr + b_cd + b_cs;
+    float* scut = reinterpret_cast<float*>(tail);
+    float* seps = reinterpret_cast<float*>(tail + b_q32);
+    int32_t* redo = reinterpret_cast<int32_t*>(tail + 2 * b_q32);
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     // The arena keeps the previous call's contents: the per-query k and
     // nprobe are written first; every other region is fully written by the
@@ -2280,9 +2391,29 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     CK(launch_dist_matrix(d_queries, nq, h->o.dimension, h->d_coarse.p, h->nlist, D, s));
     CK(launch_probe_select(D, nq, h->nlist, dnp, np, dk, h->d_live.p, h->o.fallback ? 1 : 0, pid, pd, fb,
                            h->d_fb_dev.p, s));
+    // parity mode with FP16 tables: queries the rerank cannot prove from the
+    // scan's cut are scanned again with FP32 tables (as in run_search)
+    const bool check = mode == 0 && p.adc16 && p.scanc && scan_adc_supported(h->o.num_subquantizers);
+    if (check) {
+        p.scan_cut = scut;
+        p.scan_eps = seps;
+        p.redo = redo;
+        p.redo_count = redo + nq;
+        CK(cudaMemsetAsync(redo + nq, 0, sizeof(int32_t), s));
+    }
     CK(launch_scan(p, d_queries, nq, pid, pd, dnp, np, fb, R, crow, cd, cs, nullptr, s));
     CK(launch_rerank(p, d_queries, nq, crow, cs, R, dk, k, mode, d_ids, d_distances, d_n_out, s));
     h->launches += 5;  // fill, distance matrix, probe select, scan, rerank
+    if (check) {
+        ScanParams pf = p;
+        pf.adc16 = 0;
+        pf.scan_cut = nullptr;
+        pf.qorder = redo;
+        pf.qcount = redo + nq;
+        CK(launch_scan(pf, d_queries, nq, pid, pd, dnp, np, fb, R, crow, cd, cs, nullptr, s));
+        CK(launch_rerank(pf, d_queries, nq, crow, cs, R, dk, k, mode, d_ids, d_distances, d_n_out, s));
+        h->launches += 2;
+    }
     CK(note_device_search(h, s));
     return HANN_OK;
 }

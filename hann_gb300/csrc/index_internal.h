@@ -152,6 +152,10 @@ struct SearchScratch {
     DBuf<int32_t> pcnt, pcand_id, plcount, pneed, ptodo;  // ptodo: rows left to the block kernels (+ count)
     DBuf<unsigned long long> pband;
     DBuf<int32_t> qorder, order_scratch;  // L2-friendly query order for scan and rerank
+    // parity mode with FP16 tables: per query the scan's cut and error bound,
+    // and the queries the rerank could not prove (count at credo[nq])
+    DBuf<float> scut, seps;
+    DBuf<int32_t> credo;
     // list-major tensor-core scan (kernels_lms.cu)
     DBuf<uint16_t> q16;
     DBuf<float> le2, lasl, lthr, lcand_s, lpair_base, leps;
@@ -223,6 +227,13 @@ struct hann_pqivf {
 
     DBuf<float> d_coarse, d_codebooks, d_vectors, d_term;
     DBuf<float> d_codebooks_t;  // [pqK][M][dsub], the scan's table-build layout
+    // FP16 lookup tables: centred codebooks in the table-build layout, the
+    // means, each subquantizer's largest centred codeword norm and the
+    // bounds on ||r|| and |term| (prepare_adc)
+    DBuf<float> d_adc_cb, d_adc_mu, d_adc_rm;
+    float adc_rfull = 0.0f, adc_tbound = 0.0f;
+    int adc16 = 1;              // FP16 tables in the table scan (hann_pqivf_set_adc_fp16)
+    DBuf<unsigned long long> d_adc_redo;  // queries scanned again with FP32 tables (diagnostic)
     // BF16 copy of the coarse centroids for the tensor-core preselection
     int kp = 0;
     bool tc = false;
@@ -233,16 +244,16 @@ struct hann_pqivf {
     DBuf<int64_t> d_start, d_row_id;
     DBuf<int32_t> d_len, d_live, d_row_cluster;
     DBuf<uint8_t> d_codes;
-    DBuf<uint16_t> d_scanw;   // scan words, rebuilt from the codes when rows are placed
-    DBuf<int64_t> d_swstart;  // first scan-word slot of each list
+    DBuf<uint8_t> d_scanc;    // scan codes, rebuilt from the codes when rows are placed
+    DBuf<int64_t> d_swstart;  // first scan-code slot of each list
     std::vector<int64_t> h_swstart;
-    bool scanw_dirty = false;
+    bool scanc_dirty = false;
     // the previous row arrays, kept for the next relayout to reuse
     DBuf<float> s_vectors, s_term;
     DBuf<int64_t> s_row_id;
     DBuf<int32_t> s_row_cluster;
     DBuf<uint8_t> s_codes;
-    DBuf<uint16_t> s_scanw;
+    DBuf<uint8_t> s_scanc;
 
     // list-major tensor-core scan: FP16 codebooks [M][pqK][dsub], the error
     // bound's constants, the longest list (slots) and the scan's choices
@@ -305,7 +316,18 @@ struct hann_pqivf {
         p.list_start = d_start.p;
         p.list_len = d_len.p;
         p.codes = d_codes.p;
-        p.scanw = scan_skew_supported(o.num_subquantizers) ? d_scanw.p : nullptr;
+        p.scanc = scan_adc_supported(o.num_subquantizers) ? d_scanc.p : nullptr;
+        p.adc_cb = d_adc_cb.p;
+        p.adc_mu = d_adc_mu.p;
+        p.adc_rm = d_adc_rm.p;
+        p.adc_rfull = adc_rfull;
+        p.adc_tbound = adc_tbound;
+        p.adc16 = adc16 && d_adc_cb.p ? 1 : 0;
+        p.scan_cut = nullptr;
+        p.scan_eps = nullptr;
+        p.redo = nullptr;
+        p.redo_count = nullptr;
+        p.redo_total = d_adc_redo.p;
         p.qorder = nullptr;
         p.qcount = nullptr;
         p.sw_start = d_swstart.p;

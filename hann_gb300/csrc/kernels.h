@@ -141,8 +141,20 @@ struct ScanParams {
     const int64_t* list_start;  // [nlist] first row of each list
     const int32_t* list_len;    // [nlist]
     const uint8_t* codes;     // [rows][code_stride]
-    const uint16_t* scanw;    // table offsets per row (kernels_scan.cu), blocked by groups of rows
-    const int64_t* sw_start;  // [nlist] first scan-word slot of each list
+    const uint8_t* scanc;     // scan codes (kernels_scan.cu): permuted per lane, blocked by groups of rows
+    const int64_t* sw_start;  // [nlist] first scan-code slot of each list
+    // FP16 lookup tables (kernels_scan.cu)
+    const float* adc_cb;      // [pqK][M][dsub] codewords minus their subquantizer's mean
+    const float* adc_mu;      // [dim] the subquantizers' mean codewords, concatenated
+    const float* adc_rm;      // [M] largest ||codeword - mean|| per subquantizer
+    float adc_rfull;          // bound on ||r|| over every residual the codebooks reconstruct
+    float adc_tbound;         // bound on |term| = | ||r||^2 + 2 <c, r> |
+    int adc16;                // 1: FP16 tables (0: FP32)
+    float* scan_cut;          // [nq] parity mode, FP16 tables: no row left out screened below it
+    float* scan_eps;          // [nq] bound on the screen's error
+    int32_t* redo;            // rerank: queries whose top k the FP16 screen cannot prove ...
+    int32_t* redo_count;      // ... and their count
+    unsigned long long* redo_total;  // optional: running count of those queries
     const float* term;        // [rows]
     const int32_t* row_cluster;  // [rows]
     const float* vectors;     // [rows][dim]
@@ -171,27 +183,27 @@ cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, c
                         int R, int32_t* cand_row, float* cand_d, uint32_t* cand_seq,
                         unsigned long long* rows_scanned, cudaStream_t s);
 
-// The bank-conflict-free scan (kernels_scan.cu) for M a multiple of 4 up to
-// 32; launch_scan dispatches to it when it applies. Its candidates leave
-// unsorted.
-bool scan_skew_supported(int M);
-int scan_words_per_row(int M);
+// The bank-conflict-free scan (kernels_scan.cu) for M up to 32, with FP16
+// or FP32 lookup tables; launch_scan dispatches to it when it applies. Its
+// candidates leave unsorted.
+bool scan_adc_supported(int M);
+int scan_codes_per_row(int M);
 int scan_group_rows(int M);
-size_t scan_skew_smem(int R);
-// Scan words (kernels_scan.cu) of every slot of every list, or of the rows at
+size_t scan_adc_smem(int R, int M, int fp16);
+// Scan codes (kernels_scan.cu) of every slot of every list, or of the rows at
 // positions rows[i] in lists cluster[i].
-cudaError_t launch_scan_words_lists(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
-                                    const int32_t* list_len, const int64_t* sw_start, int nlist, uint16_t* scanw,
+cudaError_t launch_scan_codes_lists(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+                                    const int32_t* list_len, const int64_t* sw_start, int nlist, uint8_t* scanc,
                                     cudaStream_t s);
-cudaError_t launch_scan_words_rows(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+cudaError_t launch_scan_codes_rows(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
                                    const int64_t* sw_start, const int64_t* rows, const int32_t* cluster, int64_t n,
-                                   uint16_t* scanw, cudaStream_t s);
+                                   uint8_t* scanc, cudaStream_t s);
 // Codebooks [M][pqK][dsub] -> [pqK][M][dsub] (the scan's table-build layout).
 cudaError_t launch_transpose_codebooks(const float* cb, int M, int pqK, int dsub, float* out, cudaStream_t s);
-cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
-                             const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
-                             int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
-                             cudaStream_t s);
+cudaError_t launch_scan_adc(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
+                            const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
+                            int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
+                            cudaStream_t s);
 
 // Rerank the R candidates of each query with an exact FP32 distance and emit
 // the k best: mode 0 = the reference's reconstructed-vector distance

@@ -1,23 +1,28 @@
-// kernels_scan.cu -- bank-conflict-free ADC list scan with warp radix
-// selection, for M up to 32. Larger M use scan_kernel in kernels_search.cu.
+// kernels_scan.cu -- the bank-conflict-free ADC list scan with warp radix
+// selection, for M up to 32 (larger M use scan_kernel in kernels_search.cu).
 //
-// Same distance as scan_kernel: ||q-c||^2 + term + sum_m T[m][code_m].
+// Distance: ||q - c||^2 + term + sum_m T[m][code_m], term = ||r||^2 +
+// 2 <c, r> stored per row, T[m][j] = -2 <q_m, codeword_mj> the lookup table
+// built per query in shared memory, in FP16 (32 KB) or FP32.
 //
-// Lookup table without bank conflicts. The table is 256 rows of 32 words,
-// entry (m, j) at row j, bank (c * M + m) for every copy c < 32 / M. A warp
-// takes G = M * (32 / M) rows of a list at a time; lane l (l < G) owns rows
-// whose position in the list is l mod G, uses copy c = l / M, and walks the
-// subquantizers in the rotated order m_s = (s + l) mod M, so in every step
-// the G lanes read G distinct banks.
+// Lookup table without bank conflicts. The table holds every subquantizer's
+// entries two or three times over (64 half-word slots per code value, see
+// adc_slot_m), so that in each step of a warp the 32 lanes read 32 distinct
+// banks whatever their codes. Each row's code bytes are stored permuted for
+// the lane that scans it ("scan codes", MP = M rounded up to 8 bytes a row,
+// rebuilt from the codes whenever rows are placed) and blocked by groups of
+// 32 rows, so a warp loads a step with contiguous 16- and 8-byte loads: 24
+// bytes a row at M = 24, the codes themselves. A lookup is a byte permute
+// (code byte and the lane's offset byte into a table offset), a shift, a
+// 16-bit shared load and an FP16-into-FP32 add.
 //
-// Scan words. Rather than its code bytes, each row stores for every step s
-// the byte offset of its table entry, (code_{m_s} * 32 + c * M + m_s) * 4,
-// as a 16-bit word ("scan words", built from the codes whenever rows are
-// placed; see launch_scan_words_*). A lookup is then one shift or mask, one
-// shared load and one add. The words of G consecutive rows are stored plane
-// by plane, so a warp step reads them with contiguous 16-byte loads: the
-// scan is bound by the L1 data pipe's wavefronts (table reads plus these
-// loads), and contiguous loads take the fewest.
+// FP16 tables and the reference's results. The FP16 entries are centred per
+// subquantizer and scaled per query; every entry's rounding error is bounded,
+// so a row's screened distance is within a per-query eps of the exact PQ
+// distance. In parity mode the scan reports the largest screened distance it
+// kept when it left rows out; the rerank proves the top k with it (the k-th
+// reference distance must lie below that cut minus eps) and lists the
+// queries it cannot prove, which the host scans again with FP32 tables.
 //
 // Selection without sorting. Each warp appends rows below the block-wide
 // threshold to its buffer; a full buffer is cut back to its R smallest keys
@@ -25,6 +30,8 @@
 // lowers the threshold. At the end warp 0 selects the query's R best from the
 // warps' survivors. Candidates leave unsorted: the rerank sorts them by exact
 // distance.
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 #include "common.cuh"
@@ -158,21 +165,177 @@ __device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count
     return out;
 }
 
-template <int MP, int MX, int DEPTH>
-__global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, const float* __restrict__ Q,
-                                                            const float* __restrict__ probe_d,
-                                                            const int32_t* __restrict__ probe_ids,
-                                                            const int32_t* __restrict__ nprobe, int np_max,
-                                                            const int32_t* __restrict__ fallback, int R, int CAPW,
-                                                            int32_t* __restrict__ cand_row,
-                                                            float* __restrict__ cand_d,
-                                                            uint32_t* __restrict__ cand_seq,
-                                                            unsigned long long* __restrict__ rows_scanned) {
-    // MP: scan words per row (M rounded up to 8); MX: M when it equals MP
-    // (known at compile time), else 0. G rows per warp step.
-    __shared__ __align__(16) float lut[256 * 32];
+// Cuts a full buffer back to a superset of its R smallest keys in one pass:
+// below the keys' common prefix, the 8-bit digit's histogram gives the bin
+// holding the R-th smallest; every key in that bin or below stays, and *tau
+// becomes the bin's (exclusive) upper edge, at or above the R-th smallest.
+// Falls back to warp_select when the kept keys would pass `limit`.
+// Warp-synchronous.
+__device__ int warp_cut(uint32_t* key, uint32_t* seq, int32_t* row, int count, int R, int limit, uint32_t* tau,
+                        uint32_t* hist) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nch = (count + 31) >> 5;
+    uint32_t band = 0xffffffffu, bor = 0;
+    for (int ch = 0; ch < nch; ch++) {
+        const int i = ch * 32 + lane;
+        if (i < count) {
+            band &= key[i];
+            bor |= key[i];
+        }
+    }
+    band = __reduce_and_sync(FULL, band);
+    bor = __reduce_or_sync(FULL, bor);
+    const uint32_t diff = band ^ bor;
+    if (diff == 0 || count <= R) return warp_select(key, seq, row, count, R, tau, hist);
+    const int top = 31 - __clz(diff);
+    const int lo = top >= 7 ? top - 7 : 0;
+    const uint32_t dmask = (1u << (top - lo + 1)) - 1u;
+#pragma unroll
+    for (int b = 0; b < 8; b++) hist[b * 32 + lane] = 0;
+    __syncwarp();
+    for (int ch = 0; ch < nch; ch++) {
+        const int i = ch * 32 + lane;
+        if (i < count) atomicAdd(&hist[(key[i] >> lo) & dmask], 1u);
+    }
+    __syncwarp();
+    uint32_t cnt[8], tot = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        cnt[j] = hist[lane * 8 + j];
+        tot += cnt[j];
+    }
+    uint32_t incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const uint32_t excl = incl - tot;
+    const uint32_t need = (uint32_t)R;
+    const bool mine = excl < need && need <= incl;
+    uint32_t pick = 0, keep = 0;
+    if (mine) {
+        uint32_t cum = excl;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            if (cum < need && need <= cum + cnt[j]) {
+                pick = (uint32_t)(lane * 8 + j);
+                keep = cum + cnt[j];
+            }
+            cum += cnt[j];
+        }
+    }
+    const int owner = __ffs(__ballot_sync(FULL, mine)) - 1;
+    pick = __shfl_sync(FULL, pick, owner);
+    keep = __shfl_sync(FULL, keep, owner);
+    __syncwarp();
+    if ((int)keep > limit) return warp_select(key, seq, row, count, R, tau, hist);
+    // keys of the common prefix in bins up to pick: below prefix + (pick + 1) << lo
+    const uint32_t prefix = top == 31 ? 0u : (band & (0xffffffffu << (top + 1)));
+    const unsigned long long edge = (unsigned long long)prefix + ((unsigned long long)(pick + 1) << lo);
+    const uint32_t bound = edge > 0xffffffffull ? 0xffffffffu : (uint32_t)edge;
+    int out = 0;
+    for (int ch = 0; ch < nch; ch++) {
+        const int i = ch * 32 + lane;
+        const bool in = i < count;
+        const uint32_t kk = in ? key[i] : 0xffffffffu;
+        const uint32_t ss = in ? seq[i] : 0u;
+        const int32_t rr = in ? row[i] : 0;
+        const bool kp = in && kk < bound;
+        const unsigned bk = __ballot_sync(FULL, kp);
+        const int pos = out + __popc(bk & lt);
+        __syncwarp();
+        if (kp) {
+            key[pos] = kk;
+            seq[pos] = ss;
+            row[pos] = rr;
+        }
+        out += __popc(bk);
+        __syncwarp();
+    }
+    *tau = bound;
+    return out;
+}
+
+// Lookup-table slots. A table row (one code value j) is 32 banks of two
+// 16-bit halves (FP16 entries: 128 bytes) or of two 32-bit words (FP32
+// entries with more than 16 subquantizers: 256 bytes, half h in the row's
+// h-th 128 bytes). Slot (b, h) holds the entries of subquantizer
+// adc_slot_m(b, h, MP); in step s lane l reads slot (l ^ s, s >= 16). So the
+// 32 lanes of a warp read 32 distinct banks in every step whatever their
+// codes, and over its MP steps each lane reads every subquantizer once
+// (MP = M rounded up to 8; subquantizers at or past M have zero entries).
+__host__ __device__ __forceinline__ int adc_slot_m(int b, int h, int MP) {
+    if (MP == 8) return b & 7;
+    if (MP == 16) return b & 15;
+    if (MP == 24) return h == 0 ? (b < 16 ? b : b - 8) : (b < 16 ? (b & 7) : 16 + (b & 7));
+    return b;
+}
+
+// The slots of subquantizer m (at most four): banks b[], halves hh[].
+__device__ __forceinline__ int adc_slots(int m, int MP, int* b, int* hh) {
+    if (MP == 8) {
+        for (int i = 0; i < 4; i++) {
+            b[i] = m + 8 * i;
+            hh[i] = 0;
+        }
+        return 4;
+    }
+    if (MP == 16) {
+        b[0] = m;
+        b[1] = m + 16;
+        hh[0] = hh[1] = 0;
+        return 2;
+    }
+    if (MP == 24) {
+        if (m >= 8 && m < 16) {
+            b[0] = m;
+            b[1] = m + 8;
+            hh[0] = hh[1] = 0;
+            return 2;
+        }
+        b[0] = m < 8 ? m : m + 8;
+        hh[0] = 0;
+        b[1] = m;
+        b[2] = m + 8;
+        hh[1] = hh[2] = 1;
+        return 3;
+    }
+    b[0] = b[1] = m;
+    hh[0] = 0;
+    hh[1] = 1;
+    return 2;
+}
+
+// Position of step s's code byte of lane l in a group of 32 rows: planes of
+// 16 bytes per lane, then a plane of 8 bytes per lane when MP is an odd
+// multiple of 8, so a lane loads its row with one 16-byte load per full
+// plane (and one 8-byte load) and the warp's loads are contiguous.
+__host__ __device__ __forceinline__ int adc_code_pos(int l, int s, int MP) {
+    const int full = MP / 16;
+    return (s >> 4) < full ? 512 * (s >> 4) + 16 * l + (s & 15) : 512 * full + 8 * l + (s & 7);
+}
+
+template <int MP, bool HALF>
+__global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, const float* __restrict__ Q,
+                                                           const float* __restrict__ probe_d,
+                                                           const int32_t* __restrict__ probe_ids,
+                                                           const int32_t* __restrict__ nprobe, int np_max,
+                                                           const int32_t* __restrict__ fallback, int R, int CAPW,
+                                                           int32_t* __restrict__ cand_row,
+                                                           float* __restrict__ cand_d,
+                                                           uint32_t* __restrict__ cand_seq,
+                                                           unsigned long long* __restrict__ rows_scanned) {
+    constexpr bool WIDE = !HALF && MP > 16;     // FP32 entries, 256-byte rows
+    constexpr int LUT_BYTES = WIDE ? 65536 : 32768;
+    constexpr int SHIFT = WIDE ? 0 : 1;        // table offset = (code * 256 + offset byte) >> SHIFT
+    constexpr int NW = MP / 4;                  // code words per row
+    constexpr int NOB = (MP + 2) / 3;           // offset registers: three offset bytes and a zero byte
+    constexpr int G = 32;
     extern __shared__ __align__(16) unsigned char smraw[];
-    uint32_t* wkey = reinterpret_cast<uint32_t*>(smraw);
+    unsigned char* lutb = smraw;
+    uint32_t* wkey = reinterpret_cast<uint32_t*>(smraw + LUT_BYTES);
     uint32_t* wseq = wkey + WARPS * CAPW;
     int32_t* wrow = reinterpret_cast<int32_t*>(wseq + WARPS * CAPW);
     uint32_t* mkey = reinterpret_cast<uint32_t*>(wrow + WARPS * CAPW);  // [WARPS * R] merge region
@@ -180,14 +343,13 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
     int32_t* mrow = reinterpret_cast<int32_t*>(mseq + WARPS * R);
     uint32_t* whist = reinterpret_cast<uint32_t*>(mrow + WARPS * R);   // [WARPS][256]
     __shared__ uint32_t s_tau;
-    __shared__ int s_big;
+    __shared__ int s_big, s_dropped;
     __shared__ int s_wcount[WARPS];
     __shared__ int s_lstart[SCAN_FLAT_LISTS], s_lsw[SCAN_FLAT_LISTS];
     __shared__ int s_llen[SCAN_FLAT_LISTS], s_lsteps[SCAN_FLAT_LISTS + 1];
     __shared__ float s_lbase[SCAN_FLAT_LISTS];
-    const int M = MX > 0 ? MX : p.M;
-    const int copies = 32 / M;
-    const int G = 32;
+    __shared__ float s_eps;
+    const int M = p.M;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     if (p.qcount && (int)blockIdx.x >= *p.qcount) return;
     const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
@@ -195,42 +357,129 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
     if (tid == 0) {
         s_tau = KEY_INF;
         s_big = 0;
+        s_dropped = 0;
+    }
+    // Every warp works out the table's scale for itself (the same values in
+    // each), so the build needs no barrier before it.
+    float scale = 1.0f, inv = 1.0f, c0 = 0.0f;
+    if (HALF) {
+        // FP16 entries -2 <q_m, c_mj - mu_m> scaled by 2^e, so that the bound
+        // b_m = 2 ||q_m|| max_j ||c_mj - mu_m|| of the largest is at most
+        // 2^15; the means' part, -2 <q, mu>, joins each list's base. Rounding
+        // one entry errs by at most 2^-11 of b_m (2^-25 below FP16's normal
+        // range), so a row's screened distance is within eps of the exact
+        // sum (with a relative allowance for the FP32 roundings of the
+        // decomposition).
+        float bm = 0.0f;
+        if (lane < M) {
+            float qq = 0.0f;
+            for (int t = 0; t < p.dsub; t++) qq = fmaf(qv[lane * p.dsub + t], qv[lane * p.dsub + t], qq);
+            bm = 2.0f * sqrtf(qq) * p.adc_rm[lane];
+        }
+        float mx = bm, sum = bm, cq = 0.0f, qn = 0.0f;
+        for (int e = lane; e < p.dim; e += 32) {
+            cq = fmaf(qv[e], p.adc_mu[e], cq);
+            qn = fmaf(qv[e], qv[e], qn);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+            sum += __shfl_xor_sync(FULL, sum, o);
+            cq += __shfl_xor_sync(FULL, cq, o);
+            qn += __shfl_xor_sync(FULL, qn, o);
+        }
+        int ex = 0;
+        const bool finite = mx > 0.0f && mx < pos_inf();
+        if (finite) frexpf(mx, &ex);
+        const int e = finite ? max(-120, min(120, 15 - ex)) : 0;
+        scale = ldexpf(1.0f, e);
+        inv = ldexpf(1.0f, -e);
+        c0 = -2.0f * cq;
+        if (tid == 0)
+            s_eps = 4.8828125e-4f * sum + (float)MP * 2.98023224e-8f * inv +
+                    1e-5f * (2.0f * sqrtf(qn) * p.adc_rfull + p.adc_tbound + 2.0f * fabsf(cq));
     }
     {
-        // Lane l fills bank l of table rows w, w + WARPS, ...: subquantizer
-        // m = l % M. Codeword j of every subquantizer sits in one row of the
-        // transposed codebooks, so a warp's loads for one table row are one
-        // contiguous read (the [M][pqK] layout spread them over M rows 1 KB+
-        // apart).
-        const bool own = lane < copies * M;
-        const int m = lane % M;
-        const float* qm = qv + m * p.dsub;
-        const bool v4 = (p.dsub & 3) == 0 &&
-                        ((reinterpret_cast<uintptr_t>(qv) | reinterpret_cast<uintptr_t>(p.codebooks_t)) & 15) == 0;
-        for (int j = w; j < 256; j += WARPS) {
-            float v = 0.0f;
-            if (own && j < p.pqK) {
-                const float* cw = p.codebooks_t + ((int64_t)j * M + m) * p.dsub;
-                float acc = 0.0f;
-                if (v4) {
-                    for (int t = 0; t < p.dsub; t += 4) {
-                        const float4 a = __ldg(reinterpret_cast<const float4*>(qm + t));
-                        const float4 b = __ldg(reinterpret_cast<const float4*>(cw + t));
-                        acc = fmaf(a.x, b.x, acc);
-                        acc = fmaf(a.y, b.y, acc);
-                        acc = fmaf(a.z, b.z, acc);
-                        acc = fmaf(a.w, b.w, acc);
-                    }
-                } else {
-                    for (int t = 0; t < p.dsub; t++) acc = fmaf(qm[t], cw[t], acc);
-                }
-                v = -2.0f * acc;
+        // Table build: warp w takes code values w, w + 8, ...; lane l < M
+        // computes subquantizer l's entry and writes it to each of its slots.
+        // Eight codeword loads are in flight per lane (the codebooks come
+        // from L2: shared memory leaves L1 little room).
+        const float* cb = HALF ? p.adc_cb : p.codebooks_t;  // [pqK][M][dsub]
+        int bs[4] = {0, 0, 0, 0}, hs[4] = {0, 0, 0, 0};
+        const int ns = lane < M ? adc_slots(lane, MP, bs, hs) : 0;
+        auto put = [&](int j, float acc) {
+            if (HALF) {
+                const __half hv = __float2half_rn(-2.0f * acc * scale);
+                for (int i = 0; i < ns; i++) *reinterpret_cast<__half*>(lutb + j * 128 + 4 * bs[i] + 2 * hs[i]) = hv;
+            } else {
+                const float v = -2.0f * acc;
+                for (int i = 0; i < ns; i++)
+                    *reinterpret_cast<float*>(lutb + j * (WIDE ? 256 : 128) + 4 * bs[i] + 128 * hs[i]) = v;
             }
-            lut[j * 32 + lane] = v;
+        };
+        const bool v4 = p.dsub == 4 &&
+                        ((reinterpret_cast<uintptr_t>(qv) | reinterpret_cast<uintptr_t>(cb)) & 15) == 0;
+        if (lane < M && v4) {
+            const float4 qa = __ldg(reinterpret_cast<const float4*>(qv) + lane);
+            constexpr int U = 8;
+            for (int j0 = w; j0 < p.pqK; j0 += WARPS * U) {
+                float4 c[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int j = j0 + u * WARPS;
+                    if (j < p.pqK) c[u] = __ldg(reinterpret_cast<const float4*>(cb) + (int64_t)j * M + lane);
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int j = j0 + u * WARPS;
+                    if (j < p.pqK) {
+                        float acc = 0.0f;
+                        acc = fmaf(qa.x, c[u].x, acc);
+                        acc = fmaf(qa.y, c[u].y, acc);
+                        acc = fmaf(qa.z, c[u].z, acc);
+                        acc = fmaf(qa.w, c[u].w, acc);
+                        put(j, acc);
+                    }
+                }
+            }
+        } else if (lane < M) {
+            const float* qm = qv + lane * p.dsub;
+            for (int j = w; j < p.pqK; j += WARPS) {
+                const float* cw = cb + ((int64_t)j * M + lane) * p.dsub;
+                float acc = 0.0f;
+                for (int t = 0; t < p.dsub; t++) acc = fmaf(qm[t], cw[t], acc);
+                put(j, acc);
+            }
+        }
+        // subquantizers past M (their codes are 0): zero entries
+        for (int m = M + tid; m < MP; m += THREADS) {
+            int b2[4], h2[4];
+            const int n2 = adc_slots(m, MP, b2, h2);
+            for (int i = 0; i < n2; i++) {
+                if (HALF) *reinterpret_cast<unsigned short*>(lutb + 4 * b2[i] + 2 * h2[i]) = 0;
+                else *reinterpret_cast<float*>(lutb + 4 * b2[i] + 128 * h2[i]) = 0.0f;
+            }
         }
     }
+    // the lane's table offset bytes, three to a register (the fourth byte
+    // zero): offset byte of step s = the in-row offset of slot (lane ^ s,
+    // s >= 16) << SHIFT
+    uint32_t ob[NOB];
+#pragma unroll
+    for (int i = 0; i < NOB; i++) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            const int s = 3 * i + kk;
+            if (s < MP) {
+                const uint32_t b = (uint32_t)(lane ^ s), hh = s >= 16 ? 1u : 0u;
+                const uint32_t o = WIDE ? 4u * b + 128u * hh : 8u * b + 4u * hh;
+                v |= o << (8 * kk);
+            }
+        }
+        ob[i] = v;
+    }
     __syncthreads();
-    const unsigned char* lutb = reinterpret_cast<const unsigned char*>(lut);
     uint32_t* key = wkey + w * CAPW;
     uint32_t* seq = wseq + w * CAPW;
     int32_t* row = wrow + w * CAPW;
@@ -238,12 +487,8 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
     const bool fb = fallback[q] != 0;
     const int nl = fb ? p.nlist : min(nprobe[q], p.nlist);
     const unsigned ltm = (1u << lane) - 1u;
-    const bool act = lane < G;
     int count = 0;
     unsigned long long scanned = 0;
-    // The warp walks its lists G rows at a time and loads the next step's
-    // rows -- in the same list or the next one -- before it computes the
-    // current, so each lane keeps two rows in flight.
     auto list_meta = [&](int i, int64_t& start, int64_t& sws, int& len, float& base) {
         const int l = fb ? i : probe_ids[q * np_max + i];
         if (fb) {
@@ -254,33 +499,57 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
-            base = part;
+            base = part + c0;
         } else {
-            base = probe_d[q * np_max + i];
+            base = probe_d[q * np_max + i] + c0;
         }
         start = p.list_start[l];
         sws = p.sw_start[l];
         len = p.list_len[l];
     };
-    // Scan words of one step: G rows, stored as MP / 8 planes of G
-    // consecutive 16-byte chunks, so the warp's loads are contiguous.
-    auto load_row = [&](int64_t sws, int step, int64_t grow, uint4 (&sw)[MP / 8], float& term) {
-        const uint4* sp = reinterpret_cast<const uint4*>(p.scanw) + sws * (MP / 8) + (int64_t)step * G * (MP / 8) + lane;
+    // one step's code words of the lane's row; gp: the group's first byte
+    auto load_codes = [&](const uint8_t* gp, uint32_t (&cw)[NW]) {
 #pragma unroll
-        for (int t = 0; t < MP / 8; t++) sw[t] = __ldg(sp + t * G);
-        term = __ldg(p.term + grow);
-    };
-    // four partial sums keep the adds off one long dependency chain
-    auto lookup = [&](const uint4 (&sw)[MP / 8], float acc) {
-        const uint32_t* wv = reinterpret_cast<const uint32_t*>(sw);
-        float part[4] = {acc, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int s2 = 0; s2 < MP / 2; s2++) {
-            const uint32_t word = wv[s2];
-            if (2 * s2 < M) part[(2 * s2) & 3] += *reinterpret_cast<const float*>(lutb + (word & 0xffffu));
-            if (2 * s2 + 1 < M) part[(2 * s2 + 1) & 3] += *reinterpret_cast<const float*>(lutb + (word >> 16));
+        for (int pl = 0; pl < MP / 16; pl++) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(gp + 512 * pl) + lane);
+            cw[4 * pl] = v.x;
+            cw[4 * pl + 1] = v.y;
+            cw[4 * pl + 2] = v.z;
+            cw[4 * pl + 3] = v.w;
         }
-        return float_key((part[0] + part[1]) + (part[2] + part[3]));
+        if (MP % 16) {
+            const uint2 v = __ldg(reinterpret_cast<const uint2*>(gp + 512 * (MP / 16)) + lane);
+            cw[NW - 2] = v.x;
+            cw[NW - 1] = v.y;
+        }
+    };
+    // A lookup is one byte permute (code byte and offset byte into a table
+    // offset), one shift, one shared load and one add; four partial sums
+    // keep the adds off one long dependency chain.
+    auto lookup = [&](const uint32_t (&cw)[NW], float bt) {
+        float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int s = 0; s < MP; s++) {
+            const uint32_t sel = (uint32_t)(4 + s % 3) | ((uint32_t)(s % 4) << 4) | 0x7700u;
+            const uint32_t a = __byte_perm(cw[s / 4], ob[s / 3], sel) >> SHIFT;
+            if (HALF) {
+                const unsigned short hb = *reinterpret_cast<const unsigned short*>(lutb + a);
+                asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(part[s & 3]) : "h"(hb));
+            } else {
+                part[s & 3] += *reinterpret_cast<const float*>(lutb + a);
+            }
+        }
+        return float_key(fmaf((part[0] + part[1]) + (part[2] + part[3]), inv, bt));
+    };
+    auto cut_back = [&]() {
+        __syncwarp();
+        uint32_t kth;
+        count = warp_cut(key, seq, row, count, R, CAPW / 2, &kth, hist);
+        if (lane == 0) {
+            atomicMin(&s_tau, kth);
+            s_dropped = 1;
+        }
+        __syncwarp();
     };
     auto offer = [&](uint32_t k, int li, int64_t grow) {
         const bool pass = k < *(volatile uint32_t*)&s_tau;
@@ -293,13 +562,7 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
                 row[pos] = (int32_t)grow;
             }
             count += __popc(bal);
-            if (count > CAPW - 32) {
-                __syncwarp();
-                uint32_t kth;
-                count = warp_select(key, seq, row, count, R, &kth, hist);
-                if (lane == 0) atomicMin(&s_tau, kth);
-                __syncwarp();
-            }
+            if (count > CAPW - 32) cut_back();
         }
     };
     bool flat = !fb && nl <= SCAN_FLAT_LISTS;
@@ -315,7 +578,7 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             s_lsw[i] = (int)p.sw_start[l];
             const int len = p.list_len[l];
             s_llen[i] = len;
-            s_lbase[i] = probe_d[q * np_max + i];
+            s_lbase[i] = probe_d[q * np_max + i] + c0;
             s_lsteps[i] = (len + G - 1) / G;
             if (len > (1 << 24) - G) s_big = 1;
         }
@@ -349,7 +612,7 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
         // Warp w takes n contiguous steps from ub in the probe-order
         // numbering (every warp within one step of the same count) and walks
         // them with a cursor held in registers: list, its boundary, the
-        // lane's row in it and the scan-word pointer.
+        // lane's row in it and the group's code bytes.
         const int total = s_lsteps[nl];
         const int per = total / WARPS, rem = total % WARPS;
         const int ub = w * per + min(w, rem);
@@ -365,23 +628,21 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
                 }
                 cl = lo;
             }
-            const uint4* sw4 = reinterpret_cast<const uint4*>(p.scanw);
             int cu = ub, cend = s_lsteps[cl + 1], crow = (ub - s_lsteps[cl]) * G + lane;
             int clen = s_llen[cl];
             const float* cterm = p.term + s_lstart[cl];
-            const uint4* csw = sw4 + ((int64_t)s_lsw[cl] + (int64_t)(ub - s_lsteps[cl]) * G) * (MP / 8) + lane;
-            // A step in flight: its words, its term (+inf past the list's end,
-            // where the words are not initialised and the lookup is skipped)
-            // and tag = probe position << 24 | row position in the list.
-            auto load_step = [&](uint4 (&sw)[MP / 8], float& term, int& tag) {
-#pragma unroll
-                for (int t = 0; t < MP / 8; t++) sw[t] = __ldg(csw + t * G);
+            const uint8_t* cgp = p.scanc + ((int64_t)s_lsw[cl] + (int64_t)(ub - s_lsteps[cl]) * G) * MP;
+            // A step in flight: its code words, its term (+inf past the
+            // list's end, where the codes are not initialised and the lookup
+            // is skipped) and tag = probe position << 24 | row position.
+            auto load_step = [&](uint32_t (&cw)[NW], float& term, int& tag) {
+                load_codes(cgp, cw);
                 term = crow < clen ? __ldg(cterm + crow) : pos_inf();
                 tag = (cl << 24) | crow;
                 cu++;
                 if (cu < cend) {
                     crow += G;
-                    csw += G * (MP / 8);
+                    cgp += G * MP;
                 } else if (cu < ub + n) {
                     do {
                         cl++;
@@ -390,13 +651,8 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
                     crow = lane;
                     clen = s_llen[cl];
                     cterm = p.term + s_lstart[cl];
-                    csw = sw4 + (int64_t)s_lsw[cl] * (MP / 8) + lane;
+                    cgp = p.scanc + (int64_t)s_lsw[cl] * MP;
                 }
-            };
-            auto compute = [&](const uint4 (&sw)[MP / 8], float term, int tag) {
-                const int li = tag >> 24;
-                const uint32_t k = term < pos_inf() ? lookup(sw, s_lbase[li] + term) : KEY_INF;
-                return k;
             };
             auto offer_tag = [&](uint32_t k, int tag) {
                 const bool pass = k < *(volatile uint32_t*)&s_tau;
@@ -410,33 +666,23 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
                         row[pos] = s_lstart[li] + (tag & 0xffffff);
                     }
                     count += __popc(bal);
-                    if (count > CAPW - 32) {
-                        __syncwarp();
-                        uint32_t kth;
-                        count = warp_select(key, seq, row, count, R, &kth, hist);
-                        if (lane == 0) atomicMin(&s_tau, kth);
-                        __syncwarp();
-                    }
+                    if (count > CAPW - 32) cut_back();
                 }
             };
-            // DEPTH steps in a ring: a step's words are loaded DEPTH - 1
-            // steps before it is computed. Two: a deeper ring spills
-            // registers at three blocks per SM, and the spills cost more
-            // than the latency it hides (2.06 ms against 2.43 ms for three
-            // and 4.19 ms for four on the 10M x 96 search).
-            uint4 sw[DEPTH][MP / 8];
-            float tm[DEPTH];
-            int tg[DEPTH];
+            // Two steps in a ring: a step's codes are loaded one step before
+            // it is computed.
+            uint32_t cw[2][NW];
+            float tm[2];
+            int tg[2];
+            load_step(cw[0], tm[0], tg[0]);
+            if (n > 1) load_step(cw[1], tm[1], tg[1]);
+            for (int i = 0; i < n; i += 2) {
 #pragma unroll
-            for (int d = 0; d < DEPTH; d++)
-                if (d < n) load_step(sw[d], tm[d], tg[d]);
-            for (int i = 0; i < n; i += DEPTH) {
-#pragma unroll
-                for (int d = 0; d < DEPTH; d++) {
+                for (int d = 0; d < 2; d++) {
                     if (i + d >= n) break;
-                    const uint32_t k = compute(sw[d], tm[d], tg[d]);
                     const int g0 = tg[d];
-                    if (i + d + DEPTH < n) load_step(sw[d], tm[d], tg[d]);
+                    const uint32_t k = tm[d] < pos_inf() ? lookup(cw[d], s_lbase[g0 >> 24] + tm[d]) : KEY_INF;
+                    if (i + d + 2 < n) load_step(cw[d], tm[d], tg[d]);
                     offer_tag(k, g0);
                 }
             }
@@ -450,28 +696,40 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
             float base;
             list_meta(li, start, sws, len, base);
             scanned += (unsigned long long)len;
-            uint4 sa[MP / 8], sb[MP / 8];
+            const uint8_t* gp = p.scanc + sws * MP;
+            uint32_t ca[NW], cbw[NW];
             float ta = 0.0f, tb = 0.0f;
-            bool va = act && lane < len;
-            if (va) load_row(sws, 0, start + lane, sa, ta);
+            bool va = lane < len;
+            if (va) {
+                load_codes(gp, ca);
+                ta = __ldg(p.term + start + lane);
+            }
             for (int st = 0; st * G < len; st += 2) {
                 const int r0 = st * G;
-                const bool vb = act && r0 + G + lane < len;
-                if (vb) load_row(sws, st + 1, start + r0 + G + lane, sb, tb);
-                offer(va ? lookup(sa, base + ta) : KEY_INF, li, start + r0 + lane);
+                const bool vb = r0 + G + lane < len;
+                if (vb) {
+                    load_codes(gp + (int64_t)(st + 1) * G * MP, cbw);
+                    tb = __ldg(p.term + start + r0 + G + lane);
+                }
+                offer(va ? lookup(ca, base + ta) : KEY_INF, li, start + r0 + lane);
                 if (r0 + G >= len) break;
-                va = act && r0 + 2 * G + lane < len;
-                if (va) load_row(sws, st + 2, start + r0 + 2 * G + lane, sa, ta);
-                offer(vb ? lookup(sb, base + tb) : KEY_INF, li, start + r0 + G + lane);
+                va = r0 + 2 * G + lane < len;
+                if (va) {
+                    load_codes(gp + (int64_t)(st + 2) * G * MP, ca);
+                    ta = __ldg(p.term + start + r0 + 2 * G + lane);
+                }
+                offer(vb ? lookup(cbw, base + tb) : KEY_INF, li, start + r0 + G + lane);
             }
         }
     }
     __syncwarp();
     {
         uint32_t kth;
+        const int before = count;
         count = warp_select(key, seq, row, count, R, &kth, hist);
         if (lane == 0) {
             s_wcount[w] = count;
+            if (before > count) s_dropped = 1;
             if (rows_scanned) atomicAdd(rows_scanned, scanned);
         }
     }
@@ -491,57 +749,62 @@ __global__ void __launch_bounds__(THREADS, 3) scan_skew_kernel(ScanParams p, con
         uint32_t kth;
         const int Rq = p.kq ? min(R, rerank_depth_for(p.kq[q], p.mode, p.rerank_fixed)) : R;
         const int kept = warp_select(mkey, mseq, mrow, total, Rq, &kth, hist);
+        uint32_t kmax = 0;
         for (int i = lane; i < R; i += 32) {
             const bool ok = i < kept;
             cand_row[q * R + i] = ok ? mrow[i] : -1;
             cand_d[q * R + i] = ok ? key_float(mkey[i]) : __int_as_float(0x7f800000);
             cand_seq[q * R + i] = ok ? mseq[i] : 0xffffffffu;
+            if (ok) kmax = max(kmax, mkey[i]);
+        }
+        if (HALF && p.scan_cut) {
+            // Every row left out has a screened distance at or above the
+            // largest kept one: the rerank proves the top k with it.
+            kmax = __reduce_max_sync(FULL, kmax);
+            const bool dropped = s_dropped != 0 || total > kept;
+            if (lane == 0) {
+                p.scan_cut[q] = dropped && kept > 0 ? key_float(kmax) : pos_inf();
+                p.scan_eps[q] = s_eps;
+            }
         }
     }
 }
 
-// Scan words of rows: for the row at position pos of its list (group
-// pos / G, lane l = pos mod G, copy c = l / M, rotation r = l mod M), word s
-// is the table offset of subquantizer m = (s + r) mod M: (code_m * 32 + c * M
-// + m) * 4; words past M are zero. A list's words start at slot sw_start
-// (MP words per slot); group g of G rows holds MP / 8 planes of G 8-word
-// chunks: word s of lane l sits at ((g * MP / 8 + s / 8) * G + l) * 8 + s % 8.
-__device__ __forceinline__ void write_scan_words(const uint8_t* __restrict__ codes, int M, int MP, int pos,
-                                                 uint16_t* __restrict__ list_words) {
-    const int copies = 32 / M, G = 32;
-    const int g = pos / G, l = pos - g * G, c = (l / M) % copies, r = l % M;
+// Scan codes of rows: for the row at position pos of its list (group
+// pos / 32, lane l = pos mod 32), byte s is the code of the subquantizer lane
+// l reads in step s (0 past M), at adc_code_pos(l, s, MP) in the group. A
+// list's codes start at slot sw_start (MP bytes per slot).
+__device__ __forceinline__ void write_scan_codes(const uint8_t* __restrict__ codes, int M, int MP, int pos,
+                                                 uint8_t* __restrict__ list_codes) {
+    const int g = pos >> 5, l = pos & 31;
+    uint8_t* gp = list_codes + (int64_t)g * 32 * MP;
     for (int s = 0; s < MP; s++) {
-        uint16_t v = 0;
-        if (s < M) {
-            int m = s + r;
-            if (m >= M) m -= M;
-            v = (uint16_t)(((int)codes[m] * 32 + c * M + m) * 4);
-        }
-        list_words[((int64_t)(g * (MP / 8) + s / 8) * G + l) * 8 + (s & 7)] = v;
+        const int m = adc_slot_m(l ^ s, s >= 16 ? 1 : 0, MP);
+        gp[adc_code_pos(l, s, MP)] = m < M ? codes[m] : (uint8_t)0;
     }
 }
 
 // One block per list: every slot in [start, start + len).
-__global__ void scan_words_lists_kernel(const uint8_t* __restrict__ codes, int code_stride, int M, int MP,
+__global__ void scan_codes_lists_kernel(const uint8_t* __restrict__ codes, int code_stride, int M, int MP,
                                         const int64_t* __restrict__ list_start, const int32_t* __restrict__ list_len,
-                                        const int64_t* __restrict__ sw_start, uint16_t* __restrict__ scanw) {
+                                        const int64_t* __restrict__ sw_start, uint8_t* __restrict__ scanc) {
     const int l = blockIdx.x;
     const int64_t start = list_start[l];
     const int len = list_len[l];
-    uint16_t* words = scanw + sw_start[l] * MP;
-    for (int j = threadIdx.x; j < len; j += blockDim.x) write_scan_words(codes + (start + j) * code_stride, M, MP, j, words);
+    uint8_t* out = scanc + sw_start[l] * MP;
+    for (int j = threadIdx.x; j < len; j += blockDim.x) write_scan_codes(codes + (start + j) * code_stride, M, MP, j, out);
 }
 
 // Rows at positions rows[i] of list cluster[i].
-__global__ void scan_words_rows_kernel(const uint8_t* __restrict__ codes, int code_stride, int M, int MP,
+__global__ void scan_codes_rows_kernel(const uint8_t* __restrict__ codes, int code_stride, int M, int MP,
                                        const int64_t* __restrict__ list_start, const int64_t* __restrict__ sw_start,
                                        const int64_t* __restrict__ rows, const int32_t* __restrict__ cluster,
-                                       int64_t n, uint16_t* __restrict__ scanw) {
+                                       int64_t n, uint8_t* __restrict__ scanc) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int64_t g = rows[i];
     const int c = cluster[i];
-    write_scan_words(codes + g * code_stride, M, MP, (int)(g - list_start[c]), scanw + sw_start[c] * MP);
+    write_scan_codes(codes + g * code_stride, M, MP, (int)(g - list_start[c]), scanc + sw_start[c] * MP);
 }
 
 __global__ void order_count_kernel(const int32_t* __restrict__ probe_ids, int64_t nq, int np_max,
@@ -653,46 +916,43 @@ cudaError_t launch_probe_order(const int32_t* probe_ids, int64_t nq, int np_max,
     return cudaGetLastError();
 }
 
-bool scan_skew_supported(int M) { return M >= 1 && M <= 32; }
-int scan_words_per_row(int M) { return (M + 7) / 8 * 8; }
+bool scan_adc_supported(int M) { return M >= 1 && M <= 32; }
+int scan_codes_per_row(int M) { return (M + 7) / 8 * 8; }
 int scan_group_rows(int) { return 32; }
 
-int scan_skew_capw(int R) {
+int scan_adc_capw(int R) {
     int c = 128;
     while (c < 2 * R + 64) c <<= 1;
     return c;
 }
 
-size_t scan_skew_smem(int R) {
-    return (size_t)WARPS * scan_skew_capw(R) * 12 + (size_t)WARPS * R * 12 + (size_t)WARPS * 256 * 4;
+size_t scan_adc_smem(int R, int M, int fp16) {
+    const size_t lut = (!fp16 && scan_codes_per_row(M) > 16) ? 65536 : 32768;
+    return lut + (size_t)WARPS * scan_adc_capw(R) * 12 + (size_t)WARPS * R * 12 + (size_t)WARPS * 256 * 4;
 }
 
-cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
-                             const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
-                             int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
-                             cudaStream_t s) {
+cudaError_t launch_scan_adc(const ScanParams& p, const float* queries, int64_t nq, const int32_t* probe_ids,
+                            const float* probe_d, const int32_t* nprobe, int np_max, const int32_t* fallback, int R,
+                            int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
+                            cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
-    if (!scan_skew_supported(p.M) || !p.scanw) return cudaErrorInvalidValue;
-    int CAPW = scan_skew_capw(R);
-    const size_t smem = scan_skew_smem(R);
+    if (!scan_adc_supported(p.M) || !p.scanc) return cudaErrorInvalidValue;
+    const bool half = p.adc16 != 0 && p.adc_cb != nullptr;
+    int CAPW = scan_adc_capw(R);
+    const size_t smem = scan_adc_smem(R, p.M, half ? 1 : 0);
     const void* fn;
-    switch (p.M) {
-    case 8: fn = (const void*)scan_skew_kernel<8, 8, 2>; break;
-    case 16: fn = (const void*)scan_skew_kernel<16, 16, 2>; break;
-    case 24: fn = (const void*)scan_skew_kernel<24, 24, 2>; break;
-    case 32: fn = (const void*)scan_skew_kernel<32, 32, 2>; break;
-    default:
-        switch (scan_words_per_row(p.M) / 8) {
-        case 1: fn = (const void*)scan_skew_kernel<8, 0, 2>; break;
-        case 2: fn = (const void*)scan_skew_kernel<16, 0, 2>; break;
-        case 3: fn = (const void*)scan_skew_kernel<24, 0, 2>; break;
-        case 4: fn = (const void*)scan_skew_kernel<32, 0, 2>; break;
-        default: return cudaErrorInvalidValue;
-        }
+    switch (scan_codes_per_row(p.M)) {
+    case 8: fn = half ? (const void*)scan_adc_kernel<8, true> : (const void*)scan_adc_kernel<8, false>; break;
+    case 16: fn = half ? (const void*)scan_adc_kernel<16, true> : (const void*)scan_adc_kernel<16, false>; break;
+    case 24: fn = half ? (const void*)scan_adc_kernel<24, true> : (const void*)scan_adc_kernel<24, false>; break;
+    case 32: fn = half ? (const void*)scan_adc_kernel<32, true> : (const void*)scan_adc_kernel<32, false>; break;
+    default: return cudaErrorInvalidValue;
     }
+    ScanParams pp = p;
+    if (!half) pp.scan_cut = nullptr;  // the FP32 screen is not checked
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    void* args[] = {(void*)&p, (void*)&queries, (void*)&probe_d, (void*)&probe_ids, (void*)&nprobe, (void*)&np_max,
+    void* args[] = {(void*)&pp, (void*)&queries, (void*)&probe_d, (void*)&probe_ids, (void*)&nprobe, (void*)&np_max,
                     (void*)&fallback, (void*)&R, (void*)&CAPW, (void*)&cand_row, (void*)&cand_d, (void*)&cand_seq,
                     (void*)&rows_scanned};
     e = cudaLaunchKernel(fn, dim3((unsigned)nq), dim3(THREADS), args, smem, s);
@@ -700,21 +960,21 @@ cudaError_t launch_scan_skew(const ScanParams& p, const float* queries, int64_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_scan_words_lists(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
-                                    const int32_t* list_len, const int64_t* sw_start, int nlist, uint16_t* scanw,
+cudaError_t launch_scan_codes_lists(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+                                    const int32_t* list_len, const int64_t* sw_start, int nlist, uint8_t* scanc,
                                     cudaStream_t s) {
-    if (nlist <= 0 || !scan_skew_supported(M)) return cudaSuccess;
-    scan_words_lists_kernel<<<(unsigned)nlist, 128, 0, s>>>(codes, code_stride, M, scan_words_per_row(M),
-                                                            list_start, list_len, sw_start, scanw);
+    if (nlist <= 0 || !scan_adc_supported(M)) return cudaSuccess;
+    scan_codes_lists_kernel<<<(unsigned)nlist, 128, 0, s>>>(codes, code_stride, M, scan_codes_per_row(M),
+                                                            list_start, list_len, sw_start, scanc);
     return cudaGetLastError();
 }
 
-cudaError_t launch_scan_words_rows(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
+cudaError_t launch_scan_codes_rows(const uint8_t* codes, int code_stride, int M, const int64_t* list_start,
                                    const int64_t* sw_start, const int64_t* rows, const int32_t* cluster, int64_t n,
-                                   uint16_t* scanw, cudaStream_t s) {
-    if (n <= 0 || !scan_skew_supported(M)) return cudaSuccess;
-    scan_words_rows_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(codes, code_stride, M, scan_words_per_row(M),
-                                                                      list_start, sw_start, rows, cluster, n, scanw);
+                                   uint8_t* scanc, cudaStream_t s) {
+    if (n <= 0 || !scan_adc_supported(M)) return cudaSuccess;
+    scan_codes_rows_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(codes, code_stride, M, scan_codes_per_row(M),
+                                                                      list_start, sw_start, rows, cluster, n, scanc);
     return cudaGetLastError();
 }
 

@@ -438,9 +438,9 @@ cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, c
                         int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
                         cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
-    if (scan_skew_supported(p.M) && p.scanw && scan_skew_smem(R) + 32 * 1024 <= 200 * 1024)
-        return launch_scan_skew(p, queries, nq, probe_ids, probe_d, nprobe, np_max, fallback, R, cand_row, cand_d,
-                                cand_seq, rows_scanned, s);
+    if (scan_adc_supported(p.M) && p.scanc && scan_adc_smem(R, p.M, p.adc16 && p.adc_cb) <= 224 * 1024)
+        return launch_scan_adc(p, queries, nq, probe_ids, probe_d, nprobe, np_max, fallback, R, cand_row, cand_d,
+                               cand_seq, rows_scanned, s);
     const int CAPW = cap_for(R);
     int P = 1;
     while (P < SC_WARPS * R) P <<= 1;
@@ -483,6 +483,14 @@ struct ReconRow {
         return __fadd_rn(c[i], cb[((int64_t)m * pqK + code[m]) * dsub + e]);
     }
 };
+
+// Whether the k-th reference distance dk proves a screened query's top k:
+// every row the scan left out has a screened distance at or above cut, so an
+// exact PQ distance above cut - eps, and FP32 roundings of the reference's
+// distance and of the screen are far below 2e-5 of the values compared.
+__device__ __forceinline__ bool proven(float dk, float cut, float eps) {
+    return cut == __int_as_float(0x7f800000) || dk + 2e-5f * (fabsf(cut) + fabsf(dk)) + eps < cut;
+}
 
 constexpr int RR_THREADS = 256;
 constexpr int RW_MAX = 128;  // candidates per query up to which one warp reranks a query
@@ -537,6 +545,10 @@ __global__ void __launch_bounds__(RR_THREADS) rerank_warp_kernel(ScanParams p, c
     __syncwarp();
     warp_sort_cand(cd, cs, cr, RP);
     const int k = min(kq[q], valid);
+    if (lane == 0 && mode == 0 && p.scan_cut && k > 0 && k == kq[q] && !proven(cd[k - 1], p.scan_cut[q], p.scan_eps[q])) {
+        p.redo[atomicAdd(p.redo_count, 1)] = (int32_t)q;
+        if (p.redo_total) atomicAdd(p.redo_total, 1ull);
+    }
     for (int i = lane; i < kmax; i += 32) {
         if (i < k) {
             ids[q * kmax + i] = p.row_id[cr[i]];
@@ -593,6 +605,10 @@ __global__ void __launch_bounds__(RR_THREADS) rerank_kernel(ScanParams p, const 
     __syncthreads();
     block_sort_cand(cd, cs, cr, RP);
     const int k = min(kq[q], s_valid);
+    if (tid == 0 && mode == 0 && p.scan_cut && k > 0 && k == kq[q] && !proven(cd[k - 1], p.scan_cut[q], p.scan_eps[q])) {
+        p.redo[atomicAdd(p.redo_count, 1)] = (int32_t)q;
+        if (p.redo_total) atomicAdd(p.redo_total, 1ull);
+    }
     for (int i = tid; i < kmax; i += RR_THREADS) {
         if (i < k) {
             ids[q * kmax + i] = p.row_id[cr[i]];

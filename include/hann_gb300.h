@@ -178,6 +178,17 @@ int hann_pqivf_tune_candidate_clusters(hann_pqivf* h, const float* queries, int6
                                        const int64_t* ground_truth, int32_t apply, int32_t* chosen,
                                        int32_t* tried_out, double* recall_out, int32_t* n_tried);
 
+/* Lookup tables of the list scan in FP16 (on = 1, the default) or FP32
+ * (on = 0). The reference decodes every candidate in FP32
+ * (pqivf/index.go:909-923); here the scan screens candidates with per-query
+ * tables and the rerank computes the reference's distance. FP16 tables take
+ * half the shared memory and read without bank conflicts; in parity mode
+ * (mode 0) each query's top k is proven against the FP16 screen's error
+ * bound, and queries it cannot prove are scanned again with FP32 tables, so
+ * parity-mode results do not depend on this switch. In exact-rerank mode
+ * (mode 1) the candidates screened can differ in the last few places. */
+int hann_pqivf_set_adc_fp16(hann_pqivf* h, int32_t on);
+
 /* Switches the plain-FP32 mode of hann_pqivf_options at run time (no
  * reference counterpart; results do not change). */
 int hann_pqivf_set_plain_fp32(hann_pqivf* h, int32_t on);
@@ -202,7 +213,7 @@ int hann_pqivf_list_lengths(hann_pqivf* h, int64_t* out, int32_t capacity, int32
  * captured), or a process whose device-memory budget is fixed at start-up.
  * All scratch comes from one fixed 16 MiB device array that every GPU which
  * loads this library holds until the process exits; a batch whose scratch
- * (about nq * (4 * nlist + 8 * nprobe + 12 * rerank depth + 12) bytes) does
+ * (about nq * (4 * nlist + 8 * nprobe + 12 * rerank depth + 24) bytes) does
  * not fit is rejected with HANN_E_UNSUPPORTED and a message that says so.
  * The coarse distances dominate: every query needs a full row of them, so
  * the number of queries per call is small when the index has many lists

@@ -43,6 +43,11 @@ int hann_pqivf_rows_decoded(void* h, int64_t* out);
  * In mode 0 results do not depend on them. */
 int hann_pqivf_scan_options(void* h, const int32_t* set8, int32_t* get8);
 
+/* Queries, over the handle's life, whose parity-mode top k the FP16
+ * lookup-table screen could not prove and that were scanned again with FP32
+ * tables (waits for the handle's searches). */
+int hann_pqivf_adc_redos(void* h, int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -108,9 +108,11 @@ ARENA = 16 << 20
 
 
 def _scratch_bytes(nq, nlist, nprobe, R):
-    """The entry point's scratch layout: every region rounded to 256 bytes."""
+    """The entry point's scratch layout: every region rounded to 256 bytes
+    (the parity-mode proof's cut, bound and rescan list included)."""
     a = lambda b: (b + 255) // 256 * 256  # noqa: E731
-    return a(nq * nlist * 4) + 2 * a(nq * nprobe * 4) + 3 * a(nq * 4) + 3 * a(nq * R * 4)
+    return (a(nq * nlist * 4) + 2 * a(nq * nprobe * 4) + 5 * a(nq * 4) + 3 * a(nq * R * 4)
+            + a((nq + 1) * 4))
 
 
 def _compare(idx, L, noalloc, q, k, nprobe, mode, stream, torch):
@@ -146,7 +148,7 @@ def test_noalloc_batch_filling_the_arena(index):
     nq = ARENA // (4 * nlist)
     while _scratch_bytes(nq, nlist, nprobe, R) > ARENA:
         nq -= 1
-    assert ARENA - _scratch_bytes(nq, nlist, nprobe, R) < _scratch_bytes(1, nlist, nprobe, R) + 8 * 256
+    assert ARENA - _scratch_bytes(nq, nlist, nprobe, R) < _scratch_bytes(1, nlist, nprobe, R) + 10 * 256
     q = torch.from_numpy(rng.normal(size=(nq, 32)).astype(np.float32)).cuda()
     _compare(idx, L, noalloc, q, k, nprobe, 0, torch.cuda.current_stream().cuda_stream, torch)
     # one query more no longer fits and is refused
