@@ -104,7 +104,7 @@ EXPORTED = (
     "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot", "hann_pqivf_retrain", "hann_gob_encode",
     "hann_gob_decode", "hann_gob_state_layout", "hann_gob_state_arrays", "hann_gob_state_free",
     "hann_gob_last_error", "hann_gob_encode_payload", "hann_pqivf_tune_candidate_clusters",
-    "hann_pqivf_autotune_scan", "hann_pqivf_set_adc_fp16",
+    "hann_pqivf_autotune_scan", "hann_pqivf_set_adc_tables",
 )
 # Entry points of include/hann_gb300_diag.h.
 EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats", "hann_pqivf_rows_decoded", "hann_pqivf_adc_redos",
@@ -149,7 +149,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_gpu_distance_batch.argtypes = [ctypes.c_int32, _P, _P, ctypes.c_size_t, ctypes.c_size_t, _P]
         L.hann_pqivf_set_profiling.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
-        L.hann_pqivf_set_adc_fp16.argtypes = [_P, ctypes.c_int32]
+        L.hann_pqivf_set_adc_tables.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_adc_redos.argtypes = [_P, _P]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_autotune_scan.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P, _P, _P]
@@ -461,10 +461,15 @@ class Index:
         """Switch the FP32 SIMT-only mode (same results, no tensor cores)."""
         self._check(self._L.hann_pqivf_set_plain_fp32(self._h, 1 if on else 0))
 
-    def SetADCFP16(self, on: bool) -> None:
-        """FP16 (default) or FP32 lookup tables in the list scan. Parity-mode
-        results do not change; exact-rerank candidates can."""
-        self._check(self._L.hann_pqivf_set_adc_fp16(self._h, 1 if on else 0))
+    ADC_TABLES = {"fp32": 0, "fp16": 1, "fixed16": 2}
+
+    def SetADCTables(self, kind: str) -> None:
+        """Lookup tables of the list scan: "fixed16" (default), "fp16" or
+        "fp32". Parity-mode results do not change; exact-rerank candidates
+        can at the rerank depth."""
+        if kind not in self.ADC_TABLES:
+            raise ValueError(f"unknown lookup-table kind {kind!r}")
+        self._check(self._L.hann_pqivf_set_adc_tables(self._h, self.ADC_TABLES[kind]))
 
     def ADCRedos(self) -> int:
         """Parity-mode queries the FP16 screen could not prove, scanned again

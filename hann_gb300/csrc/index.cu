@@ -997,7 +997,7 @@ static int run_lms(hann_pqivf* h, SearchScratch& sc, const float* qp, int64_t nc
         ScanParams ps = h->scan_params();
         ps.mode = mode;
         ps.kq = d_k;
-        ps.adc16 = 0;  // the thresholds must bound exact distances: FP32 tables
+        ps.adc_table = 0;  // the thresholds must bound exact distances: FP32 tables
         CK(launch_fill_i32(sc.lones.p, nc, 1, s));
         CK(cudaMemsetAsync(sc.lzeros.p, 0, sizeof(int32_t) * (size_t)nc, s));
         CK(launch_scan(ps, qp, nc, sc.probe_ids.p, sc.probe_d.p, sc.lones.p, np_max, sc.lzeros.p, R, sc.cand_row.p,
@@ -1089,7 +1089,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
     // Parity mode with FP16 tables: the rerank proves each query's top k
     // from the scan's cut and lists the queries it cannot prove, which are
     // scanned and reranked again with FP32 tables.
-    const bool check = mode == 0 && p.adc16 && p.scanc && scan_adc_supported(h->o.num_subquantizers);
+    const bool check = mode == 0 && p.adc_table && p.scanc && scan_adc_supported(h->o.num_subquantizers);
     auto scan_rerank = [&](int64_t q0, int64_t nc, const float* qp, const int32_t* qorder) -> int {
         p.kq = d_k + q0;
         ScanParams pt = p;  // the table scan: every query, or those the list-major scan leaves
@@ -1129,7 +1129,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
         h->launches += 2;
         if (check) {
             ScanParams pf = p;
-            pf.adc16 = 0;
+            pf.adc_table = 0;
             pf.qorder = sc.credo.p;
             pf.qcount = sc.credo.p + nc;
             CK(launch_scan(pf, qp, nc, sc.probe_ids.p, sc.probe_d.p, d_np + q0, np_max, sc.fb.p, R, sc.cand_row.p,
@@ -1658,13 +1658,14 @@ int hann_pqivf_set_candidate_clusters(hann_pqivf* h, int32_t n) {
     return HANN_OK;
 }
 
-int hann_pqivf_set_adc_fp16(hann_pqivf* h, int32_t on) {
+int hann_pqivf_set_adc_tables(hann_pqivf* h, int32_t kind) {
     if (!h) return HANN_E_INVALID;
+    if (kind < HANN_ADC_FP32 || kind > HANN_ADC_FIXED16) return h->fail(HANN_E_INVALID, "unknown lookup-table kind %d", kind);
     std::unique_lock<std::mutex> w(h->wmu);
     std::unique_lock<std::shared_mutex> g(h->mu);
     cudaSetDevice(h->o.device);
     CK(wait_device_searches(h));
-    h->adc16 = on ? 1 : 0;
+    h->adc_table = kind;
     return HANN_OK;
 }
 
@@ -2393,7 +2394,7 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
                            h->d_fb_dev.p, s));
     // parity mode with FP16 tables: queries the rerank cannot prove from the
     // scan's cut are scanned again with FP32 tables (as in run_search)
-    const bool check = mode == 0 && p.adc16 && p.scanc && scan_adc_supported(h->o.num_subquantizers);
+    const bool check = mode == 0 && p.adc_table && p.scanc && scan_adc_supported(h->o.num_subquantizers);
     if (check) {
         p.scan_cut = scut;
         p.scan_eps = seps;
@@ -2406,7 +2407,7 @@ extern "C" int hann_pqivf_search_batch_device_noalloc(hann_pqivf* h, const float
     h->launches += 5;  // fill, distance matrix, probe select, scan, rerank
     if (check) {
         ScanParams pf = p;
-        pf.adc16 = 0;
+        pf.adc_table = 0;
         pf.scan_cut = nullptr;
         pf.qorder = redo;
         pf.qcount = redo + nq;

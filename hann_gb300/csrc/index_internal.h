@@ -227,12 +227,12 @@ struct hann_pqivf {
 
     DBuf<float> d_coarse, d_codebooks, d_vectors, d_term;
     DBuf<float> d_codebooks_t;  // [pqK][M][dsub], the scan's table-build layout
-    // FP16 lookup tables: centred codebooks in the table-build layout, the
+    // 16-bit lookup tables: centred codebooks in the table-build layout, the
     // means, each subquantizer's largest centred codeword norm and the
     // bounds on ||r|| and |term| (prepare_adc)
     DBuf<float> d_adc_cb, d_adc_mu, d_adc_rm;
     float adc_rfull = 0.0f, adc_tbound = 0.0f;
-    int adc16 = 1;              // FP16 tables in the table scan (hann_pqivf_set_adc_fp16)
+    int adc_table = 2;          // table scan's lookup tables: 0 FP32, 1 FP16, 2 fixed point (hann_pqivf_set_adc_tables)
     DBuf<unsigned long long> d_adc_redo;  // queries scanned again with FP32 tables (diagnostic)
     // BF16 copy of the coarse centroids for the tensor-core preselection
     int kp = 0;
@@ -322,7 +322,7 @@ struct hann_pqivf {
         p.adc_rm = d_adc_rm.p;
         p.adc_rfull = adc_rfull;
         p.adc_tbound = adc_tbound;
-        p.adc16 = adc16 && d_adc_cb.p ? 1 : 0;
+        p.adc_table = d_adc_cb.p ? adc_table : 0;
         p.scan_cut = nullptr;
         p.scan_eps = nullptr;
         p.redo = nullptr;

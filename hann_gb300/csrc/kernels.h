@@ -149,10 +149,10 @@ struct ScanParams {
     const float* adc_rm;      // [M] largest ||codeword - mean|| per subquantizer
     float adc_rfull;          // bound on ||r|| over every residual the codebooks reconstruct
     float adc_tbound;         // bound on |term| = | ||r||^2 + 2 <c, r> |
-    int adc16;                // 1: FP16 tables (0: FP32)
-    float* scan_cut;          // [nq] parity mode, FP16 tables: no row left out screened below it
+    int adc_table;            // lookup tables: 0 FP32, 1 FP16, 2 16-bit fixed point
+    float* scan_cut;          // [nq] parity mode, 16-bit tables: no row left out screened below it
     float* scan_eps;          // [nq] bound on the screen's error
-    int32_t* redo;            // rerank: queries whose top k the FP16 screen cannot prove ...
+    int32_t* redo;            // rerank: queries whose top k the 16-bit screen cannot prove ...
     int32_t* redo_count;      // ... and their count
     unsigned long long* redo_total;  // optional: running count of those queries
     const float* term;        // [rows]

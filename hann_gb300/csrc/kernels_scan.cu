@@ -33,6 +33,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -47,12 +48,24 @@ constexpr uint32_t KEY_INF = 0xff800000u;  // float_key(+inf)
 __device__ __forceinline__ float pos_inf() { return __int_as_float(0x7f800000); }
 constexpr int SCAN_FLAT_LISTS = 128;        // probe lists held for the balanced schedule
 
+// A warp's buffer held in the free halves of a striped lookup table (rows of
+// 256 bytes whose first 128 hold the table): element i sits in row i / 32
+// of the buffer's rows, at byte 128 + 4 (i % 32).
+extern __shared__ __align__(16) unsigned char scan_smem[];  // the scan kernel's dynamic shared memory
+template <class T>
+struct Stripe {
+    uint32_t off;  // byte offset of the buffer's first element in scan_smem
+    __device__ __forceinline__ T& operator[](int i) const {
+        return *reinterpret_cast<T*>(scan_smem + off + ((i >> 5) << 8) + ((i & 31) << 2));
+    }
+};
+
 // Keeps the `R` smallest keys of entries [0, count) (ties at the cut broken
 // by position), compacted in place to [0, R). Returns through *kth a key at
 // or above the R-th smallest (exactly it unless the digit holding the cut
 // came out whole). hist: the warp's 256 counters. Warp-synchronous.
-__device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count, int R, uint32_t* kth,
-                           uint32_t* hist) {
+template <class KB, class SB, class RB, class HB>
+__device__ int warp_select(KB key, SB seq, RB row, int count, int R, uint32_t* kth, HB hist) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     if (count <= R) {
@@ -171,8 +184,8 @@ __device__ int warp_select(uint32_t* key, uint32_t* seq, int32_t* row, int count
 // becomes the bin's (exclusive) upper edge, at or above the R-th smallest.
 // Falls back to warp_select when the kept keys would pass `limit`.
 // Warp-synchronous.
-__device__ int warp_cut(uint32_t* key, uint32_t* seq, int32_t* row, int count, int R, int limit, uint32_t* tau,
-                        uint32_t* hist) {
+template <class KB, class SB, class RB, class HB>
+__device__ int warp_cut(KB key, SB seq, RB row, int count, int R, int limit, uint32_t* tau, HB hist) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const int nch = (count + 31) >> 5;
@@ -196,7 +209,7 @@ __device__ int warp_cut(uint32_t* key, uint32_t* seq, int32_t* row, int count, i
     __syncwarp();
     for (int ch = 0; ch < nch; ch++) {
         const int i = ch * 32 + lane;
-        if (i < count) atomicAdd(&hist[(key[i] >> lo) & dmask], 1u);
+        if (i < count) atomicAdd(&hist[(key[i] >> lo) & dmask], 1u);  // hist[] is a reference
     }
     __syncwarp();
     uint32_t cnt[8], tot = 0;
@@ -317,7 +330,12 @@ __host__ __device__ __forceinline__ int adc_code_pos(int l, int s, int MP) {
     return (s >> 4) < full ? 512 * (s >> 4) + 16 * l + (s & 15) : 512 * full + 8 * l + (s & 7);
 }
 
-template <int MP, bool HALF>
+// TAB: 0 FP32 entries, 1 FP16, 2 16-bit fixed point. STRIPED (16-bit
+// entries only): 256-byte table rows whose second halves hold the warps'
+// candidate buffers and histograms (one warp buffer of 256 entries, a rerank
+// depth of at most 96), so that a table offset is the byte permute's result
+// with no shift; otherwise 16-bit entries sit in 128-byte rows.
+template <int MP, int TAB, bool STRIPED>
 __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, const float* __restrict__ Q,
                                                            const float* __restrict__ probe_d,
                                                            const int32_t* __restrict__ probe_ids,
@@ -327,21 +345,27 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
                                                            float* __restrict__ cand_d,
                                                            uint32_t* __restrict__ cand_seq,
                                                            unsigned long long* __restrict__ rows_scanned) {
+    constexpr bool HALF = TAB >= 1;             // 16-bit entries
+    constexpr bool FIXED = TAB == 2;
+    static_assert(HALF || !STRIPED, "striped tables hold 16-bit entries");
     constexpr bool WIDE = !HALF && MP > 16;     // FP32 entries, 256-byte rows
-    constexpr int LUT_BYTES = WIDE ? 65536 : 32768;
-    constexpr int SHIFT = WIDE ? 0 : 1;        // table offset = (code * 256 + offset byte) >> SHIFT
+    constexpr int ROWB = (WIDE || STRIPED) ? 256 : 128;  // bytes per table row
+    constexpr int LUT_BYTES = ROWB * 256;
+    constexpr int SHIFT = ROWB == 128 ? 1 : 0;  // table offset = (code * 256 + offset byte) >> SHIFT
     constexpr int NW = MP / 4;                  // code words per row
     constexpr int NOB = (MP + 2) / 3;           // offset registers: three offset bytes and a zero byte
     constexpr int G = 32;
-    extern __shared__ __align__(16) unsigned char smraw[];
+    unsigned char* const smraw = scan_smem;
     unsigned char* lutb = smraw;
+    // flat layout: [table][warp buffers][merge region][histograms];
+    // striped: [table with buffers and histograms][merge region]
     uint32_t* wkey = reinterpret_cast<uint32_t*>(smraw + LUT_BYTES);
-    uint32_t* wseq = wkey + WARPS * CAPW;
-    int32_t* wrow = reinterpret_cast<int32_t*>(wseq + WARPS * CAPW);
-    uint32_t* mkey = reinterpret_cast<uint32_t*>(wrow + WARPS * CAPW);  // [WARPS * R] merge region
+    uint32_t* wseq = wkey + (STRIPED ? 0 : WARPS * CAPW);
+    int32_t* wrow = reinterpret_cast<int32_t*>(wseq + (STRIPED ? 0 : WARPS * CAPW));
+    uint32_t* mkey = reinterpret_cast<uint32_t*>(wrow + (STRIPED ? 0 : WARPS * CAPW));  // [WARPS * R] merge region
     uint32_t* mseq = mkey + WARPS * R;
     int32_t* mrow = reinterpret_cast<int32_t*>(mseq + WARPS * R);
-    uint32_t* whist = reinterpret_cast<uint32_t*>(mrow + WARPS * R);   // [WARPS][256]
+    uint32_t* whist = reinterpret_cast<uint32_t*>(mrow + WARPS * R);   // [WARPS][256] (flat layout)
     __shared__ uint32_t s_tau;
     __shared__ int s_big, s_dropped;
     __shared__ int s_wcount[WARPS];
@@ -363,13 +387,15 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
     // each), so the build needs no barrier before it.
     float scale = 1.0f, inv = 1.0f, c0 = 0.0f;
     if (HALF) {
-        // FP16 entries -2 <q_m, c_mj - mu_m> scaled by 2^e, so that the bound
-        // b_m = 2 ||q_m|| max_j ||c_mj - mu_m|| of the largest is at most
-        // 2^15; the means' part, -2 <q, mu>, joins each list's base. Rounding
-        // one entry errs by at most 2^-11 of b_m (2^-25 below FP16's normal
-        // range), so a row's screened distance is within eps of the exact
-        // sum (with a relative allowance for the FP32 roundings of the
-        // decomposition).
+        // 16-bit entries of -2 <q_m, c_mj - mu_m>, |.| <= b_m = 2 ||q_m||
+        // max_j ||c_mj - mu_m||; the means' part, -2 <q, mu>, joins each
+        // list's base. FP16: scaled by 2^e so that the largest b_m is at most
+        // 2^15; rounding one entry errs by at most 2^-11 of b_m (2^-25 below
+        // FP16's normal range). Fixed point: integers of the entry times
+        // 32767 / max_m b_m, rounded to nearest (at most half a unit, and a
+        // row's sum of them is exact in 32-bit integers). Either way a row's
+        // screened distance is within eps of the exact sum (with a relative
+        // allowance for the FP32 roundings of the decomposition).
         float bm = 0.0f;
         if (lane < M) {
             float qq = 0.0f;
@@ -388,16 +414,23 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
             cq += __shfl_xor_sync(FULL, cq, o);
             qn += __shfl_xor_sync(FULL, qn, o);
         }
-        int ex = 0;
         const bool finite = mx > 0.0f && mx < pos_inf();
-        if (finite) frexpf(mx, &ex);
-        const int e = finite ? max(-120, min(120, 15 - ex)) : 0;
-        scale = ldexpf(1.0f, e);
-        inv = ldexpf(1.0f, -e);
+        float round_err;
+        if (FIXED) {
+            scale = finite ? 32767.0f / mx : 1.0f;
+            inv = 1.0f / scale;
+            round_err = (float)MP * 0.51f * inv;
+        } else {
+            int ex = 0;
+            if (finite) frexpf(mx, &ex);
+            const int e = finite ? max(-120, min(120, 15 - ex)) : 0;
+            scale = ldexpf(1.0f, e);
+            inv = ldexpf(1.0f, -e);
+            round_err = 4.8828125e-4f * sum + (float)MP * 2.98023224e-8f * inv;
+        }
         c0 = -2.0f * cq;
         if (tid == 0)
-            s_eps = 4.8828125e-4f * sum + (float)MP * 2.98023224e-8f * inv +
-                    1e-5f * (2.0f * sqrtf(qn) * p.adc_rfull + p.adc_tbound + 2.0f * fabsf(cq));
+            s_eps = round_err + 1e-5f * (2.0f * sqrtf(qn) * p.adc_rfull + p.adc_tbound + 2.0f * fabsf(cq));
     }
     {
         // Table build: warp w takes code values w, w + 8, ...; lane l < M
@@ -408,13 +441,17 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
         int bs[4] = {0, 0, 0, 0}, hs[4] = {0, 0, 0, 0};
         const int ns = lane < M ? adc_slots(lane, MP, bs, hs) : 0;
         auto put = [&](int j, float acc) {
-            if (HALF) {
+            if (FIXED) {
+                const int qi = max(-32767, min(32767, __float2int_rn(-2.0f * acc * scale)));
+                for (int i = 0; i < ns; i++)
+                    *reinterpret_cast<short*>(lutb + j * ROWB + 4 * bs[i] + 2 * hs[i]) = (short)qi;
+            } else if (HALF) {
                 const __half hv = __float2half_rn(-2.0f * acc * scale);
-                for (int i = 0; i < ns; i++) *reinterpret_cast<__half*>(lutb + j * 128 + 4 * bs[i] + 2 * hs[i]) = hv;
+                for (int i = 0; i < ns; i++) *reinterpret_cast<__half*>(lutb + j * ROWB + 4 * bs[i] + 2 * hs[i]) = hv;
             } else {
                 const float v = -2.0f * acc;
                 for (int i = 0; i < ns; i++)
-                    *reinterpret_cast<float*>(lutb + j * (WIDE ? 256 : 128) + 4 * bs[i] + 128 * hs[i]) = v;
+                    *reinterpret_cast<float*>(lutb + j * ROWB + 4 * bs[i] + 128 * hs[i]) = v;
             }
         };
         const bool v4 = p.dsub == 4 &&
@@ -473,17 +510,31 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
             const int s = 3 * i + kk;
             if (s < MP) {
                 const uint32_t b = (uint32_t)(lane ^ s), hh = s >= 16 ? 1u : 0u;
-                const uint32_t o = WIDE ? 4u * b + 128u * hh : 8u * b + 4u * hh;
+                const uint32_t io = HALF ? 4u * b + 2u * hh : 4u * b + 128u * hh;  // in-row offset
+                const uint32_t o = io << SHIFT;
                 v |= o << (8 * kk);
             }
         }
         ob[i] = v;
     }
     __syncthreads();
-    uint32_t* key = wkey + w * CAPW;
-    uint32_t* seq = wseq + w * CAPW;
-    int32_t* row = wrow + w * CAPW;
-    uint32_t* hist = whist + w * 256;
+    // warp w's buffers: flat, or rows 24 w.. (keys, positions, rows: eight
+    // rows of 32 each) and 192 + 8 w.. (histogram) of the striped table
+    using KB = typename std::conditional<STRIPED, Stripe<uint32_t>, uint32_t*>::type;
+    using RB = typename std::conditional<STRIPED, Stripe<int32_t>, int32_t*>::type;
+    KB key, seq, hist;
+    RB row;
+    if constexpr (STRIPED) {
+        key = KB{(uint32_t)(128 + (24 * w) * 256)};
+        seq = KB{(uint32_t)(128 + (24 * w + 8) * 256)};
+        row = RB{(uint32_t)(128 + (24 * w + 16) * 256)};
+        hist = KB{(uint32_t)(128 + (192 + 8 * w) * 256)};
+    } else {
+        key = wkey + w * CAPW;
+        seq = wseq + w * CAPW;
+        row = wrow + w * CAPW;
+        hist = whist + w * 256;
+    }
     const bool fb = fallback[q] != 0;
     const int nl = fb ? p.nlist : min(nprobe[q], p.nlist);
     const unsigned ltm = (1u << lane) - 1u;
@@ -524,9 +575,24 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
         }
     };
     // A lookup is one byte permute (code byte and offset byte into a table
-    // offset), one shift, one shared load and one add; four partial sums
-    // keep the adds off one long dependency chain.
+    // offset; plus a shift in 128-byte rows), one shared load and an add:
+    // FP32 and FP16 entries into four FP32 partial sums, fixed-point entries
+    // two at a time into two integer sums (three-input adds).
     auto lookup = [&](const uint32_t (&cw)[NW], float bt) {
+        if constexpr (FIXED) {
+            int acc[2] = {0, 0};
+#pragma unroll
+            for (int s = 0; s < MP; s += 2) {
+                const uint32_t sa = (uint32_t)(4 + s % 3) | ((uint32_t)(s % 4) << 4) | 0x7700u;
+                const uint32_t sb = (uint32_t)(4 + (s + 1) % 3) | ((uint32_t)((s + 1) % 4) << 4) | 0x7700u;
+                const uint32_t a = __byte_perm(cw[s / 4], ob[s / 3], sa) >> SHIFT;
+                const uint32_t b = __byte_perm(cw[(s + 1) / 4], ob[(s + 1) / 3], sb) >> SHIFT;
+                const int x = *reinterpret_cast<const short*>(lutb + a);
+                const int y = *reinterpret_cast<const short*>(lutb + b);
+                acc[(s >> 1) & 1] += x + y;
+            }
+            return float_key(fmaf((float)(acc[0] + acc[1]), inv, bt));
+        }
         float part[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
         for (int s = 0; s < MP; s++) {
@@ -937,19 +1003,32 @@ cudaError_t launch_scan_adc(const ScanParams& p, const float* queries, int64_t n
                             cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
     if (!scan_adc_supported(p.M) || !p.scanc) return cudaErrorInvalidValue;
-    const bool half = p.adc16 != 0 && p.adc_cb != nullptr;
+    const int tab = p.adc_cb != nullptr && p.adc_table >= 1 && p.adc_table <= 2 ? p.adc_table : 0;
     int CAPW = scan_adc_capw(R);
-    const size_t smem = scan_adc_smem(R, p.M, half ? 1 : 0);
-    const void* fn;
+    const size_t smem = scan_adc_smem(R, p.M, tab != 0 ? 1 : 0);
+    // 16-bit tables with one 256-entry warp buffer take the striped layout
+    // (the same bytes as the flat one: 64 KB of table rows and buffers)
+    const bool striped = tab != 0 && CAPW == 256;
+    const int variant = tab == 0 ? 0 : 2 * tab - 1 + (striped ? 1 : 0);  // 0, F16 1-2, fixed 3-4
+    const void* fn = nullptr;
+#define HANN_SCAN_VARIANTS(MPV)                                                     \
+    switch (variant) {                                                                \
+    case 0: fn = (const void*)scan_adc_kernel<MPV, 0, false>; break;                  \
+    case 1: fn = (const void*)scan_adc_kernel<MPV, 1, false>; break;                  \
+    case 2: fn = (const void*)scan_adc_kernel<MPV, 1, true>; break;                   \
+    case 3: fn = (const void*)scan_adc_kernel<MPV, 2, false>; break;                  \
+    default: fn = (const void*)scan_adc_kernel<MPV, 2, true>; break;                  \
+    }
     switch (scan_codes_per_row(p.M)) {
-    case 8: fn = half ? (const void*)scan_adc_kernel<8, true> : (const void*)scan_adc_kernel<8, false>; break;
-    case 16: fn = half ? (const void*)scan_adc_kernel<16, true> : (const void*)scan_adc_kernel<16, false>; break;
-    case 24: fn = half ? (const void*)scan_adc_kernel<24, true> : (const void*)scan_adc_kernel<24, false>; break;
-    case 32: fn = half ? (const void*)scan_adc_kernel<32, true> : (const void*)scan_adc_kernel<32, false>; break;
+    case 8: HANN_SCAN_VARIANTS(8) break;
+    case 16: HANN_SCAN_VARIANTS(16) break;
+    case 24: HANN_SCAN_VARIANTS(24) break;
+    case 32: HANN_SCAN_VARIANTS(32) break;
     default: return cudaErrorInvalidValue;
     }
+#undef HANN_SCAN_VARIANTS
     ScanParams pp = p;
-    if (!half) pp.scan_cut = nullptr;  // the FP32 screen is not checked
+    if (tab == 0) pp.scan_cut = nullptr;  // the FP32 screen is not checked
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&pp, (void*)&queries, (void*)&probe_d, (void*)&probe_ids, (void*)&nprobe, (void*)&np_max,

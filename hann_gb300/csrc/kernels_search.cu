@@ -438,7 +438,7 @@ cudaError_t launch_scan(const ScanParams& p, const float* queries, int64_t nq, c
                         int32_t* cand_row, float* cand_d, uint32_t* cand_seq, unsigned long long* rows_scanned,
                         cudaStream_t s) {
     if (nq <= 0) return cudaSuccess;
-    if (scan_adc_supported(p.M) && p.scanc && scan_adc_smem(R, p.M, p.adc16 && p.adc_cb) <= 224 * 1024)
+    if (scan_adc_supported(p.M) && p.scanc && scan_adc_smem(R, p.M, p.adc_table && p.adc_cb) <= 224 * 1024)
         return launch_scan_adc(p, queries, nq, probe_ids, probe_d, nprobe, np_max, fallback, R, cand_row, cand_d,
                                cand_seq, rows_scanned, s);
     const int CAPW = cap_for(R);

@@ -178,16 +178,22 @@ int hann_pqivf_tune_candidate_clusters(hann_pqivf* h, const float* queries, int6
                                        const int64_t* ground_truth, int32_t apply, int32_t* chosen,
                                        int32_t* tried_out, double* recall_out, int32_t* n_tried);
 
-/* Lookup tables of the list scan in FP16 (on = 1, the default) or FP32
- * (on = 0). The reference decodes every candidate in FP32
- * (pqivf/index.go:909-923); here the scan screens candidates with per-query
- * tables and the rerank computes the reference's distance. FP16 tables take
- * half the shared memory and read without bank conflicts; in parity mode
- * (mode 0) each query's top k is proven against the FP16 screen's error
- * bound, and queries it cannot prove are scanned again with FP32 tables, so
- * parity-mode results do not depend on this switch. In exact-rerank mode
- * (mode 1) the candidates screened can differ in the last few places. */
-int hann_pqivf_set_adc_fp16(hann_pqivf* h, int32_t on);
+/* Lookup tables of the list scan: HANN_ADC_FP32, HANN_ADC_FP16 or
+ * HANN_ADC_FIXED16 (16-bit fixed point, the default). The reference decodes
+ * every candidate in FP32 (pqivf/index.go:909-923); here the scan screens
+ * candidates with per-query tables and the rerank computes the reference's
+ * distance. 16-bit tables take half the shared memory and read without bank
+ * conflicts; fixed point sums a row exactly in integers (its only error is
+ * each entry's rounding, a 65,534th of the largest entry bound, where FP16's
+ * is a 2,048th of each entry). In parity mode (mode 0) each query's top k
+ * is proven against the 16-bit screen's error bound, and the queries it
+ * cannot prove are scanned again with FP32 tables, so parity-mode results do
+ * not depend on this choice. In exact-rerank mode (mode 1) the screened
+ * candidates can differ at the rerank depth. */
+#define HANN_ADC_FP32 0
+#define HANN_ADC_FP16 1
+#define HANN_ADC_FIXED16 2
+int hann_pqivf_set_adc_tables(hann_pqivf* h, int32_t kind);
 
 /* Switches the plain-FP32 mode of hann_pqivf_options at run time (no
  * reference counterpart; results do not change). */

@@ -1,14 +1,15 @@
-"""FP16 against FP32 lookup tables in the table scan (kernels_scan.cu).
+"""16-bit (FP16 and fixed-point) against FP32 lookup tables in the table
+scan (kernels_scan.cu).
 
 The reference decodes every candidate to FP32 and takes its distance
 (pqivf/index.go:909-923). Here the scan screens rows through per-query ADC
-tables and the rerank computes the reference's distance. With FP16 tables
+tables and the rerank computes the reference's distance. With 16-bit tables
 parity mode must still give the reference's results: the rerank proves each
 query's top k against the screen's error bound and sends the rest to an FP32
 rescan, so the results equal the oracle's whatever the tables, and the
-proof must succeed for nearly every query (else the FP16 screen is not doing
-its work). In exact-rerank mode recall@10 against an FP64 brute force must
-not drop by more than 0.005."""
+proof must succeed for nearly every query (else the 16-bit screen is not
+doing its work). In exact-rerank mode recall@10 against an FP64 brute force
+must not drop by more than 0.005."""
 import os
 
 import numpy as np
@@ -49,13 +50,21 @@ def unit():
     idx.close()
 
 
+TABLES16 = ("fp16", "fixed16")
+
+
+@pytest.mark.parametrize("kind", TABLES16)
 @pytest.mark.parametrize("nprobe,k", [(1, 1), (8, 10), (24, 37), (64, 100)])
-def test_parity_fp16_tables(unit, nprobe, k):
+def test_parity_16bit_tables(unit, kind, nprobe, k):
     idx, _, q = unit
     ora = state_to_oracle(idx.export_state())
-    before = idx.ADCRedos()
-    g = idx.SearchBatch(q, k, nprobe=nprobe, mode=0)
-    redos = idx.ADCRedos() - before
+    idx.SetADCTables(kind)
+    try:
+        before = idx.ADCRedos()
+        g = idx.SearchBatch(q, k, nprobe=nprobe, mode=0)
+        redos = idx.ADCRedos() - before
+    finally:
+        idx.SetADCTables("fixed16")
     assert_same_results(*g, *ora.search(q, k, nprobe, nthreads=NT)[:3])
     # the screen proves almost every query's top k by itself
     assert redos <= 0.05 * len(q), redos
@@ -64,25 +73,29 @@ def test_parity_fp16_tables(unit, nprobe, k):
 def test_fp32_tables_same_results(unit):
     idx, _, q = unit
     a = idx.SearchBatch(q, 10, nprobe=16, mode=0)
-    idx.SetADCFP16(False)
+    idx.SetADCTables("fp32")
     try:
         before = idx.ADCRedos()
         b = idx.SearchBatch(q, 10, nprobe=16, mode=0)
         assert idx.ADCRedos() == before  # FP32 tables are never checked
     finally:
-        idx.SetADCFP16(True)
+        idx.SetADCTables("fixed16")
     assert_same_results(*a, *b)
+    with pytest.raises(ValueError):
+        idx.SetADCTables("fp8")
 
 
-def test_exact_rerank_recall(unit):
+@pytest.mark.parametrize("kind", TABLES16)
+def test_exact_rerank_recall(unit, kind):
     idx, x, q = unit
     gt, _ = oracle.brute_force_knn_fp64(q, x, 10)
+    idx.SetADCTables(kind)
     h = idx.SearchBatch(q, 10, nprobe=16, mode=1)
-    idx.SetADCFP16(False)
+    idx.SetADCTables("fp32")
     try:
         f = idx.SearchBatch(q, 10, nprobe=16, mode=1)
     finally:
-        idx.SetADCFP16(True)
+        idx.SetADCTables("fixed16")
 
     def recall(ids):
         return np.mean([len(set(ids[i]) & set(gt[i])) / 10 for i in range(len(gt))])
@@ -95,8 +108,9 @@ def test_exact_rerank_recall(unit):
             assert abs(h[1][i, j] - want) <= 1e-6 * max(want, 1e-12)
 
 
+@pytest.mark.parametrize("kind", TABLES16)
 @pytest.mark.parametrize("dim,M", [(16, 4), (32, 8), (40, 10), (64, 16), (96, 12), (128, 32), (60, 20)])
-def test_shapes(dim, M):
+def test_shapes(dim, M, kind):
     """Every padded table width (M rounded up to 8, 16, 24, 32)."""
     rng = np.random.default_rng(dim * 31 + M)
     x, c = gaussian_mixture(rng, 6000, dim, 30, 0.4)
@@ -106,6 +120,7 @@ def test_shapes(dim, M):
         idx.BulkAddArrays(np.arange(len(x), dtype=np.int64), x)
         idx.Train()
         idx.ScanOptions(list_major=0)
+        idx.SetADCTables(kind)
         ora = state_to_oracle(idx.export_state())
         before = idx.ADCRedos()
         g = idx.SearchBatch(q, 10, nprobe=6)
@@ -115,12 +130,14 @@ def test_shapes(dim, M):
         idx.close()
 
 
-def test_large_offset_data():
+@pytest.mark.parametrize("kind", TABLES16)
+def test_large_offset_data(kind):
     """Vectors far from the origin (every coordinate + 100): the FP32
     allowance grows with the decomposition's magnitudes; results stay the
     reference's (the FP32 rescan takes what the screen cannot prove)."""
     idx, _, q = table_index(72, n=8000, dim=32, centers=40, nlist=32, M=8, pqk=64, offset=100.0, nq=200)
     try:
+        idx.SetADCTables(kind)
         ora = state_to_oracle(idx.export_state())
         g = idx.SearchBatch(q, 10, nprobe=4, mode=0)
         assert_same_results(*g, *ora.search(q, 10, 4, nthreads=NT)[:3])
