@@ -84,6 +84,10 @@ def parse():
                     help="run the plain 20k x 128 PQIVF section (train + search, GPU and CPU oracle)")
     ap.add_argument("--train-oracle-iters", type=int, default=2,
                     help="k-means iterations of the oracle's inertia check on the 1M x 128 training shape")
+    ap.add_argument("--adc-tables", default="fixed16", choices=["fixed16", "fp16", "fp32"],
+                    help="the table scan's lookup tables in the timed steps")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="run the scan autotuner (table scan or list-major scan by nprobe) before the timed steps")
     ap.add_argument("--knn-variants", type=str,
                     default="squared_euclidean/tensor,cosine/tensor,manhattan/exact,squared_euclidean/exact,"
                             "cosine/exact")
@@ -497,6 +501,17 @@ def main():
     del x
     torch.cuda.empty_cache()
 
+    idx.SetADCTables(args.adc_tables)
+    # the scan autotuner: times the table scan and the list-major scan at
+    # nprobe 8..256 on the workload's queries and routes each nprobe to the
+    # faster (results in parity mode do not depend on it)
+    tune = None
+    if args.autotune:
+        t0 = time.perf_counter()
+        tune = idx.AutotuneScan(q_host[:min(args.nq, 10000)], args.k, mode=1)
+        tune["seconds"] = round(time.perf_counter() - t0, 2)
+        log("autotune", tune)
+
     # recall at each nprobe, exact-rerank mode and parity mode
     choice, rec = pick_nprobe(args, idx, q_host, gt, nr)
     mode = 1
@@ -635,6 +650,38 @@ def main():
                                "recall_at_10_reference_pq_distances": rec[(npb, 0)]}
     log("by nprobe", by_nprobe)
 
+    # the lookup tables of the table scan (FP32 against FP16 and 16-bit fixed
+    # point) at the chosen nprobe: the step time and recall in exact-rerank
+    # mode, and in parity mode the step time and the queries whose top k the
+    # 16-bit screen could not prove (scanned again with FP32 tables)
+    adc_tables = {}
+    for kind in ("fixed16", "fp16", "fp32"):
+        idx.SetADCTables(kind)
+        row = {}
+        for md in (1, 0):
+            def step_kind():
+                idx.SearchBatchDevice(q.data_ptr(), nq, args.k, choice, md, ids_d.data_ptr(), dist_d.data_ptr(),
+                                      nout_d.data_ptr(), stream.cuda_stream)
+            for _ in range(args.warmup):
+                step_kind()
+            torch.cuda.synchronize()
+            r0 = idx.ADCRedos()
+            k0 = torch.cuda.Event(enable_timing=True)
+            k1 = torch.cuda.Event(enable_timing=True)
+            k0.record(stream)
+            for _ in range(args.steps):
+                step_kind()
+            k1.record(stream)
+            torch.cuda.synchronize()
+            tag = "exact_rerank" if md == 1 else "parity"
+            row[f"{tag}_ms_per_step"] = k0.elapsed_time(k1) / args.steps
+            row[f"{tag}_recall_at_10"] = recall_at(ids_d[:nr].cpu().numpy(), gt)
+            if md == 0:
+                row["parity_fp32_rescans_per_step"] = (idx.ADCRedos() - r0) / args.steps
+        adc_tables[kind] = row
+    idx.SetADCTables(args.adc_tables)
+    log("lookup tables", adc_tables)
+
     # roofline of the scan kernel: algorithmic bytes = rows scanned (counted
     # by the kernel, per (query, list)) x M code bytes
     code_bytes = args.m
@@ -704,7 +751,7 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "vs_baseline": None, "dtype": "u8 codes, int16 tables, f32 rerank", "data": "synthetic",
             "config": workload_config(args, choice, mode),
             "recall_at_10": rec[(choice, mode)],
             "recall_by_nprobe": {f"{a}/{'exact' if b == 1 else 'pq'}": round(v, 4) for (a, b), v in rec.items()},
@@ -716,8 +763,11 @@ def main():
             "plain_fp32_gpu_qps": plain_fp32_qps, "plain_fp32_recall_at_10": plain_recall,
             "plain_fp32_id_overlap": plain_same,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": scan_traffic(args, choice), "kernel": "scan_skew_kernel",
+                         "frac": achieved / peak, "traffic": scan_traffic(args, choice),
+                         "kernel": f"scan_adc_kernel ({args.adc_tables} tables)",
                          "bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
+            "adc_tables": adc_tables,
+            "autotune": tune,
             "cpu_baseline": cb,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
@@ -1089,11 +1139,11 @@ def scan_traffic(args, nprobe):
     """DRAM bytes (read + write) of one scan launch on this workload, from the
     1-pass ncu capture kept in profiles/ (ncu cannot run inside the bench);
     None when the capture was of another workload."""
-    path = os.path.join(HERE, "profiles", "scan_skew_kernel_10Mx96_dram.json")
+    path = os.path.join(HERE, "profiles", "scan_adc_kernel_10Mx96_dram.json")
     try:
         rec = json.load(open(path))
         if (rec["n"], rec["dim"], rec["nlist"], rec["M"], rec["nq"], rec["nprobe"], rec["k"]) != \
-                (args.n, args.dim, args.nlist, args.m, args.nq, nprobe, args.k):
+                (args.n, args.dim, args.nlist, args.m, args.nq, nprobe, args.k) or args.adc_tables != "fixed16":
             return None
         return float(rec["dram_bytes_read_per_launch"]) + float(rec["dram_bytes_write_per_launch"])
     except Exception:
@@ -1222,9 +1272,10 @@ def workload_config(args, nprobe, mode):
                     f"{'exact FP32 rerank of raw vectors' if mode == 1 else 'reference PQ distances'}",
         "n": args.n, "dim": args.dim, "nlist": args.nlist, "M": args.m, "pq_k": args.pqk, "nq": args.nq,
         "k": args.k, "nprobe": nprobe, "mode": "exact_rerank" if mode == 1 else "parity",
-        "l2": f"inputs larger than L2 ({args.n * args.m / 1e6:.0f} MB of codes, {args.n * 2 * args.m / 1e6:.0f} MB "
-              f"of scan words + "
+        "l2": f"inputs larger than L2 ({args.n * args.m / 1e6:.0f} MB of codes, {args.n * args.m / 1e6:.0f} MB "
+              f"of scan codes + {args.n * 4 / 1e6:.0f} MB of terms + "
               f"{args.n * args.dim * 4 / 1e9:.2f} GB raw vectors), no flush",
+        "adc_tables": args.adc_tables,
     }
 
 

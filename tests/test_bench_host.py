@@ -67,10 +67,11 @@ def test_clock_record():
 def test_traffic_record_only_for_its_workload():
     a = args_for()
     t = bench.scan_traffic(a, 32)
-    assert t is not None and 6e9 < t < 2e10  # the captured launch's DRAM read + write bytes
+    assert t is not None and 2e9 < t < 2e10  # the captured launch's DRAM read + write bytes
     assert bench.scan_traffic(a, 128) is None  # another nprobe: another launch
     assert bench.scan_traffic(args_for(n=4_000_000), 32) is None
     assert bench.scan_traffic(args_for(m=16), 32) is None
+    assert bench.scan_traffic(args_for(adc_tables="fp32"), 32) is None  # another kernel
 
 
 def test_workload_config():
@@ -79,7 +80,7 @@ def test_workload_config():
     a = args_for()
     cfg = bench.workload_config(a, 32, 1)
     assert cfg["nprobe"] == 32 and cfg["mode"] == "exact_rerank"
-    assert "480 MB of scan words" in cfg["l2"] and "3.84 GB raw vectors" in cfg["l2"]
+    assert "240 MB of scan codes" in cfg["l2"] and "3.84 GB raw vectors" in cfg["l2"]
     assert "model" not in cfg
     assert bench.workload_config(a, 32, 1) == cfg
 
