@@ -104,7 +104,8 @@ EXPORTED = (
     "hann_pqivf_save_snapshot", "hann_pqivf_load_snapshot", "hann_pqivf_retrain", "hann_gob_encode",
     "hann_gob_decode", "hann_gob_state_layout", "hann_gob_state_arrays", "hann_gob_state_free",
     "hann_gob_last_error", "hann_gob_encode_payload", "hann_pqivf_tune_candidate_clusters",
-    "hann_pqivf_autotune_scan", "hann_pqivf_set_adc_tables",
+    "hann_pqivf_autotune_scan", "hann_pqivf_set_adc_tables", "hann_knn_append", "hann_knn_distance_gather",
+    "hann_knn_distance_gather_device",
 )
 # Entry points of include/hann_gb300_diag.h.
 EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats", "hann_pqivf_rows_decoded", "hann_pqivf_adc_redos",
@@ -176,6 +177,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_gpu_distance_matrix.argtypes = [ctypes.c_int32, _P, ctypes.c_int64, _P, ctypes.c_int64,
                                                ctypes.c_int32, _P]
         L.hann_knn_new.argtypes = [_P, ctypes.c_int64, ctypes.c_int32]
+        L.hann_knn_append.argtypes = [_P, _P, ctypes.c_int64]
+        L.hann_knn_distance_gather.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int64, _P, _P, _P]
+        L.hann_knn_distance_gather_device.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int64, _P, _P,
+                                                      ctypes.c_int64, _P, _P]
         L.hann_knn_new.restype = _P
         L.hann_knn_free.argtypes = [_P]
         L.hann_knn_free.restype = None
@@ -912,6 +917,32 @@ class KNN:
                                                    KNN_METHODS[method] if isinstance(method, str) else method,
                                                    ctypes.c_void_p(ids_ptr), ctypes.c_void_p(dist_ptr),
                                                    ctypes.c_void_p(stream)))
+
+    def append(self, rows) -> None:
+        """Add rows to the base (they get the next row numbers)."""
+        x = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, self.dim)
+        self._check(self._L.hann_knn_append(self._h, _ptr(x), x.shape[0]))
+        self.n += x.shape[0]
+
+    def distance_gather(self, queries, candidates, metric="squared_euclidean"):
+        """Metric.RankBatch for many queries at once: candidates[q] is a
+        sequence of row numbers; returns one float64 array of distances per
+        query (the values distance_batch gives for those pairs)."""
+        q = np.ascontiguousarray(queries, dtype=np.float32).reshape(-1, self.dim)
+        lens = np.array([len(c) for c in candidates], dtype=np.int64)
+        if len(lens) != q.shape[0]:
+            raise ValueError("one candidate list per query")
+        offsets = np.zeros(len(lens) + 1, dtype=np.int64)
+        np.cumsum(lens, out=offsets[1:])
+        ids = np.ascontiguousarray(np.concatenate([np.asarray(c, dtype=np.int64) for c in candidates])
+                                   if len(candidates) else np.zeros(0, np.int64))
+        if ids.size and (ids.min() < -2**31 or ids.max() >= 2**31):
+            raise ValueError("candidate id out of range")
+        ids32 = ids.astype(np.int32)
+        out = np.zeros(int(offsets[-1]), dtype=np.float64)
+        self._check(self._L.hann_knn_distance_gather(self._h, _metric_id(metric), _ptr(q), q.shape[0],
+                                                     _ptr(offsets), _ptr(ids32), _ptr(out)))
+        return [out[offsets[i]:offsets[i + 1]] for i in range(len(lens))]
 
     def stats(self) -> dict:
         st = _KnnStats()

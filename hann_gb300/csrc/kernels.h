@@ -78,6 +78,12 @@ cudaError_t launch_gather_cols(const float* in, int64_t ld, int off, const int64
 cudaError_t launch_tombstone(const int64_t* rows, int64_t n, float* term, int64_t* row_id, cudaStream_t s);
 
 // Reference-order batch distances of one query to n rows (simd_*_batch).
+// out[j] = distance(queries[q], base[ids[j]]) for j in [offsets[q],
+// offsets[q + 1]), total = offsets[nq] pairs; *bad is set for an id outside
+// [0, n) (its distance is NaN).
+cudaError_t launch_distance_gather(int metric, const float* queries, int64_t nq, const int64_t* offsets,
+                                   const int32_t* ids, int64_t total, const float* base, int64_t n, int dim,
+                                   double* out, int* bad, cudaStream_t s);
 cudaError_t launch_distance_rows(int metric, const float* q, const float* flat, int dim, int64_t n, double* out,
                                  cudaStream_t s);
 

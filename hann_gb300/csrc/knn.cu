@@ -74,6 +74,7 @@ struct hann_knn {
     DBuf<float> q_in;
     DBuf<int64_t> ids_out;
     DBuf<double> dist_out;
+    DBuf<int> gather_bad;             // set by the gathered-distance kernel for an id outside the base
 
     cudaStream_t stream = nullptr;
     std::mutex mu;
@@ -377,6 +378,92 @@ int hann_knn_search_device(hann_knn* h, int32_t metric, const float* queries, in
     std::lock_guard<std::mutex> g(h->mu);
     if (nq > 0 && ((!queries && h->dim > 0) || !ids || !dist)) return h->fail(HANN_E_INVALID, "null buffer");
     return knn_run(h, metric, queries, nq, k, method, ids, dist, stream ? (cudaStream_t)stream : h->stream);
+}
+
+int hann_knn_append(hann_knn* h, const float* rows, int64_t n) {
+    if (!h || n < 0 || (n > 0 && h->dim > 0 && !rows)) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> g(h->mu);
+    if (h->n + n >= ((int64_t)1 << 31)) return h->fail(HANN_E_UNSUPPORTED, "more than 2^31 base rows");
+    if (n == 0) return HANN_OK;
+    const size_t need = (size_t)(h->n + n) * h->dim;
+    if (need > h->base.n) {
+        // grow by half again, keeping the rows (device to device)
+        DBuf<float> nb;
+        if (nb.reserve(std::max(need, h->base.n + h->base.n / 2)) != cudaSuccess)
+            return h->fail(HANN_E_NOMEM, "device allocation failed");
+        if (h->n * h->dim > 0 &&
+            cudaMemcpyAsync(nb.p, h->base.p, sizeof(float) * h->n * h->dim, cudaMemcpyDeviceToDevice, h->stream) !=
+                cudaSuccess)
+            return h->fail(HANN_E_CUDA, "copy failed");
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) return h->fail(HANN_E_CUDA, "copy failed");
+        h->base.swap(nb);
+    }
+    if (h->dim > 0 && cudaMemcpyAsync(h->base.p + (size_t)h->n * h->dim, rows, sizeof(float) * n * h->dim,
+                                      cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+        return h->fail(HANN_E_CUDA, "copy failed");
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return h->fail(HANN_E_CUDA, "copy failed");
+    h->n += n;
+    // the screen's copies of the base are rebuilt on the next search
+    h->have_bf = h->have_bnorm = false;
+    h->have_terms[0] = h->have_terms[1] = false;
+    return HANN_OK;
+}
+
+static int gather_run(hann_knn* h, int32_t metric, const float* d_q, int64_t nq, const int64_t* d_off,
+                      const int32_t* d_ids, int64_t total, double* d_out, cudaStream_t s) {
+    if (h->gather_bad.reserve(1) != cudaSuccess) return h->fail(HANN_E_NOMEM, "device allocation failed");
+    if (cudaMemsetAsync(h->gather_bad.p, 0, sizeof(int), s) != cudaSuccess ||
+        launch_distance_gather(metric, d_q, nq, d_off, d_ids, total, h->base.p, h->n, h->dim, d_out,
+                               h->gather_bad.p, s) != cudaSuccess)
+        return h->fail(HANN_E_CUDA, "gathered distances failed");
+    int bad = 0;
+    if (cudaMemcpyAsync(&bad, h->gather_bad.p, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return h->fail(HANN_E_CUDA, "gathered distances failed");
+    if (bad) return h->fail(HANN_E_INVALID, "candidate id outside the base");
+    return HANN_OK;
+}
+
+int hann_knn_distance_gather(hann_knn* h, int32_t metric, const float* queries, int64_t nq, const int64_t* offsets,
+                             const int32_t* ids, double* out) {
+    if (!h) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> g(h->mu);
+    if (metric < 0 || metric > 3) return h->fail(HANN_E_INVALID, "unknown metric");
+    if (nq < 0 || (nq > 0 && !offsets)) return h->fail(HANN_E_INVALID, "null buffer");
+    if (nq == 0) return HANN_OK;
+    if (offsets[0] != 0) return h->fail(HANN_E_INVALID, "offsets must start at 0");
+    for (int64_t q = 0; q < nq; q++)
+        if (offsets[q + 1] < offsets[q]) return h->fail(HANN_E_INVALID, "offsets must not decrease");
+    const int64_t total = offsets[nq];
+    if (total == 0) return HANN_OK;
+    if ((h->dim > 0 && !queries) || !ids || !out) return h->fail(HANN_E_INVALID, "null buffer");
+    DBuf<float> dq;
+    DBuf<int64_t> doff;
+    DBuf<int32_t> dids;
+    DBuf<double> dout;
+    if (upload(dq, queries, (size_t)nq * h->dim, h->stream) != cudaSuccess ||
+        upload(doff, offsets, (size_t)nq + 1, h->stream) != cudaSuccess ||
+        upload(dids, ids, (size_t)total, h->stream) != cudaSuccess || dout.reserve((size_t)total) != cudaSuccess)
+        return h->fail(HANN_E_CUDA, "device allocation or copy failed");
+    const int rc = gather_run(h, metric, dq.p, nq, doff.p, dids.p, total, dout.p, h->stream);
+    if (rc) return rc;
+    if (cudaMemcpyAsync(out, dout.p, sizeof(double) * total, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return h->fail(HANN_E_CUDA, "copy failed");
+    return HANN_OK;
+}
+
+int hann_knn_distance_gather_device(hann_knn* h, int32_t metric, const float* d_queries, int64_t nq,
+                                    const int64_t* d_offsets, const int32_t* d_ids, int64_t total, double* d_out,
+                                    void* stream) {
+    if (!h) return HANN_E_INVALID;
+    std::lock_guard<std::mutex> g(h->mu);
+    if (metric < 0 || metric > 3) return h->fail(HANN_E_INVALID, "unknown metric");
+    if (nq < 0 || total < 0) return h->fail(HANN_E_INVALID, "negative size");
+    if (nq == 0 || total == 0) return HANN_OK;
+    if ((h->dim > 0 && !d_queries) || !d_offsets || !d_ids || !d_out) return h->fail(HANN_E_INVALID, "null buffer");
+    return gather_run(h, metric, d_queries, nq, d_offsets, d_ids, total, d_out,
+                      stream ? (cudaStream_t)stream : h->stream);
 }
 
 int hann_knn_get_stats(hann_knn* h, hann_knn_stats* out) {

@@ -437,6 +437,28 @@ int hann_knn_search(hann_knn* h, int32_t metric, const float* queries, int64_t n
 int hann_knn_search_device(hann_knn* h, int32_t metric, const float* queries, int64_t nq, int32_t k, int32_t method,
                            int64_t* ids, double* dist, void* stream);
 int hann_knn_get_stats(hann_knn* h, hann_knn_stats* out);
+/* Appends n rows [n][dim] (host) to the handle's base; they get the next
+ * row numbers. For indexes whose points arrive over time (hnsw Add,
+ * rpt Add). */
+int hann_knn_append(hann_knn* h, const float* rows, int64_t n);
+/* Gathered distances for graph and tree indexes: Metric.RankBatch over many
+ * (query, candidate list) pairs at once. The reference ranks candidates one
+ * Rank call at a time (hnsw/index.go:1178 in the greedy descent and
+ * searchLayer, rpt/index.go:461 over a leaf's ids). For query q (queries
+ * [nq][dim]) and every j in [offsets[q], offsets[q + 1]) (offsets [nq + 1],
+ * starting at 0, never decreasing): out[j] = distance(queries[q],
+ * base[ids[j]]), the value hann_gpu_distance_batch gives for that pair (FP32
+ * in the reference's NEON order, widened to double). A Metric's Rank maps
+ * to the metric whose distance equals it (Euclidean's Rank: squared
+ * Euclidean). An id outside [0, n) fails with HANN_E_INVALID. Host buffers. */
+int hann_knn_distance_gather(hann_knn* h, int32_t metric, const float* queries, int64_t nq, const int64_t* offsets,
+                             const int32_t* ids, double* out);
+/* The same with device buffers (total = offsets[nq] pairs), work enqueued on
+ * `stream` (NULL = the handle's own); returns once the results are
+ * complete. */
+int hann_knn_distance_gather_device(hann_knn* h, int32_t metric, const float* d_queries, int64_t nq,
+                                    const int64_t* d_offsets, const int32_t* d_ids, int64_t total, double* d_out,
+                                    void* stream);
 /* One-shot form: copies base, searches, frees. */
 int hann_gpu_knn(int32_t metric, const float* queries, int64_t nq, const float* base, int64_t n, int32_t dim,
                  int32_t k, int32_t method, int64_t* ids, double* dist);
