@@ -61,8 +61,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-region", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
-    ap.add_argument("--serve-seconds", type=float, default=8.0, help="served-stream phase length (0 = skip)")
-    ap.add_argument("--serve-rate", type=str, default="2000,5000",
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="served-stream phase length (0 = skip)")
+    ap.add_argument("--serve-rate", type=str, default="2000,5000,10000,20000",
                     help="Poisson request arrivals per second, one served-stream phase per value")
     ap.add_argument("--serve-batch-probes", type=int, default=32768,
                     help="served stream: bound on a batch's summed nprobe (0 = none)")
@@ -962,8 +962,10 @@ def train_section(args, torch, dev):
                 lab_q = torch.randint(0, 2000, (nq_s,), device=dev, generator=g)
                 qs = centers[lab_q] + torch.randn(nq_s, dim, device=dev, generator=g) * scales[lab_q]
                 gt = ground_truth(torch, x, qs, 10)
-                out["served_stream_1Mx128"] = serve_stream(args, idx, qs.cpu().numpy(), gt, nq_s, 2000.0,
-                                                           n_ids=n, seconds=min(4.0, args.serve_seconds))
+                out["served_stream_1Mx128"] = [
+                    serve_stream(args, idx, qs.cpu().numpy(), gt, nq_s, float(rate), n_ids=n,
+                                 seconds=min(4.0, args.serve_seconds))
+                    for rate in args.serve_rate.split(",") if rate]
                 log("served 1Mx128", out["served_stream_1Mx128"])
             except Exception as e:  # pragma: no cover
                 out["served_stream_1Mx128"] = {"error": str(e)}
@@ -1150,118 +1152,104 @@ def scan_traffic(args, nprobe):
         return None
 
 
-def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
-    """The served stream: Poisson arrivals at `rate` requests/s, each a
-    block of 1-512 queries (log-uniform), k uniform in [1, 100], nprobe
-    log-uniform in [8, 256]; BulkAdd of 1,000-vector chunks and Deletes of
-    random ids, each at 1% of the request rate, applied beside the running
-    batches. Queries are drawn from the first `nr` queries (which have ground
-    truth). Reports p50/p99 latency (submit to result, the server's clock),
-    queries/s, recall@10 over a sample of the requests with k >= 10, the
-    relayout holds and how late the submitter kept to its schedule."""
-    import threading
-    import queue as qmod
-
+def serve_schedule(args, rate, dur, nr, dim, n_ids, seed):
+    """The served stream's arrival schedule, drawn before the clock starts:
+    Poisson arrivals at `rate` requests/s for `dur` seconds; a search of
+    1-512 queries (log-uniform) with k uniform in [1, 100] and nprobe
+    log-uniform in [8, 256], or (1% each) a BulkAdd of 1,000 random unit
+    vectors or a BulkDelete of 100 random ids. Every fourth search with
+    k >= 10 keeps its ids for the recall. Returns the request records of
+    hann_serve_request and the arrays they point into."""
     import hann_gb300 as hg
 
-    rng = np.random.default_rng(args.seed + 7)
-    dur = seconds or args.serve_seconds
-    # The whole arrival schedule is drawn before the clock starts, and
-    # Python's thread switch interval is shortened for the run, so the
-    # submitting thread keeps to the schedule (a waiter holding the
-    # interpreter for a whole 5 ms switch interval used to delay it, and the
-    # delayed arrivals then came as one burst). Latency is the server's own,
-    # from submit to completion.
-    sched = []
-    t = 0.0
+    rng = np.random.default_rng(seed)
+    n_req = int(rng.poisson(rate * dur))
+    at = np.sort(rng.uniform(0.0, dur * 1000.0, n_req))
+    u = rng.random(n_req)
+    reqs = np.zeros(n_req, dtype=hg.Server.REQUEST_DTYPE)
+    reqs["at_ms"] = at
+    rows, add_ids, add_vecs, del_ids = [], [], [], []
+    n_rows = n_add = n_del = n_out = 0
     next_id = 50_000_000
-    while True:
-        t += rng.exponential(1.0 / rate)
-        if t > dur:
-            break
-        u = rng.random()
-        if u < 0.01:
+    kept, searches = [], 0
+    for i in range(n_req):
+        if u[i] < 0.01:
             # random unit vectors: far from every query, so they do not
             # disturb the recall measured against the original ground truth
-            chunk = rng.standard_normal((1000, q_host.shape[1])).astype(np.float32)
+            chunk = rng.standard_normal((1000, dim)).astype(np.float32)
             chunk /= np.linalg.norm(chunk, axis=1, keepdims=True)
-            sched.append((t, 1, (np.arange(next_id, next_id + 1000), chunk)))
+            add_vecs.append(chunk)
+            add_ids.append(np.arange(next_id, next_id + 1000, dtype=np.int64))
             next_id += 1000
-        elif u < 0.02:
-            sched.append((t, 2, rng.integers(0, n_ids or args.n, 100)))
+            reqs[i]["kind"], reqs[i]["first"], reqs[i]["count"] = 1, n_add, 1000
+            n_add += 1000
+        elif u[i] < 0.02:
+            del_ids.append(rng.integers(0, n_ids, 100).astype(np.int64))
+            reqs[i]["kind"], reqs[i]["first"], reqs[i]["count"] = 2, n_del, 100
+            n_del += 100
         else:
             nq = int(np.exp(rng.uniform(0, np.log(512))))
             k = int(rng.integers(1, 101))
             npb = int(np.exp(rng.uniform(np.log(8), np.log(256))))
-            rows = rng.integers(0, nr, nq)
-            sched.append((t, 0, (k, npb, rows)))
+            r = rng.integers(0, nr, nq)
+            rows.append(r)
+            reqs[i]["kind"], reqs[i]["k"], reqs[i]["nprobe"] = 0, k, npb
+            reqs[i]["first"], reqs[i]["count"] = n_rows, nq
+            n_rows += nq
+            reqs[i]["out_offset"] = -1
+            if k >= 10:
+                if searches % 4 == 0:
+                    reqs[i]["out_offset"] = n_out
+                    kept.append((i, r, k, n_out))
+                    n_out += nq * k
+                searches += 1
+    cat = lambda xs, dt, shape: np.concatenate(xs) if xs else np.zeros(shape, dt)  # noqa: E731
+    return (reqs, cat(rows, np.int64, (0,)), cat(add_ids, np.int64, (0,)), cat(add_vecs, np.float32, (0, dim)),
+            cat(del_ids, np.int64, (0,)), kept, n_out)
+
+
+def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
+    """The served stream (serve_schedule's requests) replayed by the
+    library's native load generator (hann_serve_replay): the calling thread
+    keeps to the arrival schedule natively and a native thread waits for
+    every request, so the interpreter sets neither the arrivals nor the
+    latencies. Reports p50/p99 latency (submit to result, the server's
+    clock), queries/s, recall@10 over the kept searches, the relayout holds
+    and how late the submissions were against the schedule."""
+    import hann_gb300 as hg
+
+    dur = seconds or args.serve_seconds
+    reqs, rows, add_ids, add_vecs, del_ids, kept, n_out = serve_schedule(
+        args, rate, dur, nr, q_host.shape[1], n_ids or args.n, args.seed + 7)
     srv = hg.Server(idx, slots=4, max_batch_queries=8192, max_k=100, max_nprobe=256, mode=1,
                     memory_budget=120 << 30, max_batch_probes=args.serve_batch_probes)
-    pending = qmod.Queue()
-    results = []
-
-    def waiter():
-        # results are copied out only for the requests the recall uses
-        # (k >= 10, every fourth), so the interpreter stays free for the
-        # submitting thread
-        i = 0
-        while True:
-            item = pending.get()
-            if item is None:
-                return
-            kind, tk, meta = item
-            keep = kind == 0 and meta[1] >= 10 and i % 4 == 0
-            i += kind == 0
-            r = srv.wait(tk, timeout_ms=120000, results=keep)
-            if keep:
-                results.append((meta, r))
-
-    old_switch = sys.getswitchinterval()
-    sys.setswitchinterval(2e-4)
-    ws = [threading.Thread(target=waiter, daemon=True) for _ in range(1)]
-    for w in ws:
-        w.start()
-    late = []
-    t0 = time.perf_counter()
-    for ta, kind, payload in sched:
-        while True:
-            now = time.perf_counter() - t0
-            if now >= ta:
-                break
-            time.sleep(min(ta - now, 0.0005))
-        late.append(now - ta)
-        if kind == 1:
-            pending.put((1, srv.submit_add(*payload), None))
-        elif kind == 2:
-            pending.put((2, srv.submit_delete(payload), None))
-        else:
-            k, npb, rows = payload
-            pending.put((0, srv.submit(q_host[rows], k, npb), (rows, k)))
-    for _ in ws:
-        pending.put(None)
-    for w in ws:
-        w.join()
-    sys.setswitchinterval(old_switch)
-    st = srv.stats()
-    srv.stop()
+    try:
+        lat, late, out = srv.replay(reqs, q_host, rows, add_ids, add_vecs, del_ids, n_out)
+        st = srv.stats()
+    finally:
+        srv.stop()
     hits = tot = 0
-    for (rows, k), (ids, dist, n, lat) in results:
-        if k < 10:
-            continue
-        for j, r in enumerate(rows):
-            hits += len(set(ids[j, :10].tolist()) & set(gt[r].tolist()))
+    for i, r, k, off in kept:
+        ids = out[off:off + len(r) * k].reshape(len(r), k)
+        for j, row in enumerate(r):
+            hits += len(set(ids[j, :10].tolist()) & set(gt[row].tolist()))
             tot += 10
+    searches = reqs["kind"] == 0
     return {"requests": int(st["requests"]), "queries": int(st["queries"]), "batches": int(st["batches"]),
             "mutations": int(st["mutations"]), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+            "search_p99_ms": round(float(np.percentile(lat[searches], 99)), 3) if searches.any() else None,
             "queries_per_s": st["queries_per_s"], "offered_requests_per_s": rate,
+            "offered_queries_per_s": float(reqs["count"][searches].sum()) / dur,
             "recall_at_10_k_ge_10": hits / tot if tot else None,
             "peak_admitted_bytes": int(st["peak_admitted_bytes"]), "relayouts": int(st["relayouts"]),
-            "submit_late_ms_p99": round(1000.0 * float(np.percentile(late, 99)), 3) if late else None,
+            "submit_late_ms_p99": round(float(np.percentile(late, 99)), 3) if len(late) else None,
+            "submit_late_ms_max": round(float(late.max()), 3) if len(late) else None,
             "mutation_ms_total": round(st["mutation_ms"], 1), "relayout_drain_ms_total": round(st["drain_ms"], 1),
             "relayout_ms_total": round(st["relayout_ms"], 1), "relayout_max_ms": round(st["relayout_max_ms"], 1),
             "stream": "Poisson arrivals; 1-512 queries/request log-uniform; k U[1,100]; nprobe log-U[8,256]; "
-                      "BulkAdd 1000-vector chunks and Deletes at 1% of the request rate; exact rerank",
-            "max_batch_probes": args.serve_batch_probes}
+                      "BulkAdd 1000-vector chunks and BulkDeletes of 100 ids at 1% of the request rate each; "
+                      "exact rerank; native load generator",
+            "max_batch_probes": args.serve_batch_probes, "seconds": dur}
 
 
 def workload_config(args, nprobe, mode):

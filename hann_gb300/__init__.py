@@ -996,6 +996,7 @@ def _serve_lib():
     L.hann_serve_last_error.argtypes = [_P]
     L.hann_serve_last_error.restype = ctypes.c_char_p
     L.hann_serve_stop.argtypes = [_P]
+    L.hann_serve_replay.argtypes = [_P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P]
     L._serve_ready = True
     return L
 
@@ -1082,6 +1083,28 @@ class Server:
         self._check(self._L.hann_serve_wait(self._h, ticket, _ptr(ids), _ptr(dist), _ptr(n), int(timeout_ms),
                                             ctypes.byref(lat)))
         return ids, dist, n[:nq], lat.value
+
+    # hann_serve_request (include/hann_gb300.h)
+    REQUEST_DTYPE = np.dtype([("at_ms", "<f8"), ("kind", "<i4"), ("k", "<i4"), ("nprobe", "<i4"), ("pad", "<i4"),
+                              ("first", "<i8"), ("count", "<i8"), ("out_offset", "<i8")])
+
+    def replay(self, reqs, queries, query_rows, add_ids=None, add_vectors=None, del_ids=None, n_out_ids=0):
+        """Drive the server from the native load generator
+        (hann_serve_replay): reqs is an array of REQUEST_DTYPE sorted by
+        at_ms. Returns (latency_ms, late_ms, out_ids) per request."""
+        reqs = np.ascontiguousarray(reqs, dtype=self.REQUEST_DTYPE)
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        rows = np.ascontiguousarray(query_rows, dtype=np.int64)
+        aid = np.ascontiguousarray(add_ids if add_ids is not None else np.zeros(0), dtype=np.int64)
+        avec = np.ascontiguousarray(add_vectors if add_vectors is not None else np.zeros((0, q.shape[1])),
+                                    dtype=np.float32)
+        did = np.ascontiguousarray(del_ids if del_ids is not None else np.zeros(0), dtype=np.int64)
+        out = np.zeros(max(int(n_out_ids), 1), dtype=np.int64)
+        lat = np.zeros(max(len(reqs), 1), dtype=np.float64)
+        late = np.zeros(max(len(reqs), 1), dtype=np.float64)
+        self._check(self._L.hann_serve_replay(self._h, reqs.ctypes.data, len(reqs), _ptr(q), _ptr(rows), _ptr(aid),
+                                              _ptr(avec), _ptr(did), _ptr(out), _ptr(lat), _ptr(late)))
+        return lat[:len(reqs)], late[:len(reqs)], out[:int(n_out_ids)]
 
     def stats(self) -> dict:
         s = _ServeStats()

@@ -26,6 +26,7 @@
 #include <deque>
 #include <memory>
 #include <thread>
+#include <vector>
 
 #include "index_internal.h"
 
@@ -613,6 +614,99 @@ int hann_serve_stop(hann_server* s) {
     if (s->mthr.joinable()) s->mthr.join();
     for (auto& sl : s->slots) free_slot(*sl);
     delete s;
+    return HANN_OK;
+}
+
+int hann_serve_replay(hann_server* s, const hann_serve_request* reqs, int64_t n, const float* queries,
+                      const int64_t* query_rows, const int64_t* add_ids, const float* add_vectors,
+                      const int64_t* del_ids, int64_t* out_ids, double* latency_ms, double* late_ms) {
+    if (!s || (n > 0 && (!reqs || !latency_ms || !late_ms))) return serve_fail(HANN_E_INVALID, "null buffer");
+    const int dim = s->h->o.dimension;
+    for (int64_t i = 0; i < n; i++) {
+        const hann_serve_request& r = reqs[i];
+        const bool ok = r.count >= 0 && r.first >= 0 &&
+                        (r.kind == 0 ? queries && query_rows && r.count > 0 && r.count <= INT32_MAX &&
+                                           (r.out_offset < 0 || out_ids)
+                                     : r.kind == 1 ? add_ids && add_vectors : r.kind == 2 && del_ids);
+        if (!ok) return serve_fail(HANN_E_INVALID, "invalid request in the schedule");
+    }
+    // The waiter takes the tickets in submission order and records each
+    // request's latency (the server's clock); results are copied out only
+    // for the searches that keep them.
+    struct Pending {
+        int64_t i;
+        uint64_t ticket;
+    };
+    std::mutex qm;
+    std::condition_variable qcv;
+    std::deque<Pending> pending;
+    bool submitted_all = false;
+    int wait_rc = HANN_OK;
+    std::string wait_msg;
+    std::thread waiter([&]() {
+        std::vector<int64_t> ids;
+        while (true) {
+            Pending p;
+            {
+                std::unique_lock<std::mutex> lk(qm);
+                qcv.wait(lk, [&] { return !pending.empty() || submitted_all; });
+                if (pending.empty()) return;
+                p = pending.front();
+                pending.pop_front();
+            }
+            const hann_serve_request& r = reqs[p.i];
+            const bool keep = r.kind == 0 && r.out_offset >= 0;
+            if (keep) ids.resize((size_t)r.count * r.k);
+            double lat = 0.0;
+            const int rc = hann_serve_wait(s, p.ticket, keep ? ids.data() : nullptr, nullptr, nullptr, -1, &lat);
+            latency_ms[p.i] = lat;
+            if (rc != HANN_OK && wait_rc == HANN_OK) {
+                wait_rc = rc;
+                wait_msg = t_serve_error;
+            }
+            if (keep && rc == HANN_OK) std::memcpy(out_ids + r.out_offset, ids.data(), sizeof(int64_t) * ids.size());
+        }
+    });
+    int rc = HANN_OK;
+    std::vector<float> qbuf;
+    const auto t0 = Clock::now();
+    for (int64_t i = 0; i < n && rc == HANN_OK; i++) {
+        const hann_serve_request& r = reqs[i];
+        const auto target = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double, std::milli>(r.at_ms));
+        // sleep to within 0.2 ms of the arrival, then spin
+        while (true) {
+            const auto now = Clock::now();
+            if (now >= target) break;
+            if (target - now > std::chrono::microseconds(300)) std::this_thread::sleep_for(target - now - std::chrono::microseconds(200));
+        }
+        late_ms[i] = std::chrono::duration<double, std::milli>(Clock::now() - target).count();
+        uint64_t ticket = 0;
+        if (r.kind == 0) {
+            qbuf.resize((size_t)r.count * dim);
+            for (int64_t j = 0; j < r.count; j++)
+                std::memcpy(qbuf.data() + (size_t)j * dim, queries + (size_t)query_rows[r.first + j] * dim,
+                            sizeof(float) * dim);
+            rc = hann_serve_submit(s, qbuf.data(), (int32_t)r.count, r.k, r.nprobe, &ticket);
+        } else if (r.kind == 1) {
+            rc = hann_serve_submit_add(s, add_ids + r.first, add_vectors + (size_t)r.first * dim, r.count, &ticket);
+        } else {
+            rc = hann_serve_submit_delete(s, del_ids + r.first, r.count, &ticket);
+        }
+        if (rc == HANN_OK) {
+            std::lock_guard<std::mutex> lk(qm);
+            pending.push_back({i, ticket});
+            qcv.notify_one();
+        }
+    }
+    const std::string submit_msg = rc == HANN_OK ? std::string() : t_serve_error;
+    {
+        std::lock_guard<std::mutex> lk(qm);
+        submitted_all = true;
+        qcv.notify_one();
+    }
+    waiter.join();
+    if (rc != HANN_OK) return serve_fail(rc, submit_msg.c_str());
+    if (wait_rc != HANN_OK) return serve_fail(wait_rc, wait_msg.c_str());
     return HANN_OK;
 }
 

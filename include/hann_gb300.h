@@ -300,6 +300,29 @@ int hann_serve_stats(hann_server* s, hann_serve_statistics* out);
 const char* hann_serve_last_error(const hann_server* s);
 /* Finishes the queued work, then releases the server. */
 int hann_serve_stop(hann_server* s);
+/* A load generator for the server (no reference counterpart: the caller
+ * side of example/run_datasets.go:84-120 driven by an arrival schedule).
+ * The calling thread submits the n requests at their arrival times (sleeping
+ * to within 0.2 ms, then spinning) while a native thread waits for each in
+ * submission order, so neither the submission schedule nor the latency
+ * depends on the caller's language runtime. Search requests take rows
+ * query_rows[first .. first + count) of queries [*][dim]; BulkAdd requests
+ * add_ids / add_vectors rows [first, first + count); BulkDelete requests
+ * del_ids [first, first + count). A search with out_offset >= 0 copies its
+ * ids ([count][k]) to out_ids + out_offset. Per request: latency_ms[i]
+ * (submit to completion, the server's clock) and late_ms[i] (how long after
+ * its arrival time it was submitted). */
+typedef struct {
+    double at_ms;        /* arrival time after the start, milliseconds */
+    int32_t kind;        /* 0 search, 1 BulkAdd, 2 BulkDelete */
+    int32_t k, nprobe;   /* search */
+    int32_t pad;
+    int64_t first, count;
+    int64_t out_offset;  /* search: where its ids go in out_ids, -1 = not kept */
+} hann_serve_request;
+int hann_serve_replay(hann_server* s, const hann_serve_request* reqs, int64_t n, const float* queries,
+                      const int64_t* query_rows, const int64_t* add_ids, const float* add_vectors,
+                      const int64_t* del_ids, int64_t* out_ids, double* latency_ms, double* late_ms);
 
 /* ---- persisted state (Save/Load, pqivf/index.go:969-1101) ----------------
  * The binding encodes/decodes the reference's gob stream itself and moves

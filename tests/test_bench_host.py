@@ -107,3 +107,31 @@ def test_compare_results_counts_only_real_mismatches():
 def test_rerank_depth_matches_the_library():
     assert bench.rerank_depth(10, 0) == 64 and bench.rerank_depth(10, 1) == 64
     assert bench.rerank_depth(100, 1) == 416 and bench.rerank_depth(1, 0) == 64
+
+
+def test_serve_schedule_records():
+    """The served stream's schedule: sorted arrivals at about the rate, 1% of
+    each mutation kind, every record's range inside the array it indexes,
+    kept searches' id slots disjoint and in order."""
+    a = args_for()
+    reqs, rows, add_ids, add_vecs, del_ids, kept, n_out = bench.serve_schedule(a, 2000.0, 3.0, 500, 16, 10_000, 5)
+    assert abs(len(reqs) - 6000) < 400
+    assert np.all(np.diff(reqs["at_ms"]) >= 0) and reqs["at_ms"].max() <= 3000.0
+    kinds = reqs["kind"]
+    assert 0.004 < np.mean(kinds == 1) < 0.02 and 0.004 < np.mean(kinds == 2) < 0.02
+    s = kinds == 0
+    assert (reqs["count"][s] >= 1).all() and (reqs["count"][s] <= 512).all()
+    assert (reqs["k"][s] >= 1).all() and (reqs["k"][s] <= 100).all()
+    assert (reqs["nprobe"][s] >= 8).all() and (reqs["nprobe"][s] <= 256).all()
+    assert (reqs["first"][s] + reqs["count"][s]).max() == len(rows) and rows.max() < 500
+    ad = kinds == 1
+    assert (reqs["first"][ad] + reqs["count"][ad]).max() == len(add_ids) == len(add_vecs)
+    np.testing.assert_allclose(np.linalg.norm(add_vecs, axis=1), 1.0, rtol=1e-5)
+    de = kinds == 2
+    assert (reqs["first"][de] + reqs["count"][de]).max() == len(del_ids) and del_ids.max() < 10_000
+    end = 0
+    for i, r, k, off in kept:
+        assert reqs[i]["out_offset"] == off == end and k >= 10 and len(r) == reqs[i]["count"]
+        end += len(r) * k
+    assert end == n_out
+    assert (reqs["out_offset"][~s] == 0).all()

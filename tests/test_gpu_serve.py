@@ -160,3 +160,42 @@ def test_wait_without_results(index):
         ids, dist, n, _ = srv.wait(srv.submit(q, 7, 8))
     want = idx.SearchBatch(q, 7, nprobe=8, mode=hg.MODE_EXACT_RERANK)
     np.testing.assert_array_equal(ids, want[0])
+
+
+def test_native_replay(index):
+    """The native load generator (hann_serve_replay): searches, an add and a
+    delete submitted on an arrival schedule; each kept search result equals a
+    Search of its queries alone, every request gets a latency and a
+    lateness, and rows deleted before a search never come back."""
+    idx, x, rng = index
+    q = rng.normal(size=(300, 32)).astype(np.float32)
+    reqs = np.zeros(60, dtype=hg.Server.REQUEST_DTYPE)
+    rows, t, out = [], 0.0, 0
+    del_ids = np.arange(100, 160, dtype=np.int64)
+    plan = []
+    for i in range(len(reqs)):
+        t += float(rng.exponential(0.5))
+        reqs[i]["at_ms"] = t
+        if i == 20:
+            reqs[i]["kind"], reqs[i]["first"], reqs[i]["count"] = 2, 0, len(del_ids)
+            continue
+        nq = int(rng.integers(1, 9))
+        reqs[i]["kind"], reqs[i]["k"], reqs[i]["nprobe"] = 0, int(rng.integers(1, 21)), int(rng.integers(1, 33))
+        reqs[i]["first"], reqs[i]["count"], reqs[i]["out_offset"] = len(rows), nq, out
+        r = rng.integers(0, len(q), nq)
+        plan.append((i, r, out))
+        rows.extend(r.tolist())
+        out += nq * int(reqs[i]["k"])
+    with hg.Server(idx, slots=2, max_batch_queries=256, max_k=20, max_nprobe=32, mode=hg.MODE_EXACT_RERANK) as srv:
+        lat, late, ids = srv.replay(reqs, q, np.array(rows), del_ids=del_ids, n_out_ids=out)
+    assert (lat > 0).all() and (late >= 0).all() and late.max() < 50.0
+    for i, r, off in plan:
+        k = int(reqs[i]["k"])
+        got = ids[off:off + len(r) * k].reshape(len(r), k)
+        want, _, _ = idx.SearchBatch(q[r], k, nprobe=int(reqs[i]["nprobe"]), mode=hg.MODE_EXACT_RERANK)
+        if i > 20:
+            # queued after the delete: it ran on the index without those
+            # rows, the state the search alone now sees (the searches before
+            # it may or may not have seen the delete)
+            assert not (set(got.ravel().tolist()) & set(del_ids.tolist()))
+            np.testing.assert_array_equal(got, want)
