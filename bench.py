@@ -962,10 +962,14 @@ def train_section(args, torch, dev):
                 lab_q = torch.randint(0, 2000, (nq_s,), device=dev, generator=g)
                 qs = centers[lab_q] + torch.randn(nq_s, dim, device=dev, generator=g) * scales[lab_q]
                 gt = ground_truth(torch, x, qs, 10)
-                out["served_stream_1Mx128"] = [
-                    serve_stream(args, idx, qs.cpu().numpy(), gt, nq_s, float(rate), n_ids=n,
-                                 seconds=min(4.0, args.serve_seconds))
-                    for rate in args.serve_rate.split(",") if rate]
+                out["served_stream_1Mx128"] = []
+                for rate in [float(r) for r in args.serve_rate.split(",") if r]:
+                    try:
+                        out["served_stream_1Mx128"].append(
+                            serve_stream(args, idx, qs.cpu().numpy(), gt, nq_s, rate, n_ids=n,
+                                         seconds=min(4.0, args.serve_seconds)))
+                    except Exception as e:  # pragma: no cover
+                        out["served_stream_1Mx128"].append({"offered_requests_per_s": rate, "error": str(e)})
                 log("served 1Mx128", out["served_stream_1Mx128"])
             except Exception as e:  # pragma: no cover
                 out["served_stream_1Mx128"] = {"error": str(e)}
@@ -1152,14 +1156,14 @@ def scan_traffic(args, nprobe):
         return None
 
 
-def serve_schedule(args, rate, dur, nr, dim, n_ids, seed):
+def serve_schedule(args, rate, dur, nr, dim, n_ids, seed, id_base=50_000_000):
     """The served stream's arrival schedule, drawn before the clock starts:
     Poisson arrivals at `rate` requests/s for `dur` seconds; a search of
     1-512 queries (log-uniform) with k uniform in [1, 100] and nprobe
     log-uniform in [8, 256], or (1% each) a BulkAdd of 1,000 random unit
-    vectors or a BulkDelete of 100 random ids. Every fourth search with
-    k >= 10 keeps its ids for the recall. Returns the request records of
-    hann_serve_request and the arrays they point into."""
+    vectors (ids from id_base up) or a BulkDelete of 100 random ids. Every
+    fourth search with k >= 10 keeps its ids for the recall. Returns the
+    request records of hann_serve_request and the arrays they point into."""
     import hann_gb300 as hg
 
     rng = np.random.default_rng(seed)
@@ -1170,7 +1174,7 @@ def serve_schedule(args, rate, dur, nr, dim, n_ids, seed):
     reqs["at_ms"] = at
     rows, add_ids, add_vecs, del_ids = [], [], [], []
     n_rows = n_add = n_del = n_out = 0
-    next_id = 50_000_000
+    next_id = id_base
     kept, searches = [], 0
     for i in range(n_req):
         if u[i] < 0.01:
@@ -1208,6 +1212,9 @@ def serve_schedule(args, rate, dur, nr, dim, n_ids, seed):
             cat(del_ids, np.int64, (0,)), kept, n_out)
 
 
+_SERVE_NEXT_ID = [50_000_000]  # ids of the rows the served streams add, fresh in every phase
+
+
 def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
     """The served stream (serve_schedule's requests) replayed by the
     library's native load generator (hann_serve_replay): the calling thread
@@ -1220,7 +1227,8 @@ def serve_stream(args, idx, q_host, gt, nr, rate, n_ids=None, seconds=None):
 
     dur = seconds or args.serve_seconds
     reqs, rows, add_ids, add_vecs, del_ids, kept, n_out = serve_schedule(
-        args, rate, dur, nr, q_host.shape[1], n_ids or args.n, args.seed + 7)
+        args, rate, dur, nr, q_host.shape[1], n_ids or args.n, args.seed + 7, _SERVE_NEXT_ID[0])
+    _SERVE_NEXT_ID[0] += len(add_ids)
     srv = hg.Server(idx, slots=4, max_batch_queries=8192, max_k=100, max_nprobe=256, mode=1,
                     memory_budget=120 << 30, max_batch_probes=args.serve_batch_probes)
     try:
