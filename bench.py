@@ -699,6 +699,14 @@ def main():
         except Exception:
             pass
 
+    fp8 = None
+    if rank == 0:
+        try:
+            fp8 = fp8_probe_study(torch, dev, idx.export_state()["coarse"], q, choice)
+            log("fp8 probe study", fp8)
+        except Exception as e:  # pragma: no cover
+            fp8 = {"error": str(e)}
+
     served = None
     if args.serve_seconds > 0:
         served = []
@@ -768,6 +776,7 @@ def main():
                          "bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
             "adc_tables": adc_tables,
             "autotune": tune,
+            "fp8_probe_study": fp8,
             "cpu_baseline": cb,
             "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
@@ -787,6 +796,44 @@ def main():
 
         dist.destroy_process_group()
     return 0
+
+
+def fp8_probe_study(torch, dev, coarse, q, nprobe, nq=2000):
+    """The FP8-e4m3 coarse-probe screen measured against the BF16 one on the
+    workload's own centroids and queries. The screen ranks centroids by
+    s~ = ||b||^2 - 2 <a~, b~> and the exact rescore must cover every centroid
+    with s~ <= T~ + 2 eps (T~ the nprobe-th smallest s~, eps the bound of the
+    operands' rounding: 2 (|a - a~| max|b| + |a~| max|b - b~|), plus FP32
+    accumulation). The band size is the exact work each screen leaves; FP8
+    rounds each operand to 3 mantissa bits (per-vector scale to e4m3's range)
+    against BF16's 8."""
+    a = q[:nq].double()
+    b = torch.as_tensor(coarse, device=dev).double()
+    bn2 = (b * b).sum(1)
+    out = {}
+
+    def rounded(x, kind):
+        if kind == "bf16":
+            return x.float().bfloat16().double()
+        scale = x.abs().amax(1, keepdim=True).clamp_min(1e-30) / 448.0
+        return (x.float() / scale.float()).to(torch.float8_e4m3fn).double() * scale
+
+    for kind in ("bf16", "fp8_e4m3"):
+        at, bt = rounded(a, kind), rounded(b, kind)
+        s_t = bn2[None, :] - 2.0 * (at @ bt.T)
+        ar = (a - at).norm(dim=1)
+        an = at.norm(dim=1)
+        bmax = b.norm(dim=1).max()
+        brmax = (b - bt).norm(dim=1).max()
+        kp = a.shape[1]
+        eps = 2.0 * (ar * bmax + an * brmax) + 2.0 * kp * 2.0 ** -22 * (an * (bmax + brmax))
+        thr = s_t.kthvalue(nprobe, dim=1).values + 2.0 * eps
+        band = (s_t <= thr[:, None]).sum(1).double()
+        out[kind] = {"band_mean": round(float(band.mean()), 1), "band_p99": float(band.quantile(0.99)),
+                     "band_max": int(band.max()), "operand_rel_err": round(float((ar / a.norm(dim=1)).mean()), 6)}
+    out["what"] = (f"{nq} queries x {b.shape[0]} centroids, nprobe {nprobe}: centroids the exact rescore must "
+                   "cover after each screen (the band), and the mean relative rounding error of the queries")
+    return out
 
 
 def config1_section(args, torch, dev):
