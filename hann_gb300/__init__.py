@@ -477,7 +477,7 @@ class Index:
         self._check(self._L.hann_pqivf_set_adc_tables(self._h, self.ADC_TABLES[kind]))
 
     def ADCRedos(self) -> int:
-        """Parity-mode queries the FP16 screen could not prove, scanned again
+        """Parity-mode queries the 16-bit screen could not prove, scanned again
         with FP32 tables, over the index's life."""
         out = np.zeros(1, dtype=np.int64)
         self._check(self._L.hann_pqivf_adc_redos(self._h, _ptr(out)))
