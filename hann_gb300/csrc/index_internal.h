@@ -182,7 +182,7 @@ struct LmsConfig {
     int seed = 0;
     int first = 1;         // probe ranks in the first chunk
     int growth = 32;       // each later chunk ends at growth x the previous end
-    int rows_max = 512;    // rows of one list per work item (the list-split threshold)
+    int rows_max = 1024;   // rows of one list per work item (the list-split threshold; the autotuner picked it on a 10M x 96 index)
     // Queries probing fewer lists take the table scan: below about this many
     // probes per query the table scan is faster (the autotuner measures it).
     int min_nprobe = 64;
