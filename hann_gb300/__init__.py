@@ -109,6 +109,7 @@ EXPORTED = (
 )
 # Entry points of include/hann_gb300_diag.h.
 EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats", "hann_pqivf_rows_decoded", "hann_pqivf_adc_redos",
+                 "hann_pqivf_train_stats",
                  "hann_pqivf_scan_options")
 
 
@@ -152,6 +153,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_plain_fp32.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_set_adc_tables.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_adc_redos.argtypes = [_P, _P]
+        L.hann_pqivf_train_stats.argtypes = [_P, _P]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_autotune_scan.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P, _P, _P]
         L.hann_pqivf_tune_candidate_clusters.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
@@ -475,6 +477,13 @@ class Index:
         if kind not in self.ADC_TABLES:
             raise ValueError(f"unknown lookup-table kind {kind!r}")
         self._check(self._L.hann_pqivf_set_adc_tables(self._h, self.ADC_TABLES[kind]))
+
+    def TrainStats(self) -> dict:
+        """Coarse k-means assignments that took the warm filter, and the rows
+        they sent to the exact kernel, over the index's life."""
+        out = np.zeros(2, dtype=np.int64)
+        self._check(self._L.hann_pqivf_train_stats(self._h, _ptr(out)))
+        return {"warm_assignments": int(out[0]), "warm_overflow_rows": int(out[1])}
 
     def ADCRedos(self) -> int:
         """Parity-mode queries the 16-bit screen could not prove, scanned again

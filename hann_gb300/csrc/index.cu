@@ -382,10 +382,35 @@ static int assign_rows(hann_pqivf* h, AssignScratch& sc, const float* x, int64_t
     CK(launch_to_bf16(cent, k, dim, kp, sc.cbf.p, sc.cn2.p, sc.cres.p, s));
     CK(launch_norm_maxes(sc.cn2.p, sc.cres.p, k, sc.cmax.p, s));
     CK(cudaMemsetAsync(sc.counters.p, 0, 2 * sizeof(int), s));
-    CK(launch_gemm_top8(sc.xbf.p, n, sc.cbf.p, k, kp, sc.cn2.p, sc.cand_idx.p, sc.cand_val.p, sc.counters.p + 1, s));
-    CK(launch_rescore_top8(x, sc.xn2.p, sc.xres.p, n, dim, kp, cent, k, sc.cmax.p, sc.cand_idx.p, sc.cand_val.p,
-                           out_idx,
-                           sc.ovf_rows.p, sc.counters.p, s));
+    CK(sc.d2.reserve((size_t)n));
+    // Warm: every row's nearest centroid is among those whose screened score
+    // lies under a bound from the row's previous centroid (launch_warm_bound),
+    // so the filter form of the GEMM keeps just those and an exact rescore
+    // picks among them; the top-8 screen otherwise.
+    constexpr int WARM_CAP = 32;
+    const bool warm = sc.warm_ok && sc.warm && !sc.warm_skip && sc.warm_k == k && sc.warm_n == n &&
+                      sc.warm_cent == cent;
+    if (warm) {
+        CK(sc.shift.reserve((size_t)k));
+        CK(sc.cterm.reserve((size_t)k));
+        CK(sc.rthr.reserve((size_t)n));
+        CK(sc.fcnt.reserve((size_t)n));
+        CK(sc.fcand.reserve((size_t)n * WARM_CAP));
+        CK(sc.fcand_s.reserve((size_t)n * WARM_CAP));
+        CK(launch_centroid_shift(cent, sc.cent_old.p, k, dim, sc.shift.p, s));
+        CK(launch_warm_bound(sc.d2.p, out_idx, sc.shift.p, sc.xn2.p, sc.xres.p, sc.cmax.p, kp, n, sc.rthr.p, s));
+        CK(launch_sq_terms(sc.cn2.p, k, sc.cterm.p, s));
+        CK(cudaMemsetAsync(sc.fcnt.p, 0, sizeof(int32_t) * (size_t)n, s));
+        CK(launch_gemm_filter(sc.xbf.p, n, sc.cbf.p, k, kp, 0, k, sc.cterm.p, 0, sc.rthr.p, WARM_CAP, sc.fcnt.p,
+                              sc.fcand.p, sc.fcand_s.p, sc.counters.p + 1, s, false));
+        CK(launch_rescore_filtered(x, n, dim, cent, sc.fcnt.p, sc.fcand.p, WARM_CAP, out_idx, sc.d2.p,
+                                   sc.ovf_rows.p, sc.counters.p, s));
+    } else {
+        CK(launch_gemm_top8(sc.xbf.p, n, sc.cbf.p, k, kp, sc.cn2.p, sc.cand_idx.p, sc.cand_val.p, sc.counters.p + 1,
+                            s));
+        CK(launch_rescore_top8(x, sc.xn2.p, sc.xres.p, n, dim, kp, cent, k, sc.cmax.p, sc.cand_idx.p,
+                               sc.cand_val.p, out_idx, sc.d2.p, sc.ovf_rows.p, sc.counters.p, s));
+    }
     int hc[2] = {0, 0};
     CK(cudaMemcpyAsync(hc, sc.counters.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -394,12 +419,28 @@ static int assign_rows(hann_pqivf* h, AssignScratch& sc, const float* x, int64_t
     if (novf > 0) {
         CK(sc.ovf_x.reserve((size_t)novf * dim));
         CK(sc.ovf_idx.reserve((size_t)novf));
+        CK(sc.ovf_d2.reserve((size_t)novf));
         DBuf<unsigned long long> keys;
         CK(keys.reserve((size_t)novf));
         CK(launch_copy_words(x, sc.ovf_rows.p, sc.ovf_x.p, nullptr, novf, dim, s));
-        CK(launch_assign_exact(sc.ovf_x.p, novf, dim, cent, k, sc.ovf_idx.p, nullptr, keys.p, s));
+        CK(launch_assign_exact(sc.ovf_x.p, novf, dim, cent, k, sc.ovf_idx.p, sc.ovf_d2.p, keys.p, s));
         CK(launch_copy_words(sc.ovf_idx.p, nullptr, out_idx, sc.ovf_rows.p, novf, 1, s));
+        CK(launch_copy_words(sc.ovf_d2.p, nullptr, sc.d2.p, sc.ovf_rows.p, novf, 1, s));
         CK(cudaStreamSynchronize(s));
+    }
+    h->warm_assignments += warm ? 1 : 0;
+    h->warm_overflow_rows += warm ? novf : 0;
+    if (sc.warm_ok) {
+        // the next assignment's bounds start from these centroids; after a
+        // warm assignment that overflowed on more than 1 row in 20 (the
+        // centroids still move far) the next one takes the top-8 screen
+        CK(sc.cent_old.reserve((size_t)k * dim));
+        CK(cudaMemcpyAsync(sc.cent_old.p, cent, sizeof(float) * (size_t)k * dim, cudaMemcpyDeviceToDevice, s));
+        sc.warm = true;
+        sc.warm_skip = warm && novf * 20 > n;
+        sc.warm_k = k;
+        sc.warm_n = n;
+        sc.warm_cent = cent;
     }
     return HANN_OK;
 }
@@ -705,6 +746,7 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     CK(C.reserve((size_t)k * dim));
     CK(asg.reserve((size_t)n));
     AssignScratch asc;
+    asc.warm_ok = true;  // iterations after the first, and the final assignment, may take the warm filter
     int rc = kmeans_device(h, X.p, dim, 0, n, dim, k, warm ? seeds.warm_iters : h->o.kmeans_iters, init, seeds, C.p,
                            asg.p, false, nullptr, 0, 0, &asc, seeds.warm_coarse);
     if (rc) return rc;
@@ -1842,6 +1884,15 @@ int hann_pqivf_rows_decoded(void* hv, int64_t* out) {
     if (!h || !out) return HANN_E_INVALID;
     std::lock_guard<std::mutex> rl(h->run_mu);
     *out = h->rows_decoded;
+    return HANN_OK;
+}
+
+int hann_pqivf_train_stats(void* hv, int64_t* out2) {
+    hann_pqivf* h = static_cast<hann_pqivf*>(hv);
+    if (!h || !out2) return HANN_E_INVALID;
+    std::unique_lock<std::mutex> w(h->wmu);
+    out2[0] = h->warm_assignments;
+    out2[1] = h->warm_overflow_rows;
     return HANN_OK;
 }
 

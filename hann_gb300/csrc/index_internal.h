@@ -115,8 +115,20 @@ struct AssignScratch {
     DBuf<int32_t> cand_idx, ovf_idx;
     DBuf<int64_t> ovf_rows;
     DBuf<int> counters;  // [0] overflow rows, [1] GEMM wait errors
-    DBuf<float> ovf_x;
+    DBuf<float> ovf_x, ovf_d2;
     bool x_ready = false;
+    // Warm assignments (k-means after its first iteration): each row's
+    // squared distance to its centroid, the centroids they were measured
+    // against, and the filter's buffers (assign_rows)
+    DBuf<float> d2, cent_old, shift, rthr, fcand_s;
+    DBuf<float2> cterm;
+    DBuf<int32_t> fcnt, fcand;
+    bool warm_ok = false;     // set by k-means for the iterations of one run
+    bool warm = false;        // d2 and cent_old hold the previous assignment's
+    bool warm_skip = false;   // the last warm assignment overflowed: take the top-8 screen once
+    int warm_k = 0;
+    int64_t warm_n = 0;
+    const float* warm_cent = nullptr;
 };
 
 // Scratch of Add/Delete, kept on the handle so mutations allocate nothing
@@ -283,6 +295,9 @@ struct hann_pqivf {
     std::atomic<bool> profile{false};
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev[4];
     std::atomic<int64_t> launches{0};  // kernels launched by searches (servers' threads included)
+    // k-means assignments that took the warm filter, and the rows they sent
+    // to the exact kernel (hann_pqivf_train_stats)
+    int64_t warm_assignments = 0, warm_overflow_rows = 0;
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];

@@ -121,8 +121,21 @@ cudaError_t launch_probe_select_band(float* S, const float* Q, const float* qn2,
 // left for the exact tiled kernel.
 cudaError_t launch_rescore_top8(const float* x, const float* xn2, const float* xres, int64_t n, int dim, int kp,
                                 const float* cent, int k, const float* cmax, const int32_t* cand_idx,
-                                const float* cand_val, int32_t* out_idx, int64_t* overflow_rows, int* n_overflow,
-                                cudaStream_t s);
+                                const float* cand_val, int32_t* out_idx, float* out_d2, int64_t* overflow_rows,
+                                int* n_overflow, cudaStream_t s);
+// Warm k-means assignment (after the first iteration): how far each centroid
+// moved, each row's bound on its best screened score from its previous
+// centroid's distance and shift, and the exact nearest among the centroids
+// the filter GEMM kept under that bound (rows over cap, or with none, to
+// overflow_rows for the exact kernel). out_d2: the reference-order squared
+// distance to the chosen centroid.
+cudaError_t launch_centroid_shift(const float* cnew, const float* cold, int k, int dim, float* shift,
+                                  cudaStream_t s);
+cudaError_t launch_warm_bound(const float* d2, const int32_t* prev, const float* shift, const float* xn2,
+                              const float* xres, const float* cmax, int kp, int64_t n, float* rthr, cudaStream_t s);
+cudaError_t launch_rescore_filtered(const float* x, int64_t n, int dim, const float* cent, const int32_t* cnt,
+                                    const int32_t* cand_id, int cap, int32_t* out_idx, float* out_d2,
+                                    int64_t* overflow_rows, int* n_overflow, cudaStream_t s);
 // Final step of the screened probe (kernels_rescore.cu): exact rescoring of
 // each query's band list, the np nearest lists ascending, fallback flags.
 // Queries flagged need_exact select on their whole exact row (Drow scratch,

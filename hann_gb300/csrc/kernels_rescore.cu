@@ -301,8 +301,8 @@ __global__ void rescore_top8_kernel(const float* __restrict__ x, const float* __
                                     const float* __restrict__ xres, int64_t n, int dim, int kp,
                                     const float* __restrict__ cent, int k, const float* __restrict__ cmax_p,
                                     const int32_t* __restrict__ cand_idx, const float* __restrict__ cand_val,
-                                    int32_t* __restrict__ out_idx, int64_t* __restrict__ overflow_rows,
-                                    int* __restrict__ n_overflow) {
+                                    int32_t* __restrict__ out_idx, float* __restrict__ out_d2,
+                                    int64_t* __restrict__ overflow_rows, int* __restrict__ n_overflow) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const float eps = bf16_score_eps(sqrtf(xn2[r]), xres[r], cmax_p[0], cmax_p[1], kp);
@@ -327,6 +327,77 @@ __global__ void rescore_top8_kernel(const float* __restrict__ x, const float* __
         }
     }
     out_idx[r] = bi == 0x7fffffff ? 0 : bi;
+    if (out_d2) out_d2[r] = bd;
+}
+
+// How far each centroid moved since the previous assignment: ||new - old||
+// (FP32, rounded up by a relative 1e-5 so it bounds the exact norm). One warp
+// per centroid.
+__global__ void centroid_shift_kernel(const float* __restrict__ cnew, const float* __restrict__ cold, int k, int dim,
+                                      float* __restrict__ shift) {
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (c >= k) return;
+    float acc = 0.0f;
+    for (int e = lane; e < dim; e += 32) {
+        const float t = cnew[(int64_t)c * dim + e] - cold[(int64_t)c * dim + e];
+        acc = fmaf(t, t, acc);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) shift[c] = sqrtf(acc) * 1.00001f + 1e-30f;
+}
+
+// The warm filter's bound on each row's best screened score. The row's
+// previous centroid c was at squared distance d2 (the reference-order FP32
+// value); it has moved by at most shift[c], so its exact score now, ||c||^2 -
+// 2 <x, c> = dist^2 - ||x||^2, is at most (sqrt(d2) + shift)^2 - ||x||^2, and
+// so is the exact score of the row's nearest centroid; its screened score
+// exceeds that by at most the screen's eps. The FP32 roundings of d2, the
+// shift and ||x||^2 (relative 1e-5 here, about 128 x 2^-24 at most) and of
+// the reference's distance (the 2e-5 slack the top-8 rescore uses) are
+// added on top.
+__global__ void warm_bound_kernel(const float* __restrict__ d2, const int32_t* __restrict__ prev,
+                                  const float* __restrict__ shift, const float* __restrict__ xn2,
+                                  const float* __restrict__ xres, const float* __restrict__ cmax_p, int kp, int64_t n,
+                                  float* __restrict__ rthr) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float eps = bf16_score_eps(sqrtf(xn2[r]), xres[r], cmax_p[0], cmax_p[1], kp);
+    const float rt = sqrtf(fmaxf(d2[r], 0.0f) * 1.00001f) + shift[prev[r]] * 1.00001f;
+    const float u = rt * rt * 1.00001f - xn2[r] * 0.99999f;
+    rthr[r] = u + eps + 2e-5f * (fabsf(u) + xn2[r]);
+}
+
+// The exact nearest centroid of every row among its filtered candidates
+// (cand_id [n][cap], count cnt[r]): reference-order FP32 distances, the
+// lowest index on a tie. The filter kept every centroid whose screened score
+// is under the row's warm bound, the nearest one among them; rows whose
+// count passed cap (or is 0) go to the exact kernel.
+__global__ void rescore_filtered_kernel(const float* __restrict__ x, int64_t n, int dim, const float* __restrict__ cent,
+                                        const int32_t* __restrict__ cnt, const int32_t* __restrict__ cand_id, int cap,
+                                        int32_t* __restrict__ out_idx, float* __restrict__ out_d2,
+                                        int64_t* __restrict__ overflow_rows, int* __restrict__ n_overflow) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int c = cnt[r];
+    if (c <= 0 || c > cap) {
+        overflow_rows[atomicAdd(n_overflow, 1)] = r;
+        return;
+    }
+    const float* xr = x + r * dim;
+    float bd = __int_as_float(0x7f800000);
+    int bi = 0x7fffffff;
+    for (int i = 0; i < c; i++) {
+        const int idx = cand_id[r * cap + i];
+        const float* cr = cent + (int64_t)idx * dim;
+        const float d = (dim & 3) == 0 ? sqeuclid_ref_v4(xr, cr, dim) : sqeuclid_ref(xr, cr, dim);
+        if (d < bd || (d == bd && idx < bi)) {
+            bd = d;
+            bi = idx;
+        }
+    }
+    out_idx[r] = bi;
+    out_d2[r] = bd;
 }
 
 __global__ void norm_maxes_kernel(const float* __restrict__ v, const float* __restrict__ res, int n,
@@ -416,11 +487,35 @@ cudaError_t launch_probe_final(const float* Q, int64_t nq, int dim, const float*
 
 cudaError_t launch_rescore_top8(const float* x, const float* xn2, const float* xres, int64_t n, int dim, int kp,
                                 const float* cent, int k, const float* cmax, const int32_t* cand_idx,
-                                const float* cand_val, int32_t* out_idx, int64_t* overflow_rows, int* n_overflow,
-                                cudaStream_t s) {
+                                const float* cand_val, int32_t* out_idx, float* out_d2, int64_t* overflow_rows,
+                                int* n_overflow, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     rescore_top8_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, xn2, xres, n, dim, kp, cent, k, cmax, cand_idx,
-                                                                   cand_val, out_idx, overflow_rows, n_overflow);
+                                                                   cand_val, out_idx, out_d2, overflow_rows,
+                                                                   n_overflow);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_centroid_shift(const float* cnew, const float* cold, int k, int dim, float* shift,
+                                  cudaStream_t s) {
+    if (k <= 0) return cudaSuccess;
+    centroid_shift_kernel<<<(unsigned)ceil_div(k, 8), 256, 0, s>>>(cnew, cold, k, dim, shift);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warm_bound(const float* d2, const int32_t* prev, const float* shift, const float* xn2,
+                              const float* xres, const float* cmax, int kp, int64_t n, float* rthr, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    warm_bound_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(d2, prev, shift, xn2, xres, cmax, kp, n, rthr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rescore_filtered(const float* x, int64_t n, int dim, const float* cent, const int32_t* cnt,
+                                    const int32_t* cand_id, int cap, int32_t* out_idx, float* out_d2,
+                                    int64_t* overflow_rows, int* n_overflow, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    rescore_filtered_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, n, dim, cent, cnt, cand_id, cap, out_idx,
+                                                                       out_d2, overflow_rows, n_overflow);
     return cudaGetLastError();
 }
 

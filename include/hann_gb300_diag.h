@@ -43,6 +43,13 @@ int hann_pqivf_rows_decoded(void* h, int64_t* out);
  * In mode 0 results do not depend on them. */
 int hann_pqivf_scan_options(void* h, const int32_t* set8, int32_t* get8);
 
+/* Coarse k-means assignments over the handle's life that took the warm
+ * filter (every row's nearest centroid bounded from its previous one, the
+ * filter GEMM keeping the centroids under the bound, an exact rescore among
+ * them) instead of the top-8 screen: out2[0] the assignments, out2[1] the
+ * rows they sent to the exact kernel. */
+int hann_pqivf_train_stats(void* h, int64_t* out2);
+
 /* Queries, over the handle's life, whose parity-mode top k the FP16
  * lookup-table screen could not prove and that were scanned again with FP32
  * tables (waits for the handle's searches). */

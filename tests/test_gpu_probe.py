@@ -73,6 +73,8 @@ def test_plain_fp32_mode_gives_identical_index_and_results(built, gpu):
     sa, sb = a.export_state(), b.export_state()
     for key in ("coarse", "codebooks", "list_len", "ids", "codes"):
         np.testing.assert_array_equal(sa[key], sb[key], err_msg=key)
+    # iterations 2 and 3 and the final assignment took the warm filter
+    assert a.TrainStats()["warm_assignments"] >= 2 and b.TrainStats()["warm_assignments"] == 0
     from tests.helpers import assert_same_results
     assert_same_results(*a.SearchBatch(q, 10, nprobe=40, mode=0), *b.SearchBatch(q, 10, nprobe=40, mode=0))
     ra = a.SearchBatch(q, 10, nprobe=40, mode=1)
