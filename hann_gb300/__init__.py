@@ -1005,7 +1005,8 @@ def _serve_lib():
     L.hann_serve_last_error.argtypes = [_P]
     L.hann_serve_last_error.restype = ctypes.c_char_p
     L.hann_serve_stop.argtypes = [_P]
-    L.hann_serve_replay.argtypes = [_P, _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P]
+    L.hann_serve_replay.argtypes = [_P, _P, ctypes.c_int64, _P, ctypes.c_int64, _P, ctypes.c_int64, _P, _P,
+                                    ctypes.c_int64, _P, ctypes.c_int64, _P, ctypes.c_int64, _P, _P]
     L._serve_ready = True
     return L
 
@@ -1108,11 +1109,14 @@ class Server:
         avec = np.ascontiguousarray(add_vectors if add_vectors is not None else np.zeros((0, q.shape[1])),
                                     dtype=np.float32)
         did = np.ascontiguousarray(del_ids if del_ids is not None else np.zeros(0), dtype=np.int64)
+        if aid.size != avec.shape[0]:
+            raise ValueError("add_ids and add_vectors must have the same rows")
         out = np.zeros(max(int(n_out_ids), 1), dtype=np.int64)
         lat = np.zeros(max(len(reqs), 1), dtype=np.float64)
         late = np.zeros(max(len(reqs), 1), dtype=np.float64)
-        self._check(self._L.hann_serve_replay(self._h, reqs.ctypes.data, len(reqs), _ptr(q), _ptr(rows), _ptr(aid),
-                                              _ptr(avec), _ptr(did), _ptr(out), _ptr(lat), _ptr(late)))
+        self._check(self._L.hann_serve_replay(self._h, reqs.ctypes.data, len(reqs), _ptr(q), q.shape[0], _ptr(rows),
+                                              rows.size, _ptr(aid), _ptr(avec), aid.size, _ptr(did), did.size,
+                                              _ptr(out), int(n_out_ids), _ptr(lat), _ptr(late)))
         return lat[:len(reqs)], late[:len(reqs)], out[:int(n_out_ids)]
 
     def stats(self) -> dict:

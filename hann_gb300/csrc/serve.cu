@@ -618,16 +618,25 @@ int hann_serve_stop(hann_server* s) {
 }
 
 int hann_serve_replay(hann_server* s, const hann_serve_request* reqs, int64_t n, const float* queries,
-                      const int64_t* query_rows, const int64_t* add_ids, const float* add_vectors,
-                      const int64_t* del_ids, int64_t* out_ids, double* latency_ms, double* late_ms) {
+                      int64_t n_queries, const int64_t* query_rows, int64_t n_query_rows, const int64_t* add_ids,
+                      const float* add_vectors, int64_t n_add, const int64_t* del_ids, int64_t n_del,
+                      int64_t* out_ids, int64_t n_out_ids, double* latency_ms, double* late_ms) {
     if (!s || (n > 0 && (!reqs || !latency_ms || !late_ms))) return serve_fail(HANN_E_INVALID, "null buffer");
     const int dim = s->h->o.dimension;
+    // every range a request names must lie inside the array it indexes
     for (int64_t i = 0; i < n; i++) {
         const hann_serve_request& r = reqs[i];
-        const bool ok = r.count >= 0 && r.first >= 0 &&
-                        (r.kind == 0 ? queries && query_rows && r.count > 0 && r.count <= INT32_MAX &&
-                                           (r.out_offset < 0 || out_ids)
-                                     : r.kind == 1 ? add_ids && add_vectors : r.kind == 2 && del_ids);
+        bool ok = r.count >= 0 && r.first >= 0 && r.at_ms >= 0.0;
+        if (ok && r.kind == 0) {
+            ok = queries && query_rows && r.count > 0 && r.count <= INT32_MAX && r.first + r.count <= n_query_rows &&
+                 (r.out_offset < 0 || (out_ids && r.k > 0 && r.out_offset + r.count * r.k <= n_out_ids));
+            for (int64_t j = 0; ok && j < r.count; j++)
+                ok = query_rows[r.first + j] >= 0 && query_rows[r.first + j] < n_queries;
+        } else if (ok && r.kind == 1) {
+            ok = add_ids && add_vectors && r.first + r.count <= n_add;
+        } else if (ok) {
+            ok = r.kind == 2 && del_ids && r.first + r.count <= n_del;
+        }
         if (!ok) return serve_fail(HANN_E_INVALID, "invalid request in the schedule");
     }
     // The waiter takes the tickets in submission order and records each

@@ -306,10 +306,12 @@ int hann_serve_stop(hann_server* s);
  * to within 0.2 ms, then spinning) while a native thread waits for each in
  * submission order, so neither the submission schedule nor the latency
  * depends on the caller's language runtime. Search requests take rows
- * query_rows[first .. first + count) of queries [*][dim]; BulkAdd requests
- * add_ids / add_vectors rows [first, first + count); BulkDelete requests
- * del_ids [first, first + count). A search with out_offset >= 0 copies its
- * ids ([count][k]) to out_ids + out_offset. Per request: latency_ms[i]
+ * query_rows[first .. first + count) of queries [n_queries][dim]; BulkAdd
+ * requests add_ids / add_vectors rows [first, first + count) of n_add;
+ * BulkDelete requests del_ids [first, first + count) of n_del. A search with
+ * out_offset >= 0 copies its ids ([count][k]) to out_ids + out_offset (of
+ * n_out_ids). A request naming a range outside its array is refused
+ * (HANN_E_INVALID) before anything is submitted. Per request: latency_ms[i]
  * (submit to completion, the server's clock) and late_ms[i] (how long after
  * its arrival time it was submitted). */
 typedef struct {
@@ -321,8 +323,9 @@ typedef struct {
     int64_t out_offset;  /* search: where its ids go in out_ids, -1 = not kept */
 } hann_serve_request;
 int hann_serve_replay(hann_server* s, const hann_serve_request* reqs, int64_t n, const float* queries,
-                      const int64_t* query_rows, const int64_t* add_ids, const float* add_vectors,
-                      const int64_t* del_ids, int64_t* out_ids, double* latency_ms, double* late_ms);
+                      int64_t n_queries, const int64_t* query_rows, int64_t n_query_rows, const int64_t* add_ids,
+                      const float* add_vectors, int64_t n_add, const int64_t* del_ids, int64_t n_del,
+                      int64_t* out_ids, int64_t n_out_ids, double* latency_ms, double* late_ms);
 
 /* ---- persisted state (Save/Load, pqivf/index.go:969-1101) ----------------
  * The binding encodes/decodes the reference's gob stream itself and moves

@@ -199,3 +199,29 @@ def test_native_replay(index):
             # it may or may not have seen the delete)
             assert not (set(got.ravel().tolist()) & set(del_ids.tolist()))
             np.testing.assert_array_equal(got, want)
+
+
+def test_native_replay_refuses_bad_ranges(index):
+    """A schedule naming a query row, an id range or an output slot outside
+    its array is refused before anything is submitted."""
+    idx, x, rng = index
+    q = rng.normal(size=(10, 32)).astype(np.float32)
+    with hg.Server(idx, slots=1, max_batch_queries=64, max_k=10, max_nprobe=8) as srv:
+        for bad in ("row", "range", "out", "del"):
+            reqs = np.zeros(1, dtype=hg.Server.REQUEST_DTYPE)
+            reqs[0]["kind"], reqs[0]["k"], reqs[0]["nprobe"], reqs[0]["count"] = 0, 5, 4, 2
+            rows = np.array([0, 1])
+            n_out = 10
+            reqs[0]["out_offset"] = 0
+            if bad == "row":
+                rows = np.array([0, 10])          # past the 10 query rows
+            elif bad == "range":
+                reqs[0]["first"] = 1              # rows [1, 3) of 2
+            elif bad == "out":
+                n_out = 9                         # 2 x 5 ids do not fit
+            else:
+                reqs[0]["kind"], reqs[0]["count"] = 2, 5  # 5 ids of an empty list
+            with pytest.raises(hg.HannError) as e:
+                srv.replay(reqs, q, rows, n_out_ids=n_out)
+            assert e.value.code == hg.HANN_E_INVALID
+        assert srv.stats()["requests"] == 0
