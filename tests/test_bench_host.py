@@ -6,6 +6,7 @@ import os
 import sys
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
@@ -135,3 +136,18 @@ def test_serve_schedule_records():
         end += len(r) * k
     assert end == n_out
     assert (reqs["out_offset"][~s] == 0).all()
+
+
+def test_fp8_probe_study_on_cpu():
+    """The FP8-against-BF16 probe study: each screen's band holds at least
+    nprobe centroids, FP8's rounding error and band are the larger."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    c = rng.standard_normal((512, 32)).astype(np.float32)
+    c /= np.linalg.norm(c, axis=1, keepdims=True)
+    q = torch.from_numpy((c[rng.integers(0, 512, 64)] + 0.3 * rng.standard_normal((64, 32))).astype(np.float32))
+    r = bench.fp8_probe_study(torch, torch.device("cpu"), c, q, 8, nq=64)
+    for kind in ("bf16", "fp8_e4m3"):
+        assert r[kind]["band_mean"] >= 8 and r[kind]["band_max"] <= 512
+    assert r["fp8_e4m3"]["operand_rel_err"] > 4 * r["bf16"]["operand_rel_err"]
+    assert r["fp8_e4m3"]["band_mean"] > r["bf16"]["band_mean"]
