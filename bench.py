@@ -949,7 +949,8 @@ def train_section(args, torch, dev):
         rows = torch.from_numpy(st["ids"]).to(dev)
         d = x[rows].double() - cent[lab_of]
         inertia = float((d * d).sum().item())
-        out[name] = {"train_s": round(el, 3), "s_per_iteration": round(el / iters, 4), "inertia_fp64": inertia}
+        out[name] = {"train_s": round(el, 3), "s_per_iteration": round(el / iters, 4), "inertia_fp64": inertia,
+                     "phases": idx.TrainPhases()}
         states[name] = st
         log("train", name, out[name])
         if not plain:

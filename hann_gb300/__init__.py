@@ -108,8 +108,9 @@ EXPORTED = (
     "hann_knn_distance_gather_device",
 )
 # Entry points of include/hann_gb300_diag.h.
-EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_pqivf_arena_stats", "hann_pqivf_rows_decoded", "hann_pqivf_adc_redos",
-                 "hann_pqivf_train_stats",
+EXPORTED_DIAG = ("hann_gpu_bf16_scores", "hann_gpu_pq_assign", "hann_pqivf_arena_stats", "hann_pqivf_rows_decoded",
+                 "hann_pqivf_adc_redos",
+                 "hann_pqivf_train_stats", "hann_pqivf_train_phases",
                  "hann_pqivf_scan_options")
 
 
@@ -154,6 +155,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         L.hann_pqivf_set_adc_tables.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_adc_redos.argtypes = [_P, _P]
         L.hann_pqivf_train_stats.argtypes = [_P, _P]
+        L.hann_pqivf_train_phases.argtypes = [_P, _P]
         L.hann_pqivf_set_candidate_clusters.argtypes = [_P, ctypes.c_int32]
         L.hann_pqivf_autotune_scan.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, _P, _P, _P]
         L.hann_pqivf_tune_candidate_clusters.argtypes = [_P, _P, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
@@ -484,6 +486,13 @@ class Index:
         out = np.zeros(2, dtype=np.int64)
         self._check(self._L.hann_pqivf_train_stats(self._h, _ptr(out)))
         return {"warm_assignments": int(out[0]), "warm_overflow_rows": int(out[1])}
+
+    def TrainPhases(self) -> dict:
+        """Wall milliseconds of the last Train or Retrain by phase: staging the
+        vectors, coarse k-means, subquantizer k-means, lists and layout."""
+        out = np.zeros(4, dtype=np.float64)
+        self._check(self._L.hann_pqivf_train_phases(self._h, _ptr(out)))
+        return dict(zip(("stage_ms", "coarse_ms", "pq_ms", "layout_ms"), (round(float(v), 2) for v in out)))
 
     def ADCRedos(self) -> int:
         """Parity-mode queries the 16-bit screen could not prove, scanned again

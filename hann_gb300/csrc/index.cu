@@ -11,6 +11,7 @@
 // Rows of one inverted list are contiguous; every list starts on a multiple
 // of 32 rows and keeps spare capacity so Adds append in place.
 #include <cuda_fp16.h>
+#include <chrono>
 
 #include "index_internal.h"
 #include "hann_gb300_diag.h"
@@ -519,7 +520,7 @@ int add_commit(hann_pqivf* h, const int64_t* ids) {
         h->list_ids[c].push_back(ids[i]);
         h->list_alive[c].push_back(1);
         h->live_count[c]++;
-        h->id_cluster[ids[i]] = c;
+        h->id_cluster.set(ids[i], c);
         h->cluster_counts[c]++;
         h->list_key[c] = 1;
     }
@@ -554,9 +555,9 @@ static int remove_rows(hann_pqivf* h, const std::vector<int64_t>& ids) {
     if (ids.empty()) return HANN_OK;
     std::vector<int64_t> rows;
     for (int64_t id : ids) {
-        auto it = h->id_cluster.find(id);
-        if (it == h->id_cluster.end()) continue;
-        const int l = it->second;
+        const int32_t* lp = h->id_cluster.find(id);
+        if (!lp) continue;
+        const int l = *lp;
         auto& lst = h->list_ids[l];
         for (size_t j = 0; j < lst.size(); j++) {
             if (h->list_alive[l][j] && lst[j] == id) {
@@ -568,7 +569,7 @@ static int remove_rows(hann_pqivf* h, const std::vector<int64_t>& ids) {
         h->live_count[l]--;
         h->cluster_counts[l]--;
         h->dead_rows++;
-        h->id_cluster.erase(it);
+        h->id_cluster.erase(id);
     }
     if (!rows.empty()) {
         CK(upload(h->mut.rows, rows.data(), rows.size(), h->stream));
@@ -689,42 +690,56 @@ static int kmeans_device(hann_pqivf* h, const float* x, int64_t ld, int off, int
     return HANN_OK;
 }
 
+static double ms_since(std::chrono::steady_clock::time_point t) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+}
+
 static int train_impl(hann_pqivf* h, SeedSource seeds) {
     h->mut.held = false;
+    auto t_phase = std::chrono::steady_clock::now();
+    for (double& v : h->train_phase_ms) v = 0;
     const int dim = h->o.dimension, M = h->o.num_subquantizers;
     // Consolidate every vector, clustered and pending, in ascending id order.
+    // Source of each vector: its row in the device lists (>= 0), or -(slot + 1)
+    // for slot `slot` of the pending array, which is uploaded whole.
     std::vector<std::pair<int64_t, int64_t>> all;  // (id, source)
     all.reserve(h->id_cluster.size() + h->pending.size());
     for (int l = 0; l < h->nlist; l++)
         for (size_t j = 0; j < h->list_ids[l].size(); j++)
             if (h->list_alive[l][j]) all.emplace_back(h->list_ids[l][j], h->h_start[l] + (int64_t)j);
-    std::vector<const std::vector<float>*> pend;
-    for (auto& kv : h->pending) {
-        all.emplace_back(kv.first, -(int64_t)pend.size() - 1);
-        pend.push_back(&kv.second);
-    }
+    const PendingStore& pend = h->pending;
+    for (size_t i = 0; i < pend.slot_id.size(); i++)
+        if (pend.slot_live[i]) all.emplace_back(pend.slot_id[i], -(int64_t)i - 1);
     const int64_t n = (int64_t)all.size();
     if (n < h->o.coarse_k)
         return h->fail(HANN_E_STATE, "not enough vectors (%lld) to train coarse quantizer with %d clusters",
                        (long long)n, h->o.coarse_k);
     if (n >= (int64_t)1 << 31) return h->fail(HANN_E_UNSUPPORTED, "more than 2^31 vectors");
-    std::sort(all.begin(), all.end());
+    if (!std::is_sorted(all.begin(), all.end())) std::sort(all.begin(), all.end());
     std::vector<int64_t> ids(n), src(n);
+    bool direct = pend.dim == dim && (int64_t)pend.slot_id.size() == n;  // every vector pending, slots in id order
     for (int64_t i = 0; i < n; i++) {
         ids[i] = all[i].first;
         src[i] = all[i].second;
+        direct = direct && src[i] == -i - 1;
     }
-    std::vector<float> staging(pend.size() * (size_t)dim);
-    for (size_t i = 0; i < pend.size(); i++) std::memcpy(&staging[i * dim], pend[i]->data(), sizeof(float) * dim);
-    DBuf<float> X, dstage;
-    DBuf<int64_t> dsrc;
+    std::vector<std::pair<int64_t, int64_t>>().swap(all);
+    DBuf<float> X;
     CK(X.reserve((size_t)n * dim));
-    CK(upload(dstage, staging.data(), staging.size(), h->stream));
-    CK(upload(dsrc, src.data(), src.size(), h->stream));
-    CK(launch_gather2(h->d_vectors.p ? h->d_vectors.p : X.p, dstage.p, dsrc.p, n, dim, X.p, h->stream));
+    if (direct) {
+        CK(cudaMemcpyAsync(X.p, pend.vec.data(), sizeof(float) * (size_t)n * dim, cudaMemcpyHostToDevice,
+                           h->stream));
+    } else {
+        DBuf<float> dstage;
+        DBuf<int64_t> dsrc;
+        if (!pend.vec.empty()) CK(upload(dstage, pend.vec.data(), pend.vec.size(), h->stream));
+        CK(upload(dsrc, src.data(), src.size(), h->stream));
+        CK(launch_gather2(h->d_vectors.p ? h->d_vectors.p : X.p, dstage.p, dsrc.p, n, dim, X.p, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
     CK(cudaStreamSynchronize(h->stream));
-    staging.clear();
-    staging.shrink_to_fit();
+    h->train_phase_ms[0] = ms_since(t_phase);
+    t_phase = std::chrono::steady_clock::now();
 
     // Coarse k-means (runKMeans(allVectors, coarseK, iters)).
     const int k = (int)std::min<int64_t>(h->o.coarse_k, n);
@@ -756,6 +771,8 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     std::vector<int32_t> hasg(n);
     CK(cudaMemcpyAsync(hasg.data(), asg.p, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    h->train_phase_ms[1] = ms_since(t_phase);
+    t_phase = std::chrono::steady_clock::now();
     std::vector<int64_t> cnt(k, 0);
     for (int64_t i = 0; i < n; i++) cnt[hasg[i]]++;
     std::vector<int64_t> off(k + 1, 0);
@@ -801,6 +818,8 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
         if (rc) return rc;
     }
     Rm.reset();
+    h->train_phase_ms[2] = ms_since(t_phase);
+    t_phase = std::chrono::steady_clock::now();
 
     // New layout and state.
     h->nlist = k;
@@ -809,10 +828,12 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     h->list_key.assign(k, 0);
     h->cluster_counts.assign(k, 0);
     h->id_cluster.clear();
+    h->id_cluster.reserve((size_t)n);
+    for (int c = 0; c < k; c++) h->list_ids[c].reserve((size_t)cnt[c]);
     for (int64_t j = 0; j < n; j++) {
         const int c = ord_cluster[j];
         h->list_ids[c].push_back(ids[order[j]]);
-        h->id_cluster[ids[order[j]]] = c;
+        h->id_cluster.set(ids[order[j]], c);
     }
     h->list_alive.assign(k, {});
     h->live_count.assign(k, 0);
@@ -868,7 +889,11 @@ static int train_impl(hann_pqivf* h, SeedSource seeds) {
     h->trained = true;
     rc = prepare_coarse(h);
     if (rc) return rc;
-    return upload_lens(h);
+    rc = upload_lens(h);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->stream));
+    h->train_phase_ms[3] = ms_since(t_phase);
+    return HANN_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1390,7 +1415,8 @@ int bulk_add_locked(hann_pqivf* h, const int64_t* ids, const float* vectors, int
     const int dim = h->o.dimension;
     std::vector<int64_t> order(n);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return ids[a] < ids[b]; });
+    if (!std::is_sorted(ids, ids + n))
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return ids[a] < ids[b]; });
     // First failing position in ascending id order; everything before it is
     // applied, as the reference's loop does (pqivf/index.go:276-296).
     int64_t f = n;
@@ -1413,9 +1439,10 @@ int bulk_add_locked(hann_pqivf* h, const int64_t* ids, const float* vectors, int
         }
     }
     if (!h->trained) {
+        h->pending.reserve_more((size_t)f, dim);
         for (int64_t i = 0; i < f; i++) {
             const int64_t r = order[i];
-            h->pending[ids[r]] = std::vector<float>(vectors + r * dim, vectors + (r + 1) * dim);
+            h->pending.put(ids[r], vectors + r * dim, dim);
         }
     } else if (f > 0) {
         std::vector<int64_t> sid(f);
@@ -1455,11 +1482,7 @@ static int delete_ids(hann_pqivf* h, std::vector<int64_t> ids, bool strict) {
     std::vector<int64_t> trained_side;
     std::unordered_set<int64_t> seen;
     for (int64_t id : ids) {
-        auto pit = h->pending.find(id);
-        if (pit != h->pending.end()) {
-            h->pending.erase(pit);
-            continue;
-        }
+        if (h->pending.erase(id)) continue;
         if (!h->id_cluster.count(id) || seen.count(id)) {
             if (strict) {
                 int rc = remove_rows(h, trained_side);
@@ -1523,7 +1546,8 @@ int hann_pqivf_bulk_update(hann_pqivf* h, const int64_t* ids, const float* vecto
     const int dim = h->o.dimension;
     std::vector<int64_t> order(n);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return ids[a] < ids[b]; });
+    if (!std::is_sorted(ids, ids + n))
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return ids[a] < ids[b]; });
     // Delete-then-add per id in ascending order; the first id that is not
     // present stops the batch (pqivf/index.go:435-442).
     int64_t f = n;
@@ -1545,7 +1569,7 @@ int hann_pqivf_bulk_update(hann_pqivf* h, const int64_t* ids, const float* vecto
     int rc = delete_ids(h, del, false);
     if (rc) return rc;
     if (!h->trained) {
-        for (int64_t r : last_pos) h->pending[ids[r]] = std::vector<float>(vectors + r * dim, vectors + (r + 1) * dim);
+        for (int64_t r : last_pos) h->pending.put(ids[r], vectors + r * dim, dim);
     } else if (!last_pos.empty()) {
         std::vector<int64_t> sid;
         std::vector<float> sv;
@@ -1896,6 +1920,14 @@ int hann_pqivf_train_stats(void* hv, int64_t* out2) {
     return HANN_OK;
 }
 
+int hann_pqivf_train_phases(void* hv, double* out4) {
+    hann_pqivf* h = static_cast<hann_pqivf*>(hv);
+    if (!h || !out4) return HANN_E_INVALID;
+    std::unique_lock<std::mutex> w(h->wmu);
+    for (int i = 0; i < 4; i++) out4[i] = h->train_phase_ms[i];
+    return HANN_OK;
+}
+
 int hann_pqivf_adc_redos(void* hv, int64_t* out) {
     hann_pqivf* h = static_cast<hann_pqivf*>(hv);
     if (!h || !out) return HANN_E_INVALID;
@@ -2147,12 +2179,10 @@ int hann_pqivf_export(hann_pqivf* h, const hann_pqivf_layout* layout, float* coa
         }
     }
     // Pending vectors in ascending id order.
-    std::vector<int64_t> pid;
-    for (auto& kv : h->pending) pid.push_back(kv.first);
-    std::sort(pid.begin(), pid.end());
+    const std::vector<int64_t> pid = h->pending.sorted_ids();
     for (size_t i = 0; i < pid.size(); i++) {
         pending_ids[i] = pid[i];
-        std::memcpy(pending_vectors + i * dim, h->pending[pid[i]].data(), sizeof(float) * dim);
+        std::memcpy(pending_vectors + i * dim, h->pending.find(pid[i]), sizeof(float) * dim);
     }
     return HANN_OK;
 }
@@ -2207,8 +2237,8 @@ int import_locked(hann_pqivf* h, const hann_pqivf_layout* L, const float* coarse
     const int dim = L->dimension, M = L->num_subquantizers;
     h->trained = L->trained != 0;
     h->pending.clear();
-    for (int64_t i = 0; i < L->n_pending; i++)
-        h->pending[pending_ids[i]] = std::vector<float>(pending_vectors + i * dim, pending_vectors + (i + 1) * dim);
+    h->pending.reserve_more((size_t)L->n_pending, dim);
+    for (int64_t i = 0; i < L->n_pending; i++) h->pending.put(pending_ids[i], pending_vectors + i * dim, dim);
     h->nlist = L->nlist;
     h->pqk_eff = L->pq_k_eff;
     h->h_coarse.assign(coarse, coarse + (size_t)L->nlist * dim);
@@ -2220,13 +2250,14 @@ int import_locked(hann_pqivf* h, const hann_pqivf_layout* L, const float* coarse
     h->list_key.assign(h->nlist, 0);
     h->cluster_counts.assign(h->nlist, 0);
     h->id_cluster.clear();
+    h->id_cluster.reserve((size_t)L->n_rows);
     int64_t r = 0;
     for (int l = 0; l < h->nlist; l++) {
         h->list_key[l] = list_key[l];
         h->cluster_counts[l] = cluster_counts[l];
         for (int64_t j = 0; j < list_len[l]; j++, r++) {
             h->list_ids[l].push_back(ids[r]);
-            h->id_cluster[ids[r]] = l;
+            h->id_cluster.set(ids[r], l);
         }
         h->list_alive[l].assign(h->list_ids[l].size(), 1);
         h->live_count[l] = (int64_t)h->list_ids[l].size();

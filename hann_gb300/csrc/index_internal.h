@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "hann_gb300.h"
+#include "host_maps.h"
 #include "common.cuh"
 #include "kernels.h"
 
@@ -218,7 +219,7 @@ struct hann_pqivf {
     bool trained = false;
     std::atomic<int64_t> fallback_searches{0};
 
-    std::unordered_map<int64_t, std::vector<float>> pending;
+    PendingStore pending;
 
     int nlist = 0, pqk_eff = 0;
     std::vector<float> h_coarse, h_codebooks;
@@ -228,7 +229,7 @@ struct hann_pqivf {
     int64_t dead_rows = 0;
     std::vector<uint8_t> list_key;
     std::vector<int64_t> cluster_counts;
-    std::unordered_map<int64_t, int32_t> id_cluster;
+    IdMap<int32_t> id_cluster;
     std::vector<int64_t> h_start, h_cap;
     // Row arena: lists packed from 0 up to arena_end, then free slack up to
     // rows_cap; a list that outgrows its capacity moves to the slack and
@@ -298,6 +299,8 @@ struct hann_pqivf {
     // k-means assignments that took the warm filter, and the rows they sent
     // to the exact kernel (hann_pqivf_train_stats)
     int64_t warm_assignments = 0, warm_overflow_rows = 0;
+    // wall milliseconds of the last training's phases (hann_pqivf_train_phases)
+    double train_phase_ms[4] = {0, 0, 0, 0};
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];

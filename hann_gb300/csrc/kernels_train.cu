@@ -6,6 +6,7 @@
 // encodeWithCodebooks do (pqivf/index.go:641-666, 738-789). Centroid sums are
 // FP64 on the device (the reference sums in FP32 in point order,
 // pqivf/index.go:816-843); the mean is rounded once to FP32.
+#include "hann_gb300.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "tile_dist.cuh"
@@ -267,6 +268,109 @@ __global__ void __launch_bounds__(256) pq_assign_kernel(const float* __restrict_
     out[p * M + m] = bi;
 }
 
+// Packed form for sub-dimensions 4, 8 and 16: two points a thread, every
+// distance computed with the FP32x2 instructions (sub/mul/fma/add.rn.f32x2,
+// each half rounded as the scalar instruction rounds it) in sqeuclid_ref's
+// order. The codebook sits in shared memory with every float stored twice,
+// so one 16-byte broadcast load gives two codeword coordinates already
+// paired for both points. sqeuclid_ref's first fma into a zero accumulator
+// equals the product (d*d is never -0), and its additions of the untouched
+// zero accumulators for sub-dimensions below 16 leave a sum of squares
+// unchanged, so both are left out: the distances are sqeuclid_ref's bits.
+using u64 = unsigned long long;
+__device__ __forceinline__ u64 pk_sub(u64 a, u64 b) {
+    u64 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 pk_mul(u64 a, u64 b) {
+    u64 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 pk_fma(u64 a, u64 b, u64 c) {
+    u64 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ u64 pk_add(u64 a, u64 b) {
+    u64 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ u64 pk_pair(float lo, float hi) {
+    return (u64)__float_as_uint(lo) | ((u64)__float_as_uint(hi) << 32);
+}
+
+template <int DSUB>
+__device__ __forceinline__ u64 pk_sqeuclid(const u64 (&s)[DSUB], const ulonglong2* __restrict__ c) {
+    u64 d[DSUB];
+#pragma unroll
+    for (int q = 0; q < DSUB / 2; q++) {
+        const ulonglong2 w = c[q];
+        d[2 * q] = pk_sub(s[2 * q], w.x);
+        d[2 * q + 1] = pk_sub(s[2 * q + 1], w.y);
+    }
+    u64 v[4];
+    if (DSUB == 4) {
+#pragma unroll
+        for (int l = 0; l < 4; l++) v[l] = pk_mul(d[l], d[l]);
+    } else if (DSUB == 8) {
+#pragma unroll
+        for (int l = 0; l < 4; l++) v[l] = pk_fma(d[4 + l], d[4 + l], pk_mul(d[l], d[l]));
+    } else {
+#pragma unroll
+        for (int l = 0; l < 4; l++)
+            v[l] = pk_add(pk_add(pk_mul(d[l], d[l]), pk_mul(d[4 + l], d[4 + l])),
+                          pk_add(pk_mul(d[8 + l], d[8 + l]), pk_mul(d[12 + l], d[12 + l])));
+    }
+    return pk_add(pk_add(v[0], v[1]), pk_add(v[2], v[3]));
+}
+
+constexpr int PQ_PACK_THREADS = 256;
+
+template <int DSUB>
+__global__ void __launch_bounds__(PQ_PACK_THREADS) pq_assign_packed_kernel(const float* __restrict__ res, int64_t n,
+                                                                           int M, const float* __restrict__ cb,
+                                                                           int pqK, int m_begin,
+                                                                           int32_t* __restrict__ out) {
+    extern __shared__ __align__(16) float scb2[];  // [pqK][DSUB][2]
+    const int m = m_begin + blockIdx.y;
+    const int dim = M * DSUB;
+    for (int e = threadIdx.x; e < pqK * DSUB; e += blockDim.x) {
+        const float v = cb[(int64_t)m * pqK * DSUB + e];
+        scb2[2 * e] = v;
+        scb2[2 * e + 1] = v;
+    }
+    __syncthreads();
+    const int64_t p0 = (int64_t)blockIdx.x * (2 * PQ_PACK_THREADS) + threadIdx.x;
+    const int64_t p1 = p0 + PQ_PACK_THREADS;
+    if (p0 >= n) return;
+    const bool has1 = p1 < n;
+    u64 s[DSUB];
+#pragma unroll
+    for (int e = 0; e < DSUB; e++)
+        s[e] = pk_pair(res[p0 * dim + m * DSUB + e], has1 ? res[p1 * dim + m * DSUB + e] : 0.0f);
+    const ulonglong2* c2 = reinterpret_cast<const ulonglong2*>(scb2);
+    u64 d = pk_sqeuclid<DSUB>(s, c2);
+    float b0 = __uint_as_float((uint32_t)d), b1 = __uint_as_float((uint32_t)(d >> 32));
+    int i0 = 0, i1 = 0;
+    for (int j = 1; j < pqK; j++) {
+        d = pk_sqeuclid<DSUB>(s, c2 + j * (DSUB / 2));
+        const float e0 = __uint_as_float((uint32_t)d), e1 = __uint_as_float((uint32_t)(d >> 32));
+        if (e0 < b0) {
+            b0 = e0;
+            i0 = j;
+        }
+        if (e1 < b1) {
+            b1 = e1;
+            i1 = j;
+        }
+    }
+    out[p0 * M + m] = i0;
+    if (has1) out[p1 * M + m] = i1;
+}
+
 // Generic sub-dimension: sub-vector read from global memory.
 __global__ void __launch_bounds__(256) pq_assign_generic_kernel(const float* __restrict__ res, int64_t n, int M,
                                                                 int dsub, const float* __restrict__ cb, int pqK,
@@ -299,6 +403,17 @@ cudaError_t launch_pq_assign(const float* res, int64_t n, int M, int dsub, const
         cudaError_t e = cudaFuncSetAttribute(pq_assign_generic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
+    }
+    const size_t smem2 = 2 * smem;
+    if ((dsub == 4 || dsub == 8 || dsub == 16) && smem2 <= 48 * 1024) {
+        dim3 g2((unsigned)ceil_div(n, 2 * PQ_PACK_THREADS), (unsigned)(m_end - m_begin));
+        if (dsub == 4)
+            pq_assign_packed_kernel<4><<<g2, PQ_PACK_THREADS, smem2, s>>>(res, n, M, codebooks, pqK, m_begin, out);
+        else if (dsub == 8)
+            pq_assign_packed_kernel<8><<<g2, PQ_PACK_THREADS, smem2, s>>>(res, n, M, codebooks, pqK, m_begin, out);
+        else
+            pq_assign_packed_kernel<16><<<g2, PQ_PACK_THREADS, smem2, s>>>(res, n, M, codebooks, pqK, m_begin, out);
+        return cudaGetLastError();
     }
     dim3 grid((unsigned)ceil_div(n, 256), (unsigned)(m_end - m_begin));
     switch (smem > 48 * 1024 ? 0 : dsub) {
@@ -687,3 +802,33 @@ cudaError_t launch_tombstone(const int64_t* rows, int64_t n, float* term, int64_
 }
 
 }  // namespace hann
+
+// Subquantizer assignment of host residuals: res [n][M * dsub], codebooks
+// [M][pqK][dsub], out [n][M] the nearest codeword of every row and
+// subquantizer, as one k-means iteration of training computes it.
+extern "C" int hann_gpu_pq_assign(const float* res, int64_t n, int32_t M, int32_t dsub, const float* codebooks,
+                                  int32_t pqK, int32_t* out) {
+    using namespace hann;
+    if (n <= 0 || M <= 0 || dsub <= 0 || pqK <= 0 || pqK > 256 || !res || !codebooks || !out) return HANN_E_INVALID;
+    float *dr = nullptr, *dc = nullptr;
+    int32_t* dout = nullptr;
+    int rc = HANN_OK;
+    auto ok = [&](cudaError_t e) {
+        if (e != cudaSuccess && rc == HANN_OK) rc = HANN_E_CUDA;
+        return e == cudaSuccess;
+    };
+    const size_t nr = (size_t)n * M * dsub, nc = (size_t)M * pqK * dsub;
+    if (ok(cudaMalloc(&dr, sizeof(float) * nr)) && ok(cudaMalloc(&dc, sizeof(float) * nc)) &&
+        ok(cudaMalloc(&dout, sizeof(int32_t) * (size_t)n * M))) {
+        ok(cudaMemcpy(dr, res, sizeof(float) * nr, cudaMemcpyHostToDevice));
+        ok(cudaMemcpy(dc, codebooks, sizeof(float) * nc, cudaMemcpyHostToDevice));
+        for (int m = 0; m < M && rc == HANN_OK; m++)
+            ok(launch_pq_assign(dr, n, M, dsub, dc, pqK, m, m + 1, dout, nullptr));
+        ok(cudaDeviceSynchronize());
+        ok(cudaMemcpy(out, dout, sizeof(int32_t) * (size_t)n * M, cudaMemcpyDeviceToHost));
+    }
+    cudaFree(dr);
+    cudaFree(dc);
+    cudaFree(dout);
+    return rc;
+}

@@ -223,11 +223,9 @@ int hann_pqivf_save_snapshot(hann_pqivf* h, const char* path) {
         if (e != cudaSuccess) rc = h->cuda_fail(e, "snapshot gather");
     }
     if (rc == HANN_OK) {
-        std::vector<int64_t> pid;
-        for (auto& kv : h->pending) pid.push_back(kv.first);
-        std::sort(pid.begin(), pid.end());
+        const std::vector<int64_t> pid = h->pending.sorted_ids();
         w.put(pid.data(), sizeof(int64_t) * pid.size());
-        for (int64_t id : pid) w.put(h->pending.at(id).data(), sizeof(float) * dim);
+        for (int64_t id : pid) w.put(h->pending.find(id), sizeof(float) * dim);
         const uint64_t sum = w.ck.value();
         if (w.ok) w.ok = std::fwrite(&sum, 8, 1, w.f) == 1 && std::fwrite(MAGIC_END, 1, 8, w.f) == 8;
         if (!w.ok) rc = h->fail(HANN_E_INVALID, "write to %s failed", path);

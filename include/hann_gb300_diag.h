@@ -21,6 +21,13 @@ extern "C" {
 int hann_gpu_bf16_scores(const float* a, int64_t n, const float* b, int32_t m, int32_t dim, float* scores,
                          int32_t* top_idx, float* top_val);
 
+/* The subquantizer assignment of training's k-means: for host residuals
+ * res [n][M * dsub] and codebooks [M][pqK][dsub] (pqK <= 256), out [n][M] the
+ * codeword nearest each row's sub-vector m, squared Euclidean distance in the
+ * reference's summation order, ties to the lower index. */
+int hann_gpu_pq_assign(const float* res, int64_t n, int32_t M, int32_t dsub, const float* codebooks, int32_t pqK,
+                       int32_t* out);
+
 /* The index's row arena: out[0] rows allocated, out[1] rows up to the end
  * of the last list (the rest is free slack), out[2] rows left as holes by
  * lists that moved, out[3] list moves and out[4] full relayouts since the
@@ -49,6 +56,13 @@ int hann_pqivf_scan_options(void* h, const int32_t* set8, int32_t* get8);
  * them) instead of the top-8 screen: out2[0] the assignments, out2[1] the
  * rows they sent to the exact kernel. */
 int hann_pqivf_train_stats(void* h, int64_t* out2);
+
+/* Wall milliseconds of the last Train or Retrain, by phase, each ending at a
+ * stream synchronisation: out4[0] gathering the vectors in id order onto the
+ * device, [1] the coarse k-means with the final assignment and its copy to
+ * the host, [2] the subquantizer k-means, [3] the inverted lists, the device
+ * layout, the encoding and the host copies of the quantizers. */
+int hann_pqivf_train_phases(void* h, double* out4);
 
 /* Queries, over the handle's life, whose parity-mode top k the FP16
  * lookup-table screen could not prove and that were scanned again with FP32
