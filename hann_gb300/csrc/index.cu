@@ -657,10 +657,15 @@ static int kmeans_device(hann_pqivf* h, const float* x, int64_t ld, int off, int
         } else {
             // cent points at codebook m inside the [M][k][dim] codebook array.
             const float* cb_all = cent - (int64_t)m * k * dim;
-            CK(launch_pq_assign(sub_full, n, M, dim, cb_all, k, m, m + 1, asg_buf, h->stream));
             CK(cudaMemsetAsync(sums.p + (size_t)m * k * dim, 0, (size_t)k * dim * sizeof(double), h->stream));
             CK(cudaMemsetAsync(counts.p + (size_t)m * k, 0, (size_t)k * sizeof(int64_t), h->stream));
-            CK(launch_pq_accumulate(sub_full, n, M, dim, asg_buf, k, m, m + 1, sums.p, counts.p, h->stream));
+            if (pq_assign_accumulate_supported(dim, k)) {
+                CK(launch_pq_assign_accumulate(sub_full, n, M, dim, cb_all, k, m, asg_buf, sums.p + (size_t)m * k * dim,
+                                               counts.p + (size_t)m * k, h->stream));
+            } else {
+                CK(launch_pq_assign(sub_full, n, M, dim, cb_all, k, m, m + 1, asg_buf, h->stream));
+                CK(launch_pq_accumulate(sub_full, n, M, dim, asg_buf, k, m, m + 1, sums.p, counts.p, h->stream));
+            }
             CK(launch_kmeans_finalize(sums.p + (size_t)m * k * dim, counts.p + (size_t)m * k, k, dim, cent,
                                       h->stream));
             CK(cudaMemcpyAsync(hcounts.data(), counts.p + (size_t)m * k, (size_t)k * sizeof(int64_t),

@@ -43,6 +43,15 @@ cudaError_t launch_pq_assign(const float* res, int64_t n, int M, int dsub, const
 cudaError_t launch_pq_accumulate(const float* res, int64_t n, int M, int dsub, const int32_t* codes,
                                  int pqK, int m_begin, int m_end, double* sums, int64_t* counts,
                                  cudaStream_t s);
+// Assignment and FP64 accumulation of one subquantizer's k-means iteration
+// in one kernel (sub-dimensions 4, 8 and 16, pqK <= 256; otherwise
+// cudaErrorNotSupported and nothing runs): out[p * M + m] the codeword of
+// row p, sums_m [pqK][dsub] and counts_m [pqK] (zeroed by the caller)
+// accumulated over the rows.
+bool pq_assign_accumulate_supported(int dsub, int pqK);
+cudaError_t launch_pq_assign_accumulate(const float* res, int64_t n, int M, int dsub, const float* codebooks,
+                                        int pqK, int m, int32_t* out, double* sums_m, int64_t* counts_m,
+                                        cudaStream_t s);
 
 // residual[i] = x[i] - coarse[cluster[i]] (FP32), rows in the given order:
 // out row i comes from x row src[i] (src may be null for identity).

@@ -273,20 +273,24 @@ __global__ void __launch_bounds__(256) pq_assign_kernel(const float* __restrict_
 // each half rounded as the scalar instruction rounds it) in sqeuclid_ref's
 // order. The codebook sits in shared memory with every float stored twice,
 // so one 16-byte broadcast load gives two codeword coordinates already
-// paired for both points. sqeuclid_ref's first fma into a zero accumulator
-// equals the product (d*d is never -0), and its additions of the untouched
-// zero accumulators for sub-dimensions below 16 leave a sum of squares
-// unchanged, so both are left out: the distances are sqeuclid_ref's bits.
+// paired for both points. Every square is sqeuclid_ref's fma into a zero
+// accumulator, written as that fma: a separate packed multiply followed by
+// a packed add was fused into one fma by the compiler (one assignment in
+// 300,000 moved by an ulp), which an fma cannot be. sqeuclid_ref's
+// additions of the untouched zero accumulators for sub-dimensions below 16
+// leave a sum of squares unchanged and are left out: the distances are
+// sqeuclid_ref's bits.
 using u64 = unsigned long long;
 __device__ __forceinline__ u64 pk_sub(u64 a, u64 b) {
     u64 d;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
-__device__ __forceinline__ u64 pk_mul(u64 a, u64 b) {
-    u64 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
+// d * d rounded once, as fma(d, d, +0): exact for every d (d * d is never -0)
+__device__ __forceinline__ u64 pk_sq(u64 d) {
+    u64 r;
+    asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(r) : "l"(d), "l"(0ull));
+    return r;
 }
 __device__ __forceinline__ u64 pk_fma(u64 a, u64 b, u64 c) {
     u64 d;
@@ -314,15 +318,14 @@ __device__ __forceinline__ u64 pk_sqeuclid(const u64 (&s)[DSUB], const ulonglong
     u64 v[4];
     if (DSUB == 4) {
 #pragma unroll
-        for (int l = 0; l < 4; l++) v[l] = pk_mul(d[l], d[l]);
+        for (int l = 0; l < 4; l++) v[l] = pk_sq(d[l]);
     } else if (DSUB == 8) {
 #pragma unroll
-        for (int l = 0; l < 4; l++) v[l] = pk_fma(d[4 + l], d[4 + l], pk_mul(d[l], d[l]));
+        for (int l = 0; l < 4; l++) v[l] = pk_fma(d[4 + l], d[4 + l], pk_sq(d[l]));
     } else {
 #pragma unroll
         for (int l = 0; l < 4; l++)
-            v[l] = pk_add(pk_add(pk_mul(d[l], d[l]), pk_mul(d[4 + l], d[4 + l])),
-                          pk_add(pk_mul(d[8 + l], d[8 + l]), pk_mul(d[12 + l], d[12 + l])));
+            v[l] = pk_add(pk_add(pk_sq(d[l]), pk_sq(d[4 + l])), pk_add(pk_sq(d[8 + l]), pk_sq(d[12 + l])));
     }
     return pk_add(pk_add(v[0], v[1]), pk_add(v[2], v[3]));
 }
@@ -355,6 +358,7 @@ __global__ void __launch_bounds__(PQ_PACK_THREADS) pq_assign_packed_kernel(const
     u64 d = pk_sqeuclid<DSUB>(s, c2);
     float b0 = __uint_as_float((uint32_t)d), b1 = __uint_as_float((uint32_t)(d >> 32));
     int i0 = 0, i1 = 0;
+#pragma unroll 4
     for (int j = 1; j < pqK; j++) {
         d = pk_sqeuclid<DSUB>(s, c2 + j * (DSUB / 2));
         const float e0 = __uint_as_float((uint32_t)d), e1 = __uint_as_float((uint32_t)(d >> 32));
@@ -369,6 +373,80 @@ __global__ void __launch_bounds__(PQ_PACK_THREADS) pq_assign_packed_kernel(const
     }
     out[p0 * M + m] = i0;
     if (has1) out[p1 * M + m] = i1;
+}
+
+// The packed assignment fused with the k-means accumulation of the same
+// iteration: a grid of at most four blocks an SM walks the rows in tiles of
+// 2 x 256; each row's sub-vector, already in registers, is added in FP64 to
+// its codeword's sum in shared memory (an odd stride of DSUB + 1 doubles a
+// codeword, so the lanes adding the same coordinate for random codewords
+// spread over all 16 bank pairs), and every block adds its sums and counts
+// to the global ones once. Same assignments as pq_assign_packed_kernel; the sums are FP64
+// additions of the same values, in another order.
+template <int DSUB>
+__global__ void __launch_bounds__(PQ_PACK_THREADS) pq_assign_accumulate_kernel(
+    const float* __restrict__ res, int64_t n, int M, const float* __restrict__ cb, int pqK, int m,
+    int32_t* __restrict__ out, double* __restrict__ sums, unsigned long long* __restrict__ counts) {
+    extern __shared__ __align__(16) float scb2[];  // [pqK][DSUB][2], then sums, then counts
+    double* ssum = reinterpret_cast<double*>(scb2 + 2 * pqK * DSUB);  // [pqK][DSUB + 1]
+    unsigned long long* scnt = reinterpret_cast<unsigned long long*>(ssum + pqK * (DSUB + 1));
+    const int dim = M * DSUB;
+    for (int e = threadIdx.x; e < pqK * DSUB; e += blockDim.x) {
+        const float v = cb[(int64_t)m * pqK * DSUB + e];
+        scb2[2 * e] = v;
+        scb2[2 * e + 1] = v;
+    }
+    for (int e = threadIdx.x; e < pqK * (DSUB + 1); e += blockDim.x) ssum[e] = 0.0;
+    for (int e = threadIdx.x; e < pqK; e += blockDim.x) scnt[e] = 0ull;
+    __syncthreads();
+    const ulonglong2* c2 = reinterpret_cast<const ulonglong2*>(scb2);
+    for (int64_t t0 = (int64_t)blockIdx.x * (2 * PQ_PACK_THREADS); t0 < n;
+         t0 += (int64_t)gridDim.x * (2 * PQ_PACK_THREADS)) {
+        const int64_t p0 = t0 + threadIdx.x, p1 = p0 + PQ_PACK_THREADS;
+        if (p0 >= n) continue;
+        const bool has1 = p1 < n;
+        float v0[DSUB], v1[DSUB];
+        u64 s[DSUB];
+#pragma unroll
+        for (int e = 0; e < DSUB; e++) {
+            v0[e] = res[p0 * dim + m * DSUB + e];
+            v1[e] = has1 ? res[p1 * dim + m * DSUB + e] : 0.0f;
+            s[e] = pk_pair(v0[e], v1[e]);
+        }
+        u64 d = pk_sqeuclid<DSUB>(s, c2);
+        float b0 = __uint_as_float((uint32_t)d), b1 = __uint_as_float((uint32_t)(d >> 32));
+        int i0 = 0, i1 = 0;
+#pragma unroll 4
+        for (int j = 1; j < pqK; j++) {
+            d = pk_sqeuclid<DSUB>(s, c2 + j * (DSUB / 2));
+            const float e0 = __uint_as_float((uint32_t)d), e1 = __uint_as_float((uint32_t)(d >> 32));
+            if (e0 < b0) {
+                b0 = e0;
+                i0 = j;
+            }
+            if (e1 < b1) {
+                b1 = e1;
+                i1 = j;
+            }
+        }
+        out[p0 * M + m] = i0;
+#pragma unroll
+        for (int e = 0; e < DSUB; e++) atomicAdd(&ssum[i0 * (DSUB + 1) + e], (double)v0[e]);
+        atomicAdd(&scnt[i0], 1ull);
+        if (has1) {
+            out[p1 * M + m] = i1;
+#pragma unroll
+            for (int e = 0; e < DSUB; e++) atomicAdd(&ssum[i1 * (DSUB + 1) + e], (double)v1[e]);
+            atomicAdd(&scnt[i1], 1ull);
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < pqK * DSUB; e += blockDim.x) {
+        const double v = ssum[(e / DSUB) * (DSUB + 1) + e % DSUB];
+        if (v != 0.0) atomicAdd(&sums[e], v);
+    }
+    for (int e = threadIdx.x; e < pqK; e += blockDim.x)
+        if (scnt[e]) atomicAdd(&counts[e], scnt[e]);
 }
 
 // Generic sub-dimension: sub-vector read from global memory.
@@ -485,6 +563,52 @@ cudaError_t launch_pq_accumulate(const float* res, int64_t n, int M, int dsub, c
     const int64_t total = n * (int64_t)(m_end - m_begin) * dsub;
     pq_accumulate_kernel<<<(unsigned)ceil_div(total, 256), 256, 0, s>>>(res, n, M, dsub, codes, pqK, m_begin,
                                                                        m_end - m_begin, sums, counts);
+    return cudaGetLastError();
+}
+
+size_t pq_assign_accumulate_smem(int dsub, int pqK) {
+    return (size_t)pqK * dsub * 2 * sizeof(float) + (size_t)pqK * (dsub + 1) * sizeof(double) +
+           (size_t)pqK * sizeof(unsigned long long);
+}
+
+bool pq_assign_accumulate_supported(int dsub, int pqK) {
+    return (dsub == 4 || dsub == 8 || dsub == 16) && pqK >= 1 && pqK <= 256;
+}
+
+cudaError_t launch_pq_assign_accumulate(const float* res, int64_t n, int M, int dsub, const float* codebooks,
+                                        int pqK, int m, int32_t* out, double* sums_m, int64_t* counts_m,
+                                        cudaStream_t s) {
+    if (!pq_assign_accumulate_supported(dsub, pqK)) return cudaErrorNotSupported;
+    if (n <= 0) return cudaSuccess;
+    const size_t smem = pq_assign_accumulate_smem(dsub, pqK);
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto* cnt = reinterpret_cast<unsigned long long*>(counts_m);
+    cudaError_t e = cudaSuccess;
+    // up to four resident blocks an SM, as many as the shared memory allows
+#define HANN_PQ_FUSED(D)                                                                                       \
+    {                                                                                                          \
+        e = cudaFuncSetAttribute(pq_assign_accumulate_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                 (int)smem);                                                                   \
+        if (e != cudaSuccess) return e;                                                                        \
+        int occ = 1;                                                                                           \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pq_assign_accumulate_kernel<D>,                \
+                                                          PQ_PACK_THREADS, smem);                              \
+        if (e != cudaSuccess) return e;                                                                        \
+        const unsigned blocks = (unsigned)std::min<int64_t>((int64_t)std::max(1, std::min(occ, 4)) * sms,      \
+                                                            ceil_div(n, 2 * PQ_PACK_THREADS));                 \
+        pq_assign_accumulate_kernel<D><<<blocks, PQ_PACK_THREADS, smem, s>>>(res, n, M, codebooks, pqK, m, out, \
+                                                                             sums_m, cnt);                     \
+    }
+    if (dsub == 4) {
+        HANN_PQ_FUSED(4)
+    } else if (dsub == 8) {
+        HANN_PQ_FUSED(8)
+    } else {
+        HANN_PQ_FUSED(16)
+    }
+#undef HANN_PQ_FUSED
     return cudaGetLastError();
 }
 
@@ -805,13 +929,19 @@ cudaError_t launch_tombstone(const int64_t* rows, int64_t n, float* term, int64_
 
 // Subquantizer assignment of host residuals: res [n][M * dsub], codebooks
 // [M][pqK][dsub], out [n][M] the nearest codeword of every row and
-// subquantizer, as one k-means iteration of training computes it.
+// subquantizer, as one k-means iteration of training computes it; with sums
+// and counts, also the iteration's FP64 codeword sums [M][pqK][dsub] and
+// counts [M][pqK], through the kernels training runs.
 extern "C" int hann_gpu_pq_assign(const float* res, int64_t n, int32_t M, int32_t dsub, const float* codebooks,
-                                  int32_t pqK, int32_t* out) {
+                                  int32_t pqK, int32_t* out, double* sums, int64_t* counts) {
     using namespace hann;
-    if (n <= 0 || M <= 0 || dsub <= 0 || pqK <= 0 || pqK > 256 || !res || !codebooks || !out) return HANN_E_INVALID;
+    if (n <= 0 || M <= 0 || dsub <= 0 || pqK <= 0 || pqK > 256 || !res || !codebooks || !out ||
+        (sums == nullptr) != (counts == nullptr))
+        return HANN_E_INVALID;
     float *dr = nullptr, *dc = nullptr;
     int32_t* dout = nullptr;
+    double* dsum = nullptr;
+    int64_t* dcnt = nullptr;
     int rc = HANN_OK;
     auto ok = [&](cudaError_t e) {
         if (e != cudaSuccess && rc == HANN_OK) rc = HANN_E_CUDA;
@@ -819,16 +949,36 @@ extern "C" int hann_gpu_pq_assign(const float* res, int64_t n, int32_t M, int32_
     };
     const size_t nr = (size_t)n * M * dsub, nc = (size_t)M * pqK * dsub;
     if (ok(cudaMalloc(&dr, sizeof(float) * nr)) && ok(cudaMalloc(&dc, sizeof(float) * nc)) &&
-        ok(cudaMalloc(&dout, sizeof(int32_t) * (size_t)n * M))) {
+        ok(cudaMalloc(&dout, sizeof(int32_t) * (size_t)n * M)) &&
+        (!sums || (ok(cudaMalloc(&dsum, sizeof(double) * nc)) && ok(cudaMalloc(&dcnt, sizeof(int64_t) * M * pqK))))) {
         ok(cudaMemcpy(dr, res, sizeof(float) * nr, cudaMemcpyHostToDevice));
         ok(cudaMemcpy(dc, codebooks, sizeof(float) * nc, cudaMemcpyHostToDevice));
-        for (int m = 0; m < M && rc == HANN_OK; m++)
-            ok(launch_pq_assign(dr, n, M, dsub, dc, pqK, m, m + 1, dout, nullptr));
+        if (sums) {
+            ok(cudaMemset(dsum, 0, sizeof(double) * nc));
+            ok(cudaMemset(dcnt, 0, sizeof(int64_t) * M * pqK));
+        }
+        for (int m = 0; m < M && rc == HANN_OK; m++) {
+            if (!sums) {
+                ok(launch_pq_assign(dr, n, M, dsub, dc, pqK, m, m + 1, dout, nullptr));
+            } else if (pq_assign_accumulate_supported(dsub, pqK)) {
+                ok(launch_pq_assign_accumulate(dr, n, M, dsub, dc, pqK, m, dout, dsum + (size_t)m * pqK * dsub,
+                                               dcnt + (size_t)m * pqK, nullptr));
+            } else {
+                ok(launch_pq_assign(dr, n, M, dsub, dc, pqK, m, m + 1, dout, nullptr));
+                ok(launch_pq_accumulate(dr, n, M, dsub, dout, pqK, m, m + 1, dsum, dcnt, nullptr));
+            }
+        }
         ok(cudaDeviceSynchronize());
         ok(cudaMemcpy(out, dout, sizeof(int32_t) * (size_t)n * M, cudaMemcpyDeviceToHost));
+        if (sums) {
+            ok(cudaMemcpy(sums, dsum, sizeof(double) * nc, cudaMemcpyDeviceToHost));
+            ok(cudaMemcpy(counts, dcnt, sizeof(int64_t) * M * pqK, cudaMemcpyDeviceToHost));
+        }
     }
     cudaFree(dr);
     cudaFree(dc);
     cudaFree(dout);
+    cudaFree(dsum);
+    cudaFree(dcnt);
     return rc;
 }

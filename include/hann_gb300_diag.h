@@ -24,9 +24,13 @@ int hann_gpu_bf16_scores(const float* a, int64_t n, const float* b, int32_t m, i
 /* The subquantizer assignment of training's k-means: for host residuals
  * res [n][M * dsub] and codebooks [M][pqK][dsub] (pqK <= 256), out [n][M] the
  * codeword nearest each row's sub-vector m, squared Euclidean distance in the
- * reference's summation order, ties to the lower index. */
+ * reference's summation order, ties to the lower index. With sums and counts
+ * (both or neither), also the k-means update's FP64 sums of the rows of
+ * every codeword, sums [M][pqK][dsub], and their counts [M][pqK], computed by
+ * the kernels training runs (the fused assignment + accumulation for dsub 4,
+ * 8 and 16). */
 int hann_gpu_pq_assign(const float* res, int64_t n, int32_t M, int32_t dsub, const float* codebooks, int32_t pqK,
-                       int32_t* out);
+                       int32_t* out, double* sums, int64_t* counts);
 
 /* The index's row arena: out[0] rows allocated, out[1] rows up to the end
  * of the last list (the rest is free slack), out[2] rows left as holes by
