@@ -911,6 +911,9 @@ int rerank_depth(const hann_pqivf* h, int kmax, int mode) { return rerank_depth_
 constexpr int SCREEN_MIN_LISTS = 2048;  // below this the full score matrix is cheaper
 constexpr int PROBE_CAP = 4096;         // screened-probe candidates per query and chunk
 constexpr int PROBE_FIRST = 256;        // first centroid chunk at least (every list enters the band)
+// Largest candidate dump of the table scan (a larger chunk of queries selects
+// inside the scan blocks instead)
+constexpr size_t SCAN_DUMP_MAX = (size_t)1 << 30;
 
 
 // Every scratch buffer run_search needs for nq queries (in chunks of at most
@@ -939,6 +942,9 @@ int reserve_search_scratch(hann_pqivf* h, SearchScratch& sc, int64_t nq, int np_
     CK(sc.scut.reserve((size_t)chunk));
     CK(sc.seps.reserve((size_t)chunk));
     CK(sc.credo.reserve((size_t)chunk + 1));
+    if (!sc.dump_off && scan_adc_supported(h->o.num_subquantizers) &&
+        (size_t)chunk * scan_dump_bytes(R) <= SCAN_DUMP_MAX)
+        CK(sc.dump.reserve((size_t)chunk * scan_dump_bytes(R)));
     if (h->tc && h->nlist >= SCREEN_MIN_LISTS) {
         const int lcap = std::max(1024, 2 * np_max);
         CK(sc.pe2.reserve((size_t)chunk));
@@ -1136,6 +1142,8 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
     const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(nq, ((int64_t)1 << 28) / std::max(1, h->nlist)));
     int rrc = reserve_search_scratch(h, sc, nq, np_max, kmax, mode);
     if (rrc) return rrc;
+    if (sc.dump.p && sc.dump.n >= (size_t)chunk * scan_dump_bytes(R)) p.dump = sc.dump.p;
+    const int scan_launches = p.dump ? 2 : 1;  // the table scan and, with a dump, its selection
     auto mark = [&](int stage, bool begin) -> cudaError_t {
         if (!h->profile) return cudaSuccess;
         cudaEvent_t e;
@@ -1198,7 +1206,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
         }
         CK(launch_rerank(pt, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
                          d_dist + q0 * kmax, d_nout + q0, s));
-        h->launches += 2;
+        h->launches += scan_launches + 1;
         if (check) {
             ScanParams pf = p;
             pf.adc_table = 0;
@@ -1208,7 +1216,7 @@ int run_search(hann_pqivf* h, SearchScratch& sc, const float* d_q, int64_t nq, c
                            sc.cand_d.p, sc.cand_seq.p, nullptr, s));
             CK(launch_rerank(pf, qp, nc, sc.cand_row.p, sc.cand_seq.p, R, d_k + q0, kmax, mode, d_ids + q0 * kmax,
                              d_dist + q0 * kmax, d_nout + q0, s));
-            h->launches += 2;
+            h->launches += scan_launches + 1;
         }
         CK(mark(3, false));
         return HANN_OK;

@@ -169,6 +169,11 @@ struct SearchScratch {
     // and the queries the rerank could not prove (count at credo[nq])
     DBuf<float> scut, seps;
     DBuf<int32_t> credo;
+    // the table scan's candidate dump (scan_dump_bytes per query); dump_off:
+    // never reserve one (a server slot sized without it must not allocate
+    // one while batches run)
+    DBuf<unsigned char> dump;
+    bool dump_off = false;
     // list-major tensor-core scan (kernels_lms.cu)
     DBuf<uint16_t> q16;
     DBuf<float> le2, lasl, lthr, lcand_s, lpair_base, leps;
@@ -354,6 +359,7 @@ struct hann_pqivf {
         p.vectors = d_vectors.p;
         p.row_id = d_row_id.p;
         p.kq = nullptr;
+        p.dump = nullptr;
         p.mode = 0;
         p.rerank_fixed = o.rerank;
         return p;

@@ -191,7 +191,15 @@ struct ScanParams {
     const int32_t* qorder;    // optional: block b works on query qorder[b] (L2-friendly order)
     const int32_t* qcount;    // optional with qorder: blocks at or past *qcount have no query
     int mode, rerank_fixed;
+    // optional (table scan): scan_dump_bytes(R) bytes per query slot where
+    // the scan's warps leave their candidates for a separate selection
+    // kernel, so that a scan block ends with its walk; null: the scan block
+    // selects its query's candidates itself
+    void* dump;
 };
+
+// Bytes of the table scan's candidate dump per query slot at rerank depth R.
+size_t scan_dump_bytes(int R);
 
 // Per query: the nprobe nearest coarse lists in ascending (distance, index)
 // order and their distances, from a distance matrix D[nq][nlist]. Also sets

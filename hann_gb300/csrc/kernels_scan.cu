@@ -28,8 +28,11 @@
 // threshold to its buffer; a full buffer is cut back to its R smallest keys
 // by a radix select on 8-bit digits (warp-private histogram), whose R-th key
 // lowers the threshold. At the end warp 0 selects the query's R best from the
-// warps' survivors. Candidates leave unsorted: the rerank sorts them by exact
-// distance.
+// warps' survivors; or, given a candidate dump, every warp leaves its buffer
+// there and exits, and scan_select_kernel (one warp per query, many per SM)
+// makes that selection, so the scan block's table and buffers are free for
+// the next query as soon as its walk ends. Candidates leave unsorted: the
+// rerank sorts them by exact distance.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -47,6 +50,13 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr uint32_t KEY_INF = 0xff800000u;  // float_key(+inf)
 __device__ __forceinline__ float pos_inf() { return __int_as_float(0x7f800000); }
 constexpr int SCAN_FLAT_LISTS = 128;        // probe lists held for the balanced schedule
+
+// A query slot of the candidate dump: keys, positions and rows of the scan
+// block's warps ([WARPS][CAPW] each), then the warps' counts (bit 31: the
+// warp cut its buffer back, so rows were left out).
+__host__ __device__ __forceinline__ size_t dump_slot_bytes(int CAPW) {
+    return ((size_t)WARPS * CAPW * 12 + WARPS * 4 + 15) / 16 * 16;
+}
 
 // A warp's buffer held in the free halves of a striped lookup table (rows of
 // 256 bytes whose first 128 hold the table): element i sits in row i / 32
@@ -607,8 +617,10 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
         }
         return float_key(fmaf((part[0] + part[1]) + (part[2] + part[3]), inv, bt));
     };
+    bool cut = false;  // this warp cut its buffer back (rows were left out)
     auto cut_back = [&]() {
         __syncwarp();
+        cut = true;
         uint32_t kth;
         count = warp_cut(key, seq, row, count, R, CAPW / 2, &kth, hist);
         if (lane == 0) {
@@ -788,6 +800,27 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
             }
         }
     }
+    if (p.dump) {
+        // Each warp leaves its candidates for scan_select_kernel and ends
+        // here: the block's life is its walk, with no barrier or selection.
+        __syncwarp();
+        uint32_t* dk = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(p.dump) +
+                                                   (size_t)blockIdx.x * dump_slot_bytes(CAPW));
+        uint32_t* ds = dk + WARPS * CAPW;
+        int32_t* dr = reinterpret_cast<int32_t*>(ds + WARPS * CAPW);
+        int32_t* dc = dr + WARPS * CAPW;
+        for (int i = lane; i < count; i += 32) {
+            dk[w * CAPW + i] = key[i];
+            ds[w * CAPW + i] = seq[i];
+            dr[w * CAPW + i] = row[i];
+        }
+        if (lane == 0) {
+            dc[w] = (int32_t)((uint32_t)count | (cut ? 0x80000000u : 0u));
+            if (rows_scanned) atomicAdd(rows_scanned, scanned);
+        }
+        if (HALF && p.scan_cut && tid == 0) p.scan_eps[q] = s_eps;
+        return;
+    }
     __syncwarp();
     {
         uint32_t kth;
@@ -833,6 +866,76 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
                 p.scan_eps[q] = s_eps;
             }
         }
+    }
+}
+
+// The end of a table scan run with a candidate dump: per query slot b, the
+// candidates the scan block's warps left are compacted in warp order, cut to
+// the query's best Rq by warp_select (ties by position, as the block's own
+// selection breaks them) and written to the candidate slots the rerank
+// reads, with the parity-mode cut. One warp per slot; many slots per SM, so
+// the selections' latencies overlap where inside the scan block they would
+// hold its table and buffers.
+constexpr int SEL_WARPS = 4;
+__global__ void __launch_bounds__(SEL_WARPS * 32) scan_select_kernel(ScanParams p, int64_t nslots, int R, int CAPW,
+                                                                     int32_t* __restrict__ cand_row,
+                                                                     float* __restrict__ cand_d,
+                                                                     uint32_t* __restrict__ cand_seq) {
+    __shared__ uint32_t hist[SEL_WARPS][256];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int64_t b = (int64_t)blockIdx.x * SEL_WARPS + wl;
+    if (b >= nslots) return;
+    if (p.qcount && b >= *p.qcount) return;
+    const int64_t q = p.qorder ? p.qorder[b] : b;
+    uint32_t* key = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(p.dump) + (size_t)b * dump_slot_bytes(CAPW));
+    uint32_t* seq = key + WARPS * CAPW;
+    int32_t* row = reinterpret_cast<int32_t*>(seq + WARPS * CAPW);
+    const int32_t* cnt = row + WARPS * CAPW;
+    // the warps' segments moved to the front in warp order (each chunk read
+    // before it is written, destinations never past their sources)
+    int total = 0;
+    bool dropped = false;
+    for (int w = 0; w < WARPS; w++) {
+        const uint32_t c0 = (uint32_t)cnt[w];
+        const int c = (int)(c0 & 0x7fffffffu);
+        dropped |= (c0 >> 31) != 0;
+        if (total != w * CAPW) {
+            for (int i0 = 0; i0 < c; i0 += 32) {
+                const int i = i0 + lane;
+                uint32_t kk = 0, ss = 0;
+                int32_t rr = 0;
+                if (i < c) {
+                    kk = key[w * CAPW + i];
+                    ss = seq[w * CAPW + i];
+                    rr = row[w * CAPW + i];
+                }
+                __syncwarp();
+                if (i < c) {
+                    key[total + i] = kk;
+                    seq[total + i] = ss;
+                    row[total + i] = rr;
+                }
+                __syncwarp();
+            }
+        }
+        total += c;
+    }
+    const int Rq = p.kq ? min(R, rerank_depth_for(p.kq[q], p.mode, p.rerank_fixed)) : R;
+    uint32_t kth;
+    const int kept = warp_select(key, seq, row, total, Rq, &kth, &hist[wl][0]);
+    __syncwarp();
+    uint32_t kmax = 0;
+    for (int i = lane; i < R; i += 32) {
+        const bool ok = i < kept;
+        cand_row[q * R + i] = ok ? row[i] : -1;
+        cand_d[q * R + i] = ok ? key_float(key[i]) : pos_inf();
+        cand_seq[q * R + i] = ok ? seq[i] : 0xffffffffu;
+        if (ok) kmax = max(kmax, key[i]);
+    }
+    if (p.scan_cut) {
+        // every row left out screened at or above the largest kept one
+        kmax = __reduce_max_sync(FULL, kmax);
+        if (lane == 0) p.scan_cut[q] = (dropped || total > kept) && kept > 0 ? key_float(kmax) : pos_inf();
     }
 }
 
@@ -992,6 +1095,8 @@ int scan_adc_capw(int R) {
     return c;
 }
 
+size_t scan_dump_bytes(int R) { return dump_slot_bytes(scan_adc_capw(R)); }
+
 size_t scan_adc_smem(int R, int M, int fp16) {
     const size_t lut = (!fp16 && scan_codes_per_row(M) > 16) ? 65536 : 32768;
     return lut + (size_t)WARPS * scan_adc_capw(R) * 12 + (size_t)WARPS * R * 12 + (size_t)WARPS * 256 * 4;
@@ -1036,6 +1141,10 @@ cudaError_t launch_scan_adc(const ScanParams& p, const float* queries, int64_t n
                     (void*)&rows_scanned};
     e = cudaLaunchKernel(fn, dim3((unsigned)nq), dim3(THREADS), args, smem, s);
     if (e != cudaSuccess) return e;
+    if (pp.dump) {
+        scan_select_kernel<<<(unsigned)ceil_div(nq, SEL_WARPS), SEL_WARPS * 32, 0, s>>>(pp, nq, R, CAPW, cand_row,
+                                                                                       cand_d, cand_seq);
+    }
     return cudaGetLastError();
 }
 

@@ -116,7 +116,8 @@ namespace {
 int64_t batch_bytes(const hann_pqivf* h, int64_t nq, int kmax, int np_max, int mode) {
     const int R = rerank_depth(h, kmax, mode);
     const int64_t dim = h->o.dimension;
-    return nq * (h->nlist * 4 + np_max * 8 + R * 12 + dim * 4 + h->kp * 2 + 4 * 6 + kmax * 16) + 4096;
+    const int64_t dump = scan_adc_supported(h->o.num_subquantizers) ? (int64_t)scan_dump_bytes(R) : 0;
+    return nq * (h->nlist * 4 + np_max * 8 + R * 12 + dim * 4 + h->kp * 2 + 4 * 6 + kmax * 16 + dump) + 4096;
 }
 
 void complete(hann_server* s, Slot& sl) {
@@ -444,6 +445,7 @@ int hann_serve_start(hann_pqivf* h, const hann_serve_options* opts, hann_server*
         // scheduler never calls the allocator while batches are in flight.
         if (e == cudaSuccess && reserve_search_scratch(h, sl->sc, Q, np_max, o.max_k, o.mode) != HANN_OK)
             e = cudaErrorMemoryAllocation;
+        sl->sc.dump_off = sl->sc.dump.p == nullptr;
         if (e != cudaSuccess) {
             free_slot(*sl);
             for (auto& x : s->slots) free_slot(*x);

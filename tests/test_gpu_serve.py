@@ -110,14 +110,16 @@ def test_admission_by_memory_budget(index):
     idx, x, rng = index
     with pytest.raises(hg.HannError, match="memory budget"):
         hg.Server(idx, slots=2, max_batch_queries=4096, memory_budget=1 << 20)
-    # a budget that admits about one 256-query batch per slot
-    srv = hg.Server(idx, slots=2, max_batch_queries=256, max_k=10, max_nprobe=16, memory_budget=2 * (1 << 20))
+    # a budget that admits about one 256-query batch per slot (each query's
+    # share includes the table scan's 24 KB candidate dump at k 10)
+    budget = 16 << 20
+    srv = hg.Server(idx, slots=2, max_batch_queries=256, max_k=10, max_nprobe=16, memory_budget=budget)
     try:
         ts = [srv.submit(rng.normal(size=(64, 32)).astype(np.float32), 10, 16) for _ in range(12)]
         for t in ts:
             srv.wait(t)
         st = srv.stats()
-        assert st["peak_admitted_bytes"] <= 2 * (1 << 20)
+        assert st["peak_admitted_bytes"] <= budget
         assert st["requests"] == 12
     finally:
         srv.stop()
