@@ -385,9 +385,26 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
     __shared__ float s_eps;
     const int M = p.M;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    // The table build's first round of codeword loads (eight a lane) goes
+    // out before anything that waits on the query, so its latency overlaps
+    // the query's own loads.
+    constexpr int U = 8;
+    const float* cb = HALF ? p.adc_cb : p.codebooks_t;  // [pqK][M][dsub]
+    const bool cb4 = p.dsub == 4 && (reinterpret_cast<uintptr_t>(cb) & 15) == 0;
+    float4 cpre[U];
+    if (lane < M && cb4) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int j = w + u * WARPS;
+            if (j < p.pqK) cpre[u] = __ldg(reinterpret_cast<const float4*>(cb) + (int64_t)j * M + lane);
+        }
+    }
     if (p.qcount && (int)blockIdx.x >= *p.qcount) return;
     const int64_t q = p.qorder ? p.qorder[blockIdx.x] : blockIdx.x;
     const float* qv = Q + q * p.dim;
+    const bool v4 = cb4 && (reinterpret_cast<uintptr_t>(qv) & 15) == 0;
+    float4 qa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (lane < M && v4) qa = __ldg(reinterpret_cast<const float4*>(qv) + lane);
     if (tid == 0) {
         s_tau = KEY_INF;
         s_big = 0;
@@ -408,9 +425,17 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
         // allowance for the FP32 roundings of the decomposition).
         float bm = 0.0f;
         if (lane < M) {
+            const float rm = p.adc_rm[lane];
             float qq = 0.0f;
-            for (int t = 0; t < p.dsub; t++) qq = fmaf(qv[lane * p.dsub + t], qv[lane * p.dsub + t], qq);
-            bm = 2.0f * sqrtf(qq) * p.adc_rm[lane];
+            if (v4) {
+                qq = fmaf(qa.x, qa.x, qq);
+                qq = fmaf(qa.y, qa.y, qq);
+                qq = fmaf(qa.z, qa.z, qq);
+                qq = fmaf(qa.w, qa.w, qq);
+            } else {
+                for (int t = 0; t < p.dsub; t++) qq = fmaf(qv[lane * p.dsub + t], qv[lane * p.dsub + t], qq);
+            }
+            bm = 2.0f * sqrtf(qq) * rm;
         }
         float mx = bm, sum = bm, cq = 0.0f, qn = 0.0f;
         for (int e = lane; e < p.dim; e += 32) {
@@ -447,7 +472,6 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
         // computes subquantizer l's entry and writes it to each of its slots.
         // Eight codeword loads are in flight per lane (the codebooks come
         // from L2: shared memory leaves L1 little room).
-        const float* cb = HALF ? p.adc_cb : p.codebooks_t;  // [pqK][M][dsub]
         int bs[4] = {0, 0, 0, 0}, hs[4] = {0, 0, 0, 0};
         const int ns = lane < M ? adc_slots(lane, MP, bs, hs) : 0;
         auto put = [&](int j, float acc) {
@@ -464,18 +488,9 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
                     *reinterpret_cast<float*>(lutb + j * ROWB + 4 * bs[i] + 128 * hs[i]) = v;
             }
         };
-        const bool v4 = p.dsub == 4 &&
-                        ((reinterpret_cast<uintptr_t>(qv) | reinterpret_cast<uintptr_t>(cb)) & 15) == 0;
         if (lane < M && v4) {
-            const float4 qa = __ldg(reinterpret_cast<const float4*>(qv) + lane);
-            constexpr int U = 8;
-            for (int j0 = w; j0 < p.pqK; j0 += WARPS * U) {
-                float4 c[U];
-#pragma unroll
-                for (int u = 0; u < U; u++) {
-                    const int j = j0 + u * WARPS;
-                    if (j < p.pqK) c[u] = __ldg(reinterpret_cast<const float4*>(cb) + (int64_t)j * M + lane);
-                }
+            // code values j0, j0 + WARPS, ... (U of them) from codewords c
+            auto round = [&](int j0, const float4 (&c)[U]) {
 #pragma unroll
                 for (int u = 0; u < U; u++) {
                     const int j = j0 + u * WARPS;
@@ -488,6 +503,16 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
                         put(j, acc);
                     }
                 }
+            };
+            round(w, cpre);
+            for (int j0 = w + WARPS * U; j0 < p.pqK; j0 += WARPS * U) {
+                float4 c[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int j = j0 + u * WARPS;
+                    if (j < p.pqK) c[u] = __ldg(reinterpret_cast<const float4*>(cb) + (int64_t)j * M + lane);
+                }
+                round(j0, c);
             }
         } else if (lane < M) {
             const float* qm = qv + lane * p.dsub;
