@@ -895,72 +895,185 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
 }
 
 // The end of a table scan run with a candidate dump: per query slot b, the
-// candidates the scan block's warps left are compacted in warp order, cut to
-// the query's best Rq by warp_select (ties by position, as the block's own
-// selection breaks them) and written to the candidate slots the rerank
-// reads, with the parity-mode cut. One warp per slot; many slots per SM, so
-// the selections' latencies overlap where inside the scan block they would
-// hold its table and buffers.
+// query's best Rq of the candidates the scan block's warps left, taken in
+// warp order then position (ties at the cut broken by that order, as the
+// block's own selection breaks them), written to the candidate slots the
+// rerank reads, with the parity-mode cut. One warp per slot, many slots per
+// SM. The slot's keys are staged in shared memory first (eight segments, all
+// loads in flight at once); the radix select runs there, and only the kept
+// entries' rows and positions are read from the dump.
 constexpr int SEL_WARPS = 4;
+size_t select_smem(int CAPW) { return (size_t)SEL_WARPS * WARPS * CAPW * sizeof(uint32_t); }
+
 __global__ void __launch_bounds__(SEL_WARPS * 32) scan_select_kernel(ScanParams p, int64_t nslots, int R, int CAPW,
                                                                      int32_t* __restrict__ cand_row,
                                                                      float* __restrict__ cand_d,
                                                                      uint32_t* __restrict__ cand_seq) {
-    __shared__ uint32_t hist[SEL_WARPS][256];
+    extern __shared__ uint32_t sel_keys[];  // [SEL_WARPS][WARPS * CAPW]
+    __shared__ uint32_t hist_all[SEL_WARPS][256];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     const int64_t b = (int64_t)blockIdx.x * SEL_WARPS + wl;
     if (b >= nslots) return;
     if (p.qcount && b >= *p.qcount) return;
     const int64_t q = p.qorder ? p.qorder[b] : b;
-    uint32_t* key = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(p.dump) + (size_t)b * dump_slot_bytes(CAPW));
-    uint32_t* seq = key + WARPS * CAPW;
-    int32_t* row = reinterpret_cast<int32_t*>(seq + WARPS * CAPW);
-    const int32_t* cnt = row + WARPS * CAPW;
-    // the warps' segments moved to the front in warp order (each chunk read
-    // before it is written, destinations never past their sources)
-    int total = 0;
-    bool dropped = false;
+    const uint32_t* dk = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(p.dump) +
+                                                           (size_t)b * dump_slot_bytes(CAPW));
+    const uint32_t* ds = dk + WARPS * CAPW;
+    const int32_t* dr = reinterpret_cast<const int32_t*>(ds + WARPS * CAPW);
+    const int32_t* dc = dr + WARPS * CAPW;
+    uint32_t* key = sel_keys + (size_t)wl * WARPS * CAPW;
+    uint32_t* hist = &hist_all[wl][0];
+    // the warps' counts (bit 31: that warp cut its buffer back) and where
+    // each segment starts in the staged order
+    const uint32_t c0 = lane < WARPS ? (uint32_t)__ldg(dc + lane) : 0u;
+    const bool dropped_any = __any_sync(FULL, (c0 >> 31) != 0);
+    int c[WARPS], off[WARPS], total = 0;
+#pragma unroll
     for (int w = 0; w < WARPS; w++) {
-        const uint32_t c0 = (uint32_t)cnt[w];
-        const int c = (int)(c0 & 0x7fffffffu);
-        dropped |= (c0 >> 31) != 0;
-        if (total != w * CAPW) {
-            for (int i0 = 0; i0 < c; i0 += 32) {
-                const int i = i0 + lane;
-                uint32_t kk = 0, ss = 0;
-                int32_t rr = 0;
-                if (i < c) {
-                    kk = key[w * CAPW + i];
-                    ss = seq[w * CAPW + i];
-                    rr = row[w * CAPW + i];
-                }
+        c[w] = (int)(__shfl_sync(FULL, c0, w) & 0x7fffffffu);
+        off[w] = total;
+        total += c[w];
+    }
+    {
+        // the first 128 entries of every segment with all loads in flight,
+        // then the rest of longer segments
+        constexpr int PER = 4;
+        uint32_t v[WARPS][PER];
+#pragma unroll
+        for (int w = 0; w < WARPS; w++)
+#pragma unroll
+            for (int u = 0; u < PER; u++) {
+                const int i = 32 * u + lane;
+                v[w][u] = i < c[w] ? __ldg(dk + w * CAPW + i) : 0u;
+            }
+#pragma unroll
+        for (int w = 0; w < WARPS; w++)
+#pragma unroll
+            for (int u = 0; u < PER; u++) {
+                const int i = 32 * u + lane;
+                if (i < c[w]) key[off[w] + i] = v[w][u];
+            }
+#pragma unroll
+        for (int w = 0; w < WARPS; w++)
+            for (int i = 32 * PER + lane; i < c[w]; i += 32) key[off[w] + i] = __ldg(dk + w * CAPW + i);
+    }
+    __syncwarp();
+    const int Rq = p.kq ? min(R, rerank_depth_for(p.kq[q], p.mode, p.rerank_fixed)) : R;
+    // Radix select on 8-bit digits below the keys' common prefix: pk (the
+    // pivot's top bits, L bits below dropped) and need (keys equal to it that
+    // stay). Every key stays when there are at most Rq.
+    uint32_t pk = 0xffffffffu, need = 0xffffffffu;
+    int L = 0;
+    bool all = total <= Rq;
+    if (!all) {
+        uint32_t band = 0xffffffffu, bor = 0;
+        for (int i = lane; i < total; i += 32) {
+            band &= key[i];
+            bor |= key[i];
+        }
+        band = __reduce_and_sync(FULL, band);
+        bor = __reduce_or_sync(FULL, bor);
+        const uint32_t diff = band ^ bor;
+        uint32_t prefix = band;
+        need = (uint32_t)Rq;
+        if (diff != 0) {
+            const int top = 31 - __clz(diff);
+            prefix = top == 31 ? 0u : (band & (0xffffffffu << (top + 1)));
+            for (int hi = top; hi >= 0; hi -= 8) {
+                const int lo = hi >= 7 ? hi - 7 : 0;
+                const uint32_t himask = hi == 31 ? 0u : (0xffffffffu << (hi + 1));
+                const uint32_t dmask = (1u << (hi - lo + 1)) - 1u;
+#pragma unroll
+                for (int j = 0; j < 8; j++) hist[j * 32 + lane] = 0;
                 __syncwarp();
-                if (i < c) {
-                    key[total + i] = kk;
-                    seq[total + i] = ss;
-                    row[total + i] = rr;
+                for (int i0 = 0; i0 < total; i0 += 32) {
+                    const int i = i0 + lane;
+                    uint32_t bin = 0xffffffffu;
+                    if (i < total) {
+                        const uint32_t kk = key[i];
+                        if ((kk & himask) == prefix) bin = (kk >> lo) & dmask;
+                    }
+                    const unsigned peers = __match_any_sync(FULL, bin);
+                    if (bin != 0xffffffffu && lane == __ffs(peers) - 1) hist[bin] += __popc(peers);
+                    __syncwarp();
                 }
+                uint32_t cnt[8], tot = 0;
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    cnt[j] = hist[lane * 8 + j];
+                    tot += cnt[j];
+                }
+                uint32_t incl = tot;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t t = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const uint32_t excl = incl - tot;
+                const bool mine = excl < need && need <= incl;
+                uint32_t pick = 0, below = 0, inbin = 0;
+                if (mine) {
+                    uint32_t cum = excl;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        if (cum < need && need <= cum + cnt[j]) {
+                            pick = (uint32_t)(lane * 8 + j);
+                            below = cum;
+                            inbin = cnt[j];
+                        }
+                        cum += cnt[j];
+                    }
+                }
+                const int owner = __ffs(__ballot_sync(FULL, mine)) - 1;
+                pick = __shfl_sync(FULL, pick, owner);
+                below = __shfl_sync(FULL, below, owner);
+                inbin = __shfl_sync(FULL, inbin, owner);
                 __syncwarp();
+                prefix |= pick << lo;
+                need -= below;
+                L = lo;
+                if (inbin == need) break;  // the whole digit stays
             }
         }
-        total += c;
+        pk = L == 0 ? prefix : (prefix >> L);
     }
-    const int Rq = p.kq ? min(R, rerank_depth_for(p.kq[q], p.mode, p.rerank_fixed)) : R;
-    uint32_t kth;
-    const int kept = warp_select(key, seq, row, total, Rq, &kth, &hist[wl][0]);
-    __syncwarp();
-    uint32_t kmax = 0;
-    for (int i = lane; i < R; i += 32) {
-        const bool ok = i < kept;
-        cand_row[q * R + i] = ok ? row[i] : -1;
-        cand_d[q * R + i] = ok ? key_float(key[i]) : pos_inf();
-        cand_seq[q * R + i] = ok ? seq[i] : 0xffffffffu;
-        if (ok) kmax = max(kmax, key[i]);
+    // the kept entries in staged order: their rows and positions come from
+    // the dump, segment w's entry i at staged index off[w] + i
+    int out = 0;
+    uint32_t eq_taken = 0, kmax = 0;
+    for (int i0 = 0; i0 < total; i0 += 32) {
+        const int i = i0 + lane;
+        const bool in = i < total;
+        const uint32_t kk = in ? key[i] : 0xffffffffu;
+        const uint32_t kp = L == 0 ? kk : (kk >> L);
+        const bool eq = in && !all && kp == pk;
+        const unsigned beq = __ballot_sync(FULL, eq);
+        const bool keep = in && (all || kp < pk || (eq && eq_taken + __popc(beq & lt) < need));
+        const unsigned bk = __ballot_sync(FULL, keep);
+        if (keep) {
+            int w = 0;
+#pragma unroll
+            for (int ww = 1; ww < WARPS; ww++) w += i >= off[ww] ? 1 : 0;
+            const int src = w * CAPW + (i - off[w]);
+            const int pos = out + __popc(bk & lt);
+            cand_row[q * R + pos] = __ldg(dr + src);
+            cand_d[q * R + pos] = key_float(kk);
+            cand_seq[q * R + pos] = __ldg(ds + src);
+            kmax = max(kmax, kk);
+        }
+        out += __popc(bk);
+        eq_taken += __popc(beq);
+    }
+    for (int i = out + lane; i < R; i += 32) {
+        cand_row[q * R + i] = -1;
+        cand_d[q * R + i] = pos_inf();
+        cand_seq[q * R + i] = 0xffffffffu;
     }
     if (p.scan_cut) {
         // every row left out screened at or above the largest kept one
         kmax = __reduce_max_sync(FULL, kmax);
-        if (lane == 0) p.scan_cut[q] = (dropped || total > kept) && kept > 0 ? key_float(kmax) : pos_inf();
+        if (lane == 0) p.scan_cut[q] = (dropped_any || total > out) && out > 0 ? key_float(kmax) : pos_inf();
     }
 }
 
@@ -1167,8 +1280,11 @@ cudaError_t launch_scan_adc(const ScanParams& p, const float* queries, int64_t n
     e = cudaLaunchKernel(fn, dim3((unsigned)nq), dim3(THREADS), args, smem, s);
     if (e != cudaSuccess) return e;
     if (pp.dump) {
-        scan_select_kernel<<<(unsigned)ceil_div(nq, SEL_WARPS), SEL_WARPS * 32, 0, s>>>(pp, nq, R, CAPW, cand_row,
-                                                                                       cand_d, cand_seq);
+        const size_t ssm = select_smem(CAPW);
+        e = cudaFuncSetAttribute(scan_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm);
+        if (e != cudaSuccess) return e;
+        scan_select_kernel<<<(unsigned)ceil_div(nq, SEL_WARPS), SEL_WARPS * 32, ssm, s>>>(pp, nq, R, CAPW, cand_row,
+                                                                                         cand_d, cand_seq);
     }
     return cudaGetLastError();
 }
