@@ -682,8 +682,9 @@ def main():
     idx.SetADCTables(args.adc_tables)
     log("lookup tables", adc_tables)
 
-    # roofline of the scan kernel: algorithmic bytes = rows scanned (counted
-    # by the kernel, per (query, list)) x M code bytes
+    # roofline of the scan: algorithmic bytes = rows scanned (counted by the
+    # kernel, per (query, list)) x M code bytes, over the scan stage's event
+    # time (the scan kernel and the selection kernel that follows it)
     code_bytes = args.m
     per_search = max(1, min(nq, (1 << 28) // args.nlist))
     scan_launches = args.steps * -(-nq // per_search)
@@ -772,7 +773,8 @@ def main():
             "plain_fp32_id_overlap": plain_same,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": scan_traffic(args, choice),
-                         "kernel": f"scan_adc_kernel ({args.adc_tables} tables)",
+                         "kernel": f"scan_adc_kernel ({args.adc_tables} tables) + scan_select_kernel: the list "
+                                   "scan and its candidate selection, timed together by the scan stage's events",
                          "bytes_per_launch": per_launch_bytes, "peak_source": peak_src},
             "adc_tables": adc_tables,
             "autotune": tune,

@@ -903,13 +903,13 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
 // loads in flight at once); the radix select runs there, and only the kept
 // entries' rows and positions are read from the dump.
 constexpr int SEL_WARPS = 4;
-size_t select_smem(int CAPW) { return (size_t)SEL_WARPS * WARPS * CAPW * sizeof(uint32_t); }
+size_t select_smem(int CAPW, int R) { return (size_t)SEL_WARPS * (WARPS * CAPW + R) * sizeof(uint32_t); }
 
 __global__ void __launch_bounds__(SEL_WARPS * 32) scan_select_kernel(ScanParams p, int64_t nslots, int R, int CAPW,
                                                                      int32_t* __restrict__ cand_row,
                                                                      float* __restrict__ cand_d,
                                                                      uint32_t* __restrict__ cand_seq) {
-    extern __shared__ uint32_t sel_keys[];  // [SEL_WARPS][WARPS * CAPW]
+    extern __shared__ uint32_t sel_keys[];  // [SEL_WARPS][WARPS * CAPW + R]: staged keys, kept entries' sources
     __shared__ uint32_t hist_all[SEL_WARPS][256];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
@@ -922,7 +922,8 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) scan_select_kernel(ScanParams 
     const uint32_t* ds = dk + WARPS * CAPW;
     const int32_t* dr = reinterpret_cast<const int32_t*>(ds + WARPS * CAPW);
     const int32_t* dc = dr + WARPS * CAPW;
-    uint32_t* key = sel_keys + (size_t)wl * WARPS * CAPW;
+    uint32_t* key = sel_keys + (size_t)wl * (WARPS * CAPW + R);
+    int32_t* src_of = reinterpret_cast<int32_t*>(key + WARPS * CAPW);  // [R] dump index of each kept entry
     uint32_t* hist = &hist_all[wl][0];
     // the warps' counts (bit 31: that warp cut its buffer back) and where
     // each segment starts in the staged order
@@ -936,27 +937,28 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) scan_select_kernel(ScanParams 
         total += c[w];
     }
     {
-        // the first 128 entries of every segment with all loads in flight,
-        // then the rest of longer segments
+        // 128 entries of every segment at a time, all their loads in flight
         constexpr int PER = 4;
-        uint32_t v[WARPS][PER];
+        int cmax = 0;
 #pragma unroll
-        for (int w = 0; w < WARPS; w++)
+        for (int w = 0; w < WARPS; w++) cmax = max(cmax, c[w]);
+        for (int i0 = 0; i0 < cmax; i0 += 32 * PER) {
+            uint32_t v[WARPS][PER];
 #pragma unroll
-            for (int u = 0; u < PER; u++) {
-                const int i = 32 * u + lane;
-                v[w][u] = i < c[w] ? __ldg(dk + w * CAPW + i) : 0u;
-            }
+            for (int w = 0; w < WARPS; w++)
 #pragma unroll
-        for (int w = 0; w < WARPS; w++)
+                for (int u = 0; u < PER; u++) {
+                    const int i = i0 + 32 * u + lane;
+                    v[w][u] = i < c[w] ? __ldg(dk + w * CAPW + i) : 0u;
+                }
 #pragma unroll
-            for (int u = 0; u < PER; u++) {
-                const int i = 32 * u + lane;
-                if (i < c[w]) key[off[w] + i] = v[w][u];
-            }
+            for (int w = 0; w < WARPS; w++)
 #pragma unroll
-        for (int w = 0; w < WARPS; w++)
-            for (int i = 32 * PER + lane; i < c[w]; i += 32) key[off[w] + i] = __ldg(dk + w * CAPW + i);
+                for (int u = 0; u < PER; u++) {
+                    const int i = i0 + 32 * u + lane;
+                    if (i < c[w]) key[off[w] + i] = v[w][u];
+                }
+        }
     }
     __syncwarp();
     const int Rq = p.kq ? min(R, rerank_depth_for(p.kq[q], p.mode, p.rerank_fixed)) : R;
@@ -1038,8 +1040,10 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) scan_select_kernel(ScanParams 
         }
         pk = L == 0 ? prefix : (prefix >> L);
     }
-    // the kept entries in staged order: their rows and positions come from
-    // the dump, segment w's entry i at staged index off[w] + i
+    // The kept entries in staged order, compacted in place (each chunk read
+    // before it is written, never past its source) with their dump indices
+    // (segment w's entry i sits at staged index off[w] + i); then their rows
+    // and positions are read from the dump, all loads in flight together.
     int out = 0;
     uint32_t eq_taken = 0, kmax = 0;
     for (int i0 = 0; i0 < total; i0 += 32) {
@@ -1051,24 +1055,42 @@ __global__ void __launch_bounds__(SEL_WARPS * 32) scan_select_kernel(ScanParams 
         const unsigned beq = __ballot_sync(FULL, eq);
         const bool keep = in && (all || kp < pk || (eq && eq_taken + __popc(beq & lt) < need));
         const unsigned bk = __ballot_sync(FULL, keep);
+        __syncwarp();
         if (keep) {
             int w = 0;
 #pragma unroll
             for (int ww = 1; ww < WARPS; ww++) w += i >= off[ww] ? 1 : 0;
-            const int src = w * CAPW + (i - off[w]);
             const int pos = out + __popc(bk & lt);
-            cand_row[q * R + pos] = __ldg(dr + src);
-            cand_d[q * R + pos] = key_float(kk);
-            cand_seq[q * R + pos] = __ldg(ds + src);
+            key[pos] = kk;
+            src_of[pos] = w * CAPW + (i - off[w]);
             kmax = max(kmax, kk);
         }
         out += __popc(bk);
         eq_taken += __popc(beq);
+        __syncwarp();
     }
-    for (int i = out + lane; i < R; i += 32) {
-        cand_row[q * R + i] = -1;
-        cand_d[q * R + i] = pos_inf();
-        cand_seq[q * R + i] = 0xffffffffu;
+    for (int i0 = 0; i0 < R; i0 += 32 * 4) {
+        int32_t rr[4];
+        uint32_t ss[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = i0 + 32 * u + lane;
+            rr[u] = -1;
+            ss[u] = 0xffffffffu;
+            if (i < out) {
+                rr[u] = __ldg(dr + src_of[i]);
+                ss[u] = __ldg(ds + src_of[i]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = i0 + 32 * u + lane;
+            if (i < R) {
+                cand_row[q * R + i] = rr[u];
+                cand_d[q * R + i] = i < out ? key_float(key[i]) : pos_inf();
+                cand_seq[q * R + i] = ss[u];
+            }
+        }
     }
     if (p.scan_cut) {
         // every row left out screened at or above the largest kept one
@@ -1280,7 +1302,7 @@ cudaError_t launch_scan_adc(const ScanParams& p, const float* queries, int64_t n
     e = cudaLaunchKernel(fn, dim3((unsigned)nq), dim3(THREADS), args, smem, s);
     if (e != cudaSuccess) return e;
     if (pp.dump) {
-        const size_t ssm = select_smem(CAPW);
+        const size_t ssm = select_smem(CAPW, R);
         e = cudaFuncSetAttribute(scan_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssm);
         if (e != cudaSuccess) return e;
         scan_select_kernel<<<(unsigned)ceil_div(nq, SEL_WARPS), SEL_WARPS * 32, ssm, s>>>(pp, nq, R, CAPW, cand_row,
