@@ -1192,9 +1192,10 @@ def knn_section(args, torch, dev):
 
 
 def scan_traffic(args, nprobe):
-    """DRAM bytes (read + write) of one scan launch on this workload, from the
-    1-pass ncu capture kept in profiles/ (ncu cannot run inside the bench);
-    None when the capture was of another workload."""
+    """DRAM bytes (read + write) of one scan stage (the scan kernel and its
+    selection kernel) on this workload, from the 1-pass ncu capture kept in
+    profiles/ (ncu cannot run inside the bench); None when the capture was of
+    another workload."""
     path = os.path.join(HERE, "profiles", "scan_adc_kernel_10Mx96_dram.json")
     try:
         rec = json.load(open(path))

@@ -358,8 +358,26 @@ __global__ void __launch_bounds__(WARPS * 32) knn_merge_band_warp_kernel(
     }
     unsigned long long* keys = mw_smem + w * CAPK;
     const int kr = krow ? max(1, min(krow[r], k)) : k;
-    for (int i = lane; i < L; i += 32) keys[i] = list[r * lcap + i];
-    for (int i = lane; i < c; i += 32) keys[L + i] = dkey(cand_s[r * cap + i], (uint32_t)cand_id[r * cap + i]);
+    // the band list and the new candidates, 128 entries of each at a time
+    // with all their loads in flight
+    for (int i0 = 0; i0 < max(L, c); i0 += 128) {
+        unsigned long long lv[4];
+        float cs[4];
+        uint32_t ci[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = i0 + 32 * u + lane;
+            lv[u] = i < L ? list[r * lcap + i] : 0ull;
+            cs[u] = i < c ? cand_s[r * cap + i] : 0.0f;
+            ci[u] = i < c ? (uint32_t)cand_id[r * cap + i] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int i = i0 + 32 * u + lane;
+            if (i < L) keys[i] = lv[u];
+            if (i < c) keys[L + i] = dkey(cs[u], ci[u]);
+        }
+    }
     const int T = L + c;
     __syncwarp();
     float t_new = __int_as_float(0x7f800000);
