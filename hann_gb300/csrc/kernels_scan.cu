@@ -405,6 +405,12 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
     const bool v4 = cb4 && (reinterpret_cast<uintptr_t>(qv) & 15) == 0;
     float4 qa = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (lane < M && v4) qa = __ldg(reinterpret_cast<const float4*>(qv) + lane);
+    // 16-bit tables with every coordinate in some lane's float4: the query's
+    // norm and its dot product with the subquantizers' means come from the
+    // lanes' float4s (their mean coordinates loaded beside them)
+    const bool vfull = HALF && v4 && M * 4 == p.dim && (reinterpret_cast<uintptr_t>(p.adc_mu) & 15) == 0;
+    float4 mu4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (lane < M && vfull) mu4 = __ldg(reinterpret_cast<const float4*>(p.adc_mu) + lane);
     if (tid == 0) {
         s_tau = KEY_INF;
         s_big = 0;
@@ -423,10 +429,9 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
         // row's sum of them is exact in 32-bit integers). Either way a row's
         // screened distance is within eps of the exact sum (with a relative
         // allowance for the FP32 roundings of the decomposition).
-        float bm = 0.0f;
+        float bm = 0.0f, qq = 0.0f;
         if (lane < M) {
             const float rm = p.adc_rm[lane];
-            float qq = 0.0f;
             if (v4) {
                 qq = fmaf(qa.x, qa.x, qq);
                 qq = fmaf(qa.y, qa.y, qq);
@@ -438,9 +443,17 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
             bm = 2.0f * sqrtf(qq) * rm;
         }
         float mx = bm, sum = bm, cq = 0.0f, qn = 0.0f;
-        for (int e = lane; e < p.dim; e += 32) {
-            cq = fmaf(qv[e], p.adc_mu[e], cq);
-            qn = fmaf(qv[e], qv[e], qn);
+        if (vfull) {
+            qn = qq;
+            cq = fmaf(qa.x, mu4.x, cq);
+            cq = fmaf(qa.y, mu4.y, cq);
+            cq = fmaf(qa.z, mu4.z, cq);
+            cq = fmaf(qa.w, mu4.w, cq);
+        } else {
+            for (int e = lane; e < p.dim; e += 32) {
+                cq = fmaf(qv[e], p.adc_mu[e], cq);
+                qn = fmaf(qv[e], qv[e], qn);
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -828,19 +841,32 @@ __global__ void __launch_bounds__(THREADS, 3) scan_adc_kernel(ScanParams p, cons
     if (p.dump) {
         // Each warp leaves its candidates for scan_select_kernel and ends
         // here: the block's life is its walk, with no barrier or selection.
+        // Candidates above the block's current threshold are left out: some
+        // warp holds at least R candidates at or below every value the
+        // threshold takes, so the query's best R are all at or below it.
         __syncwarp();
+        const uint32_t tau_end = *(volatile uint32_t*)&s_tau;
         uint32_t* dk = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(p.dump) +
                                                    (size_t)blockIdx.x * dump_slot_bytes(CAPW));
         uint32_t* ds = dk + WARPS * CAPW;
         int32_t* dr = reinterpret_cast<int32_t*>(ds + WARPS * CAPW);
         int32_t* dc = dr + WARPS * CAPW;
-        for (int i = lane; i < count; i += 32) {
-            dk[w * CAPW + i] = key[i];
-            ds[w * CAPW + i] = seq[i];
-            dr[w * CAPW + i] = row[i];
+        int kept = 0;
+        for (int i0 = 0; i0 < count; i0 += 32) {
+            const int i = i0 + lane;
+            const uint32_t kk = i < count ? key[i] : 0xffffffffu;
+            const bool keep = i < count && kk <= tau_end;
+            const unsigned bk = __ballot_sync(FULL, keep);
+            if (keep) {
+                const int pos = w * CAPW + kept + __popc(bk & ltm);
+                dk[pos] = kk;
+                ds[pos] = seq[i];
+                dr[pos] = row[i];
+            }
+            kept += __popc(bk);
         }
         if (lane == 0) {
-            dc[w] = (int32_t)((uint32_t)count | (cut ? 0x80000000u : 0u));
+            dc[w] = (int32_t)((uint32_t)kept | (cut || kept < count ? 0x80000000u : 0u));
             if (rows_scanned) atomicAdd(rows_scanned, scanned);
         }
         if (HALF && p.scan_cut && tid == 0) p.scan_eps[q] = s_eps;
