@@ -75,6 +75,19 @@ def test_traffic_record_only_for_its_workload():
     assert bench.scan_traffic(args_for(adc_tables="fp32"), 32) is None  # another kernel
 
 
+def test_traffic_record_is_the_scan_stage():
+    """The record's bytes are the scan stage's: the scan kernel and the
+    selection kernel after it, the two kernels the roofline's time covers."""
+    import json
+    import os
+    rec = json.load(open(os.path.join(os.path.dirname(bench.__file__), "profiles", "scan_adc_kernel_10Mx96_dram.json")))
+    parts = rec["per_kernel"]
+    assert set(parts) == {"scan_adc_kernel", "scan_select_kernel"}
+    assert rec["dram_bytes_read_per_launch"] == sum(k["dram_bytes_read"] for k in parts.values())
+    assert rec["dram_bytes_write_per_launch"] == sum(k["dram_bytes_write"] for k in parts.values())
+    assert bench.scan_traffic(args_for(), 32) == rec["dram_bytes_read_per_launch"] + rec["dram_bytes_write_per_launch"]
+
+
 def test_workload_config():
     """The config names the workload from the arguments alone, so both arms
     (and every rank) report the same one."""
