@@ -5,7 +5,7 @@ which releases the interpreter lock, so the handle's own locks order the
 calls.
 
 Run as a program (`python -m tests.concurrency_scenarios [name ...]`), one
-JSON line per scenario as it ends; tests/test_zzz_gpu_concurrency.py runs
+JSON line per scenario as it ends; tests/test_zy_gpu_concurrency.py runs
 it in a child process, so that a crash or a deadlock in one scenario fails
 that test alone instead of ending the test session."""
 import io

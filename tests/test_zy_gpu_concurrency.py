@@ -4,7 +4,8 @@ failed updates that keep their entries (pqivf/index_test.go:455-500).
 
 The scenarios (tests/concurrency_scenarios.py) run in one child process: a
 crash or a deadlock there fails these tests and leaves the rest of the
-session running. The file sorts last so the other GPU tests run first."""
+session running. The file sorts after the other GPU tests, so they run
+first, and before the allocation-free entry point's tests, which run last."""
 import json
 import os
 import subprocess
